@@ -1,0 +1,275 @@
+// mg_cc.cu -- connected components and multi-graph batches.
+//
+// Replaces MultiGraph_E_E / ee_kernel (edge hooking with parity-alternating
+// min/max, process.cu:969-999,1051-1077) and MultiGraph_V_V / vv_kernel
+// (pointer jumping, process.cu:940-967,1012-1049) driven by main.cu:113-119,
+// which return to the host after every hooking and jumping round.
+//
+// Here one pass over the edges does the whole job: every edge unions its two
+// endpoints in a lock-free union-find whose links always go from the larger
+// root to the smaller one (parent[x] <= x), with path halving in find; a
+// final pass compresses every vertex to its root.  The root of a component
+// is therefore its minimum vertex id, which is exactly the canonical label
+// the reference's validator derives (validate.cu:234-242,263-273).  Union
+// retries only when another thread changed the same root, so every loop is
+// lock-free and bounded by the number of successful links.
+//
+// Multi-graph batches: the graphs are laid out as one disjoint union (vertex
+// ids offset per graph), so one multi-source BFS and one CC pass cover the
+// whole batch; per-graph results are the arena results minus the offsets.
+
+#include "mg_device.cuh"
+#include "mg_ops.cuh"
+
+#include <algorithm>
+#include <cstring>
+#include <memory>
+
+namespace {
+
+constexpr int THREADS = 256;
+
+__device__ __forceinline__ int32_t cc_find(volatile int32_t *parent, int32_t v)
+{
+    int32_t p = parent[v];
+    while (p != v) {
+        int32_t gp = parent[p];
+        if (gp != p) parent[v] = gp;  // halving; benign race, keeps parent[v] <= v
+        v = p;
+        p = gp;
+    }
+    return v;
+}
+
+__device__ __forceinline__ void cc_union(int32_t *parent, int32_t a, int32_t b)
+{
+    volatile int32_t *vp = parent;
+    for (;;) {
+        a = cc_find(vp, a);
+        b = cc_find(vp, b);
+        if (!mgops::Cc::update_condition(a, b)) return;
+        if (a < b) { int32_t t = a; a = b; b = t; }
+        int32_t old = atomicCAS(&parent[a], a, b);  // link larger root under smaller
+        if (old == a) return;
+        a = old;
+    }
+}
+
+__global__ void k_cc_init(int32_t n, const int32_t *row, const int32_t *col, int32_t *parent)
+{
+    for (int32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x) {
+        int32_t p = mgops::Cc::initialize(v);
+        // first (smallest) neighbour below v starts the tree (columns ascend)
+        if (row[v + 1] > row[v]) p = min(p, col[row[v]]);
+        parent[v] = p;
+    }
+}
+
+// per-edge union over the edge-balanced row groups (group_reduce interface;
+// the reduction value is unused)
+struct HookOp {
+    using T = int;
+    static constexpr bool kRowAware = true;  // the union needs the row (source vertex)
+    static constexpr bool kWeights = false;
+    int32_t *parent;
+    int symmetric;
+    __device__ int identity() const { return 0; }
+    __device__ bool skip(int32_t) const { return false; }
+    __device__ int edge(int32_t, int32_t src, int32_t dst, int32_t) const
+    {
+        if (src != dst && (!symmetric || dst < src)) cc_union(parent, src, dst);
+        return 0;
+    }
+    __device__ int combine(int, int) const { return 0; }
+    __device__ void finish(int32_t, int) {}
+};
+
+// one pass over the pull-side arrays; symmetric graphs take each undirected
+// edge once (u > v), general graphs every entry
+__global__ void __launch_bounds__(THREADS) k_cc_hook(int32_t n, const int32_t *prow, const int32_t *pcol,
+                                                     const int32_t *grp, int32_t ngroups, const int32_t *hchunk,
+                                                     int32_t nhchunks, int32_t heavy_deg, int symmetric,
+                                                     int32_t *parent)
+{
+    const int gwarp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int nwarps = (gridDim.x * blockDim.x) >> 5;
+    __shared__ int32_t s_off[THREADS / 32][mgd::GROUP_ROWS + 1];
+    __shared__ __align__(16) int32_t s_col[THREADS / 32][mgd::GROUP_STAGE];
+    HookOp op{parent, symmetric};
+    const mgd::GroupSmem sm{s_off[threadIdx.x >> 5], s_col[threadIdx.x >> 5], nullptr};
+    for (int32_t g = gwarp; g < ngroups; g += nwarps) {
+        int32_t r0 = grp[g], r1 = grp[g + 1];
+        if (r1 - r0 == 1 && prow[r1] - prow[r0] > heavy_deg) continue;  // heavy row: chunks below
+        mgd::group_reduce(op, prow, pcol, nullptr, r0, r1, sm);
+    }
+    for (int32_t ch = blockIdx.x; ch < nhchunks; ch += gridDim.x) {
+        int32_t u = hchunk[3 * ch], b = hchunk[3 * ch + 1], e = hchunk[3 * ch + 2];
+        for (int32_t p = b + threadIdx.x; p < e; p += blockDim.x) {
+            int32_t dst = pcol[p];
+            if (u != dst && (!symmetric || dst < u)) cc_union(parent, u, dst);
+        }
+    }
+}
+
+__global__ void k_cc_compress(int32_t n, int32_t *parent)
+{
+    volatile int32_t *vp = parent;
+    for (int32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x) {
+        int32_t r = cc_find(vp, v);
+        parent[v] = r;
+    }
+}
+
+}  // namespace
+
+struct CcWS {
+    mgi::DevBuf parent;
+};
+
+namespace mgi {
+
+void free_cc_ws(mg_graph *g)
+{
+    if (!g->cws) return;
+    dev_free(g->cws->parent);
+    delete g->cws;
+    g->cws = nullptr;
+}
+
+void free_bc_ws(mg_graph *g) { (void)g; }
+
+mg_status cc_run(mg_graph *g, mg_run_info *info)
+{
+    if (!g->cws) g->cws = new CcWS();
+    MG_TRY(dev_alloc(g->cws->parent, (size_t)std::max(g->nv, 1) * 4));
+    int32_t *parent = g->cws->parent.as<int32_t>();
+    cudaStream_t s = g->stream;
+    const int grid = launch_grid(g, THREADS, 8);
+    Profiler &P = g->prof;
+    int si = P.slot("cc_init"), sh = P.slot("cc_hook"), sc = P.slot("cc_compress");
+    P.begin(si);
+    k_cc_init<<<grid, THREADS, 0, s>>>(g->nv, g->trow, g->tcol, parent);
+    P.end();
+    P.begin(sh);
+    k_cc_hook<<<grid, THREADS, 0, s>>>(g->nv, g->trow, g->tcol, g->grp.as<int32_t>(), g->ngroups,
+                                       g->hchunk.as<int32_t>(), g->nhchunks, g->heavy_deg, g->symmetric ? 1 : 0, parent);
+    P.end();
+    P.begin(sc);
+    k_cc_compress<<<grid, THREADS, 0, s>>>(g->nv, parent);
+    P.end();
+    MG_CUDA(cudaGetLastError());
+    if (info) {
+        info->iterations = 1;
+        info->edges_scanned = g->ne;
+    }
+    return MG_OK;
+}
+
+mg_status frontier_run_multi(mg_graph *g, int alg, const int32_t *srcs_host, int32_t nsrc, const mg_opts &opt,
+                             mg_run_info *info);
+const void *frontier_label(mg_graph *g);
+
+}  // namespace mgi
+
+using namespace mgi;
+
+struct mg_batch {
+    mg_graph *dg = nullptr;
+    std::vector<int32_t> voff;  // vertex offset of each graph (+ total)
+    std::vector<int32_t> local_nv;
+};
+
+extern "C" {
+
+mg_status mg_cc(mg_graph *g, const mg_opts *o, int32_t *label_out, mg_run_info *info)
+{
+    mg_opts opt;
+    MG_TRY(begin_run(g, o, opt, info));
+    MG_TRY(cc_run(g, info));
+    MG_TRY(end_run(g, opt, info));
+    g->res[MG_RES_LABEL] = g->cws->parent.p;
+    return copy_out(g, label_out, g->cws->parent.p, (size_t)g->nv * 4);
+}
+
+mg_status mg_batch_create(const mg_host_graph *const *graphs, int32_t count, int32_t device, mg_batch **out)
+{
+    clear_error();
+    if (!graphs || !out || count <= 0) return fail(MG_ERR_INVALID, "invalid argument");
+    *out = nullptr;
+    int64_t nv = 0, ne = 0;
+    for (int32_t i = 0; i < count; i++) {
+        if (!graphs[i]) return fail(MG_ERR_INVALID, "null graph %d", i);
+        nv += graphs[i]->nv;
+        ne += graphs[i]->ne;
+    }
+    if (nv >= INT32_MAX || ne >= INT32_MAX) return fail(MG_ERR_RANGE, "batch too large for int32 ids");
+    mg_host_graph arena;
+    arena.nv = (int32_t)nv;
+    arena.ne = (int32_t)ne;
+    arena.v.resize((size_t)nv + 1);
+    arena.e.resize((size_t)ne);
+    arena.ev.resize((size_t)ne);
+    std::unique_ptr<mg_batch> b(new mg_batch());
+    int32_t vo = 0, eo = 0;
+    for (int32_t i = 0; i < count; i++) {
+        const mg_host_graph *h = graphs[i];
+        b->voff.push_back(vo);
+        b->local_nv.push_back(h->nv);
+        for (int32_t v = 0; v < h->nv; v++) arena.v[vo + v] = eo + h->v[v];
+        for (int32_t p = 0; p < h->ne; p++) {
+            arena.e[eo + p] = vo + h->e[p];
+            arena.ev[eo + p] = h->ev[p];
+        }
+        vo += h->nv;
+        eo += h->ne;
+    }
+    arena.v[nv] = (int32_t)ne;
+    b->voff.push_back(vo);
+    MG_TRY(mg_graph_upload(&arena, device, &b->dg));
+    *out = b.release();
+    return MG_OK;
+}
+
+void mg_batch_free(mg_batch *b)
+{
+    if (!b) return;
+    mg_graph_free(b->dg);
+    delete b;
+}
+
+mg_status mg_batch_bfs(mg_batch *b, const int32_t *sources, const mg_opts *o, int32_t *levels_out, mg_run_info *info)
+{
+    clear_error();
+    if (!b || !sources) return fail(MG_ERR_INVALID, "invalid argument");
+    std::vector<int32_t> srcs(b->local_nv.size());
+    for (size_t i = 0; i < srcs.size(); i++) {
+        if (sources[i] < 0 || sources[i] >= b->local_nv[i])
+            return fail(MG_ERR_RANGE, "source %d of graph %zu out of range", sources[i], i);
+        srcs[i] = b->voff[i] + sources[i];
+    }
+    mg_graph *g = b->dg;
+    mg_opts opt;
+    MG_TRY(begin_run(g, o, opt, info));
+    MG_TRY(frontier_run_multi(g, 0, srcs.data(), (int32_t)srcs.size(), opt, info));
+    MG_TRY(end_run(g, opt, info));
+    g->res[MG_RES_LEVEL] = frontier_label(g);
+    return copy_out(g, levels_out, g->res[MG_RES_LEVEL], (size_t)g->nv * 4);
+}
+
+mg_status mg_batch_cc(mg_batch *b, const mg_opts *o, int32_t *labels_out, mg_run_info *info)
+{
+    clear_error();
+    if (!b) return fail(MG_ERR_INVALID, "invalid argument");
+    mg_graph *g = b->dg;
+    mg_opts opt;
+    MG_TRY(begin_run(g, o, opt, info));
+    MG_TRY(cc_run(g, info));
+    MG_TRY(end_run(g, opt, info));
+    if (!labels_out) return MG_OK;
+    MG_TRY(copy_out(g, labels_out, g->cws->parent.p, (size_t)g->nv * 4));
+    for (size_t i = 0; i + 1 < b->voff.size(); i++)
+        for (int32_t v = b->voff[i]; v < b->voff[i + 1]; v++) labels_out[v] -= b->voff[i];
+    return MG_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,483 @@
+// mg_device.cu -- device graph upload and the shared run machinery.
+//
+// mg_graph_upload replaces the reference's generate_MultiGraph
+// (gen_structure.cu:2230-2947).  The reference builds a 2-D tiled layout
+// (16-bit sparse-tile streams sp1/sp2, dense tiles, an intermediate buffer
+// i1 written and re-read every dense iteration, ~12.5 B/edge) sized for
+// Kepler's 48 KB shared memory.  On GB300 the whole pull-side gather vector
+// of these graphs (n*4 B, <= 67 MB) stays in the 126 MB L2, so the layout here
+// is the CSR itself plus two small index tables that make the pull kernels
+// edge-balanced:
+//   grp    : groups of <= 32 consecutive rows holding <= GROUP_EDGES light
+//            edges -- one warp processes one group with coalesced reads;
+//   hchunk : rows with in-degree > heavy_deg split into HCHUNK-edge chunks,
+//            processed by whole CTAs and combined in a fixed order.
+// A transposed copy is built only when the graph is not symmetric.
+
+#include "mg_device.cuh"
+
+#include <algorithm>
+#include <cstring>
+#include <memory>
+
+namespace mgi {
+
+constexpr int32_t GROUP_EDGES = mgd::GROUP_EDGES;
+constexpr int32_t HEAVY_DEG = mgd::GROUP_EDGES;  // rows above one group's edges take the chunk path
+constexpr int32_t HCHUNK = 2048;                  // = 8 edges x 256 threads of a chunk CTA
+// column / weight arrays carry this many bytes of readable tail padding (the
+// pull kernels stage column ids with aligned 16-byte loads)
+constexpr size_t COL_PAD = 16;
+
+mg_status dev_alloc(DevBuf &b, size_t bytes)
+{
+    if (b.p && b.bytes >= bytes) return MG_OK;
+    dev_free(b);
+    if (bytes == 0) bytes = 16;
+    if (inject_alloc_failure()) return fail(MG_ERR_OOM, "device allocation of %zu bytes failed (injected)", bytes);
+    cudaError_t e = cudaMalloc(&b.p, bytes);
+    if (e != cudaSuccess) {
+        b.p = nullptr;
+        cudaGetLastError();
+        return fail(e == cudaErrorMemoryAllocation ? MG_ERR_OOM : MG_ERR_CUDA, "cudaMalloc(%zu): %s", bytes,
+                    cudaGetErrorString(e));
+    }
+    b.bytes = bytes;
+    return MG_OK;
+}
+
+void dev_free(DevBuf &b)
+{
+    if (b.p) cudaFree(b.p);
+    b.p = nullptr;
+    b.bytes = 0;
+}
+
+// ---------------------------------------------------------------------------
+void Profiler::reset(cudaStream_t s, bool enable)
+{
+    stream = s;
+    on = enable;
+    slots.clear();
+    pending.clear();
+    used = 0;
+    open_slot = -1;
+}
+
+int Profiler::slot(const char *name)
+{
+    for (size_t i = 0; i < slots.size(); i++)
+        if (slots[i].name == name) return (int)i;
+    slots.push_back(Slot{name, 0, 0.0});
+    return (int)slots.size() - 1;
+}
+
+void Profiler::begin(int slot_id)
+{
+    if (!on) return;
+    if (used == pool.size()) {
+        cudaEvent_t a, b;
+        cudaEventCreate(&a);
+        cudaEventCreate(&b);
+        pool.push_back({a, b});
+    }
+    cudaEventRecord(pool[used].first, stream);
+    open_slot = slot_id;
+}
+
+void Profiler::end()
+{
+    if (!on || open_slot < 0) return;
+    cudaEventRecord(pool[used].second, stream);
+    pending.push_back({open_slot, used});
+    used++;
+    open_slot = -1;
+}
+
+mg_status Profiler::collect(mg_run_info *info)
+{
+    if (!on) return MG_OK;
+    for (auto &p : pending) {
+        float ms = 0.f;
+        MG_CUDA(cudaEventElapsedTime(&ms, pool[p.ev].first, pool[p.ev].second));
+        slots[p.slot].launches++;
+        slots[p.slot].ms += ms;
+    }
+    pending.clear();
+    used = 0;
+    if (info) {
+        info->nkernels = (int32_t)std::min<size_t>(slots.size(), MG_PROFILE_SLOTS);
+        for (int i = 0; i < info->nkernels; i++) {
+            std::snprintf(info->kernels[i].name, sizeof(info->kernels[i].name), "%s", slots[i].name.c_str());
+            info->kernels[i].launches = slots[i].launches;
+            info->kernels[i].total_ms = slots[i].ms;
+        }
+    }
+    return MG_OK;
+}
+
+Profiler::~Profiler()
+{
+    for (auto &p : pool) { cudaEventDestroy(p.first); cudaEventDestroy(p.second); }
+}
+
+// ---------------------------------------------------------------------------
+void LoopGraph::destroy()
+{
+    if (exec) cudaGraphExecDestroy(exec);
+    if (graph) cudaGraphDestroy(graph);
+    exec = nullptr;
+    graph = nullptr;
+    key = 0;
+}
+
+mg_status run_loop(int exec_mode, bool profile, cudaStream_t stream, LoopGraph &lg, uint64_t key, const BodyFn &body,
+                   const int32_t *more_dev, int32_t *more_host, int max_host_iters)
+{
+    if (exec_mode == MG_EXEC_GRAPH && !profile) {
+        if (!lg.exec || lg.key != key) {
+            lg.destroy();
+            cudaGraph_t g;
+            MG_CUDA(cudaGraphCreate(&g, 0));
+            cudaGraphConditionalHandle h;
+            cudaError_t e = cudaGraphConditionalHandleCreate(&h, g, 1, cudaGraphCondAssignDefault);
+            if (e != cudaSuccess) { cudaGraphDestroy(g); MG_CUDA(e); }
+            cudaGraphNodeParams p = {cudaGraphNodeTypeConditional};
+            p.conditional.handle = h;
+            p.conditional.type = cudaGraphCondTypeWhile;
+            p.conditional.size = 1;
+            cudaGraphNode_t node;
+            e = cudaGraphAddNode(&node, g, nullptr, nullptr, 0, &p);
+            if (e != cudaSuccess) { cudaGraphDestroy(g); MG_CUDA(e); }
+            cudaGraph_t bodyg = p.conditional.phGraph_out[0];
+            e = cudaStreamBeginCaptureToGraph(stream, bodyg, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
+            if (e != cudaSuccess) { cudaGraphDestroy(g); MG_CUDA(e); }
+            mg_status s = body(stream, h, 1);
+            cudaGraph_t captured = nullptr;
+            e = cudaStreamEndCapture(stream, &captured);
+            if (s != MG_OK) { cudaGraphDestroy(g); return s; }
+            if (e != cudaSuccess) { cudaGraphDestroy(g); MG_CUDA(e); }
+            cudaGraphExec_t ex;
+            e = cudaGraphInstantiate(&ex, g, 0);
+            if (e != cudaSuccess) { cudaGraphDestroy(g); MG_CUDA(e); }
+            lg.graph = g;
+            lg.exec = ex;
+            lg.key = key;
+        }
+        MG_CUDA(cudaGraphLaunch(lg.exec, stream));
+        return MG_OK;
+    }
+    // host-driven loop: one readback of the continue flag per iteration
+    for (int it = 0; it < max_host_iters; it++) {
+        MG_TRY(body(stream, 0, 0));
+        MG_CUDA(cudaMemcpyAsync(more_host, more_dev, sizeof(int32_t), cudaMemcpyDeviceToHost, stream));
+        MG_CUDA(cudaStreamSynchronize(stream));
+        if (*more_host == 0) return MG_OK;
+    }
+    return MG_OK;
+}
+
+int launch_grid(const mg_graph *g, int threads, int per_sm)
+{
+    (void)threads;
+    return g->num_sms * per_sm;
+}
+
+mg_status copy_out(mg_graph *g, void *host, const void *dev, size_t bytes)
+{
+    if (!host || bytes == 0) return MG_OK;
+    MG_CUDA(cudaMemcpyAsync(host, dev, bytes, cudaMemcpyDeviceToHost, g->stream));
+    MG_CUDA(cudaStreamSynchronize(g->stream));
+    return MG_OK;
+}
+
+mg_status begin_run(mg_graph *g, const mg_opts *o, mg_opts &opt, mg_run_info *info)
+{
+    clear_error();
+    if (!g) return fail(MG_ERR_INVALID, "null graph");
+    if (o) opt = *o; else mg_opts_default(&opt);
+    if (info) std::memset(info, 0, sizeof(*info));
+    MG_CUDA(cudaSetDevice(g->device));
+    g->prof.reset(g->stream, opt.profile != 0);
+    MG_CUDA(cudaEventRecord(g->ev0, g->stream));
+    return MG_OK;
+}
+
+mg_status end_run(mg_graph *g, const mg_opts &opt, mg_run_info *info)
+{
+    (void)opt;
+    MG_CUDA(cudaEventRecord(g->ev1, g->stream));
+    MG_CUDA(cudaEventSynchronize(g->ev1));
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return fail(MG_ERR_CUDA, "kernel error: %s", cudaGetErrorString(e));
+    if (info) {
+        float ms = 0.f;
+        MG_CUDA(cudaEventElapsedTime(&ms, g->ev0, g->ev1));
+        info->device_ms = ms;
+    }
+    return g->prof.collect(info);
+}
+
+}  // namespace mgi
+
+using namespace mgi;
+
+// ---------------------------------------------------------------------------
+// layout building (host side, O(n + m))
+// ---------------------------------------------------------------------------
+struct HostLayout {
+    std::vector<int32_t> trow, tcol, twt;  // transpose (empty when symmetric)
+    bool symmetric = true, wsym = true;
+    std::vector<int32_t> grp, hchunk, hrows, hrow_chunk;
+    int32_t n_dangling = 0, min_weight = 0;
+};
+
+static void build_layout(const mg_host_graph &h, HostLayout &L)
+{
+    const int32_t n = h.nv, m = h.ne;
+    // transpose by counting sort (rows come out with ascending columns)
+    std::vector<int32_t> tr(n + 1, 0), tc(m), tw(m);
+    for (int32_t i = 0; i < m; i++) tr[h.e[i] + 1]++;
+    for (int32_t i = 0; i < n; i++) tr[i + 1] += tr[i];
+    {
+        std::vector<int32_t> pos(tr.begin(), tr.end() - 1);
+        for (int32_t u = 0; u < n; u++)
+            for (int32_t p = h.v[u]; p < h.v[u + 1]; p++) {
+                int32_t q = pos[h.e[p]]++;
+                tc[q] = u;
+                tw[q] = h.ev[p];
+            }
+    }
+    L.symmetric = std::equal(tr.begin(), tr.end(), h.v.begin()) && std::equal(tc.begin(), tc.end(), h.e.begin());
+    L.wsym = L.symmetric && std::equal(tw.begin(), tw.end(), h.ev.begin());
+    if (!L.symmetric || !L.wsym) { L.trow.swap(tr); L.tcol.swap(tc); L.twt.swap(tw); }
+    const std::vector<int32_t> &prow = (!L.symmetric || !L.wsym) ? L.trow : h.v;
+    L.n_dangling = 0;
+    for (int32_t v = 0; v < n; v++) L.n_dangling += (h.v[v + 1] == h.v[v]);
+    L.min_weight = m ? *std::min_element(h.ev.begin(), h.ev.end()) : 0;
+    // heavy rows and chunks
+    L.hrow_chunk.push_back(0);
+    for (int32_t v = 0; v < n; v++) {
+        int32_t d = prow[v + 1] - prow[v];
+        if (d > HEAVY_DEG) {
+            L.hrows.push_back(v);
+            for (int32_t b = prow[v]; b < prow[v + 1]; b += HCHUNK) {
+                L.hchunk.push_back(v);
+                L.hchunk.push_back(b);
+                L.hchunk.push_back(std::min(prow[v + 1], b + HCHUNK));
+            }
+            L.hrow_chunk.push_back((int32_t)(L.hchunk.size() / 3));
+        }
+    }
+    // groups of <= GROUP_ROWS consecutive light rows with <= GROUP_EDGES
+    // edges (a single light row above the budget forms its own group); every
+    // heavy row is a one-row group that the light kernels skip
+    int32_t r = 0;
+    while (r < n) {
+        L.grp.push_back(r);
+        if (prow[r + 1] - prow[r] > HEAVY_DEG) { r++; continue; }
+        int32_t e = 0, k = 0;
+        while (r < n && k < mgd::GROUP_ROWS) {
+            int32_t d = prow[r + 1] - prow[r];
+            if (d > HEAVY_DEG) break;
+            if (k > 0 && e + d > GROUP_EDGES) break;
+            e += d; k++; r++;
+        }
+    }
+    L.grp.push_back(n);
+}
+
+static mg_status upload_arrays(mg_graph *g, const mg_host_graph *h, const HostLayout &L, bool alloc)
+{
+    const size_t n = (size_t)h->nv, m = (size_t)h->ne;
+    if (alloc) {
+        MG_TRY(dev_alloc(g->row, (n + 1) * 4));
+        MG_TRY(dev_alloc(g->col, std::max<size_t>(m, 4) * 4 + COL_PAD));
+        MG_TRY(dev_alloc(g->wt, std::max<size_t>(m, 4) * 4 + COL_PAD));
+        if (!L.trow.empty()) {
+            MG_TRY(dev_alloc(g->trow_own, (n + 1) * 4));
+            MG_TRY(dev_alloc(g->tcol_own, std::max<size_t>(m, 4) * 4 + COL_PAD));
+            MG_TRY(dev_alloc(g->twt_own, std::max<size_t>(m, 4) * 4 + COL_PAD));
+        }
+        MG_TRY(dev_alloc(g->grp, L.grp.size() * 4));
+        MG_TRY(dev_alloc(g->hchunk, std::max<size_t>(L.hchunk.size(), 3) * 4));
+        MG_TRY(dev_alloc(g->hrows, std::max<size_t>(L.hrows.size(), 1) * 4));
+        MG_TRY(dev_alloc(g->hrow_chunk, L.hrow_chunk.size() * 4));
+    }
+    cudaStream_t s = g->stream;
+    MG_CUDA(cudaMemcpyAsync(g->row.p, h->v.data(), (n + 1) * 4, cudaMemcpyHostToDevice, s));
+    if (m) {
+        MG_CUDA(cudaMemcpyAsync(g->col.p, h->e.data(), m * 4, cudaMemcpyHostToDevice, s));
+        MG_CUDA(cudaMemcpyAsync(g->wt.p, h->ev.data(), m * 4, cudaMemcpyHostToDevice, s));
+    }
+    if (!L.trow.empty()) {
+        MG_CUDA(cudaMemcpyAsync(g->trow_own.p, L.trow.data(), (n + 1) * 4, cudaMemcpyHostToDevice, s));
+        if (m) {
+            MG_CUDA(cudaMemcpyAsync(g->tcol_own.p, L.tcol.data(), m * 4, cudaMemcpyHostToDevice, s));
+            MG_CUDA(cudaMemcpyAsync(g->twt_own.p, L.twt.data(), m * 4, cudaMemcpyHostToDevice, s));
+        }
+        g->trow = g->trow_own.as<int32_t>(); g->tcol = g->tcol_own.as<int32_t>(); g->twt = g->twt_own.as<int32_t>();
+    } else {
+        g->trow = g->row.as<int32_t>(); g->tcol = g->col.as<int32_t>(); g->twt = g->wt.as<int32_t>();
+    }
+    MG_CUDA(cudaMemcpyAsync(g->grp.p, L.grp.data(), L.grp.size() * 4, cudaMemcpyHostToDevice, s));
+    if (!L.hchunk.empty())
+        MG_CUDA(cudaMemcpyAsync(g->hchunk.p, L.hchunk.data(), L.hchunk.size() * 4, cudaMemcpyHostToDevice, s));
+    if (!L.hrows.empty())
+        MG_CUDA(cudaMemcpyAsync(g->hrows.p, L.hrows.data(), L.hrows.size() * 4, cudaMemcpyHostToDevice, s));
+    MG_CUDA(cudaMemcpyAsync(g->hrow_chunk.p, L.hrow_chunk.data(), L.hrow_chunk.size() * 4, cudaMemcpyHostToDevice, s));
+    MG_CUDA(cudaStreamSynchronize(s));
+    g->ngroups = (int32_t)L.grp.size() - 1;
+    g->nhchunks = (int32_t)(L.hchunk.size() / 3);
+    g->nhrows = (int32_t)L.hrows.size();
+    g->heavy_deg = HEAVY_DEG;
+    g->symmetric = L.symmetric;
+    g->weights_symmetric = L.wsym;
+    g->n_dangling = L.n_dangling;
+    g->min_weight = L.min_weight;
+    return MG_OK;
+}
+
+static void destroy_graph(mg_graph *g)
+{
+    if (!g) return;
+    cudaSetDevice(g->device);
+    if (g->stream) cudaStreamSynchronize(g->stream);
+    free_frontier_ws(g);
+    free_pr_ws(g);
+    free_cc_ws(g);
+    free_bc_ws(g);
+    free_ppr_ws(g);
+    free_wpr_ws(g);
+    DevBuf *bufs[] = {&g->row, &g->col, &g->wt, &g->trow_own, &g->tcol_own, &g->twt_own, &g->grp,
+                      &g->hchunk, &g->hrows, &g->hrow_chunk, &g->fw, &g->ppr_hchunk, &g->ppr_hrows,
+                      &g->ppr_hrow_chunk};
+    for (DevBuf *b : bufs) dev_free(*b);
+    if (g->pinned_flag) cudaFreeHost(g->pinned_flag);
+    if (g->ev0) cudaEventDestroy(g->ev0);
+    if (g->ev1) cudaEventDestroy(g->ev1);
+    if (g->stream) cudaStreamDestroy(g->stream);
+    delete g;
+}
+
+extern "C" {
+
+void mg_opts_default(mg_opts *o)
+{
+    if (!o) return;
+    std::memset(o, 0, sizeof(*o));
+    o->exec = MG_EXEC_GRAPH;
+    o->direction = MG_DIR_AUTO;
+    o->max_iter = 0;
+    o->alpha = 15;
+    o->beta = 18;
+    o->damping = 0.85f;
+    o->tol = 1e-6f;
+    o->profile = 0;
+}
+
+mg_status mg_graph_upload(const mg_host_graph *h, int32_t device, mg_graph **out)
+{
+    clear_error();
+    if (!h || !out) return fail(MG_ERR_INVALID, "null argument");
+    *out = nullptr;
+    int ndev = 0;
+    cudaError_t e = cudaGetDeviceCount(&ndev);
+    if (e != cudaSuccess || ndev == 0) {
+        cudaGetLastError();
+        return fail(MG_ERR_CUDA, "no CUDA device available (%s)", cudaGetErrorString(e));
+    }
+    if (device < 0 || device >= ndev) return fail(MG_ERR_RANGE, "device %d out of range [0,%d)", device, ndev);
+    MG_CUDA(cudaSetDevice(device));
+    std::unique_ptr<mg_graph, void (*)(mg_graph *)> g(new mg_graph(), destroy_graph);
+    g->device = device;
+    g->nv = h->nv;
+    g->ne = h->ne;
+    MG_CUDA(cudaDeviceGetAttribute(&g->num_sms, cudaDevAttrMultiProcessorCount, device));
+    MG_CUDA(cudaStreamCreateWithFlags(&g->stream, cudaStreamNonBlocking));
+    MG_CUDA(cudaEventCreate(&g->ev0));
+    MG_CUDA(cudaEventCreate(&g->ev1));
+    MG_CUDA(cudaMallocHost(&g->pinned_flag, 64));
+    HostLayout L;
+    build_layout(*h, L);
+    MG_TRY(upload_arrays(g.get(), h, L, true));
+    *out = g.release();
+    return MG_OK;
+}
+
+mg_status mg_graph_reload(mg_graph *g, const mg_host_graph *h)
+{
+    clear_error();
+    if (!g || !h) return fail(MG_ERR_INVALID, "null argument");
+    if (h->nv != g->nv || h->ne != g->ne) return fail(MG_ERR_INVALID, "reload needs the same nv/ne");
+    MG_CUDA(cudaSetDevice(g->device));
+    // the index tables depend on the degrees only; the arrays are re-copied
+    const size_t n = (size_t)h->nv, m = (size_t)h->ne;
+    cudaStream_t s = g->stream;
+    MG_CUDA(cudaMemcpyAsync(g->row.p, h->v.data(), (n + 1) * 4, cudaMemcpyHostToDevice, s));
+    if (m) {
+        MG_CUDA(cudaMemcpyAsync(g->col.p, h->e.data(), m * 4, cudaMemcpyHostToDevice, s));
+        MG_CUDA(cudaMemcpyAsync(g->wt.p, h->ev.data(), m * 4, cudaMemcpyHostToDevice, s));
+    }
+    if (!(g->symmetric && g->weights_symmetric)) {
+        HostLayout L;
+        build_layout(*h, L);
+        MG_TRY(upload_arrays(g, h, L, false));
+    }
+    return MG_OK;
+}
+
+void mg_graph_free(mg_graph *g) { destroy_graph(g); }
+
+mg_status mg_graph_info(const mg_graph *g, int32_t *nv, int32_t *ne)
+{
+    if (!g) return fail(MG_ERR_INVALID, "null graph");
+    if (nv) *nv = g->nv;
+    if (ne) *ne = g->ne;
+    return MG_OK;
+}
+
+void *mg_graph_stream(mg_graph *g) { return g ? (void *)g->stream : nullptr; }
+
+mg_status mg_graph_set_float_weights(mg_graph *g, const float *w)
+{
+    clear_error();
+    if (!g || (!w && g->ne > 0)) return fail(MG_ERR_INVALID, "null argument");
+    MG_CUDA(cudaSetDevice(g->device));
+    MG_TRY(dev_alloc(g->fw, std::max<size_t>((size_t)g->ne, 4) * 4 + COL_PAD));
+    if (g->ne) MG_CUDA(cudaMemcpyAsync(g->fw.p, w, (size_t)g->ne * 4, cudaMemcpyHostToDevice, g->stream));
+    MG_CUDA(cudaStreamSynchronize(g->stream));
+    g->has_fw = true;
+    return MG_OK;
+}
+
+const void *mg_result_device(mg_graph *g, int32_t which)
+{
+    if (!g || which < 0 || which >= 8) return nullptr;
+    return g->res[which];
+}
+
+void mg_host_graph_free(mg_host_graph *h)
+{
+    if (!h) return;
+    if (h->pinned) {
+        if (!h->v.empty()) cudaHostUnregister(h->v.data());
+        if (!h->e.empty()) cudaHostUnregister(h->e.data());
+        if (!h->ev.empty()) cudaHostUnregister(h->ev.data());
+    }
+    delete h;
+}
+
+mg_status mg_host_graph_pin(mg_host_graph *h)
+{
+    clear_error();
+    if (!h) return fail(MG_ERR_INVALID, "null argument");
+    if (h->pinned) return MG_OK;
+    if (!h->v.empty()) MG_CUDA(cudaHostRegister(h->v.data(), h->v.size() * 4, cudaHostRegisterDefault));
+    if (!h->e.empty()) MG_CUDA(cudaHostRegister(h->e.data(), h->e.size() * 4, cudaHostRegisterDefault));
+    if (!h->ev.empty()) MG_CUDA(cudaHostRegister(h->ev.data(), h->ev.size() * 4, cudaHostRegisterDefault));
+    h->pinned = true;
+    return MG_OK;
+}
+
+}  // extern "C"

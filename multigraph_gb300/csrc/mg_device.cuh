@@ -1,0 +1,212 @@
+// mg_device.cuh -- device-side internals shared by the engine translation units.
+#pragma once
+
+#include "mg_internal.h"
+
+#include <cuda_runtime.h>
+
+#include "mg_group.cuh"
+
+#include <functional>
+#include <string>
+#include <vector>
+
+#define MG_CUDA(call)                                                                                 \
+    do {                                                                                              \
+        cudaError_t e_ = (call);                                                                      \
+        if (e_ != cudaSuccess)                                                                        \
+            return mgi::fail(MG_ERR_CUDA, "%s: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, \
+                             __LINE__);                                                               \
+    } while (0)
+
+#define MG_TRY(expr)                  \
+    do {                              \
+        mg_status s_ = (expr);        \
+        if (s_ != MG_OK) return s_;   \
+    } while (0)
+
+// "unreached" label value (common.h:37-39 of the reference)
+constexpr int32_t MG_UNSET = 0x64646464;
+
+namespace mgi {
+
+// ---------------------------------------------------------------------------
+// device buffers (allocation goes through the failure-injection counter)
+// ---------------------------------------------------------------------------
+struct DevBuf {
+    void *p = nullptr;
+    size_t bytes = 0;
+    template <class T> T *as() const { return reinterpret_cast<T *>(p); }
+};
+mg_status dev_alloc(DevBuf &b, size_t bytes);          // no-op when already >= bytes
+void dev_free(DevBuf &b);
+
+// ---------------------------------------------------------------------------
+// per-kernel profiling with cudaEvents (host-loop runs only)
+// ---------------------------------------------------------------------------
+struct Profiler {
+    bool on = false;
+    cudaStream_t stream = nullptr;
+    struct Slot { std::string name; int launches = 0; double ms = 0; };
+    std::vector<Slot> slots;
+    std::vector<std::pair<cudaEvent_t, cudaEvent_t>> pool;
+    struct Pending { int slot; size_t ev; };
+    std::vector<Pending> pending;
+    size_t used = 0;
+    void reset(cudaStream_t s, bool enable);
+    int slot(const char *name);
+    // bracket one launch: begin() before, end() after
+    void begin(int slot_id);
+    void end();
+    mg_status collect(mg_run_info *info);  // after the stream is synchronised
+    ~Profiler();
+private:
+    int open_slot = -1;
+};
+
+// ---------------------------------------------------------------------------
+// iteration loops: CUDA graph with a device-side WHILE node, or a host loop
+// ---------------------------------------------------------------------------
+// `body(stream, handle, use_cond)` enqueues one iteration; its last kernel
+// must set the loop condition with cudaGraphSetConditional when use_cond is
+// set, and always write the continue flag to *more_dev.
+using BodyFn = std::function<mg_status(cudaStream_t, cudaGraphConditionalHandle, int)>;
+
+struct LoopGraph {
+    cudaGraphExec_t exec = nullptr;
+    cudaGraph_t graph = nullptr;
+    uint64_t key = 0;
+    void destroy();
+};
+
+mg_status run_loop(int exec_mode, bool profile, cudaStream_t stream, LoopGraph &lg, uint64_t key,
+                   const BodyFn &body, const int32_t *more_dev, int32_t *more_host, int max_host_iters);
+
+}  // namespace mgi
+
+// ---------------------------------------------------------------------------
+// algorithm workspaces (defined in their translation units)
+// ---------------------------------------------------------------------------
+struct FrontierWS;
+struct PrWS;
+struct CcWS;
+struct BcWS;
+struct PprWS;
+struct WprWS;
+
+struct mg_graph {
+    int device = 0;
+    int num_sms = 0;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    int32_t nv = 0, ne = 0;
+    bool symmetric = true;         // transpose == graph (pull uses the same arrays)
+    bool weights_symmetric = true; // weight of (u,v) == weight of (v,u)
+    // CSR (push side, out-edges)
+    mgi::DevBuf row, col, wt;
+    // transpose (pull side, in-edges); aliases row/col/wt when symmetric
+    mgi::DevBuf trow_own, tcol_own, twt_own;
+    const int32_t *trow = nullptr, *tcol = nullptr, *twt = nullptr;
+    // edge-balanced groups of <= 32 consecutive pull rows (light rows only)
+    mgi::DevBuf grp;               // int32 [ngroups+1] first row of each group
+    int32_t ngroups = 0;
+    // heavy pull rows split into chunks: (row, begin, end) triplets
+    mgi::DevBuf hchunk;            // int32 [3*nhchunks]
+    int32_t nhchunks = 0;
+    mgi::DevBuf hrows;             // int32 [nhrows] heavy row ids
+    mgi::DevBuf hrow_chunk;        // int32 [nhrows+1] first chunk of each heavy row
+    int32_t nhrows = 0;
+    int32_t heavy_deg = 0;         // rows with in-degree > heavy_deg are heavy
+    int32_t n_dangling = 0;        // vertices with out-degree 0
+    int32_t min_weight = 0;        // smallest integer edge weight
+    // PPR heavy rows: rows with in-degree > PPR_HEAVY split in PPR_CHUNK pieces
+    mgi::DevBuf ppr_hchunk, ppr_hrows, ppr_hrow_chunk;
+    int32_t ppr_nhchunks = -1, ppr_nhrows = 0;
+    // float edge weights for weighted PageRank (CSR order)
+    mgi::DevBuf fw;
+    bool has_fw = false;
+    // per-algorithm workspaces
+    FrontierWS *fws = nullptr;
+    PrWS *pws = nullptr;
+    CcWS *cws = nullptr;
+    BcWS *bws = nullptr;
+    PprWS *ppws = nullptr;
+    WprWS *wpws = nullptr;
+    mgi::Profiler prof;
+    int32_t *pinned_flag = nullptr; // pinned host word for host-loop readbacks
+    // result pointers for mg_result_device
+    const void *res[8] = {nullptr};
+};
+
+namespace mgi {
+void free_frontier_ws(mg_graph *g);
+void free_pr_ws(mg_graph *g);
+void free_cc_ws(mg_graph *g);
+void free_bc_ws(mg_graph *g);
+void free_ppr_ws(mg_graph *g);
+void free_wpr_ws(mg_graph *g);
+mg_status begin_run(mg_graph *g, const mg_opts *o, mg_opts &opt, mg_run_info *info);
+mg_status end_run(mg_graph *g, const mg_opts &opt, mg_run_info *info);
+mg_status copy_out(mg_graph *g, void *host, const void *dev, size_t bytes);
+int launch_grid(const mg_graph *g, int threads, int per_sm);
+}  // namespace mgi
+
+// ---------------------------------------------------------------------------
+// device helpers
+// ---------------------------------------------------------------------------
+namespace mgd {
+
+__device__ __forceinline__ int lane() { return threadIdx.x & 31; }
+
+// warp-aggregated append: returns this lane's slot in the queue at *ctr
+__device__ __forceinline__ int warp_append(int *ctr, bool pred)
+{
+    unsigned m = __ballot_sync(__activemask(), pred);
+    if (!pred) return -1;
+    int leader = __ffs(m) - 1;
+    int base = 0;
+    if (lane() == leader) base = atomicAdd(ctr, __popc(m));
+    base = __shfl_sync(m, base, leader);
+    return base + __popc(m & ((1u << lane()) - 1u));
+}
+
+// inclusive warp scan
+__device__ __forceinline__ int warp_scan_incl(int v)
+{
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        int t = __shfl_up_sync(0xffffffffu, v, o);
+        if (lane() >= o) v += t;
+    }
+    return v;
+}
+
+// lane whose exclusive offset range [off, off+deg) contains k, given the
+// exclusive offsets held one per lane (monotone).  Binary search by shuffles.
+__device__ __forceinline__ int owner_lane(int excl_off, int k)
+{
+    int lo = 0;
+#pragma unroll
+    for (int step = 16; step > 0; step >>= 1) {
+        int probe = __shfl_sync(0xffffffffu, excl_off, lo + step);
+        if (probe <= k) lo += step;
+    }
+    return lo;
+}
+
+// Per-warp staging of newly reached vertices: lanes push with a shared
+// atomic, then the warp reserves one global slice and copies.
+struct WarpStage {
+    int32_t *buf;   // >= GROUP_ROWS entries
+    int32_t *cnt;   // shared counter
+    __device__ __forceinline__ void push(int32_t v) { buf[atomicAdd(cnt, 1)] = v; }
+};
+
+__device__ __forceinline__ bool bm_test(const uint32_t *bm, int v) { return (bm[v >> 5] >> (v & 31)) & 1u; }
+__device__ __forceinline__ bool bm_set(uint32_t *bm, int v)  // returns true if this call set it
+{
+    uint32_t bit = 1u << (v & 31);
+    return (atomicOr(&bm[v >> 5], bit) & bit) == 0;
+}
+
+}  // namespace mgd

@@ -1,0 +1,911 @@
+// mg_frontier.cu -- hybrid push/pull frontier engine for BFS, SSSP and the
+// BC forward sweep; the BC backward sweep; multi-source BC.
+//
+// Replaces MultiGraph_V_E_V (process.cu:1079-1368) with its kernels
+// process_f1 / make_frontier / phase1 / phase11 / phase2 and the sampling
+// heuristic, and MultiGraph_V_E_V_pull (process2.cu:263-325).
+//
+// One iteration is three launches, all with a fixed persistent grid so the
+// loop can live inside a CUDA graph with a device-side WHILE node:
+//   k_push   frontier queue -> neighbours (warp load-balanced search over the
+//            degrees of 32 queue entries; vertices above PUSH_HEAVY split over
+//            the whole grid), claims / relaxes destinations with the
+//            operator hooks, appends the next queue with warp-aggregated
+//            atomics and sets the next-frontier bitmap;
+//   k_pull   (when the frontier is dense) every unvisited vertex scans its
+//            in-edges against the frontier bitmap (BFS stops at the first
+//            parent; SSSP/BC reduce over all in-edges), light rows in
+//            edge-balanced warp groups, heavy rows in 2048-edge chunks;
+//   k_decide 1 warp: next size, direction switch (frontier edges against
+//            unvisited edges, Beamer), iteration cap, loop condition.
+// Only one of k_push / k_pull does work in an iteration; the other returns
+// at once.  Frontier bitmaps are triple-buffered: the active kernel clears
+// the buffer the next iteration will write.
+
+#include "mg_device.cuh"
+#include "mg_ops.cuh"
+
+#include <algorithm>
+#include <cstring>
+
+namespace {
+
+constexpr int ALG_BFS = 0, ALG_SSSP = 1, ALG_BC = 2;
+constexpr int MODE_PUSH = 0, MODE_PULL = 1;
+constexpr int32_t PUSH_HEAVY = 4096;
+constexpr int THREADS = 256;
+
+struct FCtl {
+    int32_t more;       // continue flag (host loop readback)
+    int32_t iter;       // level / round being expanded
+    int32_t mode;       // MODE_PUSH / MODE_PULL
+    int32_t cur;        // current bitmap buffer 0..2
+    int32_t qoff, qsize;  // current queue slice
+    int32_t nqoff, nq;    // next queue slice (nq: atomic counter)
+    int32_t hcur, nhcur;  // heavy list sizes: current / next (atomic)
+    int32_t hpar;         // heavy list parity
+    int32_t status;       // 0 ok, 1 iteration cap
+    int32_t pull_iters;
+    int32_t max_iter;
+    int32_t dirmode;      // MG_DIR_*
+    int32_t alpha, beta;
+    int32_t nlevels;      // BC: levels archived
+    int32_t archive;      // 1: queue slices are appended (BFS/BC), 0: ping-pong (SSSP)
+    int32_t pad0;
+    long long nf_edges;      // out-edges of the next frontier (atomic)
+    long long visited_edges; // out-edges of every vertex visited so far
+    long long scanned;       // edges scanned (statistics, atomic)
+};
+
+struct Args {
+    int32_t n;
+    int32_t m;
+    const int32_t *row, *col, *wt;     // push side
+    const int32_t *trow, *tcol, *twt;  // pull side
+    const int32_t *grp;
+    int32_t ngroups;
+    const int32_t *hchunk;
+    int32_t nhchunks;
+    int32_t heavy_deg;
+    int32_t *label;
+    double *sigma;
+    uint32_t *bm;        // 3 * words
+    uint32_t *visited;
+    int32_t words;
+    int32_t *queue;
+    int32_t *heavy;      // 2 * n (parity)
+    int32_t *stamp;
+    int32_t *lvl_off;
+    FCtl *ctl;
+};
+
+__device__ __forceinline__ uint32_t *bm_buf(const Args &a, int idx) { return a.bm + (size_t)idx * a.words; }
+
+// warp-wide: add v (64-bit) from every lane to *dst with one atomic
+__device__ __forceinline__ void warp_add64(long long *dst, long long v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if (mgd::lane() == 0 && v) atomicAdd((unsigned long long *)dst, (unsigned long long)v);
+}
+
+// record a newly reached vertex in the next frontier (all lanes call)
+__device__ __forceinline__ void emit_next(const Args &a, const FCtl &c, int nextbuf, bool found, int32_t v)
+{
+    int slot = mgd::warp_append(&a.ctl->nq, found);
+    long long d = 0;
+    if (found) {
+        a.queue[c.nqoff + slot] = v;
+        mgd::bm_set(bm_buf(a, nextbuf), v);
+        int32_t dg = a.row[v + 1] - a.row[v];
+        d = dg;
+        if (dg > PUSH_HEAVY) {
+            int h = atomicAdd(&a.ctl->nhcur, 1);
+            a.heavy[(size_t)(c.hpar ^ 1) * a.n + h] = v;
+        }
+    }
+    warp_add64(&a.ctl->nf_edges, d);
+}
+
+// ----------------------------------------------------------------------------
+// push: one edge (u -> v) with the source's payload
+// ----------------------------------------------------------------------------
+template <int ALG>
+__device__ __forceinline__ bool push_edge(const Args &a, int it1, int32_t v, int32_t payload_i, double payload_d,
+                                          int32_t w)
+{
+    if (ALG == ALG_BFS) {
+        if (mgd::bm_test(a.visited, v)) return false;
+        if (!mgd::bm_set(a.visited, v)) return false;
+        a.label[v] = mgops::Bfs::get_partial_result(it1 - 1, 0);
+        return true;
+    } else if (ALG == ALG_SSSP) {
+        int32_t nd = mgops::Sssp::get_partial_result(payload_i, w);
+        return mgops::Sssp::fused_update_condition(&a.label[v], nd, it1, &a.stamp[v]);
+    } else {
+        bool on_level;
+        bool claimed = mgops::BcForward::fused_update_condition(&a.label[v], it1, on_level);
+        if (on_level) mgops::BcForward::accumulate(&a.sigma[v], payload_d);
+        if (claimed) mgd::bm_set(a.visited, v);
+        return claimed;
+    }
+}
+
+template <int ALG>
+__global__ void __launch_bounds__(THREADS) k_push(Args a)
+{
+    const FCtl c = *a.ctl;
+    if (c.mode != MODE_PUSH || c.more == 0) return;
+    const int it1 = c.iter + 1;
+    const int nextbuf = (c.cur + 1) % 3, sparebuf = (c.cur + 2) % 3;
+    // clear the buffer the next iteration writes
+    {
+        uint32_t *sp = bm_buf(a, sparebuf);
+        for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.words; i += gridDim.x * blockDim.x) sp[i] = 0;
+    }
+    const int lane = mgd::lane();
+    const int gwarp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int nwarps = (gridDim.x * blockDim.x) >> 5;
+    long long scanned = 0;
+    // heavy frontier vertices: every thread of the grid strides over their edges
+    for (int h = 0; h < c.hcur; h++) {
+        int32_t u = a.heavy[(size_t)c.hpar * a.n + h];
+        int32_t b = a.row[u], e = a.row[u + 1];
+        int32_t pi = a.label[u];
+        double pd = (ALG == ALG_BC) ? a.sigma[u] : 0.0;
+        int32_t span = e - b;
+        int32_t rounds = (span + gridDim.x * blockDim.x - 1) / (gridDim.x * blockDim.x);
+        for (int r = 0; r < rounds; r++) {
+            int32_t k = b + r * gridDim.x * blockDim.x + blockIdx.x * blockDim.x + threadIdx.x;
+            bool found = false;
+            int32_t v = 0;
+            if (k < e) {
+                v = a.col[k];
+                found = push_edge<ALG>(a, it1, v, pi, pd, (ALG == ALG_SSSP) ? a.wt[k] : 0);
+            }
+            emit_next(a, c, nextbuf, found, v);
+        }
+        scanned += (threadIdx.x == 0 && blockIdx.x == 0) ? span : 0;
+    }
+    // light frontier vertices: 32 per warp, load-balanced over their edges
+    for (int base = gwarp * 32; base < c.qsize; base += nwarps * 32) {
+        int32_t u = -1, start = 0, deg = 0, pi = 0;
+        double pd = 0.0;
+        if (base + lane < c.qsize) {
+            u = a.queue[c.qoff + base + lane];
+            start = a.row[u];
+            deg = a.row[u + 1] - start;
+            if (deg > PUSH_HEAVY) deg = 0;
+            pi = a.label[u];
+            if (ALG == ALG_BC) pd = a.sigma[u];
+        }
+        int incl = mgd::warp_scan_incl(deg);
+        int excl = incl - deg;
+        int total = __shfl_sync(0xffffffffu, incl, 31);
+        scanned += (lane == 0) ? total : 0;
+        for (int k0 = 0; k0 < total; k0 += 32) {
+            int k = k0 + lane;
+            int kk = k < total ? k : total - 1;
+            int own = mgd::owner_lane(excl, kk);
+            int32_t e = __shfl_sync(0xffffffffu, start, own) + (kk - __shfl_sync(0xffffffffu, excl, own));
+            int32_t opi = __shfl_sync(0xffffffffu, pi, own);
+            double opd = __shfl_sync(0xffffffffu, pd, own);
+            bool found = false;
+            int32_t v = 0;
+            if (k < total) {
+                v = a.col[e];
+                found = push_edge<ALG>(a, it1, v, opi, opd, (ALG == ALG_SSSP) ? a.wt[e] : 0);
+            }
+            emit_next(a, c, nextbuf, found, v);
+        }
+    }
+    if (lane == 0 && scanned) atomicAdd((unsigned long long *)&a.ctl->scanned, (unsigned long long)scanned);
+}
+
+// ----------------------------------------------------------------------------
+// pull: row reductions over in-edges against the frontier bitmap
+// ----------------------------------------------------------------------------
+template <int ALG>
+struct PullOp;
+
+// SSSP: min over frontier in-neighbours of dist[u] + w (accumulate_nonAtomics
+// in row order), then one atomicMin + stamp on the row (fused_update_condition)
+template <>
+struct PullOp<ALG_SSSP> {
+    using T = int32_t;
+    static constexpr bool kRowAware = false;
+    static constexpr bool kWeights = true;
+    const Args &a;
+    const uint32_t *fb;
+    int it1;
+    mgd::WarpStage st;
+    int pad;
+    __device__ T identity() const { return mgops::Sssp::initialize(); }
+    __device__ bool skip(int32_t) const { return false; }
+    __device__ T edge(int32_t, int32_t, int32_t u, int32_t w) const
+    {
+        return mgd::bm_test(fb, u) ? mgops::Sssp::get_partial_result(a.label[u], w) : mgops::UNSET;
+    }
+    __device__ T combine(T x, T y) const
+    {
+        mgops::Sssp::accumulate_nonAtomics(x, y, 0);
+        return x;
+    }
+    __device__ void finish(int32_t v, T best)
+    {
+        if (mgops::Sssp::fused_update_condition(&a.label[v], best, it1, &a.stamp[v])) st.push(v);
+    }
+};
+
+// BC forward: unvisited rows sum the path counts of frontier in-neighbours
+template <>
+struct PullOp<ALG_BC> {
+    using T = double;
+    static constexpr bool kRowAware = true;  // visited rows are skipped
+    static constexpr bool kWeights = false;
+    const Args &a;
+    const uint32_t *fb;
+    int it1;
+    mgd::WarpStage st;
+    int pad;
+    __device__ T identity() const { return 0.0; }
+    __device__ bool skip(int32_t v) const { return mgd::bm_test(a.visited, v); }
+    __device__ T edge(int32_t, int32_t, int32_t u, int32_t) const { return mgd::bm_test(fb, u) ? a.sigma[u] : 0.0; }
+    __device__ T combine(T x, T y) const
+    {
+        mgops::BcForward::accumulate_nonAtomics(x, y);
+        return x;
+    }
+    __device__ void finish(int32_t v, T s)
+    {
+        if (s > 0.0) {
+            a.label[v] = it1;
+            a.sigma[v] = s;
+            mgd::bm_set(a.visited, v);
+            st.push(v);
+        }
+    }
+};
+
+template <int ALG>
+__global__ void __launch_bounds__(THREADS) k_pull(Args a)
+{
+    const FCtl c = *a.ctl;
+    if (c.mode != MODE_PULL || c.more == 0) return;
+    const int it1 = c.iter + 1;
+    const int nextbuf = (c.cur + 1) % 3, sparebuf = (c.cur + 2) % 3;
+    const uint32_t *fb = bm_buf(a, c.cur);
+    {
+        uint32_t *sp = bm_buf(a, sparebuf);
+        for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.words; i += gridDim.x * blockDim.x) sp[i] = 0;
+    }
+    const int lane = mgd::lane();
+    const int gwarp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int nwarps = (gridDim.x * blockDim.x) >> 5;
+    long long scanned = 0;
+
+    if constexpr (ALG == ALG_BFS) {
+        // bottom-up: a thread per unvisited light row, first frontier parent wins
+        const int32_t stride = gridDim.x * blockDim.x;
+        const int32_t nround = (a.n + stride - 1) / stride;
+        for (int32_t r = 0; r < nround; r++) {
+            int32_t v = r * stride + blockIdx.x * blockDim.x + threadIdx.x;
+            bool found = false;
+            if (v < a.n && !mgd::bm_test(a.visited, v)) {
+                int32_t b = a.trow[v], e = a.trow[v + 1];
+                if (e - b <= a.heavy_deg) {
+                    for (int32_t p = b; p < e; p++) {
+                        scanned++;
+                        if (mgd::bm_test(fb, a.tcol[p])) { found = true; break; }
+                    }
+                    if (found) {
+                        a.label[v] = it1;
+                        mgd::bm_set(a.visited, v);
+                    }
+                }
+            }
+            emit_next(a, c, nextbuf, found, v);
+        }
+    } else {
+        // edge-balanced row groups, one warp each; reached rows are staged
+        // per warp and appended with one reservation per group
+        constexpr bool W = PullOp<ALG>::kWeights;
+        __shared__ int32_t s_off[THREADS / 32][mgd::GROUP_ROWS + 1];
+        __shared__ __align__(16) int32_t s_col[THREADS / 32][mgd::GROUP_STAGE];
+        __shared__ __align__(16) int32_t s_wt[W ? THREADS / 32 : 1][W ? mgd::GROUP_STAGE : 4];
+        __shared__ int32_t s_stage[THREADS / 32][mgd::GROUP_ROWS];
+        __shared__ int32_t s_cnt[THREADS / 32];
+        const int wib = threadIdx.x >> 5;
+        PullOp<ALG> op{a, fb, it1, {s_stage[wib], &s_cnt[wib]}, 0};
+        const mgd::GroupSmem sm{s_off[wib], s_col[wib], W ? s_wt[wib] : nullptr};
+        for (int32_t g = gwarp; g < a.ngroups; g += nwarps) {
+            int32_t r0 = a.grp[g], r1 = a.grp[g + 1];
+            if (r1 - r0 == 1 && a.trow[r1] - a.trow[r0] > a.heavy_deg) continue;  // heavy row: chunks below
+            if (lane == 0) s_cnt[wib] = 0;
+            __syncwarp();
+            mgd::group_reduce(op, a.trow, a.tcol, a.twt, r0, r1, sm);
+            int cnt = s_cnt[wib];
+            int base = 0;
+            if (lane == 0 && cnt) base = atomicAdd(&a.ctl->nq, cnt);
+            base = __shfl_sync(0xffffffffu, base, 0);
+            long long dsum = 0;
+            for (int i = lane; i < cnt; i += 32) {
+                int32_t v = s_stage[wib][i];
+                a.queue[c.nqoff + base + i] = v;
+                mgd::bm_set(bm_buf(a, nextbuf), v);
+                int32_t dg = a.row[v + 1] - a.row[v];
+                dsum += dg;
+                if (dg > PUSH_HEAVY) a.heavy[(size_t)(c.hpar ^ 1) * a.n + atomicAdd(&a.ctl->nhcur, 1)] = v;
+            }
+            warp_add64(&a.ctl->nf_edges, dsum);
+            scanned += (lane == 0) ? (a.trow[r1] - a.trow[r0]) : 0;
+            __syncwarp();
+        }
+    }
+
+    // heavy rows: one CTA per 2048-edge chunk
+    __shared__ int32_t s_min[THREADS / 32];
+    __shared__ double s_sum[THREADS / 32];
+    __shared__ int s_hit, s_skip;
+    for (int32_t ch = blockIdx.x; ch < a.nhchunks; ch += gridDim.x) {
+        int32_t v = a.hchunk[3 * ch], b = a.hchunk[3 * ch + 1], e = a.hchunk[3 * ch + 2];
+        // thread 0 decides for the block (the row may be claimed concurrently
+        // by another chunk, so a per-thread test could diverge)
+        if (threadIdx.x == 0)
+            s_skip = (ALG != ALG_SSSP) && mgd::bm_test(a.visited, v) && a.label[v] != it1;
+        __syncthreads();
+        const bool skip = s_skip;
+        __syncthreads();
+        if (skip) continue;
+        int32_t best = mgops::UNSET;
+        double ssum = 0.0;
+        int hit = 0;
+        for (int32_t p = b + threadIdx.x; p < e; p += blockDim.x) {
+            int32_t u = a.tcol[p];
+            if (mgd::bm_test(fb, u)) {
+                hit = 1;
+                if (ALG == ALG_SSSP) mgops::Sssp::accumulate_nonAtomics(best, mgops::Sssp::get_partial_result(a.label[u], a.twt[p]), 0);
+                if (ALG == ALG_BC) ssum += a.sigma[u];
+            }
+        }
+        if (threadIdx.x == 0) s_hit = 0;
+        __syncthreads();
+        if (hit) s_hit = 1;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            best = min(best, __shfl_xor_sync(0xffffffffu, best, o));
+            ssum += __shfl_xor_sync(0xffffffffu, ssum, o);
+        }
+        if (lane == 0) { s_min[threadIdx.x >> 5] = best; s_sum[threadIdx.x >> 5] = ssum; }
+        __syncthreads();
+        bool found = false;
+        if (threadIdx.x == 0) {
+            int32_t bm = mgops::UNSET;
+            double bs = 0.0;
+            for (int w = 0; w < THREADS / 32; w++) { bm = min(bm, s_min[w]); bs += s_sum[w]; }
+            if (s_hit) {
+                if (ALG == ALG_BFS) {
+                    if (atomicCAS(&a.label[v], mgops::UNSET, it1) == mgops::UNSET) { mgd::bm_set(a.visited, v); found = true; }
+                } else if (ALG == ALG_SSSP) {
+                    int32_t old = atomicMin(&a.label[v], bm);
+                    if (bm < old && atomicMax(&a.stamp[v], it1) < it1) found = true;
+                } else {
+                    bool on_level;
+                    found = mgops::BcForward::fused_update_condition(&a.label[v], it1, on_level);
+                    if (on_level) mgops::BcForward::accumulate(&a.sigma[v], bs);
+                    if (found) mgd::bm_set(a.visited, v);
+                }
+            }
+            scanned += e - b;
+        }
+        __syncthreads();
+        if (threadIdx.x < 32) emit_next(a, c, nextbuf, found && threadIdx.x == 0, v);
+        __syncthreads();
+    }
+    warp_add64(&a.ctl->scanned, scanned);
+}
+
+// ----------------------------------------------------------------------------
+// decide: 1 thread
+// ----------------------------------------------------------------------------
+__global__ void k_decide(Args a, cudaGraphConditionalHandle h, int use_cond)
+{
+    FCtl *c = a.ctl;
+    if (threadIdx.x != 0) return;
+    int more = c->more;
+    if (more) {
+        int32_t nq = c->nq;
+        if (c->mode == MODE_PULL) c->pull_iters++;
+        c->iter += 1;
+        if (c->archive && c->iter + 1 < a.n + 3) {
+            a.lvl_off[c->iter + 1] = c->nqoff + nq;
+            if (nq > 0) c->nlevels = c->iter + 1;
+        }
+        c->qoff = c->nqoff;
+        c->qsize = nq;
+        c->nqoff = c->archive ? (c->qoff + nq) : (c->qoff == 0 ? a.n : 0);
+        c->nq = 0;
+        c->hcur = c->nhcur;
+        c->nhcur = 0;
+        c->hpar ^= 1;
+        c->cur = (c->cur + 1) % 3;
+        long long nfe = c->nf_edges;
+        c->visited_edges += nfe;
+        c->nf_edges = 0;
+        if (nq == 0) {
+            more = 0;
+        } else {
+            if (c->dirmode == MG_DIR_PUSH) c->mode = MODE_PUSH;
+            else if (c->dirmode == MG_DIR_PULL) c->mode = MODE_PULL;
+            else if (c->archive) {
+                // Beamer: push -> pull when frontier edges exceed unvisited
+                // edges / alpha; pull -> push when the frontier is below n / beta
+                long long unvisited = (long long)a.m - c->visited_edges;
+                if (c->mode == MODE_PUSH) {
+                    if (nfe * (long long)c->alpha > unvisited && nq > 64) c->mode = MODE_PULL;
+                } else {
+                    if ((long long)nq * c->beta < a.n) c->mode = MODE_PUSH;
+                }
+            } else {
+                // SSSP: pull when the frontier's edges are a large share of m
+                c->mode = (nfe * (long long)c->alpha > (long long)a.m) ? MODE_PULL : MODE_PUSH;
+            }
+            if (c->iter >= c->max_iter) { c->status = 1; more = 0; }
+        }
+        c->more = more;
+    }
+    if (use_cond) cudaGraphSetConditional(h, more ? 1u : 0u);
+}
+
+// ----------------------------------------------------------------------------
+// init: source
+// ----------------------------------------------------------------------------
+// sources: srcs[0..nsrc) when srcs is non-null, else the single `src`
+// (several sources = one traversal of a disjoint union of graphs)
+template <int ALG>
+__global__ void k_init(Args a, int32_t src, const int32_t *srcs, int32_t nsrc, int dirmode, int alpha, int beta,
+                       int max_iter)
+{
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    FCtl *c = a.ctl;
+    std::memset(c, 0, sizeof(FCtl));
+    c->more = 1;
+    c->archive = (ALG != ALG_SSSP);
+    c->max_iter = max_iter;
+    c->dirmode = dirmode;
+    c->alpha = alpha;
+    c->beta = beta;
+    c->mode = (dirmode == MG_DIR_PULL) ? MODE_PULL : MODE_PUSH;
+    int32_t q = 0;
+    long long ve = 0;
+    for (int32_t i = 0; i < (srcs ? nsrc : 1); i++) {
+        int32_t s = srcs ? srcs[i] : src;
+        if (!mgd::bm_set(a.visited, s)) continue;  // duplicate source
+        a.label[s] = 0;
+        if (ALG == ALG_BC) a.sigma[s] = 1.0;
+        if (ALG == ALG_SSSP) a.stamp[s] = 0;
+        mgd::bm_set(a.bm, s);  // buffer 0 is the current frontier
+        a.queue[q++] = s;
+        int32_t d = a.row[s + 1] - a.row[s];
+        ve += d;
+        if (d > PUSH_HEAVY) a.heavy[c->hcur++] = s;
+    }
+    c->qoff = 0;
+    c->qsize = q;
+    c->nqoff = (ALG == ALG_SSSP) ? a.n : q;
+    c->visited_edges = ve;
+    if (ALG != ALG_SSSP) { a.lvl_off[0] = 0; a.lvl_off[1] = q; c->nlevels = 1; }
+}
+
+// ----------------------------------------------------------------------------
+// BC backward: delta[v] = sigma[v] * sum_{w succ, level[w] = L} q[w],
+// q[w] = (1 + delta[w]) / sigma[w]  (bc_phase1/2 of process2.cu:135-261 and
+// process_fbc :5-132 in one pull form over the archived level lists)
+// ----------------------------------------------------------------------------
+struct BCtl {
+    int32_t more;
+    int32_t L;       // level whose predecessors are being finalised
+    int32_t nheavy;
+    int32_t src;     // source of this sweep (excluded from the BC sum)
+};
+
+__global__ void k_bc_q_init(int32_t n, const double *sigma, const int32_t *label, float *q, float *delta)
+{
+    for (int32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x) {
+        delta[v] = 0.0f;
+        q[v] = (label[v] != mgops::UNSET && sigma[v] > 0.0) ? (float)(1.0 / sigma[v]) : 0.0f;
+    }
+}
+
+__device__ __forceinline__ void bc_finish_vertex(int32_t v, float s, const double *sigma, float *delta, float *q,
+                                                 float *bc, int32_t src)
+{
+    float dv = (float)(sigma[v] * (double)s);
+    delta[v] = dv;
+    q[v] = (float)((1.0 + (double)dv) / sigma[v]);
+    if (bc && v != src) bc[v] += dv;
+}
+
+__global__ void __launch_bounds__(THREADS) k_bc_back(Args a, BCtl *bc_ctl, float *q, float *delta, float *bcacc,
+                                                     int32_t *heavy_list)
+{
+    const BCtl bctl = *bc_ctl;
+    if (bctl.more == 0) return;
+    const int32_t L = bctl.L, src = bctl.src;
+    const int32_t b0 = a.lvl_off[L - 1], b1 = a.lvl_off[L];
+    const int lane = mgd::lane();
+    const int gwarp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int nwarps = (gridDim.x * blockDim.x) >> 5;
+    for (int base = b0 + gwarp * 32; base < b1; base += nwarps * 32) {
+        int32_t v = -1, start = 0, deg = 0;
+        if (base + lane < b1) {
+            v = a.queue[base + lane];
+            start = a.row[v];
+            deg = a.row[v + 1] - start;
+            if (deg > PUSH_HEAVY) {
+                int h = atomicAdd(&bc_ctl->nheavy, 1);
+                heavy_list[h] = v;
+                deg = 0;
+                v = -1;
+            }
+        }
+        int incl = mgd::warp_scan_incl(deg);
+        int excl = incl - deg;
+        int total = __shfl_sync(0xffffffffu, incl, 31);
+        float acc = 0.0f;
+        for (int k0 = 0; k0 < total; k0 += 32) {
+            int k = k0 + lane;
+            int kk = k < total ? k : total - 1;
+            int own = mgd::owner_lane(excl, kk);
+            int32_t e = __shfl_sync(0xffffffffu, start, own) + (kk - __shfl_sync(0xffffffffu, excl, own));
+            float t = 0.0f;
+            if (k < total) {
+                int32_t w = a.col[e];
+                if (a.label[w] == L) t = q[w];
+            } else {
+                own = -1;
+            }
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                int oo = __shfl_down_sync(0xffffffffu, own, o);
+                float ot = __shfl_down_sync(0xffffffffu, t, o);
+                if (lane + o < 32 && oo == own) t += ot;
+            }
+            int prev_own = __shfl_up_sync(0xffffffffu, own, 1);
+            bool head = (own >= 0) && (lane == 0 || prev_own != own);
+            unsigned heads = __ballot_sync(0xffffffffu, head);
+            while (heads) {
+                int hl = __ffs(heads) - 1;
+                heads &= heads - 1;
+                int ho = __shfl_sync(0xffffffffu, own, hl);
+                float ht = __shfl_sync(0xffffffffu, t, hl);
+                if (lane == ho) acc += ht;
+            }
+        }
+        if (v >= 0) bc_finish_vertex(v, acc, a.sigma, delta, q, bcacc, src);
+    }
+}
+
+__global__ void __launch_bounds__(THREADS) k_bc_back_heavy(Args a, BCtl *bc_ctl, float *q, float *delta,
+                                                           float *bcacc, const int32_t *heavy_list)
+{
+    const BCtl bctl = *bc_ctl;
+    if (bctl.more == 0) return;
+    const int32_t L = bctl.L, src = bctl.src;
+    __shared__ float s_part[THREADS / 32];
+    for (int32_t h = blockIdx.x; h < bctl.nheavy; h += gridDim.x) {
+        int32_t v = heavy_list[h];
+        int32_t b = a.row[v], e = a.row[v + 1];
+        float acc = 0.0f;
+        for (int32_t p = b + threadIdx.x; p < e; p += blockDim.x) {
+            int32_t w = a.col[p];
+            if (a.label[w] == L) acc += q[w];
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+        if ((threadIdx.x & 31) == 0) s_part[threadIdx.x >> 5] = acc;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            float s = 0.0f;
+            for (int w = 0; w < THREADS / 32; w++) s += s_part[w];
+            bc_finish_vertex(v, s, a.sigma, delta, q, bcacc, src);
+        }
+        __syncthreads();
+    }
+}
+
+__global__ void k_bc_back_decide(BCtl *bc_ctl, cudaGraphConditionalHandle h, int use_cond)
+{
+    if (threadIdx.x != 0) return;
+    int more = bc_ctl->more;
+    if (more) {
+        bc_ctl->L -= 1;
+        bc_ctl->nheavy = 0;
+        if (bc_ctl->L < 1) more = 0;
+        bc_ctl->more = more;
+    }
+    if (use_cond) cudaGraphSetConditional(h, more ? 1u : 0u);
+}
+
+__global__ void k_bc_back_init(const FCtl *fc, BCtl *bc_ctl, int32_t src)
+{
+    if (threadIdx.x != 0) return;
+    bc_ctl->src = src;
+    bc_ctl->L = fc->nlevels - 1;
+    bc_ctl->nheavy = 0;
+    bc_ctl->more = bc_ctl->L >= 1 ? 1 : 0;
+}
+
+}  // namespace
+
+// ----------------------------------------------------------------------------
+// workspace
+// ----------------------------------------------------------------------------
+struct FrontierWS {
+    mgi::DevBuf label, sigma, bm, visited, queue, heavy, stamp, lvl_off, ctl;
+    mgi::DevBuf q, delta, bc, bctl, bheavy, srcbuf;
+    mgi::LoopGraph lg[3];
+    mgi::LoopGraph lg_back;
+};
+
+namespace mgi {
+
+void free_frontier_ws(mg_graph *g)
+{
+    if (!g->fws) return;
+    FrontierWS *w = g->fws;
+    DevBuf *bufs[] = {&w->label, &w->sigma, &w->bm, &w->visited, &w->queue, &w->heavy, &w->stamp,
+                      &w->lvl_off, &w->ctl, &w->q, &w->delta, &w->bc, &w->bctl, &w->bheavy, &w->srcbuf};
+    for (DevBuf *b : bufs) dev_free(*b);
+    for (auto &l : w->lg) l.destroy();
+    w->lg_back.destroy();
+    delete w;
+    g->fws = nullptr;
+}
+
+static mg_status ensure_ws(mg_graph *g, int alg)
+{
+    if (!g->fws) g->fws = new FrontierWS();
+    FrontierWS *w = g->fws;
+    const size_t n = (size_t)std::max(g->nv, 1);
+    const size_t words = (n + 31) / 32;
+    MG_TRY(dev_alloc(w->label, n * 4));
+    MG_TRY(dev_alloc(w->bm, 3 * words * 4));
+    MG_TRY(dev_alloc(w->visited, words * 4));
+    MG_TRY(dev_alloc(w->queue, 2 * n * 4));
+    MG_TRY(dev_alloc(w->heavy, 2 * n * 4));
+    MG_TRY(dev_alloc(w->ctl, sizeof(FCtl)));
+    MG_TRY(dev_alloc(w->lvl_off, (n + 3) * 4));
+    if (alg == ALG_SSSP) MG_TRY(dev_alloc(w->stamp, n * 4));
+    if (alg == ALG_BC) MG_TRY(dev_alloc(w->sigma, n * 8));
+    return MG_OK;
+}
+
+static Args make_args(mg_graph *g)
+{
+    FrontierWS *w = g->fws;
+    Args a;
+    std::memset(&a, 0, sizeof(a));
+    a.n = g->nv;
+    a.m = g->ne;
+    a.row = g->row.as<int32_t>(); a.col = g->col.as<int32_t>(); a.wt = g->wt.as<int32_t>();
+    a.trow = g->trow; a.tcol = g->tcol; a.twt = g->twt;
+    a.grp = g->grp.as<int32_t>(); a.ngroups = g->ngroups;
+    a.hchunk = g->hchunk.as<int32_t>(); a.nhchunks = g->nhchunks;
+    a.heavy_deg = g->heavy_deg;
+    a.label = w->label.as<int32_t>();
+    a.sigma = w->sigma.as<double>();
+    a.bm = w->bm.as<uint32_t>();
+    a.visited = w->visited.as<uint32_t>();
+    a.words = (std::max(g->nv, 1) + 31) / 32;
+    a.queue = w->queue.as<int32_t>();
+    a.heavy = w->heavy.as<int32_t>();
+    a.stamp = w->stamp.as<int32_t>();
+    a.lvl_off = w->lvl_off.as<int32_t>();
+    a.ctl = w->ctl.as<FCtl>();
+    return a;
+}
+
+static uint64_t key_of(const Args &a, int alg)
+{
+    uint64_t k = 1469598103934665603ull ^ (uint64_t)alg;
+    const void *ptrs[] = {a.row, a.col, a.trow, a.tcol, a.label, a.sigma, a.bm, a.queue, a.heavy, a.stamp, a.ctl, a.grp};
+    for (const void *p : ptrs) k = (k ^ (uint64_t)(uintptr_t)p) * 1099511628211ull;
+    return k;
+}
+
+// Forward traversal of `alg` from src (or from the nsrc sources in srcs_host
+// when it is non-null); results stay in the workspace.
+static mg_status frontier_run_impl(mg_graph *g, int alg, int32_t src, const int32_t *srcs_host, int32_t nsrc,
+                                   const mg_opts &opt, mg_run_info *info)
+{
+    if (!srcs_host && (src < 0 || src >= g->nv)) return fail(MG_ERR_RANGE, "source %d out of range [0,%d)", src, g->nv);
+    if (alg == ALG_SSSP && g->min_weight < 0)
+        return fail(MG_ERR_INVALID, "SSSP needs non-negative edge weights (min weight %d)", g->min_weight);
+    MG_TRY(ensure_ws(g, alg));
+    const int32_t *srcs_dev = nullptr;
+    if (srcs_host) {
+        if (nsrc <= 0 || nsrc > g->nv) return fail(MG_ERR_INVALID, "invalid source count %d", nsrc);
+        MG_TRY(dev_alloc(g->fws->srcbuf, (size_t)nsrc * 4));
+        MG_CUDA(cudaMemcpyAsync(g->fws->srcbuf.p, srcs_host, (size_t)nsrc * 4, cudaMemcpyHostToDevice, g->stream));
+        srcs_dev = g->fws->srcbuf.as<int32_t>();
+    }
+    FrontierWS *w = g->fws;
+    Args a = make_args(g);
+    cudaStream_t s = g->stream;
+    const size_t n = (size_t)g->nv;
+    MG_CUDA(cudaMemsetAsync(a.label, 0x64, n * 4, s));
+    MG_CUDA(cudaMemsetAsync(a.bm, 0, 3 * (size_t)a.words * 4, s));
+    MG_CUDA(cudaMemsetAsync(a.visited, 0, (size_t)a.words * 4, s));
+    if (alg == ALG_SSSP) MG_CUDA(cudaMemsetAsync(a.stamp, 0xff, n * 4, s));
+    if (alg == ALG_BC) MG_CUDA(cudaMemsetAsync(a.sigma, 0, n * 8, s));
+    int max_iter = opt.max_iter > 0 ? opt.max_iter : (alg == ALG_SSSP ? 4 * g->nv + 16 : g->nv + 2);
+    int alpha = opt.alpha > 0 ? opt.alpha : 15, beta = opt.beta > 0 ? opt.beta : 18;
+    if (alg == ALG_SSSP && opt.alpha <= 0) alpha = 4;
+    switch (alg) {
+    case ALG_BFS: k_init<ALG_BFS><<<1, 32, 0, s>>>(a, src, srcs_dev, nsrc, opt.direction, alpha, beta, max_iter); break;
+    case ALG_SSSP: k_init<ALG_SSSP><<<1, 32, 0, s>>>(a, src, srcs_dev, nsrc, opt.direction, alpha, beta, max_iter); break;
+    default: k_init<ALG_BC><<<1, 32, 0, s>>>(a, src, srcs_dev, nsrc, opt.direction, alpha, beta, max_iter); break;
+    }
+    MG_CUDA(cudaGetLastError());
+    const int grid = launch_grid(g, THREADS, 4);
+    Profiler &P = g->prof;
+    const int sp = P.slot(alg == ALG_SSSP ? "sssp_push" : alg == ALG_BC ? "bc_push" : "bfs_push");
+    const int sl = P.slot(alg == ALG_SSSP ? "sssp_pull" : alg == ALG_BC ? "bc_pull" : "bfs_pull");
+    const int sd = P.slot("frontier_decide");
+    BodyFn body = [&](cudaStream_t st, cudaGraphConditionalHandle h, int use_cond) -> mg_status {
+        P.begin(sp);
+        switch (alg) {
+        case ALG_BFS: k_push<ALG_BFS><<<grid, THREADS, 0, st>>>(a); break;
+        case ALG_SSSP: k_push<ALG_SSSP><<<grid, THREADS, 0, st>>>(a); break;
+        default: k_push<ALG_BC><<<grid, THREADS, 0, st>>>(a); break;
+        }
+        P.end();
+        P.begin(sl);
+        switch (alg) {
+        case ALG_BFS: k_pull<ALG_BFS><<<grid, THREADS, 0, st>>>(a); break;
+        case ALG_SSSP: k_pull<ALG_SSSP><<<grid, THREADS, 0, st>>>(a); break;
+        default: k_pull<ALG_BC><<<grid, THREADS, 0, st>>>(a); break;
+        }
+        P.end();
+        P.begin(sd);
+        k_decide<<<1, 32, 0, st>>>(a, h, use_cond);
+        P.end();
+        MG_CUDA(cudaGetLastError());
+        return MG_OK;
+    };
+    MG_TRY(run_loop(opt.profile ? MG_EXEC_HOST : opt.exec, opt.profile != 0, s, w->lg[alg], key_of(a, alg), body,
+                    &a.ctl->more, g->pinned_flag, max_iter + 2));
+    // status readback
+    FCtl hc;
+    MG_CUDA(cudaMemcpyAsync(&hc, a.ctl, sizeof(FCtl), cudaMemcpyDeviceToHost, s));
+    MG_CUDA(cudaStreamSynchronize(s));
+    if (info) {
+        info->iterations = hc.iter;
+        info->pull_iterations = hc.pull_iters;
+        info->edges_scanned = hc.scanned;
+    }
+    if (hc.status != 0) return fail(MG_ERR_ITER_LIMIT, "iteration cap %d reached", max_iter);
+    return MG_OK;
+}
+
+mg_status frontier_run(mg_graph *g, int alg, int32_t src, const mg_opts &opt, mg_run_info *info)
+{
+    return frontier_run_impl(g, alg, src, nullptr, 0, opt, info);
+}
+
+mg_status frontier_run_multi(mg_graph *g, int alg, const int32_t *srcs_host, int32_t nsrc, const mg_opts &opt,
+                             mg_run_info *info)
+{
+    return frontier_run_impl(g, alg, 0, srcs_host, nsrc, opt, info);
+}
+
+const void *frontier_label(mg_graph *g) { return g->fws ? g->fws->label.p : nullptr; }
+
+mg_status bc_backward(mg_graph *g, int32_t src, const mg_opts &opt, float *bcacc)
+{
+    FrontierWS *w = g->fws;
+    const size_t n = (size_t)std::max(g->nv, 1);
+    MG_TRY(dev_alloc(w->q, n * 4));
+    MG_TRY(dev_alloc(w->delta, n * 4));
+    MG_TRY(dev_alloc(w->bctl, sizeof(BCtl)));
+    MG_TRY(dev_alloc(w->bheavy, n * 4));
+    Args a = make_args(g);
+    cudaStream_t s = g->stream;
+    float *q = w->q.as<float>(), *delta = w->delta.as<float>();
+    BCtl *bc = w->bctl.as<BCtl>();
+    int32_t *hl = w->bheavy.as<int32_t>();
+    const int grid = launch_grid(g, THREADS, 4);
+    k_bc_q_init<<<grid, THREADS, 0, s>>>(g->nv, a.sigma, a.label, q, delta);
+    k_bc_back_init<<<1, 32, 0, s>>>(a.ctl, bc, src);
+    MG_CUDA(cudaGetLastError());
+    Profiler &P = g->prof;
+    const int sb = P.slot("bc_back"), sh = P.slot("bc_back_heavy"), sd = P.slot("bc_back_decide");
+    BodyFn body = [&](cudaStream_t st, cudaGraphConditionalHandle h, int use_cond) -> mg_status {
+        P.begin(sb);
+        k_bc_back<<<grid, THREADS, 0, st>>>(a, bc, q, delta, bcacc, hl);
+        P.end();
+        P.begin(sh);
+        k_bc_back_heavy<<<grid, THREADS, 0, st>>>(a, bc, q, delta, bcacc, hl);
+        P.end();
+        P.begin(sd);
+        k_bc_back_decide<<<1, 32, 0, st>>>(bc, h, use_cond);
+        P.end();
+        MG_CUDA(cudaGetLastError());
+        return MG_OK;
+    };
+    // the graph bakes in the bc accumulator (null for single-source runs)
+    uint64_t key = key_of(a, 7) ^ ((uint64_t)(uintptr_t)bcacc * 31) ^ ((uint64_t)(uintptr_t)q * 17);
+    return run_loop(opt.profile ? MG_EXEC_HOST : opt.exec, opt.profile != 0, s, w->lg_back, key, body, &bc->more,
+                    g->pinned_flag, g->nv + 4);
+}
+
+}  // namespace mgi
+
+using namespace mgi;
+
+extern "C" {
+
+mg_status mg_bfs(mg_graph *g, int32_t source, const mg_opts *o, int32_t *level_out, mg_run_info *info)
+{
+    mg_opts opt;
+    MG_TRY(begin_run(g, o, opt, info));
+    MG_TRY(frontier_run(g, ALG_BFS, source, opt, info));
+    MG_TRY(end_run(g, opt, info));
+    g->res[MG_RES_LEVEL] = g->fws->label.p;
+    return copy_out(g, level_out, g->fws->label.p, (size_t)g->nv * 4);
+}
+
+mg_status mg_sssp(mg_graph *g, int32_t source, const mg_opts *o, int32_t *dist_out, mg_run_info *info)
+{
+    mg_opts opt;
+    MG_TRY(begin_run(g, o, opt, info));
+    MG_TRY(frontier_run(g, ALG_SSSP, source, opt, info));
+    MG_TRY(end_run(g, opt, info));
+    g->res[MG_RES_DIST] = g->fws->label.p;
+    return copy_out(g, dist_out, g->fws->label.p, (size_t)g->nv * 4);
+}
+
+mg_status mg_bc(mg_graph *g, int32_t source, const mg_opts *o, int32_t *level_out, double *sigma_out,
+                float *delta_out, mg_run_info *info)
+{
+    mg_opts opt;
+    MG_TRY(begin_run(g, o, opt, info));
+    MG_TRY(frontier_run(g, ALG_BC, source, opt, info));
+    MG_TRY(bc_backward(g, source, opt, nullptr));
+    MG_TRY(end_run(g, opt, info));
+    FrontierWS *w = g->fws;
+    g->res[MG_RES_LEVEL] = w->label.p;
+    g->res[MG_RES_SIGMA] = w->sigma.p;
+    g->res[MG_RES_DELTA] = w->delta.p;
+    MG_TRY(copy_out(g, level_out, w->label.p, (size_t)g->nv * 4));
+    MG_TRY(copy_out(g, sigma_out, w->sigma.p, (size_t)g->nv * 8));
+    return copy_out(g, delta_out, w->delta.p, (size_t)g->nv * 4);
+}
+
+mg_status mg_bc_multi(mg_graph *g, const int32_t *sources, int32_t nsrc, const mg_opts *o, float *bc_out,
+                      mg_run_info *info)
+{
+    mg_opts opt;
+    MG_TRY(begin_run(g, o, opt, info));
+    if (nsrc < 0 || (nsrc > 0 && !sources)) return fail(MG_ERR_INVALID, "invalid sources");
+    for (int32_t i = 0; i < nsrc; i++)
+        if (sources[i] < 0 || sources[i] >= g->nv) return fail(MG_ERR_RANGE, "source %d out of range", sources[i]);
+    MG_TRY(ensure_ws(g, ALG_BC));
+    FrontierWS *w = g->fws;
+    MG_TRY(dev_alloc(w->bc, (size_t)std::max(g->nv, 1) * 4));
+    MG_CUDA(cudaMemsetAsync(w->bc.p, 0, (size_t)g->nv * 4, g->stream));
+    int32_t iters = 0;
+    for (int32_t i = 0; i < nsrc; i++) {
+        mg_run_info sub;
+        MG_TRY(frontier_run(g, ALG_BC, sources[i], opt, &sub));
+        MG_TRY(bc_backward(g, sources[i], opt, w->bc.as<float>()));
+        iters += sub.iterations;
+    }
+    MG_TRY(end_run(g, opt, info));
+    if (info) info->iterations = iters;
+    g->res[MG_RES_BC] = w->bc.p;
+    return copy_out(g, bc_out, w->bc.p, (size_t)g->nv * 4);
+}
+
+}  // extern "C"

@@ -1,0 +1,956 @@
+// mg_pr.cu -- PageRank engines: the reference's PR_T / PR_D recurrences,
+// normalised topology- and data-driven PageRank, batched personalised
+// PageRank, weighted PageRank and its adjoint (edge-weight gradient).
+//
+// Replaces MultiGraph_V_E_V_NOTIDEM (processi.cu:682-894) with _phase1 /
+// _phase11 / _phase2.  The reference scatters pr/deg with FP32 atomicAdd into
+// an intermediate buffer and gathers it in shared memory (order-dependent
+// sums, ~12.5 B/edge).  Here every sweep is a pull (gather) over in-edges:
+//   k_pr_light  edge-balanced warp groups (<= 32 rows, <= 512 edges): lanes
+//               read 32 consecutive column ids (one 128 B line), gather the
+//               contributions from L2, segmented-reduce by row in registers;
+//   k_pr_heavy  rows above 2048 in-edges in 2048-edge chunks, one CTA each,
+//               partial sums written per chunk;
+//   k_pr_finish one CTA: heavy rows summed chunk by chunk in order, block
+//               residuals summed in order, convergence test, loop condition.
+// Sums are therefore deterministic (fixed order) run to run.
+// Algorithmic bytes per sweep: 4m (column ids) + 4(n+1) (offsets) + 12n
+// (old value read, new value and contribution written); the contribution
+// gathers (4n bytes) are served by L2.
+
+#include "mg_device.cuh"
+#include "mg_ops.cuh"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+
+namespace {
+
+constexpr int THREADS = 256;
+
+enum { V_T_REF = MG_PR_TOPOLOGY_REF, V_D_REF = MG_PR_DATA_REF, V_T = MG_PR_TOPOLOGY, V_D = MG_PR_DATA, V_WEIGHTED = 4, V_ADJ = 5 };
+
+struct PCtl {
+    int32_t more;
+    int32_t iter;
+    int32_t cur;
+    int32_t status;
+    int32_t max_iter;
+    int32_t any;          // a vertex changed beyond tolerance / is active
+    int32_t done;         // blocks of k_pr_apply that have finished this sweep
+    int32_t pad2;
+    double resid;         // L1 change of the last sweep
+    double dangling;      // sum of x over zero out-degree vertices (current iterate)
+    double lam_mean;      // adjoint: mean of lambda (dangling rows)
+    float damping, tol;
+    int32_t n;
+    int32_t pad;
+};
+
+struct PArgs {
+    int32_t n;
+    const int32_t *prow;     // rows scanned (in-edges for PR, out-edges for the adjoint)
+    const int32_t *pcol;
+    const float *pw;         // per-entry weights of the scanned rows (weighted / adjoint), or null
+    const int32_t *outrow;   // push-side offsets (out-degrees)
+    float *S;                // weighted: out-weight sums
+    const int32_t *grp;
+    int32_t ngroups;
+    const int32_t *hchunk;
+    int32_t nhchunks;
+    const int32_t *hrows;
+    const int32_t *hrow_chunk;
+    int32_t nhrows;
+    int32_t heavy_deg;
+    float *x[2];             // iterate (ping-pong)
+    float *c[2];             // gathered quantity: contribution x/deg (PR) or lambda (adjoint)
+    const float *gvec;       // adjoint: g
+    int32_t *active;         // data-driven masks
+    float *hpart;            // heavy chunk partial sums
+    double *bpart;           // per-block partials: [3*grid] (resid, dangling, any)
+    int32_t nblocks;
+    PCtl *ctl;
+};
+
+// ---------------------------------------------------------------------------
+// per-row update.  s = gathered sum.  Returns |change|; sets *any when the
+// row counts as changed / active; *dang = x_new when the row's out-degree is 0.
+// ---------------------------------------------------------------------------
+template <int V>
+__device__ __forceinline__ float pr_apply(const PArgs &a, const PCtl &c, int32_t v, float s, int &any, float &dang)
+{
+    const int cur = c.cur, nxt = cur ^ 1;
+    float xo = a.x[cur][v];
+    float xn;
+    int32_t od = a.outrow[v + 1] - a.outrow[v];
+    if (V == V_T_REF) {
+        // processi.cu:631-638 / validate.cu:59-70
+        float f1 = mgops::PrRef::apply(s);
+        if (fabsf(f1 - xo) > mgops::PrRef::TOL) { xn = f1; any = 1; }
+        else xn = xo;
+        a.x[nxt][v] = xn;
+        a.c[nxt][v] = mgops::PrRef::get_partial_result(xn, od);
+    } else if (V == V_D_REF) {
+        // processi.cu:640-655 / validate.cu:71-84 (values always move; the
+        // sticky mask only decides termination)
+        float f1 = mgops::PrRef::apply(s);
+        if (a.active[v] == 1 && fabsf(f1 - xo) > mgops::PrRef::TOL * xo) any = 1;
+        else a.active[v] = 0;
+        xn = f1;
+        a.x[nxt][v] = xn;
+        a.c[nxt][v] = mgops::PrRef::get_partial_result(xn, od);
+    } else if (V == V_T || V == V_D) {
+        const float d = c.damping;
+        float base = (float)((1.0 - (double)d) / c.n + (double)d * c.dangling / c.n);
+        if (V == V_D && a.active[v] == 0) {
+            xn = xo;  // frozen
+        } else {
+            xn = base + d * s;
+            if (V == V_D) {
+                if (fabsf(xn - xo) <= c.tol / (float)c.n) a.active[v] = 0;
+                else any = 1;
+            }
+        }
+        a.x[nxt][v] = xn;
+        a.c[nxt][v] = od > 0 ? xn / (float)od : 0.0f;
+        if (od == 0) dang = xn;
+    } else if (V == V_WEIGHTED) {
+        const float d = c.damping;
+        float base = (float)((1.0 - (double)d) / c.n + (double)d * c.dangling / c.n);
+        xn = base + d * s;
+        a.x[nxt][v] = xn;
+        float Su = a.S[v];
+        a.c[nxt][v] = Su > 0.0f ? xn / Su : 0.0f;
+        if (!(Su > 0.0f)) dang = xn;
+    } else {  // V_ADJ: lambda_new = g + d * (t + [S_u == 0] * mean(lambda))
+        const float d = c.damping;
+        float Su = a.S[v];
+        float t = Su > 0.0f ? s / Su : (float)c.lam_mean;
+        xn = a.gvec[v] + d * t;
+        xo = a.c[cur][v];
+        a.c[nxt][v] = xn;
+        dang = xn;  // sum of lambda for the mean
+    }
+    return fabsf(xn - xo);
+}
+
+// gathered value for edge e from source u
+template <int V>
+__device__ __forceinline__ float pr_gather(const PArgs &a, int cur, int32_t e, int32_t u)
+{
+    float cv = a.c[cur][u];
+    if (V == V_WEIGHTED || V == V_ADJ) cv *= a.pw[e];
+    return cv;
+}
+
+template <int V>
+__device__ __forceinline__ bool pr_row_skipped(const PArgs &a, int32_t v)
+{
+    return V == V_D && a.active[v] == 0;
+}
+
+__device__ __forceinline__ void block_partials(const PArgs &a, int slot, double r, double dg, int any)
+{
+    __shared__ double sr[THREADS / 32], sd[THREADS / 32];
+    __shared__ int sa[THREADS / 32];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        r += __shfl_xor_sync(0xffffffffu, r, o);
+        dg += __shfl_xor_sync(0xffffffffu, dg, o);
+        any |= __shfl_xor_sync(0xffffffffu, any, o);
+    }
+    if ((threadIdx.x & 31) == 0) { sr[threadIdx.x >> 5] = r; sd[threadIdx.x >> 5] = dg; sa[threadIdx.x >> 5] = any; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double R = 0, D = 0;
+        int A = 0;
+        for (int w = 0; w < THREADS / 32; w++) { R += sr[w]; D += sd[w]; A |= sa[w]; }
+        a.bpart[3 * slot] = R;
+        a.bpart[3 * slot + 1] = D;
+        a.bpart[3 * slot + 2] = (double)A;
+    }
+}
+
+// row reduction for one PageRank sweep (group_reduce interface)
+template <int V>
+struct PrRowOp {
+    using T = float;
+    static constexpr bool kRowAware = (V == V_D);                      // inactive rows are skipped
+    static constexpr bool kWeights = (V == V_WEIGHTED || V == V_ADJ);  // staged float weight bits
+    const PArgs &a;
+    const PCtl &c;
+    double resid = 0.0, dangs = 0.0;
+    int any = 0;
+    __device__ float identity() const { return 0.0f; }
+    __device__ bool skip(int32_t v) const { return pr_row_skipped<V>(a, v); }
+    __device__ float edge(int32_t, int32_t, int32_t u, int32_t w) const
+    {
+        float cv = a.c[c.cur][u];
+        if (kWeights) cv *= __int_as_float(w);
+        return cv;
+    }
+    __device__ float combine(float x, float y) const { return x + y; }
+    __device__ void finish(int32_t v, float s)
+    {
+        float dg = 0.0f;
+        resid += pr_apply<V>(a, c, v, s, any, dg);
+        dangs += dg;
+    }
+};
+
+template <int V>
+__global__ void __launch_bounds__(THREADS) k_pr_light(PArgs a)
+{
+    const PCtl c = *a.ctl;
+    if (c.more == 0) return;
+    const int lane = mgd::lane();
+    const int gwarp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int nwarps = (gridDim.x * blockDim.x) >> 5;
+    constexpr bool W = PrRowOp<V>::kWeights;
+    __shared__ int32_t s_off[THREADS / 32][mgd::GROUP_ROWS + 1];
+    __shared__ __align__(16) int32_t s_col[THREADS / 32][mgd::GROUP_STAGE];
+    __shared__ __align__(16) int32_t s_wt[W ? THREADS / 32 : 1][W ? mgd::GROUP_STAGE : 4];
+    PrRowOp<V> op{a, c};
+    (void)lane;
+    const int wib = threadIdx.x >> 5;
+    const mgd::GroupSmem sm{s_off[wib], s_col[wib], W ? s_wt[wib] : nullptr};
+    const int32_t *pwt = reinterpret_cast<const int32_t *>(a.pw);
+    for (int32_t g = gwarp; g < a.ngroups; g += nwarps) {
+        int32_t r0 = a.grp[g], r1 = a.grp[g + 1];
+        if (r1 - r0 == 1 && a.prow[r1] - a.prow[r0] > a.heavy_deg) continue;  // heavy row: chunks below
+        mgd::group_reduce(op, a.prow, a.pcol, pwt, r0, r1, sm);
+    }
+    // heavy-row chunks of HCHUNK = 8 * THREADS edges, one per CTA: each
+    // thread issues its 8 column loads, then its 8 gathers
+    __shared__ float s_part[THREADS / 32];
+    for (int32_t ch = blockIdx.x; ch < a.nhchunks; ch += gridDim.x) {
+        int32_t v = a.hchunk[3 * ch], b = a.hchunk[3 * ch + 1], e = a.hchunk[3 * ch + 2];
+        float acc = 0.0f;
+        if (!pr_row_skipped<V>(a, v)) {
+            int32_t u[8];
+#pragma unroll
+            for (int j = 0; j < 8; j++) {
+                int32_t p = b + threadIdx.x + j * THREADS;
+                u[j] = p < e ? __ldg(&a.pcol[p]) : -1;
+            }
+#pragma unroll
+            for (int j = 0; j < 8; j++)
+                if (u[j] >= 0) acc += pr_gather<V>(a, c.cur, b + threadIdx.x + j * THREADS, u[j]);
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+        if ((threadIdx.x & 31) == 0) s_part[threadIdx.x >> 5] = acc;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            float s = 0.0f;
+            for (int w = 0; w < THREADS / 32; w++) s += s_part[w];
+            a.hpart[ch] = s;
+        }
+        __syncthreads();
+    }
+    block_partials(a, blockIdx.x, op.resid, op.dangs, op.any);
+}
+
+// Heavy rows (warp per row, chunk partials summed lane-strided then by a
+// fixed shuffle tree), then the last block to arrive reduces every block's
+// partials in slot order and updates the loop state -- no block waits.
+template <int V>
+__global__ void __launch_bounds__(THREADS) k_pr_apply(PArgs a, cudaGraphConditionalHandle h, int use_cond)
+{
+    PCtl *cp = a.ctl;
+    const PCtl c = *cp;
+    if (c.more == 0) {
+        if (blockIdx.x == 0 && threadIdx.x == 0 && use_cond) cudaGraphSetConditional(h, 0u);
+        return;
+    }
+    const int lane = mgd::lane();
+    const int gwarp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int nwarps = (gridDim.x * blockDim.x) >> 5;
+    double resid = 0.0, dangs = 0.0;
+    int any = 0;
+    for (int32_t i = gwarp; i < a.nhrows; i += nwarps) {
+        int32_t v = a.hrows[i];
+        float s = 0.0f;
+        for (int32_t k = a.hrow_chunk[i] + lane; k < a.hrow_chunk[i + 1]; k += 32) s += a.hpart[k];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+        if (lane == 0) {
+            float dg = 0.0f;
+            resid += pr_apply<V>(a, c, v, s, any, dg);
+            dangs += dg;
+        }
+    }
+    block_partials(a, a.nblocks + blockIdx.x, resid, dangs, any);
+    __shared__ int s_last;
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) s_last = (atomicAdd(&cp->done, 1) == (int)gridDim.x - 1);
+    __syncthreads();
+    if (!s_last) return;
+    __shared__ double sr[THREADS / 32], sd[THREADS / 32];
+    __shared__ int sa[THREADS / 32];
+    resid = 0.0;
+    dangs = 0.0;
+    any = 0;
+    const int nslots = a.nblocks + gridDim.x;
+    for (int b = threadIdx.x; b < nslots; b += blockDim.x) {
+        resid += __ldcg(&a.bpart[3 * b]);
+        dangs += __ldcg(&a.bpart[3 * b + 1]);
+        any |= __ldcg(&a.bpart[3 * b + 2]) != 0.0;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        resid += __shfl_xor_sync(0xffffffffu, resid, o);
+        dangs += __shfl_xor_sync(0xffffffffu, dangs, o);
+        any |= __shfl_xor_sync(0xffffffffu, any, o);
+    }
+    if (lane == 0) { sr[threadIdx.x >> 5] = resid; sd[threadIdx.x >> 5] = dangs; sa[threadIdx.x >> 5] = any; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int more = 1;
+        {
+            double R = 0, D = 0;
+            int A = 0;
+            for (int w = 0; w < THREADS / 32; w++) { R += sr[w]; D += sd[w]; A |= sa[w]; }
+            cp->done = 0;
+            cp->iter = c.iter + 1;
+            cp->cur = c.cur ^ 1;
+            cp->resid = R;
+            cp->any = A;
+            if (V == V_ADJ) cp->lam_mean = D / c.n;
+            else cp->dangling = D;
+            if (V == V_T_REF || V == V_D_REF) more = A;
+            else if (V == V_D) more = (A && R > (double)c.tol) ? 1 : 0;
+            else more = R > (double)c.tol ? 1 : 0;
+            if (more && cp->iter >= c.max_iter) { cp->status = 1; more = 0; }
+            cp->more = more;
+        }
+        if (use_cond) cudaGraphSetConditional(h, more ? 1u : 0u);
+    }
+}
+
+// init: x = x0, contributions, masks
+template <int V>
+__global__ void k_pr_init(PArgs a, float x0)
+{
+    for (int32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < a.n; v += gridDim.x * blockDim.x) {
+        if (V == V_ADJ) {
+            a.c[0][v] = a.gvec[v];
+            continue;
+        }
+        a.x[0][v] = x0;
+        if (V == V_WEIGHTED) {
+            float Su = a.S[v];
+            a.c[0][v] = Su > 0.0f ? x0 / Su : 0.0f;
+        } else {
+            int32_t od = a.outrow[v + 1] - a.outrow[v];
+            a.c[0][v] = od > 0 ? x0 / (float)od : 0.0f;
+        }
+        if (a.active) a.active[v] = 1;
+    }
+}
+
+__global__ void k_pr_ctl_init(PCtl *c, int32_t n, int32_t max_iter, float damping, float tol, double dangling0,
+                              double lam_mean0)
+{
+    if (threadIdx.x != 0) return;
+    std::memset(c, 0, sizeof(PCtl));
+    c->more = 1;
+    c->max_iter = max_iter;
+    c->damping = damping;
+    c->tol = tol;
+    c->n = n;
+    c->dangling = dangling0;
+    c->lam_mean = lam_mean0;
+}
+
+// weighted: out-weight sums S[u] = sum_e w[e] (CSR order)
+__global__ void k_row_sums(int32_t n, const int32_t *row, const float *w, float *S)
+{
+    for (int32_t u = blockIdx.x * blockDim.x + threadIdx.x; u < n; u += gridDim.x * blockDim.x) {
+        float s = 0.0f;
+        for (int32_t p = row[u]; p < row[u + 1]; p++) s += w[p];
+        S[u] = s;
+    }
+}
+
+// adjoint edge scatter: grad[e] = d x_u / S_u * (lambda_v - t_u),
+// t_u = sum_k P_uk lambda_k recomputed over the row (warp per row)
+__global__ void __launch_bounds__(THREADS) k_wpr_grad(int32_t n, const int32_t *row, const int32_t *col,
+                                                      const float *w, const float *S, const float *x,
+                                                      const float *lam, float damping, float *grad)
+{
+    const int lane = mgd::lane();
+    const int gwarp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int nwarps = (gridDim.x * blockDim.x) >> 5;
+    for (int32_t u = gwarp; u < n; u += nwarps) {
+        int32_t b = row[u], e = row[u + 1];
+        float Su = S[u];
+        float t = 0.0f;
+        for (int32_t p = b + lane; p < e; p += 32) t += w[p] * lam[col[p]];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+        float coef = Su > 0.0f ? damping * x[u] / Su : 0.0f;
+        float tu = Su > 0.0f ? t / Su : 0.0f;
+        for (int32_t p = b + lane; p < e; p += 32) grad[p] = coef * (lam[col[p]] - tu);
+    }
+}
+
+// personalised PageRank, 32 seeds per pass: lane = seed, X / C are [n][32]
+// for the current seed block (one 128 B line per vertex).  Rows with more
+// than PPR_HEAVY in-edges are split into PPR_HEAVY-edge chunks (warp per
+// chunk, partial sums per chunk) and combined in order by k_ppr_heavy.
+constexpr int32_t PPR_HEAVY = 256;
+
+struct PPCtl {
+    int32_t more, iter, cur, status, max_iter, pad;
+    double resid[32];
+};
+
+struct PPArgs {
+    int32_t n;
+    const int32_t *prow, *pcol, *outrow;
+    const int32_t *seeds;
+    int32_t nseed;
+    const int32_t *hchunk;   // (row, begin, end)
+    int32_t nhchunks;
+    const int32_t *hrows, *hrow_chunk;
+    int32_t nhrows;
+    float *X0, *C0, *X1, *C1;
+    float *hpart;            // [nhchunks][32]
+    double *bpart;           // [2*grid][32][2]
+    double *dang;            // [32] dangling mass of the current iterate
+    PPCtl *ctl;
+    float damping;
+};
+
+__global__ void k_ppr_init(PPArgs a, int32_t max_iter)
+{
+    const size_t total = (size_t)a.n * 32;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
+        int32_t v = (int32_t)(i >> 5);
+        int s = (int)(i & 31);
+        float x = (s < a.nseed && a.seeds[s] == v) ? 1.0f : 0.0f;
+        a.X0[i] = x;
+        int32_t od = a.outrow[v + 1] - a.outrow[v];
+        a.C0[i] = od > 0 ? x / (float)od : 0.0f;
+    }
+    if (blockIdx.x == 0 && threadIdx.x < 32) {
+        int s = threadIdx.x;
+        double dg = 0.0;
+        if (s < a.nseed) { int32_t v = a.seeds[s]; dg = (a.outrow[v + 1] == a.outrow[v]) ? 1.0 : 0.0; }
+        a.dang[s] = dg;
+        if (s == 0) {
+            std::memset(a.ctl, 0, sizeof(PPCtl));
+            a.ctl->more = 1;
+            a.ctl->max_iter = max_iter;
+        }
+    }
+}
+
+__device__ __forceinline__ void ppr_apply(const PPArgs &a, const PPCtl &c, int32_t v, float s, int lane, float dang,
+                                          int32_t seed, double &resid, double &dnext)
+{
+    const float *Xc = c.cur ? a.X1 : a.X0;
+    float *Xn = c.cur ? a.X0 : a.X1;
+    float *Cn = c.cur ? a.C0 : a.C1;
+    float base = (v == seed) ? (1.0f - a.damping) + a.damping * dang : 0.0f;
+    float xn = base + a.damping * s;
+    float xo = Xc[(size_t)v * 32 + lane];
+    Xn[(size_t)v * 32 + lane] = xn;
+    int32_t od = a.outrow[v + 1] - a.outrow[v];
+    Cn[(size_t)v * 32 + lane] = od > 0 ? xn / (float)od : 0.0f;
+    if (od == 0) dnext += xn;
+    resid += fabsf(xn - xo);
+}
+
+__device__ __forceinline__ void ppr_block_partials(const PPArgs &a, int slot, double resid, double dnext)
+{
+    __shared__ double sr[THREADS / 32][32], sd[THREADS / 32][32];
+    const int lane = mgd::lane();
+    sr[threadIdx.x >> 5][lane] = resid;
+    sd[threadIdx.x >> 5][lane] = dnext;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        double R = 0, D = 0;
+        for (int w = 0; w < THREADS / 32; w++) { R += sr[w][threadIdx.x]; D += sd[w][threadIdx.x]; }
+        a.bpart[((size_t)slot * 32 + threadIdx.x) * 2] = R;
+        a.bpart[((size_t)slot * 32 + threadIdx.x) * 2 + 1] = D;
+    }
+}
+
+// gather sum of C[u][lane] over [b, e)
+__device__ __forceinline__ float ppr_gather(const float *Cc, const int32_t *pcol, int32_t b, int32_t e, int lane)
+{
+    float s0 = 0.f, s1 = 0.f, s2 = 0.f, s3 = 0.f;
+    int32_t p = b;
+    for (; p + 8 <= e; p += 8) {
+        int32_t u[8];
+#pragma unroll
+        for (int j = 0; j < 8; j++) u[j] = pcol[p + j];
+        float t[8];
+#pragma unroll
+        for (int j = 0; j < 8; j++) t[j] = Cc[(size_t)u[j] * 32 + lane];
+        s0 += t[0] + t[4];
+        s1 += t[1] + t[5];
+        s2 += t[2] + t[6];
+        s3 += t[3] + t[7];
+    }
+    for (; p < e; p++) s0 += Cc[(size_t)pcol[p] * 32 + lane];
+    return (s0 + s1) + (s2 + s3);
+}
+
+__global__ void __launch_bounds__(THREADS) k_ppr_sweep(PPArgs a)
+{
+    const PPCtl c = *a.ctl;
+    if (c.more == 0) return;
+    const float *Cc = c.cur ? a.C1 : a.C0;
+    const int lane = mgd::lane();
+    const int gwarp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int nwarps = (gridDim.x * blockDim.x) >> 5;
+    const int32_t seed = lane < a.nseed ? a.seeds[lane] : -1;
+    const float dang = (float)a.dang[lane];
+    double resid = 0.0, dnext = 0.0;
+    for (int32_t v = gwarp; v < a.n; v += nwarps) {
+        int32_t b = a.prow[v], e = a.prow[v + 1];
+        if (e - b > PPR_HEAVY) continue;  // warp-uniform
+        float s = ppr_gather(Cc, a.pcol, b, e, lane);
+        ppr_apply(a, c, v, s, lane, dang, seed, resid, dnext);
+    }
+    for (int32_t ch = gwarp; ch < a.nhchunks; ch += nwarps) {
+        int32_t b = a.hchunk[3 * ch + 1], e = a.hchunk[3 * ch + 2];
+        a.hpart[(size_t)ch * 32 + lane] = ppr_gather(Cc, a.pcol, b, e, lane);
+    }
+    ppr_block_partials(a, blockIdx.x, resid, dnext);
+}
+
+__global__ void __launch_bounds__(THREADS) k_ppr_heavy(PPArgs a)
+{
+    const PPCtl c = *a.ctl;
+    if (c.more == 0) return;
+    const int lane = mgd::lane();
+    const int gwarp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int nwarps = (gridDim.x * blockDim.x) >> 5;
+    const int32_t seed = lane < a.nseed ? a.seeds[lane] : -1;
+    const float dang = (float)a.dang[lane];
+    double resid = 0.0, dnext = 0.0;
+    for (int32_t i = gwarp; i < a.nhrows; i += nwarps) {
+        int32_t v = a.hrows[i];
+        float s = 0.0f;
+        for (int32_t k = a.hrow_chunk[i]; k < a.hrow_chunk[i + 1]; k++) s += a.hpart[(size_t)k * 32 + lane];
+        ppr_apply(a, c, v, s, lane, dang, seed, resid, dnext);
+    }
+    ppr_block_partials(a, gridDim.x + blockIdx.x, resid, dnext);
+}
+
+__global__ void k_ppr_finish(PPArgs a, int nslots, float tol, cudaGraphConditionalHandle h, int use_cond)
+{
+    const int lane = threadIdx.x;  // 32 threads, lane = seed
+    PPCtl *ctl = a.ctl;
+    int more = ctl->more;
+    if (more) {
+        double R = 0, D = 0;
+        for (int b = 0; b < nslots; b++) {
+            R += a.bpart[((size_t)b * 32 + lane) * 2];
+            D += a.bpart[((size_t)b * 32 + lane) * 2 + 1];
+        }
+        ctl->resid[lane] = R;
+        a.dang[lane] = D;
+        int cont = (lane < a.nseed) && (R > (double)tol);
+        cont = __any_sync(0xffffffffu, cont);
+        if (lane == 0) {
+            ctl->iter += 1;
+            ctl->cur ^= 1;
+            if (cont && ctl->iter >= ctl->max_iter) { ctl->status = 1; cont = 0; }
+            ctl->more = cont;
+        }
+        more = cont;
+    }
+    if (lane == 0 && use_cond) cudaGraphSetConditional(h, more ? 1u : 0u);
+}
+
+__global__ void k_ppr_store(int32_t n, const float *X, int32_t nseed, int32_t s0, float *out)
+{
+    const size_t total = (size_t)n * 32;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
+        int s = (int)(i & 31);
+        if (s < nseed) out[(size_t)(s0 + s) * n + (i >> 5)] = X[i];
+    }
+}
+
+}  // namespace
+
+struct PrWS {
+    mgi::DevBuf x0, x1, c0, c1, active, hpart, bpart, ctl, S, wT, gvec, grad, lam_keep, xkeep;
+    mgi::LoopGraph lg[6];
+};
+
+struct PprWS {
+    mgi::DevBuf X0, X1, C0, C1, seeds, ctl, bpart, dang, hpart, out;
+    mgi::LoopGraph lg;
+};
+
+struct WprWS {};
+
+namespace mgi {
+
+void free_pr_ws(mg_graph *g)
+{
+    if (!g->pws) return;
+    PrWS *w = g->pws;
+    DevBuf *bufs[] = {&w->x0, &w->x1, &w->c0, &w->c1, &w->active, &w->hpart, &w->bpart, &w->ctl, &w->S,
+                      &w->wT, &w->gvec, &w->grad, &w->lam_keep, &w->xkeep};
+    for (DevBuf *b : bufs) dev_free(*b);
+    for (auto &l : w->lg) l.destroy();
+    delete w;
+    g->pws = nullptr;
+}
+
+void free_ppr_ws(mg_graph *g)
+{
+    if (!g->ppws) return;
+    PprWS *w = g->ppws;
+    DevBuf *bufs[] = {&w->X0, &w->X1, &w->C0, &w->C1, &w->seeds, &w->ctl, &w->bpart, &w->dang, &w->hpart, &w->out};
+    for (DevBuf *b : bufs) dev_free(*b);
+    w->lg.destroy();
+    delete w;
+    g->ppws = nullptr;
+}
+
+void free_wpr_ws(mg_graph *g) { (void)g; }
+
+static uint64_t pkey(const PArgs &a, int v)
+{
+    uint64_t k = 0xcbf29ce484222325ull ^ (uint64_t)v;
+    const void *ptrs[] = {a.prow, a.pcol, a.pw, a.x[0], a.x[1], a.c[0], a.c[1], a.active, a.hpart, a.bpart, a.ctl, a.S, a.gvec};
+    for (const void *p : ptrs) k = (k ^ (uint64_t)(uintptr_t)p) * 0x100000001b3ull;
+    return k;
+}
+
+// Runs sweeps of variant V until convergence; the result is x[ctl.cur]
+// (c[ctl.cur] for the adjoint).
+template <int V>
+static mg_status pr_loop(mg_graph *g, PArgs &a, const mg_opts &opt, const char *name, mg_run_info *info,
+                         int *final_cur)
+{
+    cudaStream_t s = g->stream;
+    const int grid = a.nblocks;
+    Profiler &P = g->prof;
+    const int sl = P.slot(name);
+    std::string hn = std::string(name) + "_apply";
+    const int sh = P.slot(hn.c_str());
+    const int apply_grid = std::max(1, std::min(grid, (a.nhrows + 7) / 8));
+    BodyFn body = [&](cudaStream_t st, cudaGraphConditionalHandle h, int use_cond) -> mg_status {
+        P.begin(sl);
+        k_pr_light<V><<<grid, THREADS, 0, st>>>(a);
+        P.end();
+        P.begin(sh);
+        k_pr_apply<V><<<apply_grid, THREADS, 0, st>>>(a, h, use_cond);
+        P.end();
+        MG_CUDA(cudaGetLastError());
+        return MG_OK;
+    };
+    int max_iter = opt.max_iter > 0 ? opt.max_iter : 10000;
+    MG_TRY(run_loop(opt.profile ? MG_EXEC_HOST : opt.exec, opt.profile != 0, s, g->pws->lg[V], pkey(a, V), body,
+                    &a.ctl->more, g->pinned_flag, max_iter + 2));
+    PCtl hc;
+    MG_CUDA(cudaMemcpyAsync(&hc, a.ctl, sizeof(PCtl), cudaMemcpyDeviceToHost, s));
+    MG_CUDA(cudaStreamSynchronize(s));
+    if (info) {
+        info->iterations = hc.iter;
+        info->pull_iterations = hc.iter;
+        info->residual = hc.resid;
+        info->edges_scanned = (int64_t)hc.iter * g->ne;
+    }
+    *final_cur = hc.cur;
+    if (hc.status != 0) return fail(MG_ERR_ITER_LIMIT, "PageRank did not converge in %d sweeps (residual %g)", max_iter, hc.resid);
+    return MG_OK;
+}
+
+static mg_status pr_setup(mg_graph *g, PArgs &a, bool weighted_or_adj)
+{
+    if (!g->pws) g->pws = new PrWS();
+    PrWS *w = g->pws;
+    const size_t n = (size_t)std::max(g->nv, 1);
+    const int grid = launch_grid(g, THREADS, 8);
+    MG_TRY(dev_alloc(w->x0, n * 4));
+    MG_TRY(dev_alloc(w->x1, n * 4));
+    MG_TRY(dev_alloc(w->c0, n * 4));
+    MG_TRY(dev_alloc(w->c1, n * 4));
+    MG_TRY(dev_alloc(w->active, n * 4));
+    MG_TRY(dev_alloc(w->hpart, (size_t)std::max(g->nhchunks, 1) * 4));
+    MG_TRY(dev_alloc(w->bpart, (size_t)grid * 2 * 3 * 8));  // sweep blocks + apply blocks
+    MG_TRY(dev_alloc(w->ctl, sizeof(PCtl)));
+    std::memset(&a, 0, sizeof(a));
+    a.n = g->nv;
+    a.prow = g->trow;
+    a.pcol = g->tcol;
+    a.outrow = g->row.as<int32_t>();
+    a.grp = g->grp.as<int32_t>(); a.ngroups = g->ngroups;
+    a.hchunk = g->hchunk.as<int32_t>(); a.nhchunks = g->nhchunks;
+    a.hrows = g->hrows.as<int32_t>(); a.hrow_chunk = g->hrow_chunk.as<int32_t>(); a.nhrows = g->nhrows;
+    a.heavy_deg = g->heavy_deg;
+    a.x[0] = w->x0.as<float>(); a.x[1] = w->x1.as<float>();
+    a.c[0] = w->c0.as<float>(); a.c[1] = w->c1.as<float>();
+    a.active = w->active.as<int32_t>();
+    a.hpart = w->hpart.as<float>();
+    a.bpart = w->bpart.as<double>();
+    a.nblocks = grid;
+    a.ctl = w->ctl.as<PCtl>();
+    if (weighted_or_adj) {
+        if (!g->has_fw) return fail(MG_ERR_UNSUPPORTED, "float edge weights not set (mg_graph_set_float_weights)");
+        if (!g->symmetric) return fail(MG_ERR_UNSUPPORTED, "weighted PageRank needs a structurally symmetric graph");
+        MG_TRY(dev_alloc(w->S, n * 4));
+        a.S = w->S.as<float>();
+    }
+    return MG_OK;
+}
+
+// transposed float weights: wT[pos of (v,u) in row v] = w[pos of (u,v) in row u]
+__global__ void k_transpose_weights(int32_t n, const int32_t *row, const int32_t *col, const float *w, float *wT)
+{
+    for (int32_t u = blockIdx.x * blockDim.x + threadIdx.x; u < n; u += gridDim.x * blockDim.x) {
+        for (int32_t p = row[u]; p < row[u + 1]; p++) {
+            int32_t v = col[p];
+            // binary search u in row v (columns ascending)
+            int32_t lo = row[v], hi = row[v + 1] - 1, q = -1;
+            while (lo <= hi) {
+                int32_t mid = (lo + hi) >> 1;
+                int32_t cm = col[mid];
+                if (cm == u) { q = mid; break; }
+                if (cm < u) lo = mid + 1; else hi = mid - 1;
+            }
+            if (q >= 0) wT[q] = w[p];
+        }
+    }
+}
+
+}  // namespace mgi
+
+using namespace mgi;
+
+extern "C" {
+
+mg_status mg_pagerank(mg_graph *g, int32_t variant, const mg_opts *o, float *rank_out, mg_run_info *info)
+{
+    mg_opts opt;
+    MG_TRY(begin_run(g, o, opt, info));
+    if (variant < 0 || variant > 3) return fail(MG_ERR_INVALID, "unknown PageRank variant %d", variant);
+    PArgs a;
+    MG_TRY(pr_setup(g, a, false));
+    cudaStream_t s = g->stream;
+    const int grid = a.nblocks;
+    const bool ref = variant == MG_PR_TOPOLOGY_REF || variant == MG_PR_DATA_REF;
+    float d = opt.damping > 0 ? opt.damping : 0.85f;
+    float tol = opt.tol > 0 ? opt.tol : 1e-6f;
+    int max_iter = opt.max_iter > 0 ? opt.max_iter : 10000;
+    // dangling mass of the start vector: (#zero out-degree) / n
+    double dang0 = (!ref && g->nv > 0) ? (double)g->n_dangling / g->nv : 0.0;
+    float x0 = ref ? 0.0f : (g->nv > 0 ? 1.0f / g->nv : 0.0f);
+    k_pr_ctl_init<<<1, 32, 0, s>>>(a.ctl, g->nv, max_iter, d, tol, dang0, 0.0);
+    int cur = 0;
+    switch (variant) {
+    case MG_PR_TOPOLOGY_REF:
+        k_pr_init<V_T_REF><<<grid, THREADS, 0, s>>>(a, x0);
+        MG_TRY(pr_loop<V_T_REF>(g, a, opt, "pr_pull", info, &cur));
+        break;
+    case MG_PR_DATA_REF:
+        k_pr_init<V_D_REF><<<grid, THREADS, 0, s>>>(a, x0);
+        MG_TRY(pr_loop<V_D_REF>(g, a, opt, "pr_pull", info, &cur));
+        break;
+    case MG_PR_TOPOLOGY:
+        k_pr_init<V_T><<<grid, THREADS, 0, s>>>(a, x0);
+        MG_TRY(pr_loop<V_T>(g, a, opt, "pr_pull", info, &cur));
+        break;
+    default:
+        k_pr_init<V_D><<<grid, THREADS, 0, s>>>(a, x0);
+        MG_TRY(pr_loop<V_D>(g, a, opt, "pr_pull", info, &cur));
+        break;
+    }
+    MG_TRY(end_run(g, opt, info));
+    g->res[MG_RES_RANK] = a.x[cur];
+    return copy_out(g, rank_out, a.x[cur], (size_t)g->nv * 4);
+}
+
+mg_status mg_wpagerank(mg_graph *g, const mg_opts *o, float *x_out, mg_run_info *info)
+{
+    mg_opts opt;
+    MG_TRY(begin_run(g, o, opt, info));
+    PArgs a;
+    MG_TRY(pr_setup(g, a, true));
+    PrWS *w = g->pws;
+    cudaStream_t s = g->stream;
+    const int grid = a.nblocks;
+    const size_t n = (size_t)std::max(g->nv, 1), m = (size_t)std::max(g->ne, 1);
+    MG_TRY(dev_alloc(w->wT, m * 4 + 16));  // 16 bytes of tail padding for aligned staging
+    MG_TRY(dev_alloc(w->xkeep, n * 4));
+    k_row_sums<<<grid, THREADS, 0, s>>>(g->nv, g->row.as<int32_t>(), g->fw.as<float>(), a.S);
+    k_transpose_weights<<<grid, THREADS, 0, s>>>(g->nv, g->row.as<int32_t>(), g->col.as<int32_t>(), g->fw.as<float>(),
+                                                  w->wT.as<float>());
+    a.pw = w->wT.as<float>();
+    float d = opt.damping > 0 ? opt.damping : 0.85f;
+    float tol = opt.tol > 0 ? opt.tol : 1e-6f;
+    int max_iter = opt.max_iter > 0 ? opt.max_iter : 10000;
+    // rows without out-edges are dangling (their mass is spread uniformly)
+    float x0 = g->nv > 0 ? 1.0f / g->nv : 0.0f;
+    k_pr_ctl_init<<<1, 32, 0, s>>>(a.ctl, g->nv, max_iter, d, tol, g->nv ? (double)g->n_dangling / g->nv : 0.0, 0.0);
+    k_pr_init<V_WEIGHTED><<<grid, THREADS, 0, s>>>(a, x0);
+    int cur = 0;
+    MG_TRY(pr_loop<V_WEIGHTED>(g, a, opt, "wpr_pull", info, &cur));
+    MG_CUDA(cudaMemcpyAsync(w->xkeep.p, a.x[cur], (size_t)g->nv * 4, cudaMemcpyDeviceToDevice, s));
+    MG_TRY(end_run(g, opt, info));
+    g->res[MG_RES_RANK] = w->xkeep.p;
+    return copy_out(g, x_out, w->xkeep.p, (size_t)g->nv * 4);
+}
+
+mg_status mg_wpagerank_backward(mg_graph *g, const float *g_host, const mg_opts *o, float *grad_w_out,
+                                float *lambda_out, mg_run_info *info)
+{
+    mg_opts opt;
+    MG_TRY(begin_run(g, o, opt, info));
+    if (!g_host && g->nv > 0) return fail(MG_ERR_INVALID, "null loss weights");
+    if (!g->pws || !g->pws->xkeep.p || !g->pws->wT.p) return fail(MG_ERR_INVALID, "run mg_wpagerank first");
+    PArgs a;
+    MG_TRY(pr_setup(g, a, true));
+    PrWS *w = g->pws;
+    cudaStream_t s = g->stream;
+    const int grid = a.nblocks;
+    const size_t n = (size_t)std::max(g->nv, 1), m = (size_t)std::max(g->ne, 1);
+    MG_TRY(dev_alloc(w->gvec, n * 4));
+    MG_TRY(dev_alloc(w->grad, m * 4));
+    MG_TRY(dev_alloc(w->lam_keep, n * 4));
+    if (g->nv) MG_CUDA(cudaMemcpyAsync(w->gvec.p, g_host, (size_t)g->nv * 4, cudaMemcpyHostToDevice, s));
+    k_row_sums<<<grid, THREADS, 0, s>>>(g->nv, g->row.as<int32_t>(), g->fw.as<float>(), a.S);
+    // lambda = g + d * P lambda : rows of P are the CSR rows (out-edges) with weights w
+    a.prow = g->row.as<int32_t>();
+    a.pcol = g->col.as<int32_t>();
+    a.pw = g->fw.as<float>();
+    a.gvec = w->gvec.as<float>();
+    float d = opt.damping > 0 ? opt.damping : 0.85f;
+    float tol = opt.tol > 0 ? opt.tol : 1e-6f;
+    int max_iter = opt.max_iter > 0 ? opt.max_iter : 10000;
+    // initial mean of lambda = mean of g (for dangling rows)
+    std::vector<float> gh(g_host, g_host + g->nv);
+    double gm = 0.0;
+    for (float v : gh) gm += v;
+    gm = g->nv ? gm / g->nv : 0.0;
+    k_pr_ctl_init<<<1, 32, 0, s>>>(a.ctl, g->nv, max_iter, d, tol, 0.0, gm);
+    k_pr_init<V_ADJ><<<grid, THREADS, 0, s>>>(a, 0.0f);
+    int cur = 0;
+    MG_TRY(pr_loop<V_ADJ>(g, a, opt, "wpr_adjoint", info, &cur));
+    float *lam = a.c[cur];
+    MG_CUDA(cudaMemcpyAsync(w->lam_keep.p, lam, (size_t)g->nv * 4, cudaMemcpyDeviceToDevice, s));
+    int sg = g->prof.slot("wpr_grad");
+    g->prof.begin(sg);
+    k_wpr_grad<<<grid, THREADS, 0, s>>>(g->nv, g->row.as<int32_t>(), g->col.as<int32_t>(), g->fw.as<float>(), a.S,
+                                        w->xkeep.as<float>(), w->lam_keep.as<float>(), d, w->grad.as<float>());
+    g->prof.end();
+    MG_CUDA(cudaGetLastError());
+    MG_TRY(end_run(g, opt, info));
+    MG_TRY(copy_out(g, lambda_out, w->lam_keep.p, (size_t)g->nv * 4));
+    return copy_out(g, grad_w_out, w->grad.p, (size_t)g->ne * 4);
+}
+
+mg_status mg_ppr_batch(mg_graph *g, const int32_t *seeds, int32_t nseeds, const mg_opts *o, float *out,
+                       mg_run_info *info)
+{
+    mg_opts opt;
+    MG_TRY(begin_run(g, o, opt, info));
+    if (nseeds < 0 || (nseeds > 0 && !seeds)) return fail(MG_ERR_INVALID, "invalid seeds");
+    for (int32_t i = 0; i < nseeds; i++)
+        if (seeds[i] < 0 || seeds[i] >= g->nv) return fail(MG_ERR_RANGE, "seed %d out of range", seeds[i]);
+    if (!g->ppws) g->ppws = new PprWS();
+    PprWS *w = g->ppws;
+    const size_t n = (size_t)std::max(g->nv, 1);
+    const int grid = launch_grid(g, THREADS, 8);
+    cudaStream_t s = g->stream;
+    // heavy-row chunk table for PPR (built once per graph from the pull offsets)
+    if (g->ppr_nhchunks < 0) {
+        std::vector<int32_t> pr(n + 1);
+        MG_CUDA(cudaMemcpyAsync(pr.data(), g->trow, (size_t)(g->nv + 1) * 4, cudaMemcpyDeviceToHost, s));
+        MG_CUDA(cudaStreamSynchronize(s));
+        std::vector<int32_t> hc, hr, hrc{0};
+        for (int32_t v = 0; v < g->nv; v++) {
+            if (pr[v + 1] - pr[v] <= PPR_HEAVY) continue;
+            hr.push_back(v);
+            for (int32_t b = pr[v]; b < pr[v + 1]; b += PPR_HEAVY) {
+                hc.push_back(v); hc.push_back(b); hc.push_back(std::min(pr[v + 1], b + PPR_HEAVY));
+            }
+            hrc.push_back((int32_t)(hc.size() / 3));
+        }
+        MG_TRY(dev_alloc(g->ppr_hchunk, std::max<size_t>(hc.size(), 3) * 4));
+        MG_TRY(dev_alloc(g->ppr_hrows, std::max<size_t>(hr.size(), 1) * 4));
+        MG_TRY(dev_alloc(g->ppr_hrow_chunk, hrc.size() * 4));
+        if (!hc.empty()) MG_CUDA(cudaMemcpyAsync(g->ppr_hchunk.p, hc.data(), hc.size() * 4, cudaMemcpyHostToDevice, s));
+        if (!hr.empty()) MG_CUDA(cudaMemcpyAsync(g->ppr_hrows.p, hr.data(), hr.size() * 4, cudaMemcpyHostToDevice, s));
+        MG_CUDA(cudaMemcpyAsync(g->ppr_hrow_chunk.p, hrc.data(), hrc.size() * 4, cudaMemcpyHostToDevice, s));
+        MG_CUDA(cudaStreamSynchronize(s));
+        g->ppr_nhchunks = (int32_t)(hc.size() / 3);
+        g->ppr_nhrows = (int32_t)hr.size();
+    }
+    MG_TRY(dev_alloc(w->X0, n * 32 * 4));
+    MG_TRY(dev_alloc(w->X1, n * 32 * 4));
+    MG_TRY(dev_alloc(w->C0, n * 32 * 4));
+    MG_TRY(dev_alloc(w->C1, n * 32 * 4));
+    MG_TRY(dev_alloc(w->seeds, (size_t)std::max(nseeds, 1) * 4));
+    MG_TRY(dev_alloc(w->ctl, sizeof(PPCtl)));
+    MG_TRY(dev_alloc(w->bpart, (size_t)2 * grid * 32 * 2 * 8));
+    MG_TRY(dev_alloc(w->dang, 32 * 8));
+    MG_TRY(dev_alloc(w->hpart, (size_t)std::max(g->ppr_nhchunks, 1) * 32 * 4));
+    MG_TRY(dev_alloc(w->out, (size_t)std::max(nseeds, 1) * n * 4));
+    if (nseeds) MG_CUDA(cudaMemcpyAsync(w->seeds.p, seeds, (size_t)nseeds * 4, cudaMemcpyHostToDevice, s));
+    float tol = opt.tol > 0 ? opt.tol : 1e-6f;
+    int max_iter = opt.max_iter > 0 ? opt.max_iter : 10000;
+    PPArgs a;
+    std::memset(&a, 0, sizeof(a));
+    a.n = g->nv;
+    a.prow = g->trow; a.pcol = g->tcol; a.outrow = g->row.as<int32_t>();
+    a.hchunk = g->ppr_hchunk.as<int32_t>(); a.nhchunks = g->ppr_nhchunks;
+    a.hrows = g->ppr_hrows.as<int32_t>(); a.hrow_chunk = g->ppr_hrow_chunk.as<int32_t>(); a.nhrows = g->ppr_nhrows;
+    a.X0 = w->X0.as<float>(); a.X1 = w->X1.as<float>(); a.C0 = w->C0.as<float>(); a.C1 = w->C1.as<float>();
+    a.hpart = w->hpart.as<float>();
+    a.bpart = w->bpart.as<double>();
+    a.dang = w->dang.as<double>();
+    a.ctl = w->ctl.as<PPCtl>();
+    a.damping = opt.damping > 0 ? opt.damping : 0.85f;
+    Profiler &P = g->prof;
+    const int sl = P.slot("ppr_pull"), sh = P.slot("ppr_heavy"), sf = P.slot("ppr_finish");
+    int32_t total_iters = 0;
+    double max_resid = 0.0;
+    for (int32_t s0 = 0; s0 < nseeds; s0 += 32) {
+        a.nseed = std::min(32, nseeds - s0);
+        a.seeds = w->seeds.as<int32_t>() + s0;
+        k_ppr_init<<<grid, THREADS, 0, s>>>(a, max_iter);
+        BodyFn body = [&](cudaStream_t st, cudaGraphConditionalHandle h, int use_cond) -> mg_status {
+            P.begin(sl);
+            k_ppr_sweep<<<grid, THREADS, 0, st>>>(a);
+            P.end();
+            P.begin(sh);
+            k_ppr_heavy<<<grid, THREADS, 0, st>>>(a);
+            P.end();
+            P.begin(sf);
+            k_ppr_finish<<<1, 32, 0, st>>>(a, 2 * grid, tol, h, use_cond);
+            P.end();
+            MG_CUDA(cudaGetLastError());
+            return MG_OK;
+        };
+        uint64_t key = 0x51ed270b27ull ^ (uint64_t)(uintptr_t)a.seeds ^ ((uint64_t)a.nseed << 48) ^
+                       ((uint64_t)(uintptr_t)a.X0 * 3) ^ ((uint64_t)(uintptr_t)a.hpart * 7) ^ ((uint64_t)(uintptr_t)a.ctl * 11);
+        MG_TRY(run_loop(opt.profile ? MG_EXEC_HOST : opt.exec, opt.profile != 0, s, w->lg, key, body, &a.ctl->more,
+                        g->pinned_flag, max_iter + 2));
+        PPCtl hc;
+        MG_CUDA(cudaMemcpyAsync(&hc, w->ctl.p, sizeof(PPCtl), cudaMemcpyDeviceToHost, s));
+        MG_CUDA(cudaStreamSynchronize(s));
+        if (hc.status) return fail(MG_ERR_ITER_LIMIT, "PPR did not converge in %d sweeps", max_iter);
+        total_iters += hc.iter;
+        for (int i = 0; i < a.nseed; i++) max_resid = std::max(max_resid, hc.resid[i]);
+        const float *X = hc.cur ? a.X1 : a.X0;
+        k_ppr_store<<<grid, THREADS, 0, s>>>(g->nv, X, a.nseed, s0, w->out.as<float>());
+        MG_CUDA(cudaGetLastError());
+    }
+    MG_TRY(end_run(g, opt, info));
+    if (info) { info->iterations = total_iters; info->residual = max_resid; }
+    return copy_out(g, out, w->out.p, (size_t)nseeds * g->nv * 4);
+}
+}  // extern "C"

@@ -1,0 +1,124 @@
+// mg_tune.cu -- autotuner for the sparse/dense (push/pull) switch.
+//
+// The reference decides between its sparse and dense paths with a runtime
+// sampler that times a pseudo iteration of each (process.cu:1115-1246,
+// pseudo_phase1/11/2 and pseudo_process_f1 with real side effects) and with
+// compile-time constants (common.h:10-52: DENSE_THRESHOLD, sampling factors).
+// Here the switch rule is fixed (Beamer's frontier-edges vs unvisited-edges
+// test for BFS/BC, frontier-edges vs m for SSSP) and its two thresholds are
+// tuned per graph: every candidate runs the real traversal in a CUDA graph,
+// the median of three timed runs decides, and the winner is cached in a text
+// file keyed by a graph signature (n, m and a log2 degree histogram).
+
+#include "mg_device.cuh"
+
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+namespace {
+
+uint64_t graph_signature(mg_graph *g)
+{
+    std::vector<int32_t> row(g->nv + 1);
+    cudaMemcpy(row.data(), g->row.p, (size_t)(g->nv + 1) * 4, cudaMemcpyDeviceToHost);
+    uint64_t hist[33] = {0};
+    for (int32_t v = 0; v < g->nv; v++) {
+        int32_t d = row[v + 1] - row[v];
+        int b = 0;
+        while (d > 0) { b++; d >>= 1; }
+        hist[b]++;
+    }
+    uint64_t h = 1469598103934665603ull;
+    auto mix = [&](uint64_t x) { h = (h ^ x) * 1099511628211ull; };
+    mix((uint64_t)g->nv);
+    mix((uint64_t)g->ne);
+    for (uint64_t x : hist) mix(x);
+    return h;
+}
+
+bool cache_lookup(const char *path, uint64_t sig, int algo, mg_opts *o)
+{
+    if (!path) return false;
+    FILE *f = std::fopen(path, "r");
+    if (!f) return false;
+    char line[256];
+    bool found = false;
+    while (std::fgets(line, sizeof(line), f)) {
+        unsigned long long s;
+        int a, alpha, beta, dir;
+        if (std::sscanf(line, "%llx %d %d %d %d", &s, &a, &alpha, &beta, &dir) == 5 && s == sig && a == algo) {
+            o->alpha = alpha;
+            o->beta = beta;
+            o->direction = dir;
+            found = true;  // the last entry wins
+        }
+    }
+    std::fclose(f);
+    return found;
+}
+
+void cache_store(const char *path, uint64_t sig, int algo, const mg_opts &o, double ms)
+{
+    if (!path) return;
+    FILE *f = std::fopen(path, "a");
+    if (!f) return;
+    std::fprintf(f, "%llx %d %d %d %d %.4f\n", (unsigned long long)sig, algo, o.alpha, o.beta, o.direction, ms);
+    std::fclose(f);
+}
+
+}  // namespace
+
+extern "C" mg_status mg_autotune(mg_graph *g, int32_t algo, int32_t source, const char *cache_path, mg_opts *tuned)
+{
+    mgi::clear_error();
+    if (!g || !tuned) return mgi::fail(MG_ERR_INVALID, "null argument");
+    if (algo != MG_ALGO_BFS && algo != MG_ALGO_SSSP && algo != MG_ALGO_BC)
+        return mgi::fail(MG_ERR_UNSUPPORTED, "nothing to tune for algorithm %d", algo);
+    if (source < 0 || source >= g->nv) return mgi::fail(MG_ERR_RANGE, "source out of range");
+    MG_CUDA(cudaSetDevice(g->device));
+    mg_opts base = *tuned;
+    uint64_t sig = graph_signature(g);
+    if (cache_lookup(cache_path, sig, algo, tuned)) return MG_OK;
+
+    struct Cand { int alpha, beta, dir; };
+    std::vector<Cand> cands;
+    if (algo == MG_ALGO_SSSP) {
+        for (int a : {1, 2, 4, 8, 16, 64}) cands.push_back({a, 18, MG_DIR_AUTO});
+        cands.push_back({4, 18, MG_DIR_PUSH});
+    } else {
+        for (int a : {4, 8, 15, 30, 60})
+            for (int b : {6, 18, 54}) cands.push_back({a, b, MG_DIR_AUTO});
+        cands.push_back({15, 18, MG_DIR_PUSH});
+    }
+    double best_ms = 1e30;
+    Cand best = cands[0];
+    for (const Cand &c : cands) {
+        mg_opts o = base;
+        o.alpha = c.alpha;
+        o.beta = c.beta;
+        o.direction = c.dir;
+        o.exec = MG_EXEC_GRAPH;
+        o.profile = 0;
+        std::vector<double> t;
+        for (int rep = 0; rep < 4; rep++) {
+            mg_run_info info;
+            mg_status s;
+            if (algo == MG_ALGO_BFS) s = mg_bfs(g, source, &o, nullptr, &info);
+            else if (algo == MG_ALGO_SSSP) s = mg_sssp(g, source, &o, nullptr, &info);
+            else s = mg_bc(g, source, &o, nullptr, nullptr, nullptr, &info);
+            if (s != MG_OK) return s;
+            if (rep > 0) t.push_back(info.device_ms);  // first run warms the graph
+        }
+        std::sort(t.begin(), t.end());
+        double med = t[t.size() / 2];
+        if (med < best_ms) { best_ms = med; best = c; }
+    }
+    tuned->alpha = best.alpha;
+    tuned->beta = best.beta;
+    tuned->direction = best.dir;
+    cache_store(cache_path, sig, algo, *tuned, best_ms);
+    return MG_OK;
+}

@@ -1,0 +1,95 @@
+/*
+ * mg_oracle.h -- CPU oracle for the frontier-processing path.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This library is the checker: it restates, in
+ * plain C, the CPU algorithms of the reference's code/validate.cu and the
+ * MTX loader of code/read_input.cu, plus the FP64 extensions the accuracy
+ * contracts need (FP64-sigma Brandes, normalised / personalised PageRank and
+ * the PageRank edge-weight adjoint).  Only the tests, the smoke check and the
+ * CPU-baseline leg of bench.py may load it; the product library never does.
+ *
+ * Parity pins: the loader and the BFS / SSSP / CC / PR outputs of this
+ * restatement are checked against the reference's own generate_CSC and
+ * verifyResults, compiled from the reference sources by oracle/Makefile into
+ * oracle/_ref/ (see tests/test_oracle_ref.py and tests/golden/).
+ */
+#ifndef MG_ORACLE_H
+#define MG_ORACLE_H
+
+#include <stdint.h>
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* 0x64646464: the reference's "unreached" label (common.h:37-39). */
+#define ORC_IUNUSED 0x64646464
+
+/* loader flags (read_input.cu:31-44, :111-113) */
+#define ORC_LOAD_SYM     1u  /* -DSYM: force symmetric */
+#define ORC_LOAD_NSYM    2u  /* -DNSYM: force general */
+#define ORC_LOAD_CC      4u  /* -DCC: keep only src<dst edges */
+
+typedef struct orc_csr {
+    int32_t nv, ne;        /* after dedup + compaction                 */
+    int32_t start_p;       /* source renumbered through compaction     */
+    int32_t tra;           /* any degree >= 128 (read_input.cu:169)     */
+    int32_t *csc_v;        /* [nv+1]                                    */
+    int32_t *csc_e;        /* [ne]                                      */
+    int32_t *csc_ev;       /* [ne] integer weights                      */
+} orc_csr;
+
+/* Status codes shared with the product library's mg_status values. */
+enum { ORC_OK = 0, ORC_ERR_IO = 1, ORC_ERR_PARSE = 2, ORC_ERR_RANGE = 3, ORC_ERR_OOM = 4 };
+
+/* read_input.cu:11-254.  Pattern files get weights 1 + (splitmix64(seed ^ i) % 64)
+ * where i is the 0-based entry index in the file (the reference uses rand()
+ * seeded by time(), which is not reproducible). */
+int  orc_load_mtx(const char *path, int32_t source, uint32_t flags, uint64_t seed, orc_csr *out);
+void orc_csr_free(orc_csr *g);
+uint32_t orc_pattern_weight(uint64_t seed, uint64_t entry);
+
+/* validate.cu:106-130 -- FIFO BFS levels, ORC_IUNUSED for unreached. */
+void orc_bfs(const orc_csr *g, int32_t src, int32_t *level);
+/* validate.cu:131-148 -- Bellman-Ford sweeps in vertex order.  Returns sweeps. */
+int  orc_sssp(const orc_csr *g, int32_t src, int32_t *dist, int32_t max_sweeps);
+/* validate.cu:149-189 -- Brandes: int sigma, float delta (reference types). */
+void orc_bc(const orc_csr *g, int32_t src, int32_t *level, int32_t *sigma, float *delta);
+/* FP64 extension: sigma and delta in double. */
+void orc_bc_f64(const orc_csr *g, int32_t src, int32_t *level, double *sigma, double *delta);
+/* Multi-source BC scores: sum over sources of delta_s(v), v != s, FP64. */
+void orc_bc_multi_f64(const orc_csr *g, const int32_t *src, int32_t nsrc, double *bc);
+/* validate.cu:223-273 -- min-label propagation to the fixed point (labels = min id). */
+int  orc_cc_minlabel(const orc_csr *g, int32_t *label);
+/* validate.cu:234-242 / :263-273 -- relabel by first appearance, in place. */
+void orc_cc_relabel(int32_t nv, int32_t *label);
+/* validate.cu:34-91 -- reference PR recurrence in FP32 (PR_T: mode 0, PR_D: mode 1).
+ * Returns the number of sweeps. */
+int  orc_pr_ref(const orc_csr *g, int mode, float *pr, int32_t max_iter);
+/* same recurrence in FP64 */
+int  orc_pr_ref_f64(const orc_csr *g, int mode, double *pr, int32_t max_iter);
+/* Normalised PageRank in FP64: x' = (1-d)/n + d*(sum_u x_u/deg_u + dangling/n).
+ * Jacobi sweeps from x = 1/n until the L1 change <= tol.  Returns sweeps. */
+int  orc_pr_norm_f64(const orc_csr *g, double damping, double tol, int32_t max_iter, double *x);
+/* Personalised PageRank (one-hot seed): x' = (1-d)*e_seed + d*(P^T x + dangling*e_seed). */
+int  orc_ppr_f64(const orc_csr *g, int32_t seed, double damping, double tol, int32_t max_iter, double *x);
+
+/* Weighted PageRank and its adjoint (FP64).  w[e] is the weight of CSR entry e
+ * (row u -> col v).  P_uv = w_uv / S_u with S_u the row sum.
+ *   forward : x = (1-d)/n + d * P^T x
+ *   loss    : L = sum_i g_i x_i
+ *   adjoint : lambda = g + d * P lambda
+ *   grad_w  : dL/dw_e = (d x_u / S_u) * (lambda_v - sum_k P_uk lambda_k)
+ *   grad_p  : dL/dP_e = d x_u lambda_v                                    */
+int    orc_wpr_f64(const orc_csr *g, const double *w, double damping, double tol, int32_t max_iter, double *x);
+int    orc_wpr_adjoint_f64(const orc_csr *g, const double *w, const double *x, const double *gvec,
+                           double damping, double tol, int32_t max_iter, double *lambda,
+                           double *grad_w, double *grad_p);
+double orc_wpr_loss_f64(const orc_csr *g, const double *w, const double *gvec, double damping,
+                        double tol, int32_t max_iter);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

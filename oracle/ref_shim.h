@@ -1,0 +1,25 @@
+/*
+ * ref_shim.h -- force-included when oracle/Makefile compiles the reference's
+ * read_input.cu and validate.cu into oracle/_ref/ (test infrastructure).
+ *
+ * 1. The reference's common.h uses the pre-Volta warp intrinsics (__shfl,
+ *    __shfl_up, __shfl_down, __ballot) that CUDA 13 removed; they appear only
+ *    in device helpers that the loader and validator never call, so they are
+ *    mapped to the *_sync forms purely to let the headers compile.
+ * 2. verifyResults (validate.cu:22,28,197,200) reads the results through
+ *    cudaMemcpyAsync.  The driver hands it host arrays, so the copy becomes a
+ *    host memcpy and the reference validator runs on a machine with no GPU.
+ */
+#pragma once
+#include <cuda_runtime.h>
+#include <string.h>
+#define __shfl(v, l) __shfl_sync(0xffffffffu, (v), (l))
+#define __shfl_up(v, d) __shfl_up_sync(0xffffffffu, (v), (d))
+#define __shfl_down(v, d) __shfl_down_sync(0xffffffffu, (v), (d))
+#define __ballot(p) __ballot_sync(0xffffffffu, (p))
+static inline cudaError_t ref_host_copy(void *d, const void *s, size_t n)
+{
+    memcpy(d, s, n);
+    return cudaSuccess;
+}
+#define cudaMemcpyAsync(d, s, n, k) ref_host_copy((d), (s), (n))

@@ -1,0 +1,111 @@
+"""GPU parity: every engine through the C ABI against the CPU oracle.
+
+Integer results (BFS levels, SSSP distances, CC labels, BC levels) must be
+bit-exact; PageRank within 1e-6 max-abs of the FP64 oracle (normalised form);
+BC sigma exact (integer-valued FP64) and delta within 1e-5 relative.
+"""
+import numpy as np
+import pytest
+
+import multigraph_gb300 as mg
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+DIRS = [mg.DIR_AUTO, mg.DIR_PUSH, mg.DIR_PULL]
+EXECS = [mg.EXEC_GRAPH, mg.EXEC_HOST]
+
+
+def _graphs():
+    out = []
+    for scale, seed in [(8, 1), (11, 2), (13, 3)]:
+        out.append((f"rmat{scale}", mg.HostGraph.rmat(scale, 16, seed=seed)))
+    out.append(("lattice48", mg.HostGraph.lattice(48, 40, 0.05, seed=5)))
+    # two components + isolated vertex dropped by compaction
+    src = [0, 1, 2, 4, 5, 6]
+    dst = [1, 2, 0, 5, 6, 7]
+    out.append(("twocomp", mg.HostGraph.from_entries(9, src, dst, [3, 1, 4, 1, 5, 9])))
+    # a general (non-symmetric) graph: pull kernels use the transpose
+    rng = np.random.default_rng(11)
+    s = rng.integers(0, 500, 4000)
+    d = (s + rng.integers(1, 40, 4000)) % 500
+    out.append(("general", mg.HostGraph.from_entries(500, s, d, rng.integers(1, 64, 4000), flags=mg.LOAD_NSYM)))
+    return out
+
+
+@pytest.fixture(scope="module")
+def graphs():
+    res = []
+    for name, h in _graphs():
+        rp, col, wt = h.arrays()
+        res.append((name, mg.Graph(h), O.csr_from_arrays(rp, col, wt), h))
+    yield res
+    for _, g, _, h in res:
+        g.free()
+        h.free()
+
+
+def _sources(og):
+    return sorted({0, og.nv // 2, og.nv - 1})
+
+
+@pytest.mark.parametrize("direction", DIRS)
+@pytest.mark.parametrize("exec_mode", EXECS)
+def test_bfs(graphs, direction, exec_mode):
+    for name, g, og, _ in graphs:
+        for s in _sources(og):
+            lv, info = g.bfs(s, direction=direction, exec=exec_mode)
+            ref = O.bfs(og, s)
+            assert np.array_equal(lv, ref), (name, s, int(np.sum(lv != ref)))
+
+
+@pytest.mark.parametrize("direction", DIRS)
+@pytest.mark.parametrize("exec_mode", EXECS)
+def test_sssp(graphs, direction, exec_mode):
+    for name, g, og, _ in graphs:
+        for s in _sources(og):
+            d, _ = g.sssp(s, direction=direction, exec=exec_mode)
+            ref, _ = O.sssp(og, s)
+            assert np.array_equal(d, ref), (name, s, int(np.sum(d != ref)))
+
+
+def test_cc(graphs):
+    for name, g, og, _ in graphs:
+        lab, _ = g.cc()
+        assert np.array_equal(lab, O.cc_minlabel(og)), name
+        assert np.array_equal(O.cc_relabel(lab), O.cc_relabel(O.cc_minlabel(og))), name
+
+
+@pytest.mark.parametrize("direction", DIRS)
+def test_bc_single(graphs, direction):
+    for name, g, og, _ in graphs:
+        if name == "general":
+            continue
+        for s in _sources(og):
+            (lv, sg, dl), _ = g.bc(s, direction=direction)
+            rlv, rsg, rdl = O.bc_f64(og, s)
+            assert np.array_equal(lv, rlv), (name, s)
+            assert np.array_equal(sg, rsg), (name, s)
+            den = np.maximum(np.abs(rdl), 1.0)
+            rel = float(np.max(np.abs(dl.astype(np.float64) - rdl) / den)) if og.nv else 0.0
+            assert rel < 1e-5, (name, s, rel)
+
+
+@pytest.mark.parametrize("exec_mode", EXECS)
+def test_pagerank_normalised(graphs, exec_mode):
+    for name, g, og, _ in graphs:
+        x, info = g.pagerank(mg.PR_TOPOLOGY, tol=1e-6, exec=exec_mode)
+        ref, it = O.pr_norm_f64(og, 0.85, 1e-6, info.iterations)
+        err = float(np.max(np.abs(x.astype(np.float64) - ref)))
+        assert err < 1e-6, (name, err)
+        assert abs(info.iterations - it) == 0, (name, info.iterations, it)
+
+
+def test_pagerank_reference_forms(graphs):
+    for name, g, og, _ in graphs:
+        for variant, mode in [(mg.PR_TOPOLOGY_REF, 0), (mg.PR_DATA_REF, 1)]:
+            x, info = g.pagerank(variant)
+            ref, it = O.pr_ref_f64(og, mode)
+            t = np.maximum(np.abs(ref), 1e-12)
+            rel = float(np.max(np.abs(x - ref) / t))
+            assert rel < 0.05, (name, variant, rel)  # validate.cu:93-100 (THR = 5%)
