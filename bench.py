@@ -1,0 +1,294 @@
+#!/usr/bin/env python3
+"""Headline benchmark: SSSP + PageRank on R-MAT scale 22 (one step = one SSSP
+from vertex 0 plus one normalised topology-driven PageRank to L1 change 1e-6).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl mg|reference]
+
+Metric: GTEPS in the reference's convention (main.cu:46,154: directed edges
+per processing run / time), two runs per step.  One JSON line on rank 0:
+value (inputs resident in HBM), e2e (through the C ABI with pinned host CSR
+copied in and results copied out every step), roofline of the dominant
+kernel (the PageRank pull sweep), cpu_baseline (the oracle's restatement of
+validate.cu's CPU algorithms on this host), clocks sampled during the run.
+
+--impl reference times the reference's CPU implementation of the path (the
+oracle port of validate.cu: Bellman-Ford SSSP and the PageRank recurrence)
+on the host cores; rank 0 only.
+
+Multi-GPU: the path does not shard (one traversal per graph), so N GPUs run
+N independent replicas (weak scaling); value = all ranks' edges / max time.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+SCALE = 22
+EDGE_FACTOR = 16
+DAMPING = 0.85
+TOL = 1e-6
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=20)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="mg", choices=["mg", "reference"])
+    p.add_argument("--scale", type=int, default=SCALE)
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    return p.parse_args()
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled during the measurement."""
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,utilization.gpu,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons, load = [], None, set(), []
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 10:
+                continue
+            try:
+                s, mx, util = float(f[1]), float(f[2]), float(f[4])
+            except ValueError:
+                continue
+            smax = mx
+            if util > 0:
+                load.append(s)
+                for name, val in zip(["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"],
+                                     f[6:10]):
+                    if val.lower().startswith("active"):
+                        reasons.add(name)
+            sm.append(s)
+        use = load if load else sm
+        return {"sm_mhz": statistics.median(use) if use else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm), "samples_under_load": len(load)}
+
+
+def build_graph(scale):
+    import multigraph_gb300 as mg
+    return mg.HostGraph.rmat(scale, EDGE_FACTOR, seed=scale)
+
+
+def cpu_oracle_run(rp, col, wt, counts=None):
+    """The oracle's restatement of validate.cu on this host: Bellman-Ford SSSP
+    (validate.cu:131-148) and FP64 normalised PageRank.  Runs the full
+    workload (counts=None) or `counts = (sweeps, iterations)` of it."""
+    from oracle import oracle as O
+    g = O.csr_from_arrays(rp, col, wt)
+    t0 = time.perf_counter()
+    _, sweeps = O.sssp(g, 0, counts[0] if counts else 0)
+    t1 = time.perf_counter()
+    _, iters = O.pr_norm_f64(g, DAMPING, TOL, counts[1] if counts else 0)
+    t2 = time.perf_counter()
+    return t1 - t0, sweeps, t2 - t1, iters
+
+
+def reference_arm(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    h = build_graph(args.scale)
+    rp, col, wt = h.arrays()
+    m = int(len(col))
+    # one full run gives the sweep / iteration counts of the whole workload;
+    # timed steps are bounded samples (2 sweeps + 2 iterations) scaled to them
+    ts, S, tp, I = cpu_oracle_run(rp, col, wt)
+    step_times = []
+    for i in range(args.warmup + args.steps):
+        a, s, b, it = cpu_oracle_run(rp, col, wt, (2, 2))
+        est = a / s * S + b / it * I
+        if i >= args.warmup:
+            step_times.append(est)
+    t = statistics.median(step_times)
+    value = 2 * m / t / 1e9
+    line = {
+        "impl": "reference", "metric": "GTEPS", "value": value, "unit": "GTEPS", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "int32/fp64", "data": "synthetic",
+        "config": {"workload": f"rmat{args.scale}_ef{EDGE_FACTOR}: SSSP(src 0) + PageRank(d=0.85, L1 tol 1e-6)",
+                   "nv": h.nv, "ne": m},
+        "cpu_baseline": {"value": value, "unit": "GTEPS", "cores": 1, "kind": "port",
+                         "sample": f"full run once ({S} Bellman-Ford sweeps, {I} PageRank sweeps, "
+                                   f"{ts + tp:.1f} s); steps time 2 sweeps + 2 iterations, scaled to the full counts"},
+        "e2e": {"value": value, "unit": "GTEPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return reference_arm(args)
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    import torch
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    import __graft_entry__
+    __graft_entry__.build()
+    import multigraph_gb300 as mg
+
+    h = build_graph(args.scale)
+    h.pin()
+    g = mg.Graph(h, local)
+    n, m = g.nv, g.ne
+    stream = torch.cuda.ExternalStream(g.stream(), device=torch.device("cuda", local))
+    opts = mg.default_opts(tol=TOL, damping=DAMPING)
+
+    def step(out=False):
+        _, si = g.sssp(0, opts, out=out)
+        _, pi = g.pagerank(mg.PR_TOPOLOGY, opts, out=out)
+        return si, pi
+
+    for _ in range(args.warmup):
+        si, pi = step()
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.3)
+    # ---- device-resident timed region
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    launches = 0
+    for _ in range(args.steps):
+        si, pi = step()
+        # SSSP: init + (push, pull, decide) per iteration; PageRank: 2 inits + (sweep, apply) per sweep
+        launches += 1 + 3 * si.iterations + 2 + 2 * pi.iterations
+    e1.record(stream)
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    ms = e0.elapsed_time(e1)
+    if dist:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    ms_per_step = ms / args.steps
+    value = world * 2 * m * args.steps / (ms / 1e3) / 1e9
+
+    # ---- end to end through the C ABI: pinned host CSR in, results out
+    h2d = 4 * (n + 1) + 8 * m
+    d2h = 8 * n
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        g.reload(h)
+        step(out=True)
+    e2e_s = time.perf_counter() - t0
+    e2e_val = 2 * m * args.steps / e2e_s / 1e9
+
+    # ---- per-kernel times (cudaEvents around every launch, host-driven loop)
+    popts = mg.default_opts(tol=TOL, damping=DAMPING, profile=1)
+    kt = {}
+    for _ in range(max(1, min(args.steps, 5))):
+        for fn in (lambda: g.sssp(0, popts, out=False), lambda: g.pagerank(mg.PR_TOPOLOGY, popts, out=False)):
+            _, info = fn()
+            for k, (l, tms) in info.kernel_times().items():
+                a = kt.setdefault(k, [0, 0.0])
+                a[0] += l
+                a[1] += tms
+    clk = clocks.stop()
+
+    if rank != 0:
+        return 0
+    peak, peak_kind = peaks()
+    sweep = kt.get("pr_pull", [1, 0.0])
+    avg_ms = sweep[1] / max(sweep[0], 1)
+    alg_bytes = 4 * m + 4 * (n + 1) + 12 * n
+    achieved = alg_bytes / (avg_ms / 1e3) / 1e9 if avg_ms > 0 else None
+    traffic = None
+    try:
+        with open(os.path.join(ROOT, "profiles", "pr_sweep_traffic.json")) as f:
+            tr = json.load(f)
+        traffic = tr["dram_bytes_per_edge"] * m + tr["dram_bytes_per_vertex"] * n
+    except Exception:
+        pass
+    total_ms = sum(v[1] for v in kt.values())
+    cpu = None
+    if world == 1 and not args.no_cpu_baseline:
+        rp, col, wt = h.arrays()
+        ts, S, tp, I = cpu_oracle_run(rp, col, wt)
+        cpu = {"value": 2 * m / (ts + tp) / 1e9, "unit": "GTEPS", "cores": 1, "kind": "port",
+               "sample": f"one full step on the host: Bellman-Ford SSSP ({S} sweeps, {ts:.1f} s) + FP64 "
+                         f"PageRank ({I} sweeps, {tp:.1f} s), single thread as validate.cu"}
+    line = {
+        "metric": "GTEPS", "value": value, "unit": "GTEPS", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "int32/fp32", "data": "synthetic",
+        "config": {"workload": f"rmat{args.scale}_ef{EDGE_FACTOR}: SSSP(src 0) + PageRank(d=0.85, L1 tol 1e-6)",
+                   "nv": n, "ne": m, "sssp_iterations": si.iterations, "pr_sweeps": pi.iterations,
+                   "parallelism": f"replicas x{world}", "l2": "inputs (column ids + weights, 1 GB) exceed L2",
+                   "baseline_metric": "GTEPS & HBM GB/s vs peak (BASELINE.json)"},
+        "e2e": {"value": e2e_val, "unit": "GTEPS", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": (achieved / peak) if achieved else None, "traffic": traffic,
+                     "kernel": "k_pr_light (PageRank pull sweep)", "algorithmic_bytes": alg_bytes,
+                     "avg_launch_ms": avg_ms, "peak_kind": peak_kind,
+                     "kernel_share": (sweep[1] / total_ms) if total_ms else None},
+        "cpu_baseline": cpu,
+        "clocks": clk,
+        "gpu_launches": launches,
+        "kernel_ms": {k: {"launches": v[0], "total_ms": round(v[1], 4)} for k, v in kt.items()},
+    }
+    print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())
