@@ -65,7 +65,7 @@ __global__ void k_cc_init(int32_t n, const int32_t *row, const int32_t *col, int
     }
 }
 
-// per-edge union over the edge-balanced row groups (group_reduce interface;
+// per-edge union over the degree-binned rows (bins_reduce interface;
 // the reduction value is unused)
 struct HookOp {
     using T = int;
@@ -81,27 +81,20 @@ struct HookOp {
         return 0;
     }
     __device__ int combine(int, int) const { return 0; }
+    __device__ void flush() {}
     __device__ void finish(int32_t, int) {}
 };
 
 // one pass over the pull-side arrays; symmetric graphs take each undirected
 // edge once (u > v), general graphs every entry
 __global__ void __launch_bounds__(THREADS) k_cc_hook(int32_t n, const int32_t *prow, const int32_t *pcol,
-                                                     const int32_t *grp, int32_t ngroups, const int32_t *hchunk,
-                                                     int32_t nhchunks, int32_t heavy_deg, int symmetric,
-                                                     int32_t *parent)
+                                                     const int32_t *wrows, int32_t nwrows, const int32_t *trows,
+                                                     int32_t ntrows, const int32_t *hchunk, int32_t nhchunks,
+                                                     int32_t heavy_deg, int symmetric, int32_t *parent)
 {
-    const int gwarp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int nwarps = (gridDim.x * blockDim.x) >> 5;
-    __shared__ int32_t s_off[THREADS / 32][mgd::GROUP_ROWS + 1];
-    __shared__ __align__(16) int32_t s_col[THREADS / 32][mgd::GROUP_STAGE];
     HookOp op{parent, symmetric};
-    const mgd::GroupSmem sm{s_off[threadIdx.x >> 5], s_col[threadIdx.x >> 5], nullptr};
-    for (int32_t g = gwarp; g < ngroups; g += nwarps) {
-        int32_t r0 = grp[g], r1 = grp[g + 1];
-        if (r1 - r0 == 1 && prow[r1] - prow[r0] > heavy_deg) continue;  // heavy row: chunks below
-        mgd::group_reduce(op, prow, pcol, nullptr, r0, r1, sm);
-    }
+    (void)heavy_deg;
+    mgd::bins_reduce(op, prow, pcol, nullptr, wrows, nwrows, trows, ntrows);
     for (int32_t ch = blockIdx.x; ch < nhchunks; ch += gridDim.x) {
         int32_t u = hchunk[3 * ch], b = hchunk[3 * ch + 1], e = hchunk[3 * ch + 2];
         for (int32_t p = b + threadIdx.x; p < e; p += blockDim.x) {
@@ -151,8 +144,9 @@ mg_status cc_run(mg_graph *g, mg_run_info *info)
     k_cc_init<<<grid, THREADS, 0, s>>>(g->nv, g->trow, g->tcol, parent);
     P.end();
     P.begin(sh);
-    k_cc_hook<<<grid, THREADS, 0, s>>>(g->nv, g->trow, g->tcol, g->grp.as<int32_t>(), g->ngroups,
-                                       g->hchunk.as<int32_t>(), g->nhchunks, g->heavy_deg, g->symmetric ? 1 : 0, parent);
+    k_cc_hook<<<grid, THREADS, 0, s>>>(g->nv, g->trow, g->tcol, g->wrows.as<int32_t>(), g->nwrows,
+                                       g->trows.as<int32_t>(), g->ntrows, g->hchunk.as<int32_t>(), g->nhchunks,
+                                       g->heavy_deg, g->symmetric ? 1 : 0, parent);
     P.end();
     P.begin(sc);
     k_cc_compress<<<grid, THREADS, 0, s>>>(g->nv, parent);
@@ -186,9 +180,9 @@ mg_status mg_cc(mg_graph *g, const mg_opts *o, int32_t *label_out, mg_run_info *
     mg_opts opt;
     MG_TRY(begin_run(g, o, opt, info));
     MG_TRY(cc_run(g, info));
+    MG_TRY(cc_to_caller(g, g->cws->parent.as<int32_t>(), &g->res[MG_RES_LABEL]));
     MG_TRY(end_run(g, opt, info));
-    g->res[MG_RES_LABEL] = g->cws->parent.p;
-    return copy_out(g, label_out, g->cws->parent.p, (size_t)g->nv * 4);
+    return copy_out(g, label_out, g->res[MG_RES_LABEL], (size_t)g->nv * 4);
 }
 
 mg_status mg_batch_create(const mg_host_graph *const *graphs, int32_t count, int32_t device, mg_batch **out)
@@ -245,14 +239,14 @@ mg_status mg_batch_bfs(mg_batch *b, const int32_t *sources, const mg_opts *o, in
     for (size_t i = 0; i < srcs.size(); i++) {
         if (sources[i] < 0 || sources[i] >= b->local_nv[i])
             return fail(MG_ERR_RANGE, "source %d of graph %zu out of range", sources[i], i);
-        srcs[i] = b->voff[i] + sources[i];
+        srcs[i] = to_engine(b->dg, b->voff[i] + sources[i]);
     }
     mg_graph *g = b->dg;
     mg_opts opt;
     MG_TRY(begin_run(g, o, opt, info));
     MG_TRY(frontier_run_multi(g, 0, srcs.data(), (int32_t)srcs.size(), opt, info));
+    MG_TRY(to_caller(g, MG_RES_LEVEL, frontier_label(g), 4, 1, &g->res[MG_RES_LEVEL]));
     MG_TRY(end_run(g, opt, info));
-    g->res[MG_RES_LEVEL] = frontier_label(g);
     return copy_out(g, levels_out, g->res[MG_RES_LEVEL], (size_t)g->nv * 4);
 }
 
@@ -264,9 +258,10 @@ mg_status mg_batch_cc(mg_batch *b, const mg_opts *o, int32_t *labels_out, mg_run
     mg_opts opt;
     MG_TRY(begin_run(g, o, opt, info));
     MG_TRY(cc_run(g, info));
+    MG_TRY(cc_to_caller(g, g->cws->parent.as<int32_t>(), &g->res[MG_RES_LABEL]));
     MG_TRY(end_run(g, opt, info));
     if (!labels_out) return MG_OK;
-    MG_TRY(copy_out(g, labels_out, g->cws->parent.p, (size_t)g->nv * 4));
+    MG_TRY(copy_out(g, labels_out, g->res[MG_RES_LABEL], (size_t)g->nv * 4));
     for (size_t i = 0; i + 1 < b->voff.size(); i++)
         for (int32_t v = b->voff[i]; v < b->voff[i + 1]; v++) labels_out[v] -= b->voff[i];
     return MG_OK;

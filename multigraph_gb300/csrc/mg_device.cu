@@ -6,12 +6,13 @@
 // i1 written and re-read every dense iteration, ~12.5 B/edge) sized for
 // Kepler's 48 KB shared memory.  On GB300 the whole pull-side gather vector
 // of these graphs (n*4 B, <= 67 MB) stays in the 126 MB L2, so the layout here
-// is the CSR itself plus two small index tables that make the pull kernels
-// edge-balanced:
-//   grp    : groups of <= 32 consecutive rows holding <= GROUP_EDGES light
-//            edges -- one warp processes one group with coalesced reads;
-//   hchunk : rows with in-degree > heavy_deg split into HCHUNK-edge chunks,
-//            processed by whole CTAs and combined in a fixed order.
+// is the CSR itself, renumbered hub-first when the degrees are skewed (the
+// engine-order CSR is rebuilt on the device from the caller's CSR), plus
+// small index tables that balance the pull kernels:
+//   wrows / trows : degree bins -- rows of 33..512 in-edges (a warp each)
+//                   and rows of <= 32 in-edges (a thread each);
+//   hchunk        : rows with in-degree > heavy_deg split into HCHUNK-edge
+//                   chunks, processed by whole CTAs, combined in a fixed order.
 // A transposed copy is built only when the graph is not symmetric.
 
 #include "mg_device.cuh"
@@ -22,8 +23,7 @@
 
 namespace mgi {
 
-constexpr int32_t GROUP_EDGES = mgd::GROUP_EDGES;
-constexpr int32_t HEAVY_DEG = mgd::GROUP_EDGES;  // rows above one group's edges take the chunk path
+constexpr int32_t HEAVY_DEG = 512;                // pull rows above this take the CTA-chunk path
 constexpr int32_t HCHUNK = 2048;                  // = 8 edges x 256 threads of a chunk CTA
 // column / weight arrays carry this many bytes of readable tail padding (the
 // pull kernels stage column ids with aligned 16-byte loads)
@@ -226,15 +226,54 @@ using namespace mgi;
 // layout building (host side, O(n + m))
 // ---------------------------------------------------------------------------
 struct HostLayout {
-    std::vector<int32_t> trow, tcol, twt;  // transpose (empty when symmetric)
+    std::vector<int32_t> trow, tcol, twt;  // transpose in engine ids (empty when symmetric)
     bool symmetric = true, wsym = true;
-    std::vector<int32_t> grp, hchunk, hrows, hrow_chunk;
+    std::vector<int32_t> hchunk, hrows, hrow_chunk;
+    std::vector<int32_t> wrows, trows;  // degree bins (engine ids)
     int32_t n_dangling = 0, min_weight = 0;
+    // hub-first relabeling (engine id = rank by descending log2 out-degree)
+    bool relabel = false;
+    std::vector<int32_t> new2old, old2new, row_new;
 };
+
+// Hub-first order: vertices grouped by floor(log2(out-degree)), largest
+// group first, caller order kept inside a group (counting sort, O(n)).  The
+// reference reorders by degree groups when some degree reaches 128
+// (read_input.cu:169 sets `tra`, gen_structure.cu:2435-2556 builds _itable);
+// the same trigger is used here.  Hubs then sit at the lowest ids, so the
+// gathered values of the most frequently read sources share cache lines.
+static void hub_first_order(const mg_host_graph &h, std::vector<int32_t> &new2old, std::vector<int32_t> &old2new)
+{
+    const int32_t n = h.nv;
+    auto bucket = [&](int32_t v) {
+        int32_t d = h.v[v + 1] - h.v[v];
+        int b = 0;
+        while (d > 1) { d >>= 1; b++; }
+        return 31 - b;  // descending degree -> ascending key
+    };
+    std::vector<int32_t> cnt(33, 0);
+    for (int32_t v = 0; v < n; v++) cnt[bucket(v) + 1]++;
+    for (int i = 0; i < 32; i++) cnt[i + 1] += cnt[i];
+    new2old.resize(n);
+    old2new.resize(n);
+    for (int32_t v = 0; v < n; v++) {
+        int32_t p = cnt[bucket(v)]++;
+        new2old[p] = v;
+        old2new[v] = p;
+    }
+}
 
 static void build_layout(const mg_host_graph &h, HostLayout &L)
 {
     const int32_t n = h.nv, m = h.ne;
+    bool skewed = false;
+    for (int32_t v = 0; v < n && !skewed; v++) skewed = (h.v[v + 1] - h.v[v] >= 128);
+    L.relabel = skewed;
+    if (L.relabel) {
+        hub_first_order(h, L.new2old, L.old2new);
+        L.row_new.assign(n + 1, 0);
+        for (int32_t i = 0; i < n; i++) L.row_new[i + 1] = L.row_new[i] + (h.v[L.new2old[i] + 1] - h.v[L.new2old[i]]);
+    }
     // transpose by counting sort (rows come out with ascending columns)
     std::vector<int32_t> tr(n + 1, 0), tc(m), tw(m);
     for (int32_t i = 0; i < m; i++) tr[h.e[i] + 1]++;
@@ -250,8 +289,22 @@ static void build_layout(const mg_host_graph &h, HostLayout &L)
     }
     L.symmetric = std::equal(tr.begin(), tr.end(), h.v.begin()) && std::equal(tc.begin(), tc.end(), h.e.begin());
     L.wsym = L.symmetric && std::equal(tw.begin(), tw.end(), h.ev.begin());
-    if (!L.symmetric || !L.wsym) { L.trow.swap(tr); L.tcol.swap(tc); L.twt.swap(tw); }
-    const std::vector<int32_t> &prow = (!L.symmetric || !L.wsym) ? L.trow : h.v;
+    if (!L.symmetric || !L.wsym) {
+        if (L.relabel) {
+            // transpose in engine ids: row i' = transpose row new2old[i'], columns mapped
+            L.trow.assign(n + 1, 0);
+            for (int32_t i = 0; i < n; i++) L.trow[i + 1] = L.trow[i] + (tr[L.new2old[i] + 1] - tr[L.new2old[i]]);
+            L.tcol.resize(m);
+            L.twt.resize(m);
+            for (int32_t i = 0; i < n; i++) {
+                int32_t u = L.new2old[i], o = L.trow[i];
+                for (int32_t p = tr[u]; p < tr[u + 1]; p++, o++) { L.tcol[o] = L.old2new[tc[p]]; L.twt[o] = tw[p]; }
+            }
+        } else {
+            L.trow.swap(tr); L.tcol.swap(tc); L.twt.swap(tw);
+        }
+    }
+    const std::vector<int32_t> &prow = (!L.symmetric || !L.wsym) ? L.trow : (L.relabel ? L.row_new : h.v);
     L.n_dangling = 0;
     for (int32_t v = 0; v < n; v++) L.n_dangling += (h.v[v + 1] == h.v[v]);
     L.min_weight = m ? *std::min_element(h.ev.begin(), h.ev.end()) : 0;
@@ -269,23 +322,159 @@ static void build_layout(const mg_host_graph &h, HostLayout &L)
             L.hrow_chunk.push_back((int32_t)(L.hchunk.size() / 3));
         }
     }
-    // groups of <= GROUP_ROWS consecutive light rows with <= GROUP_EDGES
-    // edges (a single light row above the budget forms its own group); every
-    // heavy row is a one-row group that the light kernels skip
-    int32_t r = 0;
-    while (r < n) {
-        L.grp.push_back(r);
-        if (prow[r + 1] - prow[r] > HEAVY_DEG) { r++; continue; }
-        int32_t e = 0, k = 0;
-        while (r < n && k < mgd::GROUP_ROWS) {
-            int32_t d = prow[r + 1] - prow[r];
-            if (d > HEAVY_DEG) break;
-            if (k > 0 && e + d > GROUP_EDGES) break;
-            e += d; k++; r++;
+    // degree bins for the row-reduction kernels
+    for (int32_t v = 0; v < n; v++) {
+        int32_t d = prow[v + 1] - prow[v];
+        if (d > HEAVY_DEG) continue;
+        if (d > 32) L.wrows.push_back(v);
+        else L.trows.push_back(v);
+    }
+}
+
+// new row i' of the engine CSR = caller row new2old[i'] (same entry order);
+// column ids mapped through old2new when map_ids
+__global__ void k_relabel_edges(int32_t n, const int32_t *new2old, const int32_t *old2new, const int32_t *o_row,
+                                const uint32_t *src, const int32_t *row_new, uint32_t *dst, int map_ids)
+{
+    const int lane = threadIdx.x & 31;
+    for (int32_t i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < n; i += (gridDim.x * blockDim.x) >> 5) {
+        const int32_t u = new2old[i];
+        const int32_t b = o_row[u], len = o_row[u + 1] - b, o = row_new[i];
+        for (int32_t j = lane; j < len; j += 32) {
+            uint32_t x = src[b + j];
+            dst[o + j] = map_ids ? (uint32_t)old2new[x] : x;
         }
     }
-    L.grp.push_back(n);
 }
+
+// inverse of k_relabel_edges for per-edge payloads (engine order -> caller order)
+__global__ void k_unrelabel_edges(int32_t n, const int32_t *new2old, const int32_t *o_row, const uint32_t *src,
+                                  const int32_t *row_new, uint32_t *dst)
+{
+    const int lane = threadIdx.x & 31;
+    for (int32_t i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < n; i += (gridDim.x * blockDim.x) >> 5) {
+        const int32_t u = new2old[i];
+        const int32_t b = o_row[u], len = o_row[u + 1] - b, o = row_new[i];
+        for (int32_t j = lane; j < len; j += 32) dst[b + j] = src[o + j];
+    }
+}
+
+// caller-order result: dst[r*n + v] = src[r*n + old2new[v]]
+template <class T>
+__global__ void k_to_caller(int32_t n, int32_t rows, const int32_t *old2new, const T *src, T *dst)
+{
+    const size_t total = (size_t)n * rows;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
+        size_t r = i / n;
+        int32_t v = (int32_t)(i - r * n);
+        dst[i] = src[r * n + old2new[v]];
+    }
+}
+
+// CC labels: minimum caller id of every engine-space root, then per vertex
+__global__ void k_cc_min_old(int32_t n, const int32_t *parent, const int32_t *new2old, int32_t *minold)
+{
+    for (int32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x)
+        atomicMin(&minold[parent[v]], new2old[v]);
+}
+
+__global__ void k_cc_label_old(int32_t n, const int32_t *parent, const int32_t *old2new, const int32_t *minold,
+                               int32_t *out)
+{
+    for (int32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x)
+        out[v] = minold[parent[old2new[v]]];
+}
+
+static mg_status relabel_device(mg_graph *g)
+{
+    const int grid = g->num_sms * 8;
+    k_relabel_edges<<<grid, 256, 0, g->stream>>>(g->nv, g->new2old.as<int32_t>(), g->old2new.as<int32_t>(),
+                                                 g->o_row.as<int32_t>(), g->o_col.as<uint32_t>(), g->row.as<int32_t>(),
+                                                 g->col.as<uint32_t>(), 1);
+    k_relabel_edges<<<grid, 256, 0, g->stream>>>(g->nv, g->new2old.as<int32_t>(), g->old2new.as<int32_t>(),
+                                                 g->o_row.as<int32_t>(), g->o_wt.as<uint32_t>(), g->row.as<int32_t>(),
+                                                 g->wt.as<uint32_t>(), 0);
+    MG_CUDA(cudaGetLastError());
+    return MG_OK;
+}
+
+namespace mgi {
+
+int32_t to_engine(const mg_graph *g, int32_t v) { return g->relabeled ? g->h_old2new[v] : v; }
+
+mg_status to_caller(mg_graph *g, int which, const void *src, size_t elem, int32_t rows, const void **out)
+{
+    if (!g->relabeled) { *out = src; return MG_OK; }
+    const size_t total = (size_t)g->nv * rows;
+    MG_TRY(dev_alloc(g->res_out[which], std::max<size_t>(total, 1) * elem));
+    const int grid = g->num_sms * 8;
+    if (elem == 8)
+        k_to_caller<unsigned long long><<<grid, 256, 0, g->stream>>>(
+            g->nv, rows, g->old2new.as<int32_t>(), (const unsigned long long *)src, g->res_out[which].as<unsigned long long>());
+    else
+        k_to_caller<uint32_t><<<grid, 256, 0, g->stream>>>(g->nv, rows, g->old2new.as<int32_t>(),
+                                                           (const uint32_t *)src, g->res_out[which].as<uint32_t>());
+    MG_CUDA(cudaGetLastError());
+    *out = g->res_out[which].p;
+    return MG_OK;
+}
+
+mg_status vertices_to_engine(mg_graph *g, const void *src_caller, void *dst_engine)
+{
+    if (!g->relabeled) {
+        if (src_caller != dst_engine)
+            MG_CUDA(cudaMemcpyAsync(dst_engine, src_caller, (size_t)g->nv * 4, cudaMemcpyDeviceToDevice, g->stream));
+        return MG_OK;
+    }
+    k_to_caller<uint32_t><<<g->num_sms * 8, 256, 0, g->stream>>>(g->nv, 1, g->new2old.as<int32_t>(),
+                                                                 (const uint32_t *)src_caller, (uint32_t *)dst_engine);
+    MG_CUDA(cudaGetLastError());
+    return MG_OK;
+}
+
+mg_status cc_to_caller(mg_graph *g, const int32_t *parent, const void **out)
+{
+    if (!g->relabeled) { *out = parent; return MG_OK; }
+    const size_t n = (size_t)std::max(g->nv, 1);
+    MG_TRY(dev_alloc(g->res_out[MG_RES_LABEL], n * 4));
+    MG_TRY(dev_alloc(g->res_out[7], n * 4));
+    MG_CUDA(cudaMemsetAsync(g->res_out[7].p, 0x7f, n * 4, g->stream));
+    const int grid = g->num_sms * 8;
+    k_cc_min_old<<<grid, 256, 0, g->stream>>>(g->nv, parent, g->new2old.as<int32_t>(), g->res_out[7].as<int32_t>());
+    k_cc_label_old<<<grid, 256, 0, g->stream>>>(g->nv, parent, g->old2new.as<int32_t>(), g->res_out[7].as<int32_t>(),
+                                                g->res_out[MG_RES_LABEL].as<int32_t>());
+    MG_CUDA(cudaGetLastError());
+    *out = g->res_out[MG_RES_LABEL].p;
+    return MG_OK;
+}
+
+mg_status edges_to_engine(mg_graph *g, const void *src_caller, void *dst_engine)
+{
+    if (!g->relabeled) {
+        MG_CUDA(cudaMemcpyAsync(dst_engine, src_caller, (size_t)g->ne * 4, cudaMemcpyDeviceToDevice, g->stream));
+        return MG_OK;
+    }
+    k_relabel_edges<<<g->num_sms * 8, 256, 0, g->stream>>>(g->nv, g->new2old.as<int32_t>(), nullptr,
+                                                           g->o_row.as<int32_t>(), (const uint32_t *)src_caller,
+                                                           g->row.as<int32_t>(), (uint32_t *)dst_engine, 0);
+    MG_CUDA(cudaGetLastError());
+    return MG_OK;
+}
+
+mg_status edges_to_caller(mg_graph *g, const void *src_engine, void *dst_caller)
+{
+    if (!g->relabeled) {
+        MG_CUDA(cudaMemcpyAsync(dst_caller, src_engine, (size_t)g->ne * 4, cudaMemcpyDeviceToDevice, g->stream));
+        return MG_OK;
+    }
+    k_unrelabel_edges<<<g->num_sms * 8, 256, 0, g->stream>>>(g->nv, g->new2old.as<int32_t>(), g->o_row.as<int32_t>(),
+                                                             (const uint32_t *)src_engine, g->row.as<int32_t>(),
+                                                             (uint32_t *)dst_caller);
+    MG_CUDA(cudaGetLastError());
+    return MG_OK;
+}
+
+}  // namespace mgi
 
 static mg_status upload_arrays(mg_graph *g, const mg_host_graph *h, const HostLayout &L, bool alloc)
 {
@@ -294,21 +483,44 @@ static mg_status upload_arrays(mg_graph *g, const mg_host_graph *h, const HostLa
         MG_TRY(dev_alloc(g->row, (n + 1) * 4));
         MG_TRY(dev_alloc(g->col, std::max<size_t>(m, 4) * 4 + COL_PAD));
         MG_TRY(dev_alloc(g->wt, std::max<size_t>(m, 4) * 4 + COL_PAD));
+        if (L.relabel) {
+            MG_TRY(dev_alloc(g->o_row, (n + 1) * 4));
+            MG_TRY(dev_alloc(g->o_col, std::max<size_t>(m, 4) * 4 + COL_PAD));
+            MG_TRY(dev_alloc(g->o_wt, std::max<size_t>(m, 4) * 4 + COL_PAD));
+            MG_TRY(dev_alloc(g->old2new, std::max<size_t>(n, 1) * 4));
+            MG_TRY(dev_alloc(g->new2old, std::max<size_t>(n, 1) * 4));
+        }
         if (!L.trow.empty()) {
             MG_TRY(dev_alloc(g->trow_own, (n + 1) * 4));
             MG_TRY(dev_alloc(g->tcol_own, std::max<size_t>(m, 4) * 4 + COL_PAD));
             MG_TRY(dev_alloc(g->twt_own, std::max<size_t>(m, 4) * 4 + COL_PAD));
         }
-        MG_TRY(dev_alloc(g->grp, L.grp.size() * 4));
         MG_TRY(dev_alloc(g->hchunk, std::max<size_t>(L.hchunk.size(), 3) * 4));
         MG_TRY(dev_alloc(g->hrows, std::max<size_t>(L.hrows.size(), 1) * 4));
         MG_TRY(dev_alloc(g->hrow_chunk, L.hrow_chunk.size() * 4));
+        MG_TRY(dev_alloc(g->wrows, std::max<size_t>(L.wrows.size(), 1) * 4));
+        MG_TRY(dev_alloc(g->trows, std::max<size_t>(L.trows.size(), 1) * 4));
     }
     cudaStream_t s = g->stream;
-    MG_CUDA(cudaMemcpyAsync(g->row.p, h->v.data(), (n + 1) * 4, cudaMemcpyHostToDevice, s));
-    if (m) {
-        MG_CUDA(cudaMemcpyAsync(g->col.p, h->e.data(), m * 4, cudaMemcpyHostToDevice, s));
-        MG_CUDA(cudaMemcpyAsync(g->wt.p, h->ev.data(), m * 4, cudaMemcpyHostToDevice, s));
+    g->relabeled = L.relabel;
+    if (L.relabel) {
+        g->h_old2new = L.old2new;
+        MG_CUDA(cudaMemcpyAsync(g->old2new.p, L.old2new.data(), n * 4, cudaMemcpyHostToDevice, s));
+        MG_CUDA(cudaMemcpyAsync(g->new2old.p, L.new2old.data(), n * 4, cudaMemcpyHostToDevice, s));
+        MG_CUDA(cudaMemcpyAsync(g->row.p, L.row_new.data(), (n + 1) * 4, cudaMemcpyHostToDevice, s));
+        MG_CUDA(cudaMemcpyAsync(g->o_row.p, h->v.data(), (n + 1) * 4, cudaMemcpyHostToDevice, s));
+        if (m) {
+            MG_CUDA(cudaMemcpyAsync(g->o_col.p, h->e.data(), m * 4, cudaMemcpyHostToDevice, s));
+            MG_CUDA(cudaMemcpyAsync(g->o_wt.p, h->ev.data(), m * 4, cudaMemcpyHostToDevice, s));
+        }
+        g->nv = h->nv;
+        MG_TRY(relabel_device(g));
+    } else {
+        MG_CUDA(cudaMemcpyAsync(g->row.p, h->v.data(), (n + 1) * 4, cudaMemcpyHostToDevice, s));
+        if (m) {
+            MG_CUDA(cudaMemcpyAsync(g->col.p, h->e.data(), m * 4, cudaMemcpyHostToDevice, s));
+            MG_CUDA(cudaMemcpyAsync(g->wt.p, h->ev.data(), m * 4, cudaMemcpyHostToDevice, s));
+        }
     }
     if (!L.trow.empty()) {
         MG_CUDA(cudaMemcpyAsync(g->trow_own.p, L.trow.data(), (n + 1) * 4, cudaMemcpyHostToDevice, s));
@@ -320,14 +532,18 @@ static mg_status upload_arrays(mg_graph *g, const mg_host_graph *h, const HostLa
     } else {
         g->trow = g->row.as<int32_t>(); g->tcol = g->col.as<int32_t>(); g->twt = g->wt.as<int32_t>();
     }
-    MG_CUDA(cudaMemcpyAsync(g->grp.p, L.grp.data(), L.grp.size() * 4, cudaMemcpyHostToDevice, s));
     if (!L.hchunk.empty())
         MG_CUDA(cudaMemcpyAsync(g->hchunk.p, L.hchunk.data(), L.hchunk.size() * 4, cudaMemcpyHostToDevice, s));
     if (!L.hrows.empty())
         MG_CUDA(cudaMemcpyAsync(g->hrows.p, L.hrows.data(), L.hrows.size() * 4, cudaMemcpyHostToDevice, s));
     MG_CUDA(cudaMemcpyAsync(g->hrow_chunk.p, L.hrow_chunk.data(), L.hrow_chunk.size() * 4, cudaMemcpyHostToDevice, s));
+    if (!L.wrows.empty())
+        MG_CUDA(cudaMemcpyAsync(g->wrows.p, L.wrows.data(), L.wrows.size() * 4, cudaMemcpyHostToDevice, s));
+    if (!L.trows.empty())
+        MG_CUDA(cudaMemcpyAsync(g->trows.p, L.trows.data(), L.trows.size() * 4, cudaMemcpyHostToDevice, s));
+    g->nwrows = (int32_t)L.wrows.size();
+    g->ntrows = (int32_t)L.trows.size();
     MG_CUDA(cudaStreamSynchronize(s));
-    g->ngroups = (int32_t)L.grp.size() - 1;
     g->nhchunks = (int32_t)(L.hchunk.size() / 3);
     g->nhrows = (int32_t)L.hrows.size();
     g->heavy_deg = HEAVY_DEG;
@@ -349,10 +565,12 @@ static void destroy_graph(mg_graph *g)
     free_bc_ws(g);
     free_ppr_ws(g);
     free_wpr_ws(g);
-    DevBuf *bufs[] = {&g->row, &g->col, &g->wt, &g->trow_own, &g->tcol_own, &g->twt_own, &g->grp,
-                      &g->hchunk, &g->hrows, &g->hrow_chunk, &g->fw, &g->ppr_hchunk, &g->ppr_hrows,
-                      &g->ppr_hrow_chunk};
+    DevBuf *bufs[] = {&g->row, &g->col, &g->wt, &g->trow_own, &g->tcol_own, &g->twt_own,
+                      &g->hchunk, &g->hrows, &g->hrow_chunk, &g->fw, &g->o_fw, &g->ppr_hchunk, &g->ppr_hrows,
+                      &g->ppr_hrow_chunk, &g->o_row, &g->o_col, &g->o_wt, &g->old2new, &g->new2old,
+                      &g->wrows, &g->trows};
     for (DevBuf *b : bufs) dev_free(*b);
+    for (DevBuf &b : g->res_out) dev_free(b);
     if (g->pinned_flag) cudaFreeHost(g->pinned_flag);
     if (g->ev0) cudaEventDestroy(g->ev0);
     if (g->ev1) cudaEventDestroy(g->ev1);
@@ -411,13 +629,23 @@ mg_status mg_graph_reload(mg_graph *g, const mg_host_graph *h)
     if (!g || !h) return fail(MG_ERR_INVALID, "null argument");
     if (h->nv != g->nv || h->ne != g->ne) return fail(MG_ERR_INVALID, "reload needs the same nv/ne");
     MG_CUDA(cudaSetDevice(g->device));
-    // the index tables depend on the degrees only; the arrays are re-copied
+    // Same degrees: the order, the index tables and the row offsets stay;
+    // the edge arrays are re-copied (and relabeled on the device).
     const size_t n = (size_t)h->nv, m = (size_t)h->ne;
     cudaStream_t s = g->stream;
-    MG_CUDA(cudaMemcpyAsync(g->row.p, h->v.data(), (n + 1) * 4, cudaMemcpyHostToDevice, s));
-    if (m) {
-        MG_CUDA(cudaMemcpyAsync(g->col.p, h->e.data(), m * 4, cudaMemcpyHostToDevice, s));
-        MG_CUDA(cudaMemcpyAsync(g->wt.p, h->ev.data(), m * 4, cudaMemcpyHostToDevice, s));
+    if (g->relabeled) {
+        MG_CUDA(cudaMemcpyAsync(g->o_row.p, h->v.data(), (n + 1) * 4, cudaMemcpyHostToDevice, s));
+        if (m) {
+            MG_CUDA(cudaMemcpyAsync(g->o_col.p, h->e.data(), m * 4, cudaMemcpyHostToDevice, s));
+            MG_CUDA(cudaMemcpyAsync(g->o_wt.p, h->ev.data(), m * 4, cudaMemcpyHostToDevice, s));
+        }
+        MG_TRY(relabel_device(g));
+    } else {
+        MG_CUDA(cudaMemcpyAsync(g->row.p, h->v.data(), (n + 1) * 4, cudaMemcpyHostToDevice, s));
+        if (m) {
+            MG_CUDA(cudaMemcpyAsync(g->col.p, h->e.data(), m * 4, cudaMemcpyHostToDevice, s));
+            MG_CUDA(cudaMemcpyAsync(g->wt.p, h->ev.data(), m * 4, cudaMemcpyHostToDevice, s));
+        }
     }
     if (!(g->symmetric && g->weights_symmetric)) {
         HostLayout L;
@@ -445,7 +673,15 @@ mg_status mg_graph_set_float_weights(mg_graph *g, const float *w)
     if (!g || (!w && g->ne > 0)) return fail(MG_ERR_INVALID, "null argument");
     MG_CUDA(cudaSetDevice(g->device));
     MG_TRY(dev_alloc(g->fw, std::max<size_t>((size_t)g->ne, 4) * 4 + COL_PAD));
-    if (g->ne) MG_CUDA(cudaMemcpyAsync(g->fw.p, w, (size_t)g->ne * 4, cudaMemcpyHostToDevice, g->stream));
+    if (g->relabeled) {
+        // keep the caller-order copy (the transposed weights are found there,
+        // where rows have ascending columns) and relabel into engine order
+        MG_TRY(dev_alloc(g->o_fw, std::max<size_t>((size_t)g->ne, 4) * 4 + COL_PAD));
+        if (g->ne) MG_CUDA(cudaMemcpyAsync(g->o_fw.p, w, (size_t)g->ne * 4, cudaMemcpyHostToDevice, g->stream));
+        MG_TRY(edges_to_engine(g, g->o_fw.p, g->fw.p));
+    } else if (g->ne) {
+        MG_CUDA(cudaMemcpyAsync(g->fw.p, w, (size_t)g->ne * 4, cudaMemcpyHostToDevice, g->stream));
+    }
     MG_CUDA(cudaStreamSynchronize(g->stream));
     g->has_fw = true;
     return MG_OK;

@@ -5,7 +5,7 @@
 
 #include <cuda_runtime.h>
 
-#include "mg_group.cuh"
+#include "mg_bins.cuh"
 
 #include <functional>
 #include <string>
@@ -107,9 +107,10 @@ struct mg_graph {
     // transpose (pull side, in-edges); aliases row/col/wt when symmetric
     mgi::DevBuf trow_own, tcol_own, twt_own;
     const int32_t *trow = nullptr, *tcol = nullptr, *twt = nullptr;
-    // edge-balanced groups of <= 32 consecutive pull rows (light rows only)
-    mgi::DevBuf grp;               // int32 [ngroups+1] first row of each group
-    int32_t ngroups = 0;
+    // degree bins of the pull rows: warp rows (32 < deg <= heavy_deg) and
+    // thread rows (deg <= 32), in engine order
+    mgi::DevBuf wrows, trows;
+    int32_t nwrows = 0, ntrows = 0;
     // heavy pull rows split into chunks: (row, begin, end) triplets
     mgi::DevBuf hchunk;            // int32 [3*nhchunks]
     int32_t nhchunks = 0;
@@ -125,6 +126,14 @@ struct mg_graph {
     // float edge weights for weighted PageRank (CSR order)
     mgi::DevBuf fw;
     bool has_fw = false;
+    // hub-first relabeling: the engines run on ids ordered by descending
+    // log2 degree; results are mapped back before they leave the library
+    bool relabeled = false;
+    mgi::DevBuf o_row, o_col, o_wt;        // the CSR in the caller's ids (as uploaded)
+    mgi::DevBuf o_fw;                      // float weights in caller CSR order
+    mgi::DevBuf old2new, new2old;          // int32 [nv]
+    std::vector<int32_t> h_old2new;        // host copy for mapping sources
+    mgi::DevBuf res_out[8];                // results in the caller's ids
     // per-algorithm workspaces
     FrontierWS *fws = nullptr;
     PrWS *pws = nullptr;
@@ -149,6 +158,18 @@ mg_status begin_run(mg_graph *g, const mg_opts *o, mg_opts &opt, mg_run_info *in
 mg_status end_run(mg_graph *g, const mg_opts &opt, mg_run_info *info);
 mg_status copy_out(mg_graph *g, void *host, const void *dev, size_t bytes);
 int launch_grid(const mg_graph *g, int threads, int per_sm);
+// caller ids <-> engine ids (identity unless the graph was relabeled)
+int32_t to_engine(const mg_graph *g, int32_t v);
+// result in engine order (rows x nv elements of elem = 4 or 8 bytes) -> a
+// buffer in caller order owned by the graph (slot `which`); *out = src when
+// the graph is not relabeled
+mg_status to_caller(mg_graph *g, int which, const void *src, size_t elem, int32_t rows, const void **out);
+mg_status vertices_to_engine(mg_graph *g, const void *src_caller, void *dst_engine);  // 4-byte elements
+// CC roots in engine ids -> minimum caller id of each component, per caller vertex
+mg_status cc_to_caller(mg_graph *g, const int32_t *parent, const void **out);
+// per-edge 4-byte payloads between caller CSR order and engine CSR order
+mg_status edges_to_engine(mg_graph *g, const void *src_caller, void *dst_engine);
+mg_status edges_to_caller(mg_graph *g, const void *src_engine, void *dst_caller);
 }  // namespace mgi
 
 // ---------------------------------------------------------------------------
@@ -197,7 +218,7 @@ __device__ __forceinline__ int owner_lane(int excl_off, int k)
 // Per-warp staging of newly reached vertices: lanes push with a shared
 // atomic, then the warp reserves one global slice and copies.
 struct WarpStage {
-    int32_t *buf;   // >= GROUP_ROWS entries
+    int32_t *buf;   // >= 32 entries (one per lane between flushes)
     int32_t *cnt;   // shared counter
     __device__ __forceinline__ void push(int32_t v) { buf[atomicAdd(cnt, 1)] = v; }
 };

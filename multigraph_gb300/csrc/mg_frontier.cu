@@ -15,7 +15,8 @@
 //   k_pull   (when the frontier is dense) every unvisited vertex scans its
 //            in-edges against the frontier bitmap (BFS stops at the first
 //            parent; SSSP/BC reduce over all in-edges), light rows in
-//            edge-balanced warp groups, heavy rows in 2048-edge chunks;
+//            degree bins (warp / thread per row), heavy rows in 2048-edge
+//            chunks;
 //   k_decide 1 warp: next size, direction switch (frontier edges against
 //            unvisited edges, Beamer), iteration cap, loop condition.
 // Only one of k_push / k_pull does work in an iteration; the other returns
@@ -62,8 +63,8 @@ struct Args {
     int32_t m;
     const int32_t *row, *col, *wt;     // push side
     const int32_t *trow, *tcol, *twt;  // pull side
-    const int32_t *grp;
-    int32_t ngroups;
+    const int32_t *wrows, *trows;  // degree bins of the pull rows
+    int32_t nwrows, ntrows;
     const int32_t *hchunk;
     int32_t nhchunks;
     int32_t heavy_deg;
@@ -205,21 +206,53 @@ __global__ void __launch_bounds__(THREADS) k_push(Args a)
 // ----------------------------------------------------------------------------
 // pull: row reductions over in-edges against the frontier bitmap
 // ----------------------------------------------------------------------------
+// Rows reached in a pull sweep are staged per warp (shared memory) and
+// appended to the next frontier at warp-uniform points with one global
+// reservation per flush.
+struct PullEmit {
+    const Args &a;
+    mgd::WarpStage st;
+    int32_t nqoff;
+    int nextbuf;
+    int hpar;
+    long long scanned;
+    __device__ void flush()
+    {
+        __syncwarp();
+        const int cnt = *st.cnt;
+        if (cnt == 0) return;  // uniform: every lane reads the same word
+        const int ln = threadIdx.x & 31;
+        int base = 0;
+        if (ln == 0) base = atomicAdd(&a.ctl->nq, cnt);
+        base = __shfl_sync(0xffffffffu, base, 0);
+        long long dsum = 0;
+        for (int i = ln; i < cnt; i += 32) {
+            int32_t v = st.buf[i];
+            a.queue[nqoff + base + i] = v;
+            mgd::bm_set(bm_buf(a, nextbuf), v);
+            int32_t dg = a.row[v + 1] - a.row[v];
+            dsum += dg;
+            if (dg > PUSH_HEAVY) a.heavy[(size_t)(hpar ^ 1) * a.n + atomicAdd(&a.ctl->nhcur, 1)] = v;
+        }
+        warp_add64(&a.ctl->nf_edges, dsum);
+        __syncwarp();
+        if (ln == 0) *st.cnt = 0;
+        __syncwarp();
+    }
+};
+
 template <int ALG>
 struct PullOp;
 
 // SSSP: min over frontier in-neighbours of dist[u] + w (accumulate_nonAtomics
 // in row order), then one atomicMin + stamp on the row (fused_update_condition)
 template <>
-struct PullOp<ALG_SSSP> {
+struct PullOp<ALG_SSSP> : PullEmit {
     using T = int32_t;
     static constexpr bool kRowAware = false;
     static constexpr bool kWeights = true;
-    const Args &a;
     const uint32_t *fb;
     int it1;
-    mgd::WarpStage st;
-    int pad;
     __device__ T identity() const { return mgops::Sssp::initialize(); }
     __device__ bool skip(int32_t) const { return false; }
     __device__ T edge(int32_t, int32_t, int32_t u, int32_t w) const
@@ -239,15 +272,12 @@ struct PullOp<ALG_SSSP> {
 
 // BC forward: unvisited rows sum the path counts of frontier in-neighbours
 template <>
-struct PullOp<ALG_BC> {
+struct PullOp<ALG_BC> : PullEmit {
     using T = double;
     static constexpr bool kRowAware = true;  // visited rows are skipped
     static constexpr bool kWeights = false;
-    const Args &a;
     const uint32_t *fb;
     int it1;
-    mgd::WarpStage st;
-    int pad;
     __device__ T identity() const { return 0.0; }
     __device__ bool skip(int32_t v) const { return mgd::bm_test(a.visited, v); }
     __device__ T edge(int32_t, int32_t, int32_t u, int32_t) const { return mgd::bm_test(fb, u) ? a.sigma[u] : 0.0; }
@@ -307,40 +337,16 @@ __global__ void __launch_bounds__(THREADS) k_pull(Args a)
             emit_next(a, c, nextbuf, found, v);
         }
     } else {
-        // edge-balanced row groups, one warp each; reached rows are staged
-        // per warp and appended with one reservation per group
-        constexpr bool W = PullOp<ALG>::kWeights;
-        __shared__ int32_t s_off[THREADS / 32][mgd::GROUP_ROWS + 1];
-        __shared__ __align__(16) int32_t s_col[THREADS / 32][mgd::GROUP_STAGE];
-        __shared__ __align__(16) int32_t s_wt[W ? THREADS / 32 : 1][W ? mgd::GROUP_STAGE : 4];
-        __shared__ int32_t s_stage[THREADS / 32][mgd::GROUP_ROWS];
+        // degree-binned rows; reached rows staged per warp (<= 32 between flushes)
+        __shared__ int32_t s_stage[THREADS / 32][32];
         __shared__ int32_t s_cnt[THREADS / 32];
         const int wib = threadIdx.x >> 5;
-        PullOp<ALG> op{a, fb, it1, {s_stage[wib], &s_cnt[wib]}, 0};
-        const mgd::GroupSmem sm{s_off[wib], s_col[wib], W ? s_wt[wib] : nullptr};
-        for (int32_t g = gwarp; g < a.ngroups; g += nwarps) {
-            int32_t r0 = a.grp[g], r1 = a.grp[g + 1];
-            if (r1 - r0 == 1 && a.trow[r1] - a.trow[r0] > a.heavy_deg) continue;  // heavy row: chunks below
-            if (lane == 0) s_cnt[wib] = 0;
-            __syncwarp();
-            mgd::group_reduce(op, a.trow, a.tcol, a.twt, r0, r1, sm);
-            int cnt = s_cnt[wib];
-            int base = 0;
-            if (lane == 0 && cnt) base = atomicAdd(&a.ctl->nq, cnt);
-            base = __shfl_sync(0xffffffffu, base, 0);
-            long long dsum = 0;
-            for (int i = lane; i < cnt; i += 32) {
-                int32_t v = s_stage[wib][i];
-                a.queue[c.nqoff + base + i] = v;
-                mgd::bm_set(bm_buf(a, nextbuf), v);
-                int32_t dg = a.row[v + 1] - a.row[v];
-                dsum += dg;
-                if (dg > PUSH_HEAVY) a.heavy[(size_t)(c.hpar ^ 1) * a.n + atomicAdd(&a.ctl->nhcur, 1)] = v;
-            }
-            warp_add64(&a.ctl->nf_edges, dsum);
-            scanned += (lane == 0) ? (a.trow[r1] - a.trow[r0]) : 0;
-            __syncwarp();
-        }
+        if (lane == 0) s_cnt[wib] = 0;
+        __syncwarp();
+        PullOp<ALG> op{{a, {s_stage[wib], &s_cnt[wib]}, c.nqoff, nextbuf, c.hpar, 0}, fb, it1};
+        mgd::bins_reduce(op, a.trow, a.tcol, a.twt, a.wrows, a.nwrows, a.trows, a.ntrows);
+        (void)gwarp;
+        (void)nwarps;
     }
 
     // heavy rows: one CTA per 2048-edge chunk
@@ -690,7 +696,8 @@ static Args make_args(mg_graph *g)
     a.m = g->ne;
     a.row = g->row.as<int32_t>(); a.col = g->col.as<int32_t>(); a.wt = g->wt.as<int32_t>();
     a.trow = g->trow; a.tcol = g->tcol; a.twt = g->twt;
-    a.grp = g->grp.as<int32_t>(); a.ngroups = g->ngroups;
+    a.wrows = g->wrows.as<int32_t>(); a.nwrows = g->nwrows;
+    a.trows = g->trows.as<int32_t>(); a.ntrows = g->ntrows;
     a.hchunk = g->hchunk.as<int32_t>(); a.nhchunks = g->nhchunks;
     a.heavy_deg = g->heavy_deg;
     a.label = w->label.as<int32_t>();
@@ -709,7 +716,7 @@ static Args make_args(mg_graph *g)
 static uint64_t key_of(const Args &a, int alg)
 {
     uint64_t k = 1469598103934665603ull ^ (uint64_t)alg;
-    const void *ptrs[] = {a.row, a.col, a.trow, a.tcol, a.label, a.sigma, a.bm, a.queue, a.heavy, a.stamp, a.ctl, a.grp};
+    const void *ptrs[] = {a.row, a.col, a.trow, a.tcol, a.label, a.sigma, a.bm, a.queue, a.heavy, a.stamp, a.ctl, a.wrows};
     for (const void *p : ptrs) k = (k ^ (uint64_t)(uintptr_t)p) * 1099511628211ull;
     return k;
 }
@@ -846,24 +853,41 @@ using namespace mgi;
 
 extern "C" {
 
+// result slot `which` in caller ids (mapped on the device before the run ends)
+static mg_status publish(mg_graph *g, int which, const void *src, size_t elem)
+{
+    const void *p = nullptr;
+    MG_TRY(to_caller(g, which, src, elem, 1, &p));
+    g->res[which] = p;
+    return MG_OK;
+}
+
+static mg_status check_source(const mg_graph *g, int32_t s)
+{
+    if (s < 0 || s >= g->nv) return fail(MG_ERR_RANGE, "source %d out of range [0,%d)", s, g->nv);
+    return MG_OK;
+}
+
 mg_status mg_bfs(mg_graph *g, int32_t source, const mg_opts *o, int32_t *level_out, mg_run_info *info)
 {
     mg_opts opt;
     MG_TRY(begin_run(g, o, opt, info));
-    MG_TRY(frontier_run(g, ALG_BFS, source, opt, info));
+    MG_TRY(check_source(g, source));
+    MG_TRY(frontier_run(g, ALG_BFS, to_engine(g, source), opt, info));
+    MG_TRY(publish(g, MG_RES_LEVEL, g->fws->label.p, 4));
     MG_TRY(end_run(g, opt, info));
-    g->res[MG_RES_LEVEL] = g->fws->label.p;
-    return copy_out(g, level_out, g->fws->label.p, (size_t)g->nv * 4);
+    return copy_out(g, level_out, g->res[MG_RES_LEVEL], (size_t)g->nv * 4);
 }
 
 mg_status mg_sssp(mg_graph *g, int32_t source, const mg_opts *o, int32_t *dist_out, mg_run_info *info)
 {
     mg_opts opt;
     MG_TRY(begin_run(g, o, opt, info));
-    MG_TRY(frontier_run(g, ALG_SSSP, source, opt, info));
+    MG_TRY(check_source(g, source));
+    MG_TRY(frontier_run(g, ALG_SSSP, to_engine(g, source), opt, info));
+    MG_TRY(publish(g, MG_RES_DIST, g->fws->label.p, 4));
     MG_TRY(end_run(g, opt, info));
-    g->res[MG_RES_DIST] = g->fws->label.p;
-    return copy_out(g, dist_out, g->fws->label.p, (size_t)g->nv * 4);
+    return copy_out(g, dist_out, g->res[MG_RES_DIST], (size_t)g->nv * 4);
 }
 
 mg_status mg_bc(mg_graph *g, int32_t source, const mg_opts *o, int32_t *level_out, double *sigma_out,
@@ -871,16 +895,18 @@ mg_status mg_bc(mg_graph *g, int32_t source, const mg_opts *o, int32_t *level_ou
 {
     mg_opts opt;
     MG_TRY(begin_run(g, o, opt, info));
-    MG_TRY(frontier_run(g, ALG_BC, source, opt, info));
-    MG_TRY(bc_backward(g, source, opt, nullptr));
-    MG_TRY(end_run(g, opt, info));
+    MG_TRY(check_source(g, source));
+    const int32_t s = to_engine(g, source);
+    MG_TRY(frontier_run(g, ALG_BC, s, opt, info));
+    MG_TRY(bc_backward(g, s, opt, nullptr));
     FrontierWS *w = g->fws;
-    g->res[MG_RES_LEVEL] = w->label.p;
-    g->res[MG_RES_SIGMA] = w->sigma.p;
-    g->res[MG_RES_DELTA] = w->delta.p;
-    MG_TRY(copy_out(g, level_out, w->label.p, (size_t)g->nv * 4));
-    MG_TRY(copy_out(g, sigma_out, w->sigma.p, (size_t)g->nv * 8));
-    return copy_out(g, delta_out, w->delta.p, (size_t)g->nv * 4);
+    MG_TRY(publish(g, MG_RES_LEVEL, w->label.p, 4));
+    MG_TRY(publish(g, MG_RES_SIGMA, w->sigma.p, 8));
+    MG_TRY(publish(g, MG_RES_DELTA, w->delta.p, 4));
+    MG_TRY(end_run(g, opt, info));
+    MG_TRY(copy_out(g, level_out, g->res[MG_RES_LEVEL], (size_t)g->nv * 4));
+    MG_TRY(copy_out(g, sigma_out, g->res[MG_RES_SIGMA], (size_t)g->nv * 8));
+    return copy_out(g, delta_out, g->res[MG_RES_DELTA], (size_t)g->nv * 4);
 }
 
 mg_status mg_bc_multi(mg_graph *g, const int32_t *sources, int32_t nsrc, const mg_opts *o, float *bc_out,
@@ -898,14 +924,15 @@ mg_status mg_bc_multi(mg_graph *g, const int32_t *sources, int32_t nsrc, const m
     int32_t iters = 0;
     for (int32_t i = 0; i < nsrc; i++) {
         mg_run_info sub;
-        MG_TRY(frontier_run(g, ALG_BC, sources[i], opt, &sub));
-        MG_TRY(bc_backward(g, sources[i], opt, w->bc.as<float>()));
+        const int32_t s = to_engine(g, sources[i]);
+        MG_TRY(frontier_run(g, ALG_BC, s, opt, &sub));
+        MG_TRY(bc_backward(g, s, opt, w->bc.as<float>()));
         iters += sub.iterations;
     }
+    MG_TRY(publish(g, MG_RES_BC, w->bc.p, 4));
     MG_TRY(end_run(g, opt, info));
     if (info) info->iterations = iters;
-    g->res[MG_RES_BC] = w->bc.p;
-    return copy_out(g, bc_out, w->bc.p, (size_t)g->nv * 4);
+    return copy_out(g, bc_out, g->res[MG_RES_BC], (size_t)g->nv * 4);
 }
 
 }  // extern "C"

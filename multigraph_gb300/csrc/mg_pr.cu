@@ -6,13 +6,14 @@
 // _phase11 / _phase2.  The reference scatters pr/deg with FP32 atomicAdd into
 // an intermediate buffer and gathers it in shared memory (order-dependent
 // sums, ~12.5 B/edge).  Here every sweep is a pull (gather) over in-edges:
-//   k_pr_light  edge-balanced warp groups (<= 32 rows, <= 512 edges): lanes
-//               read 32 consecutive column ids (one 128 B line), gather the
-//               contributions from L2, segmented-reduce by row in registers;
-//   k_pr_heavy  rows above 2048 in-edges in 2048-edge chunks, one CTA each,
-//               partial sums written per chunk;
-//   k_pr_finish one CTA: heavy rows summed chunk by chunk in order, block
-//               residuals summed in order, convergence test, loop condition.
+//   k_pr_light  degree bins (mg_bins.cuh): a warp per row of 33..512 in-edges
+//               (lanes read one 128 B line of column ids per step, a fixed
+//               shuffle tree sums them), a thread per row of <= 32 in-edges;
+//               then rows above 512 in-edges in 2048-edge chunks, one CTA
+//               each, partial sums written per chunk;
+//   k_pr_apply  heavy rows summed chunk by chunk in order (warp per row),
+//               then the last block to finish sums every block's residual
+//               partials in slot order: convergence test, loop condition.
 // Sums are therefore deterministic (fixed order) run to run.
 // Algorithmic bytes per sweep: 4m (column ids) + 4(n+1) (offsets) + 12n
 // (old value read, new value and contribution written); the contribution
@@ -45,8 +46,18 @@ struct PCtl {
     double lam_mean;      // adjoint: mean of lambda (dangling rows)
     float damping, tol;
     int32_t n;
-    int32_t pad;
+    float base;           // (1-d)/n + d*dangling/n of the current sweep (set once per sweep)
+    float tol_row;        // tol / n: per-vertex activity threshold of the data-driven form
+    float lam_meanf;      // lam_mean as float
 };
+
+// per-sweep constants derived once (FP64 math stays out of the per-row path)
+__device__ __forceinline__ void pctl_derive(PCtl *c)
+{
+    c->base = (float)((1.0 - (double)c->damping) / c->n + (double)c->damping * c->dangling / c->n);
+    c->tol_row = c->tol / (float)c->n;
+    c->lam_meanf = (float)c->lam_mean;
+}
 
 struct PArgs {
     int32_t n;
@@ -55,8 +66,8 @@ struct PArgs {
     const float *pw;         // per-entry weights of the scanned rows (weighted / adjoint), or null
     const int32_t *outrow;   // push-side offsets (out-degrees)
     float *S;                // weighted: out-weight sums
-    const int32_t *grp;
-    int32_t ngroups;
+    const int32_t *wrows, *trows;  // degree bins
+    int32_t nwrows, ntrows;
     const int32_t *hchunk;
     int32_t nhchunks;
     const int32_t *hrows;
@@ -102,13 +113,12 @@ __device__ __forceinline__ float pr_apply(const PArgs &a, const PCtl &c, int32_t
         a.c[nxt][v] = mgops::PrRef::get_partial_result(xn, od);
     } else if (V == V_T || V == V_D) {
         const float d = c.damping;
-        float base = (float)((1.0 - (double)d) / c.n + (double)d * c.dangling / c.n);
         if (V == V_D && a.active[v] == 0) {
             xn = xo;  // frozen
         } else {
-            xn = base + d * s;
+            xn = c.base + d * s;
             if (V == V_D) {
-                if (fabsf(xn - xo) <= c.tol / (float)c.n) a.active[v] = 0;
+                if (fabsf(xn - xo) <= c.tol_row) a.active[v] = 0;
                 else any = 1;
             }
         }
@@ -117,8 +127,7 @@ __device__ __forceinline__ float pr_apply(const PArgs &a, const PCtl &c, int32_t
         if (od == 0) dang = xn;
     } else if (V == V_WEIGHTED) {
         const float d = c.damping;
-        float base = (float)((1.0 - (double)d) / c.n + (double)d * c.dangling / c.n);
-        xn = base + d * s;
+        xn = c.base + d * s;
         a.x[nxt][v] = xn;
         float Su = a.S[v];
         a.c[nxt][v] = Su > 0.0f ? xn / Su : 0.0f;
@@ -126,7 +135,7 @@ __device__ __forceinline__ float pr_apply(const PArgs &a, const PCtl &c, int32_t
     } else {  // V_ADJ: lambda_new = g + d * (t + [S_u == 0] * mean(lambda))
         const float d = c.damping;
         float Su = a.S[v];
-        float t = Su > 0.0f ? s / Su : (float)c.lam_mean;
+        float t = Su > 0.0f ? s / Su : c.lam_meanf;
         xn = a.gvec[v] + d * t;
         xo = a.c[cur][v];
         a.c[nxt][v] = xn;
@@ -172,7 +181,7 @@ __device__ __forceinline__ void block_partials(const PArgs &a, int slot, double 
     }
 }
 
-// row reduction for one PageRank sweep (group_reduce interface)
+// row reduction for one PageRank sweep (bins_reduce interface)
 template <int V>
 struct PrRowOp {
     using T = float;
@@ -180,7 +189,7 @@ struct PrRowOp {
     static constexpr bool kWeights = (V == V_WEIGHTED || V == V_ADJ);  // staged float weight bits
     const PArgs &a;
     const PCtl &c;
-    double resid = 0.0, dangs = 0.0;
+    float resid = 0.0f, dangs = 0.0f;  // per-thread partials (blocks sum in FP64)
     int any = 0;
     __device__ float identity() const { return 0.0f; }
     __device__ bool skip(int32_t v) const { return pr_row_skipped<V>(a, v); }
@@ -191,6 +200,7 @@ struct PrRowOp {
         return cv;
     }
     __device__ float combine(float x, float y) const { return x + y; }
+    __device__ void flush() {}
     __device__ void finish(int32_t v, float s)
     {
         float dg = 0.0f;
@@ -207,20 +217,12 @@ __global__ void __launch_bounds__(THREADS) k_pr_light(PArgs a)
     const int lane = mgd::lane();
     const int gwarp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int nwarps = (gridDim.x * blockDim.x) >> 5;
-    constexpr bool W = PrRowOp<V>::kWeights;
-    __shared__ int32_t s_off[THREADS / 32][mgd::GROUP_ROWS + 1];
-    __shared__ __align__(16) int32_t s_col[THREADS / 32][mgd::GROUP_STAGE];
-    __shared__ __align__(16) int32_t s_wt[W ? THREADS / 32 : 1][W ? mgd::GROUP_STAGE : 4];
     PrRowOp<V> op{a, c};
     (void)lane;
-    const int wib = threadIdx.x >> 5;
-    const mgd::GroupSmem sm{s_off[wib], s_col[wib], W ? s_wt[wib] : nullptr};
+    (void)gwarp;
+    (void)nwarps;
     const int32_t *pwt = reinterpret_cast<const int32_t *>(a.pw);
-    for (int32_t g = gwarp; g < a.ngroups; g += nwarps) {
-        int32_t r0 = a.grp[g], r1 = a.grp[g + 1];
-        if (r1 - r0 == 1 && a.prow[r1] - a.prow[r0] > a.heavy_deg) continue;  // heavy row: chunks below
-        mgd::group_reduce(op, a.prow, a.pcol, pwt, r0, r1, sm);
-    }
+    mgd::bins_reduce(op, a.prow, a.pcol, pwt, a.wrows, a.nwrows, a.trows, a.ntrows);
     // heavy-row chunks of HCHUNK = 8 * THREADS edges, one per CTA: each
     // thread issues its 8 column loads, then its 8 gathers
     __shared__ float s_part[THREADS / 32];
@@ -320,6 +322,7 @@ __global__ void __launch_bounds__(THREADS) k_pr_apply(PArgs a, cudaGraphConditio
             cp->any = A;
             if (V == V_ADJ) cp->lam_mean = D / c.n;
             else cp->dangling = D;
+            pctl_derive(cp);
             if (V == V_T_REF || V == V_D_REF) more = A;
             else if (V == V_D) more = (A && R > (double)c.tol) ? 1 : 0;
             else more = R > (double)c.tol ? 1 : 0;
@@ -363,6 +366,7 @@ __global__ void k_pr_ctl_init(PCtl *c, int32_t n, int32_t max_iter, float dampin
     c->n = n;
     c->dangling = dangling0;
     c->lam_mean = lam_mean0;
+    pctl_derive(c);
 }
 
 // weighted: out-weight sums S[u] = sum_e w[e] (CSR order)
@@ -583,6 +587,7 @@ __global__ void k_ppr_store(int32_t n, const float *X, int32_t nseed, int32_t s0
 
 struct PrWS {
     mgi::DevBuf x0, x1, c0, c1, active, hpart, bpart, ctl, S, wT, gvec, grad, lam_keep, xkeep;
+    mgi::DevBuf wT_caller, gvec_caller, grad_caller;  // caller-order staging of a relabeled graph
     mgi::LoopGraph lg[6];
 };
 
@@ -600,7 +605,8 @@ void free_pr_ws(mg_graph *g)
     if (!g->pws) return;
     PrWS *w = g->pws;
     DevBuf *bufs[] = {&w->x0, &w->x1, &w->c0, &w->c1, &w->active, &w->hpart, &w->bpart, &w->ctl, &w->S,
-                      &w->wT, &w->gvec, &w->grad, &w->lam_keep, &w->xkeep};
+                      &w->wT, &w->gvec, &w->grad, &w->lam_keep, &w->xkeep, &w->wT_caller, &w->gvec_caller,
+                      &w->grad_caller};
     for (DevBuf *b : bufs) dev_free(*b);
     for (auto &l : w->lg) l.destroy();
     delete w;
@@ -687,7 +693,8 @@ static mg_status pr_setup(mg_graph *g, PArgs &a, bool weighted_or_adj)
     a.prow = g->trow;
     a.pcol = g->tcol;
     a.outrow = g->row.as<int32_t>();
-    a.grp = g->grp.as<int32_t>(); a.ngroups = g->ngroups;
+    a.wrows = g->wrows.as<int32_t>(); a.nwrows = g->nwrows;
+    a.trows = g->trows.as<int32_t>(); a.ntrows = g->ntrows;
     a.hchunk = g->hchunk.as<int32_t>(); a.nhchunks = g->nhchunks;
     a.hrows = g->hrows.as<int32_t>(); a.hrow_chunk = g->hrow_chunk.as<int32_t>(); a.nhrows = g->nhrows;
     a.heavy_deg = g->heavy_deg;
@@ -768,9 +775,9 @@ mg_status mg_pagerank(mg_graph *g, int32_t variant, const mg_opts *o, float *ran
         MG_TRY(pr_loop<V_D>(g, a, opt, "pr_pull", info, &cur));
         break;
     }
+    MG_TRY(to_caller(g, MG_RES_RANK, a.x[cur], 4, 1, &g->res[MG_RES_RANK]));
     MG_TRY(end_run(g, opt, info));
-    g->res[MG_RES_RANK] = a.x[cur];
-    return copy_out(g, rank_out, a.x[cur], (size_t)g->nv * 4);
+    return copy_out(g, rank_out, g->res[MG_RES_RANK], (size_t)g->nv * 4);
 }
 
 mg_status mg_wpagerank(mg_graph *g, const mg_opts *o, float *x_out, mg_run_info *info)
@@ -786,8 +793,17 @@ mg_status mg_wpagerank(mg_graph *g, const mg_opts *o, float *x_out, mg_run_info 
     MG_TRY(dev_alloc(w->wT, m * 4 + 16));  // 16 bytes of tail padding for aligned staging
     MG_TRY(dev_alloc(w->xkeep, n * 4));
     k_row_sums<<<grid, THREADS, 0, s>>>(g->nv, g->row.as<int32_t>(), g->fw.as<float>(), a.S);
-    k_transpose_weights<<<grid, THREADS, 0, s>>>(g->nv, g->row.as<int32_t>(), g->col.as<int32_t>(), g->fw.as<float>(),
-                                                  w->wT.as<float>());
+    if (g->relabeled) {
+        // transposed weights are located in the caller's CSR (ascending
+        // columns), then carried to engine order like the column ids
+        MG_TRY(dev_alloc(w->wT_caller, m * 4 + 16));
+        k_transpose_weights<<<grid, THREADS, 0, s>>>(g->nv, g->o_row.as<int32_t>(), g->o_col.as<int32_t>(),
+                                                      g->o_fw.as<float>(), w->wT_caller.as<float>());
+        MG_TRY(edges_to_engine(g, w->wT_caller.p, w->wT.p));
+    } else {
+        k_transpose_weights<<<grid, THREADS, 0, s>>>(g->nv, g->row.as<int32_t>(), g->col.as<int32_t>(),
+                                                      g->fw.as<float>(), w->wT.as<float>());
+    }
     a.pw = w->wT.as<float>();
     float d = opt.damping > 0 ? opt.damping : 0.85f;
     float tol = opt.tol > 0 ? opt.tol : 1e-6f;
@@ -799,9 +815,9 @@ mg_status mg_wpagerank(mg_graph *g, const mg_opts *o, float *x_out, mg_run_info 
     int cur = 0;
     MG_TRY(pr_loop<V_WEIGHTED>(g, a, opt, "wpr_pull", info, &cur));
     MG_CUDA(cudaMemcpyAsync(w->xkeep.p, a.x[cur], (size_t)g->nv * 4, cudaMemcpyDeviceToDevice, s));
+    MG_TRY(to_caller(g, MG_RES_RANK, w->xkeep.p, 4, 1, &g->res[MG_RES_RANK]));
     MG_TRY(end_run(g, opt, info));
-    g->res[MG_RES_RANK] = w->xkeep.p;
-    return copy_out(g, x_out, w->xkeep.p, (size_t)g->nv * 4);
+    return copy_out(g, x_out, g->res[MG_RES_RANK], (size_t)g->nv * 4);
 }
 
 mg_status mg_wpagerank_backward(mg_graph *g, const float *g_host, const mg_opts *o, float *grad_w_out,
@@ -820,7 +836,10 @@ mg_status mg_wpagerank_backward(mg_graph *g, const float *g_host, const mg_opts 
     MG_TRY(dev_alloc(w->gvec, n * 4));
     MG_TRY(dev_alloc(w->grad, m * 4));
     MG_TRY(dev_alloc(w->lam_keep, n * 4));
-    if (g->nv) MG_CUDA(cudaMemcpyAsync(w->gvec.p, g_host, (size_t)g->nv * 4, cudaMemcpyHostToDevice, s));
+    MG_TRY(dev_alloc(w->gvec_caller, n * 4));
+    MG_TRY(dev_alloc(w->grad_caller, m * 4));
+    if (g->nv) MG_CUDA(cudaMemcpyAsync(w->gvec_caller.p, g_host, (size_t)g->nv * 4, cudaMemcpyHostToDevice, s));
+    MG_TRY(vertices_to_engine(g, w->gvec_caller.p, w->gvec.p));
     k_row_sums<<<grid, THREADS, 0, s>>>(g->nv, g->row.as<int32_t>(), g->fw.as<float>(), a.S);
     // lambda = g + d * P lambda : rows of P are the CSR rows (out-edges) with weights w
     a.prow = g->row.as<int32_t>();
@@ -847,9 +866,12 @@ mg_status mg_wpagerank_backward(mg_graph *g, const float *g_host, const mg_opts 
                                         w->xkeep.as<float>(), w->lam_keep.as<float>(), d, w->grad.as<float>());
     g->prof.end();
     MG_CUDA(cudaGetLastError());
+    const void *lam_out = nullptr;
+    MG_TRY(to_caller(g, MG_RES_DELTA, w->lam_keep.p, 4, 1, &lam_out));
+    MG_TRY(edges_to_caller(g, w->grad.p, w->grad_caller.p));
     MG_TRY(end_run(g, opt, info));
-    MG_TRY(copy_out(g, lambda_out, w->lam_keep.p, (size_t)g->nv * 4));
-    return copy_out(g, grad_w_out, w->grad.p, (size_t)g->ne * 4);
+    MG_TRY(copy_out(g, lambda_out, lam_out, (size_t)g->nv * 4));
+    return copy_out(g, grad_w_out, w->grad_caller.p, (size_t)g->ne * 4);
 }
 
 mg_status mg_ppr_batch(mg_graph *g, const int32_t *seeds, int32_t nseeds, const mg_opts *o, float *out,
@@ -899,7 +921,9 @@ mg_status mg_ppr_batch(mg_graph *g, const int32_t *seeds, int32_t nseeds, const 
     MG_TRY(dev_alloc(w->dang, 32 * 8));
     MG_TRY(dev_alloc(w->hpart, (size_t)std::max(g->ppr_nhchunks, 1) * 32 * 4));
     MG_TRY(dev_alloc(w->out, (size_t)std::max(nseeds, 1) * n * 4));
-    if (nseeds) MG_CUDA(cudaMemcpyAsync(w->seeds.p, seeds, (size_t)nseeds * 4, cudaMemcpyHostToDevice, s));
+    std::vector<int32_t> eseeds(seeds, seeds + nseeds);
+    for (int32_t &v : eseeds) v = to_engine(g, v);
+    if (nseeds) MG_CUDA(cudaMemcpyAsync(w->seeds.p, eseeds.data(), (size_t)nseeds * 4, cudaMemcpyHostToDevice, s));
     float tol = opt.tol > 0 ? opt.tol : 1e-6f;
     int max_iter = opt.max_iter > 0 ? opt.max_iter : 10000;
     PPArgs a;
@@ -949,8 +973,10 @@ mg_status mg_ppr_batch(mg_graph *g, const int32_t *seeds, int32_t nseeds, const 
         k_ppr_store<<<grid, THREADS, 0, s>>>(g->nv, X, a.nseed, s0, w->out.as<float>());
         MG_CUDA(cudaGetLastError());
     }
+    const void *res = nullptr;
+    MG_TRY(to_caller(g, 7, w->out.p, 4, nseeds, &res));
     MG_TRY(end_run(g, opt, info));
     if (info) { info->iterations = total_iters; info->residual = max_resid; }
-    return copy_out(g, out, w->out.p, (size_t)nseeds * g->nv * 4);
+    return copy_out(g, out, res, (size_t)nseeds * g->nv * 4);
 }
 }  // extern "C"

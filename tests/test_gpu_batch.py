@@ -1,0 +1,130 @@
+"""GPU parity of the batched and differentiable paths against the oracle.
+
+Tolerances (stated per spec contract):
+  multi-source BC      : 1e-5 relative (normwise: max|err| / max|ref|)
+  personalised PR      : 1e-6 max-abs against FP64 run for the same sweeps
+  weighted PR forward  : 1e-6 max-abs against FP64
+  PR edge gradient     : 1e-4 relative (normwise) against the FP64 adjoint
+  multi-graph BFS / CC : bit-exact per graph
+"""
+import numpy as np
+import pytest
+
+import multigraph_gb300 as mg
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+
+def _pair(h):
+    rp, col, wt = h.arrays()
+    return mg.Graph(h), O.csr_from_arrays(rp, col, wt)
+
+
+def test_bc_multi_sources():
+    h = mg.HostGraph.rmat(11, 16, seed=4)
+    g, og = _pair(h)
+    rng = np.random.default_rng(1)
+    src = rng.integers(0, og.nv, 12)
+    bc, info = g.bc_multi(src)
+    ref = O.bc_multi_f64(og, src)
+    err = float(np.max(np.abs(bc.astype(np.float64) - ref)) / np.max(np.abs(ref)))
+    assert err < 1e-5, err
+    g.free()
+
+
+def test_bc_multi_lattice():
+    h = mg.HostGraph.lattice(40, 30, 0.05, seed=2)
+    g, og = _pair(h)
+    src = [0, 17, 600, og.nv - 1]
+    bc, _ = g.bc_multi(src)
+    ref = O.bc_multi_f64(og, src)
+    err = float(np.max(np.abs(bc.astype(np.float64) - ref)) / np.max(np.abs(ref)))
+    assert err < 1e-5, err
+    g.free()
+
+
+def test_ppr_batch_one_block():
+    h = mg.HostGraph.rmat(11, 16, seed=6)
+    g, og = _pair(h)
+    rng = np.random.default_rng(2)
+    seeds = rng.integers(0, og.nv, 20)
+    x, info = g.ppr_batch(seeds, tol=1e-6)
+    for i, s in enumerate(seeds):
+        ref, _ = O.ppr_f64(og, int(s), 0.85, 0.0, info.iterations)
+        err = float(np.max(np.abs(x[i].astype(np.float64) - ref)))
+        assert err < 1e-6, (i, s, err)
+    g.free()
+
+
+def test_ppr_batch_many_blocks():
+    h = mg.HostGraph.rmat(10, 16, seed=7)
+    g, og = _pair(h)
+    seeds = np.arange(0, 70) * 7 % og.nv
+    x, info = g.ppr_batch(seeds, tol=1e-6)
+    assert x.shape == (70, og.nv)
+    for i in (0, 31, 32, 69):
+        ref, _ = O.ppr_f64(og, int(seeds[i]), 0.85, 1e-12)
+        err = float(np.max(np.abs(x[i].astype(np.float64) - ref)))
+        assert err < 1e-5, (i, err)
+    g.free()
+
+
+def _weighted(scale=10, seed=9):
+    h = mg.HostGraph.rmat(scale, 16, seed=seed)
+    g, og = _pair(h)
+    rng = np.random.default_rng(seed)
+    w = rng.uniform(0.0, 1.0, og.ne)
+    w = np.where(w == 0.0, 1.0, w).astype(np.float32)
+    g.set_float_weights(w)
+    return g, og, w
+
+
+def test_weighted_pagerank_forward():
+    g, og, w = _weighted()
+    x, info = g.wpagerank(tol=1e-7)
+    ref, _ = O.wpr_f64(og, w.astype(np.float64), 0.85, 1e-13)
+    err = float(np.max(np.abs(x.astype(np.float64) - ref)))
+    assert err < 1e-6, err
+    g.free()
+
+
+def test_pagerank_adjoint_gradient():
+    g, og, w = _weighted()
+    rng = np.random.default_rng(3)
+    gv = rng.standard_normal(og.nv)
+    g.wpagerank(tol=1e-8, max_iter=2000)
+    (grad, lam), info = g.wpagerank_backward(gv.astype(np.float32), tol=1e-7, max_iter=2000)
+    w64 = w.astype(np.float64)
+    x64, _ = O.wpr_f64(og, w64, 0.85, 1e-14)
+    lam64, gw64, gp64, _ = O.wpr_adjoint_f64(og, w64, x64, gv, 0.85, 1e-14)
+    rel = float(np.max(np.abs(grad.astype(np.float64) - gw64)) / np.max(np.abs(gw64)))
+    assert rel < 1e-4, rel
+    # central finite differences (FP64 oracle forward), eps = 1e-3, 8 random edges
+    idx = rng.choice(og.ne, 8, replace=False)
+    for e in idx:
+        wp, wm = w64.copy(), w64.copy()
+        wp[e] += 1e-3
+        wm[e] -= 1e-3
+        fd = (O.wpr_loss_f64(og, wp, gv) - O.wpr_loss_f64(og, wm, gv)) / 2e-3
+        assert abs(fd - grad[e]) <= 1e-4 * np.max(np.abs(gw64)) + 1e-3 * abs(fd), (e, fd, grad[e])
+    g.free()
+
+
+def test_multi_graph_batch():
+    rng = np.random.default_rng(5)
+    hs = [mg.HostGraph.rmat(int(s), int(ef), seed=int(i) + 1) for i, (s, ef) in
+          enumerate(zip(rng.integers(6, 11, 7), rng.integers(8, 33, 7)))]
+    hs.append(mg.HostGraph.lattice(20, 17, 0.05, seed=3))
+    ogs = []
+    for h in hs:
+        rp, col, wt = h.arrays()
+        ogs.append(O.csr_from_arrays(rp, col, wt))
+    b = mg.Batch(hs)
+    srcs = [int(rng.integers(0, og.nv)) for og in ogs]
+    levels, _ = b.bfs(srcs)
+    labels, _ = b.cc()
+    for og, s, lv, lab in zip(ogs, srcs, levels, labels):
+        assert np.array_equal(lv, O.bfs(og, s))
+        assert np.array_equal(lab, O.cc_minlabel(og))
+    b.free()

@@ -30,6 +30,11 @@ def _graphs():
     s = rng.integers(0, 500, 4000)
     d = (s + rng.integers(1, 40, 4000)) % 500
     out.append(("general", mg.HostGraph.from_entries(500, s, d, rng.integers(1, 64, 4000), flags=mg.LOAD_NSYM)))
+    # general graph with a hub of out-degree >= 128: relabeled, non-symmetric
+    s2 = np.concatenate([np.zeros(300, np.int64), rng.integers(0, 800, 3000)])
+    d2 = np.concatenate([np.arange(1, 301), rng.integers(0, 800, 3000)])
+    out.append(("general_hub", mg.HostGraph.from_entries(800, s2, d2, rng.integers(1, 64, len(s2)),
+                                                         flags=mg.LOAD_NSYM)))
     return out
 
 
@@ -79,7 +84,7 @@ def test_cc(graphs):
 @pytest.mark.parametrize("direction", DIRS)
 def test_bc_single(graphs, direction):
     for name, g, og, _ in graphs:
-        if name == "general":
+        if name.startswith("general"):
             continue
         for s in _sources(og):
             (lv, sg, dl), _ = g.bc(s, direction=direction)
