@@ -258,6 +258,30 @@ mg_status mg_batch_cc(mg_batch *b, const mg_opts *o, int32_t *labels_out, mg_run
 enum { MG_ALGO_BFS = 0, MG_ALGO_SSSP = 1, MG_ALGO_BC = 2, MG_ALGO_CC = 3, MG_ALGO_PR = 4 };
 mg_status mg_autotune(mg_graph *dg, int32_t algo, int32_t source, const char *cache_path, mg_opts *tuned);
 
+/* ------------------------------------------------------------------------ */
+/* PageRank without allocation (no counterpart in the reference)            */
+/* ------------------------------------------------------------------------ */
+/* For callers that cannot call cudaMalloc -- code running inside a custom
+ * device allocator or pool callback, applications that reserve all device
+ * memory at start-up, latency-bound loops where an allocation could
+ * synchronise the device.  The caller passes device arrays it already owns:
+ * a symmetric CSR (d_row [nv+1], d_col [ne], every edge stored both ways as
+ * the loader's MG_LOAD_SYM produces it) and d_rank [nv] for the result.
+ * Every intermediate lives in one fixed device array inside libmg sized for
+ * MG_NOALLOC_MAX_VERTICES vertices (about 12 MB, held by each GPU that loads
+ * the library until the process exits); larger graphs are rejected with
+ * MG_ERR_RANGE.  Nothing is allocated: no cudaMalloc, cudaFree or allocating
+ * library call.  Same result as mg_pagerank(MG_PR_TOPOLOGY): normalised
+ * PageRank from x = 1/n until the L1 change <= tol.  Works on the current
+ * device and enqueues on `stream` (a cudaStream_t, NULL = default stream).
+ * The first call on a device looks up the array's device address; make it
+ * before any stream capture.  All calls share the array: calls that overlap
+ * on the GPU race. */
+#define MG_NOALLOC_MAX_VERTICES (1 << 20)
+mg_status mg_pagerank_noalloc(const int32_t *d_row, const int32_t *d_col, int32_t nv, int32_t ne, float damping,
+                              float tol, int32_t max_iter, float *d_rank, void *stream, int32_t *iterations_out,
+                              double *residual_out);
+
 #ifdef __cplusplus
 }
 #endif

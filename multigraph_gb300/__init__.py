@@ -110,6 +110,7 @@ def _load_lib():
         "mg_batch_bfs": ([vp, vp, P(Opts), vp, P(RunInfo)], i32),
         "mg_batch_cc": ([vp, P(Opts), vp, P(RunInfo)], i32),
         "mg_autotune": ([vp, i32, i32, C.c_char_p, P(Opts)], i32),
+        "mg_pagerank_noalloc": ([vp, vp, i32, i32, f32, f32, i32, vp, vp, P(i32), P(C.c_double)], i32),
     }
     for name, (args, res) in sig.items():
         fn = getattr(L, name)
@@ -137,8 +138,24 @@ EXPORTED = [
     "mg_gen_rmat", "mg_gen_lattice", "mg_graph_upload", "mg_graph_reload", "mg_graph_free", "mg_graph_info",
     "mg_graph_stream", "mg_graph_set_float_weights", "mg_opts_default", "mg_result_device", "mg_bfs", "mg_sssp",
     "mg_cc", "mg_bc", "mg_bc_multi", "mg_pagerank", "mg_ppr_batch", "mg_wpagerank", "mg_wpagerank_backward",
-    "mg_batch_create", "mg_batch_free", "mg_batch_bfs", "mg_batch_cc", "mg_autotune",
+    "mg_batch_create", "mg_batch_free", "mg_batch_bfs", "mg_batch_cc", "mg_autotune", "mg_pagerank_noalloc",
 ]
+NOALLOC_MAX_VERTICES = 1 << 20
+
+
+def pagerank_noalloc(d_row: int, d_col: int, nv: int, ne: int, d_rank: int, stream: int = 0,
+                     damping: float = 0.85, tol: float = 1e-6, max_iter: int = 0):
+    """mg_pagerank_noalloc on caller-owned device buffers (raw device pointers).
+
+    For callers that cannot allocate device memory: libmg uses only a fixed
+    internal device array (up to NOALLOC_MAX_VERTICES vertices).  Returns
+    (iterations, residual)."""
+    it = C.c_int32(0)
+    res = C.c_double(0.0)
+    _check(lib.mg_pagerank_noalloc(C.c_void_p(d_row), C.c_void_p(d_col), nv, ne, damping, tol, max_iter,
+                                   C.c_void_p(d_rank), C.c_void_p(stream) if stream else None, C.byref(it),
+                                   C.byref(res)), "mg_pagerank_noalloc")
+    return it.value, res.value
 
 
 def _status_name(s: int) -> str:
