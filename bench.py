@@ -111,6 +111,18 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm), "samples_under_load": len(load)}
 
 
+def aggregate(ms_local, edges_per_step, steps, world, dist=None, device=None):
+    """Replicas: the slowest rank bounds the job (max over ranks), and every
+    rank processed edges_per_step per step.  Returns (ms, GTEPS)."""
+    ms = float(ms_local)
+    if dist is not None and world > 1:
+        import torch
+        t = torch.tensor([ms], dtype=torch.float64, device=device)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    return ms, world * edges_per_step * steps / (ms / 1e3) / 1e9
+
+
 def build_graph(scale):
     import multigraph_gb300 as mg
     return mg.HostGraph.rmat(scale, EDGE_FACTOR, seed=scale)
@@ -212,13 +224,8 @@ def main():
     torch.cuda.synchronize()
     if dist:
         dist.barrier()
-    ms = e0.elapsed_time(e1)
-    if dist:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    ms, value = aggregate(e0.elapsed_time(e1), 2 * m, args.steps, world, dist, torch.device("cuda", local))
     ms_per_step = ms / args.steps
-    value = world * 2 * m * args.steps / (ms / 1e3) / 1e9
 
     # ---- end to end through the C ABI: pinned host CSR in, results out
     h2d = 4 * (n + 1) + 8 * m

@@ -1,0 +1,209 @@
+"""CPU tests of the host side: loader error handling, generators, the C ABI
+surface, failure injection, the CLI shell, and (where oracle/_ref was built
+from the reference sources) the oracle and product loader against the
+reference's own loader and validator on random graphs."""
+import os
+import re
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+import pytest
+
+import multigraph_gb300 as mg
+from oracle import oracle as O
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HAVE_REF = O.RefTool.available("BFS") and O.RefTool.available("SSSP")
+
+
+def _write(tmp, name, text):
+    p = os.path.join(tmp, name)
+    with open(p, "w") as f:
+        f.write(text)
+    return p
+
+
+# --------------------------------------------------------------------------
+# C ABI surface
+# --------------------------------------------------------------------------
+def test_library_exports_every_declared_symbol():
+    hdr = open(os.path.join(ROOT, "include", "mg.h")).read()
+    hdr = re.sub(r"/\*.*?\*/", "", hdr, flags=re.S)
+    declared = set(re.findall(r"\b(mg_[a-z0-9_]+)\s*\(", hdr))
+    assert declared == set(mg.EXPORTED), declared ^ set(mg.EXPORTED)
+    nm = subprocess.run(["nm", "-D", "--defined-only", mg.LIB_PATH], capture_output=True, text=True, check=True).stdout
+    exported = set(re.findall(r"\sT\s(mg_[a-z0-9_]+)$", nm, flags=re.M))
+    missing = declared - exported
+    assert not missing, missing
+    for name in declared:
+        assert getattr(mg.lib, name) is not None
+
+
+def test_status_strings_and_version():
+    assert mg.version().startswith("multigraph-gb300")
+    for s in range(9):
+        assert mg.lib.mg_status_string(s)
+    o = mg.default_opts()
+    assert o.alpha > 0 and o.beta > 0 and abs(o.damping - 0.85) < 1e-6
+
+
+# --------------------------------------------------------------------------
+# loader errors (the reference exits or crashes on these, read_input.cu:24,73-76)
+# --------------------------------------------------------------------------
+def test_loader_errors():
+    tmp = tempfile.mkdtemp()
+    with pytest.raises(mg.MGError) as e:
+        mg.HostGraph.load_mtx(os.path.join(tmp, "missing.mtx"))
+    assert e.value.status == mg.MG_ERR_IO
+    p = _write(tmp, "trunc.mtx", "%%MatrixMarket matrix coordinate pattern general\n4 4 3\n1 2\n2 3\n")
+    with pytest.raises(mg.MGError) as e:
+        mg.HostGraph.load_mtx(p)
+    assert e.value.status == mg.MG_ERR_PARSE
+    p = _write(tmp, "range.mtx", "%%MatrixMarket matrix coordinate pattern general\n4 4 2\n1 2\n2 5\n")
+    with pytest.raises(mg.MGError) as e:
+        mg.HostGraph.load_mtx(p)
+    assert e.value.status == mg.MG_ERR_RANGE
+    p = _write(tmp, "ok.mtx", "%%MatrixMarket matrix coordinate pattern general\n4 4 2\n1 2\n2 3\n")
+    with pytest.raises(mg.MGError) as e:
+        mg.HostGraph.load_mtx(p, source=9)
+    assert e.value.status == mg.MG_ERR_RANGE
+    p = _write(tmp, "nosize.mtx", "%%MatrixMarket matrix coordinate pattern general\n% only comments\n")
+    with pytest.raises(mg.MGError) as e:
+        mg.HostGraph.load_mtx(p)
+    assert e.value.status == mg.MG_ERR_PARSE
+    # general file whose only entry is dropped by compaction: the reference
+    # would write past its arrays; the loader refuses the graph
+    p = _write(tmp, "degenerate.mtx", "%%MatrixMarket matrix coordinate pattern general\n6 6 1\n6 5\n")
+    with pytest.raises(mg.MGError) as e:
+        mg.HostGraph.load_mtx(p, flags=mg.LOAD_NSYM)
+    assert e.value.status == mg.MG_ERR_INVALID
+    with pytest.raises(OSError):
+        O.load_mtx(p, 0, O.LOAD_NSYM)
+
+
+def test_multi_line_entries_use_stream_parser():
+    tmp = tempfile.mkdtemp()
+    p1 = _write(tmp, "a.mtx", "%%MatrixMarket matrix coordinate integer general\n4 4 3\n1 2 5\n2 3 6\n3 4 7\n")
+    p2 = _write(tmp, "b.mtx", "%%MatrixMarket matrix coordinate integer general\n4 4 3\n1 2\n5 2 3 6\n\n3\n4 7\n")
+    a, b = mg.HostGraph.load_mtx(p1).arrays(), mg.HostGraph.load_mtx(p2).arrays()
+    for x, y in zip(a, b):
+        assert np.array_equal(x, y)
+
+
+def test_from_entries_and_csr_validation():
+    h = mg.HostGraph.from_entries(5, [0, 1, 2], [1, 2, 3], [4, 5, 6])
+    rp, col, wt = h.arrays()
+    assert h.nv == 4 and h.ne == 6 and rp.tolist() == [0, 1, 3, 5, 6]
+    with pytest.raises(mg.MGError):
+        mg.HostGraph.from_entries(3, [0], [5])
+    with pytest.raises(mg.MGError):
+        mg.HostGraph.from_csr([0, 2, 1], [0, 1])
+    g = mg.HostGraph.from_csr([0, 1, 2], [1, 0])
+    assert g.nv == 2 and g.ne == 2
+
+
+# --------------------------------------------------------------------------
+# generators and the writer
+# --------------------------------------------------------------------------
+def test_rmat_deterministic_and_threads_independent():
+    a = mg.HostGraph.rmat(10, 8, seed=5, nthreads=1).arrays()
+    b = mg.HostGraph.rmat(10, 8, seed=5, nthreads=4).arrays()
+    c = mg.HostGraph.rmat(10, 8, seed=6).arrays()
+    for x, y in zip(a, b):
+        assert np.array_equal(x, y)
+    assert not np.array_equal(a[1], c[1])
+    rp, col, wt = a
+    n = len(rp) - 1
+    rows = np.repeat(np.arange(n), np.diff(rp))
+    assert not np.any(rows == col)                      # no self-loops
+    key = rows.astype(np.int64) * n + col
+    assert len(np.unique(key)) == len(key)              # no duplicates
+    assert np.all(np.diff(rp) > 0)                      # compaction: no isolated vertices
+    assert wt.min() >= 1 and wt.max() <= 64
+    rkey = col.astype(np.int64) * n + rows
+    assert np.array_equal(np.sort(rkey), np.sort(key))  # symmetric
+
+
+def test_lattice_shape():
+    h = mg.HostGraph.lattice(5, 4, 0.0)
+    assert h.nv == 20 and h.ne == 2 * (5 * 3 + 4 * 4)
+    h2 = mg.HostGraph.lattice(30, 30, 0.05, seed=1)
+    assert h2.ne > 2 * (30 * 29 * 2)
+
+
+def test_write_mtx_round_trip():
+    tmp = tempfile.mkdtemp()
+    h = mg.HostGraph.rmat(9, 8, seed=2)
+    p = os.path.join(tmp, "r.mtx")
+    h.write_mtx(p, True)
+    back = mg.HostGraph.load_mtx(p, 0, mg.LOAD_SYM)
+    for x, y in zip(h.arrays(), back.arrays()):
+        assert np.array_equal(x, y)
+    o = O.load_mtx(p, 0, O.LOAD_SYM)
+    assert np.array_equal(o.csc_e, h.arrays()[1])
+
+
+# --------------------------------------------------------------------------
+# failure injection (host side): the k-th allocation fails
+# --------------------------------------------------------------------------
+def test_allocation_failure_injection():
+    code = ("import multigraph_gb300 as mg\n"
+            "try:\n    mg.HostGraph.rmat(8, 8)\n    print('NOFAIL')\n"
+            "except mg.MGError as e:\n    print('STATUS', e.status)\n")
+    for k in (1, 3, 6):
+        env = dict(os.environ, MG_FAIL_ALLOC_AT=str(k), PYTHONPATH=ROOT)
+        r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, env=env, timeout=120)
+        assert f"STATUS {mg.MG_ERR_OOM}" in r.stdout, (k, r.stdout, r.stderr)
+
+
+# --------------------------------------------------------------------------
+# CLI shell (no GPU needed for the argument checks)
+# --------------------------------------------------------------------------
+def test_cli_usage_and_errors():
+    cli = os.path.join(mg.BIN_DIR, "BFS")
+    r = subprocess.run([cli], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 2 and "usage" in r.stderr
+    r = subprocess.run([cli, "/nonexistent.mtx", "0", "1"], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 10 + mg.MG_ERR_IO and "load failed" in r.stderr
+
+
+# --------------------------------------------------------------------------
+# against the reference's own loader / validator (oracle/_ref), random graphs
+# --------------------------------------------------------------------------
+@pytest.mark.skipif(not HAVE_REF, reason="oracle/_ref not built (needs the reference tree)")
+@pytest.mark.parametrize("seed", [1, 2, 3])
+def test_loaders_and_oracle_against_reference(seed):
+    tmp = tempfile.mkdtemp()
+    p = os.path.join(tmp, "g.mtx")
+    mg.HostGraph.rmat(9 + seed, 8, seed=seed).write_mtx(p, True)
+    src = 3 * seed
+    ref = O.RefTool("SSSP").load(p, src, tmp)
+    orc = O.load_mtx(p, src, O.LOAD_SYM)
+    prod = mg.HostGraph.load_mtx(p, src, mg.LOAD_SYM)
+    for a, b, c in zip((ref.csc_v, ref.csc_e, ref.csc_ev), (orc.csc_v, orc.csc_e, orc.csc_ev), prod.arrays()):
+        assert np.array_equal(a, b) and np.array_equal(a, c)
+    assert ref.start_p == orc.start_p == prod.start_p
+    s = orc.start_p
+    assert O.RefTool("BFS").validate(p, src, [O.bfs(orc, s)], tmp).endswith("PASS")
+    assert O.RefTool("SSSP").validate(p, src, [O.sssp(orc, s)[0]], tmp).endswith("PASS")
+    assert O.RefTool("BC").validate(p, src, list(O.bc(orc, s)), tmp).endswith("PASS")
+    occ = O.load_mtx(p, 0, O.LOAD_SYM | O.LOAD_CC)
+    assert O.RefTool("CC").validate(p, 0, [O.cc_minlabel(occ)], tmp).endswith("PASS")
+    for mode, alg in ((0, "PR_T"), (1, "PR_D")):
+        assert O.RefTool(alg).validate(p, 0, [O.pr_ref(orc, mode)[0]], tmp).endswith("PASS")
+
+
+@pytest.mark.skipif(not HAVE_REF, reason="oracle/_ref not built (needs the reference tree)")
+def test_reference_validator_catches_planted_mistakes():
+    tmp = tempfile.mkdtemp()
+    p = os.path.join(tmp, "g.mtx")
+    mg.HostGraph.rmat(9, 8, seed=4).write_mtx(p, True)
+    orc = O.load_mtx(p, 0, O.LOAD_SYM)
+    lv = O.bfs(orc, 0)
+    lv[lv.argmax()] -= 1  # planted in the oracle's result, on the CPU
+    assert "FAIL" in O.RefTool("BFS").validate(p, 0, [lv], tmp)
+    d = O.sssp(orc, 0)[0]
+    d[5] += 1
+    assert "FAIL" in O.RefTool("SSSP").validate(p, 0, [d], tmp)
