@@ -75,7 +75,6 @@ struct Args {
     int32_t words;
     int32_t *queue;
     int32_t *heavy;      // 2 * n (parity)
-    int32_t *stamp;
     int32_t *lvl_off;
     FCtl *ctl;
 };
@@ -90,14 +89,16 @@ __device__ __forceinline__ void warp_add64(long long *dst, long long v)
     if (mgd::lane() == 0 && v) atomicAdd((unsigned long long *)dst, (unsigned long long)v);
 }
 
-// record a newly reached vertex in the next frontier (all lanes call)
+// record a newly reached vertex in the next frontier (push sweeps; all lanes
+// call).  SSSP has already set the vertex's bit when it claimed it.
+template <int ALG>
 __device__ __forceinline__ void emit_next(const Args &a, const FCtl &c, int nextbuf, bool found, int32_t v)
 {
     int slot = mgd::warp_append(&a.ctl->nq, found);
     long long d = 0;
     if (found) {
         a.queue[c.nqoff + slot] = v;
-        mgd::bm_set(bm_buf(a, nextbuf), v);
+        if (ALG != ALG_SSSP) mgd::bm_set(bm_buf(a, nextbuf), v);
         int32_t dg = a.row[v + 1] - a.row[v];
         d = dg;
         if (dg > PUSH_HEAVY) {
@@ -113,7 +114,7 @@ __device__ __forceinline__ void emit_next(const Args &a, const FCtl &c, int next
 // ----------------------------------------------------------------------------
 template <int ALG>
 __device__ __forceinline__ bool push_edge(const Args &a, int it1, int32_t v, int32_t payload_i, double payload_d,
-                                          int32_t w)
+                                          int32_t w, uint32_t *next_bm)
 {
     if (ALG == ALG_BFS) {
         if (mgd::bm_test(a.visited, v)) return false;
@@ -122,7 +123,7 @@ __device__ __forceinline__ bool push_edge(const Args &a, int it1, int32_t v, int
         return true;
     } else if (ALG == ALG_SSSP) {
         int32_t nd = mgops::Sssp::get_partial_result(payload_i, w);
-        return mgops::Sssp::fused_update_condition(&a.label[v], nd, it1, &a.stamp[v]);
+        return mgops::Sssp::fused_update_condition(&a.label[v], nd, next_bm, v);
     } else {
         bool on_level;
         bool claimed = mgops::BcForward::fused_update_condition(&a.label[v], it1, on_level);
@@ -162,9 +163,9 @@ __global__ void __launch_bounds__(THREADS) k_push(Args a)
             int32_t v = 0;
             if (k < e) {
                 v = a.col[k];
-                found = push_edge<ALG>(a, it1, v, pi, pd, (ALG == ALG_SSSP) ? a.wt[k] : 0);
+                found = push_edge<ALG>(a, it1, v, pi, pd, (ALG == ALG_SSSP) ? a.wt[k] : 0, bm_buf(a, nextbuf));
             }
-            emit_next(a, c, nextbuf, found, v);
+            emit_next<ALG>(a, c, nextbuf, found, v);
         }
         scanned += (threadIdx.x == 0 && blockIdx.x == 0) ? span : 0;
     }
@@ -195,9 +196,9 @@ __global__ void __launch_bounds__(THREADS) k_push(Args a)
             int32_t v = 0;
             if (k < total) {
                 v = a.col[e];
-                found = push_edge<ALG>(a, it1, v, opi, opd, (ALG == ALG_SSSP) ? a.wt[e] : 0);
+                found = push_edge<ALG>(a, it1, v, opi, opd, (ALG == ALG_SSSP) ? a.wt[e] : 0, bm_buf(a, nextbuf));
             }
-            emit_next(a, c, nextbuf, found, v);
+            emit_next<ALG>(a, c, nextbuf, found, v);
         }
     }
     if (lane == 0 && scanned) atomicAdd((unsigned long long *)&a.ctl->scanned, (unsigned long long)scanned);
@@ -206,46 +207,21 @@ __global__ void __launch_bounds__(THREADS) k_push(Args a)
 // ----------------------------------------------------------------------------
 // pull: row reductions over in-edges against the frontier bitmap
 // ----------------------------------------------------------------------------
-// Rows reached in a pull sweep are staged per warp (shared memory) and
-// appended to the next frontier at warp-uniform points with one global
-// reservation per flush.
+// A pull sweep only marks the rows it reaches in the next-frontier bitmap
+// (atomicOr on distinct words, no shared counter); k_compact then builds the
+// queue, the frontier's edge count and its heavy list from the bitmap.
 struct PullEmit {
     const Args &a;
-    mgd::WarpStage st;
-    int32_t nqoff;
-    int nextbuf;
-    int hpar;
-    long long scanned;
-    __device__ void flush()
-    {
-        __syncwarp();
-        const int cnt = *st.cnt;
-        if (cnt == 0) return;  // uniform: every lane reads the same word
-        const int ln = threadIdx.x & 31;
-        int base = 0;
-        if (ln == 0) base = atomicAdd(&a.ctl->nq, cnt);
-        base = __shfl_sync(0xffffffffu, base, 0);
-        long long dsum = 0;
-        for (int i = ln; i < cnt; i += 32) {
-            int32_t v = st.buf[i];
-            a.queue[nqoff + base + i] = v;
-            mgd::bm_set(bm_buf(a, nextbuf), v);
-            int32_t dg = a.row[v + 1] - a.row[v];
-            dsum += dg;
-            if (dg > PUSH_HEAVY) a.heavy[(size_t)(hpar ^ 1) * a.n + atomicAdd(&a.ctl->nhcur, 1)] = v;
-        }
-        warp_add64(&a.ctl->nf_edges, dsum);
-        __syncwarp();
-        if (ln == 0) *st.cnt = 0;
-        __syncwarp();
-    }
+    uint32_t *next_bm;
+    __device__ void flush() {}
 };
 
 template <int ALG>
 struct PullOp;
 
 // SSSP: min over frontier in-neighbours of dist[u] + w (accumulate_nonAtomics
-// in row order), then one atomicMin + stamp on the row (fused_update_condition)
+// in row order), then one atomicMin + next-frontier bit on the row
+// (fused_update_condition)
 template <>
 struct PullOp<ALG_SSSP> : PullEmit {
     using T = int32_t;
@@ -264,10 +240,7 @@ struct PullOp<ALG_SSSP> : PullEmit {
         mgops::Sssp::accumulate_nonAtomics(x, y, 0);
         return x;
     }
-    __device__ void finish(int32_t v, T best)
-    {
-        if (mgops::Sssp::fused_update_condition(&a.label[v], best, it1, &a.stamp[v])) st.push(v);
-    }
+    __device__ void finish(int32_t v, T best) { mgops::Sssp::fused_update_condition(&a.label[v], best, next_bm, v); }
 };
 
 // BC forward: unvisited rows sum the path counts of frontier in-neighbours
@@ -292,7 +265,7 @@ struct PullOp<ALG_BC> : PullEmit {
             a.label[v] = it1;
             a.sigma[v] = s;
             mgd::bm_set(a.visited, v);
-            st.push(v);
+            mgd::bm_set(next_bm, v);
         }
     }
 };
@@ -331,19 +304,14 @@ __global__ void __launch_bounds__(THREADS) k_pull(Args a)
                     if (found) {
                         a.label[v] = it1;
                         mgd::bm_set(a.visited, v);
+                        mgd::bm_set(bm_buf(a, nextbuf), v);
                     }
                 }
             }
-            emit_next(a, c, nextbuf, found, v);
         }
     } else {
-        // degree-binned rows; reached rows staged per warp (<= 32 between flushes)
-        __shared__ int32_t s_stage[THREADS / 32][32];
-        __shared__ int32_t s_cnt[THREADS / 32];
-        const int wib = threadIdx.x >> 5;
-        if (lane == 0) s_cnt[wib] = 0;
-        __syncwarp();
-        PullOp<ALG> op{{a, {s_stage[wib], &s_cnt[wib]}, c.nqoff, nextbuf, c.hpar, 0}, fb, it1};
+        // degree-binned rows; reached rows marked in the next-frontier bitmap
+        PullOp<ALG> op{{a, bm_buf(a, nextbuf)}, fb, it1};
         mgd::bins_reduce(op, a.trow, a.tcol, a.twt, a.wrows, a.nwrows, a.trows, a.ntrows);
         (void)gwarp;
         (void)nwarps;
@@ -384,31 +352,70 @@ __global__ void __launch_bounds__(THREADS) k_pull(Args a)
         }
         if (lane == 0) { s_min[threadIdx.x >> 5] = best; s_sum[threadIdx.x >> 5] = ssum; }
         __syncthreads();
-        bool found = false;
         if (threadIdx.x == 0) {
             int32_t bm = mgops::UNSET;
             double bs = 0.0;
             for (int w = 0; w < THREADS / 32; w++) { bm = min(bm, s_min[w]); bs += s_sum[w]; }
+            uint32_t *nb = bm_buf(a, nextbuf);
             if (s_hit) {
                 if (ALG == ALG_BFS) {
-                    if (atomicCAS(&a.label[v], mgops::UNSET, it1) == mgops::UNSET) { mgd::bm_set(a.visited, v); found = true; }
+                    if (atomicCAS(&a.label[v], mgops::UNSET, it1) == mgops::UNSET) {
+                        mgd::bm_set(a.visited, v);
+                        mgd::bm_set(nb, v);
+                    }
                 } else if (ALG == ALG_SSSP) {
-                    int32_t old = atomicMin(&a.label[v], bm);
-                    if (bm < old && atomicMax(&a.stamp[v], it1) < it1) found = true;
+                    mgops::Sssp::fused_update_condition(&a.label[v], bm, nb, v);
                 } else {
                     bool on_level;
-                    found = mgops::BcForward::fused_update_condition(&a.label[v], it1, on_level);
+                    bool found = mgops::BcForward::fused_update_condition(&a.label[v], it1, on_level);
                     if (on_level) mgops::BcForward::accumulate(&a.sigma[v], bs);
-                    if (found) mgd::bm_set(a.visited, v);
+                    if (found) {
+                        mgd::bm_set(a.visited, v);
+                        mgd::bm_set(nb, v);
+                    }
                 }
             }
             scanned += e - b;
         }
         __syncthreads();
-        if (threadIdx.x < 32) emit_next(a, c, nextbuf, found && threadIdx.x == 0, v);
-        __syncthreads();
     }
     warp_add64(&a.ctl->scanned, scanned);
+}
+
+// ----------------------------------------------------------------------------
+// compact: after a pull sweep, the next frontier's bitmap -> queue slice,
+// edge count and heavy list.  Each warp takes 32 bitmap words (1024
+// vertices) and reserves its queue slots with one atomicAdd.
+// ----------------------------------------------------------------------------
+__global__ void __launch_bounds__(THREADS) k_compact(Args a)
+{
+    const FCtl c = *a.ctl;
+    if (c.mode != MODE_PULL || c.more == 0) return;
+    const uint32_t *nb = bm_buf(a, (c.cur + 1) % 3);
+    const int lane = mgd::lane();
+    const int gwarp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int nwarps = (gridDim.x * blockDim.x) >> 5;
+    long long dsum = 0;
+    for (int32_t w0 = gwarp * 32; w0 < a.words; w0 += nwarps * 32) {
+        const int32_t wi = w0 + lane;
+        uint32_t bits = wi < a.words ? nb[wi] : 0u;
+        const int cnt = __popc(bits);
+        const int incl = mgd::warp_scan_incl(cnt);
+        const int total = __shfl_sync(0xffffffffu, incl, 31);
+        int base = 0;
+        if (lane == 31 && total) base = atomicAdd(&a.ctl->nq, total);
+        base = __shfl_sync(0xffffffffu, base, 31) + incl - cnt;
+        while (bits) {
+            const int b = __ffs(bits) - 1;
+            bits &= bits - 1;
+            const int32_t v = wi * 32 + b;
+            a.queue[c.nqoff + base++] = v;
+            const int32_t dg = a.row[v + 1] - a.row[v];
+            dsum += dg;
+            if (dg > PUSH_HEAVY) a.heavy[(size_t)(c.hpar ^ 1) * a.n + atomicAdd(&a.ctl->nhcur, 1)] = v;
+        }
+    }
+    warp_add64(&a.ctl->nf_edges, dsum);
 }
 
 // ----------------------------------------------------------------------------
@@ -489,7 +496,6 @@ __global__ void k_init(Args a, int32_t src, const int32_t *srcs, int32_t nsrc, i
         if (!mgd::bm_set(a.visited, s)) continue;  // duplicate source
         a.label[s] = 0;
         if (ALG == ALG_BC) a.sigma[s] = 1.0;
-        if (ALG == ALG_SSSP) a.stamp[s] = 0;
         mgd::bm_set(a.bm, s);  // buffer 0 is the current frontier
         a.queue[q++] = s;
         int32_t d = a.row[s + 1] - a.row[s];
@@ -648,7 +654,7 @@ __global__ void k_bc_back_init(const FCtl *fc, BCtl *bc_ctl, int32_t src)
 // workspace
 // ----------------------------------------------------------------------------
 struct FrontierWS {
-    mgi::DevBuf label, sigma, bm, visited, queue, heavy, stamp, lvl_off, ctl;
+    mgi::DevBuf label, sigma, bm, visited, queue, heavy, lvl_off, ctl;
     mgi::DevBuf q, delta, bc, bctl, bheavy, srcbuf;
     mgi::LoopGraph lg[3];
     mgi::LoopGraph lg_back;
@@ -660,7 +666,7 @@ void free_frontier_ws(mg_graph *g)
 {
     if (!g->fws) return;
     FrontierWS *w = g->fws;
-    DevBuf *bufs[] = {&w->label, &w->sigma, &w->bm, &w->visited, &w->queue, &w->heavy, &w->stamp,
+    DevBuf *bufs[] = {&w->label, &w->sigma, &w->bm, &w->visited, &w->queue, &w->heavy,
                       &w->lvl_off, &w->ctl, &w->q, &w->delta, &w->bc, &w->bctl, &w->bheavy, &w->srcbuf};
     for (DevBuf *b : bufs) dev_free(*b);
     for (auto &l : w->lg) l.destroy();
@@ -682,7 +688,6 @@ static mg_status ensure_ws(mg_graph *g, int alg)
     MG_TRY(dev_alloc(w->heavy, 2 * n * 4));
     MG_TRY(dev_alloc(w->ctl, sizeof(FCtl)));
     MG_TRY(dev_alloc(w->lvl_off, (n + 3) * 4));
-    if (alg == ALG_SSSP) MG_TRY(dev_alloc(w->stamp, n * 4));
     if (alg == ALG_BC) MG_TRY(dev_alloc(w->sigma, n * 8));
     return MG_OK;
 }
@@ -707,7 +712,6 @@ static Args make_args(mg_graph *g)
     a.words = (std::max(g->nv, 1) + 31) / 32;
     a.queue = w->queue.as<int32_t>();
     a.heavy = w->heavy.as<int32_t>();
-    a.stamp = w->stamp.as<int32_t>();
     a.lvl_off = w->lvl_off.as<int32_t>();
     a.ctl = w->ctl.as<FCtl>();
     return a;
@@ -716,7 +720,7 @@ static Args make_args(mg_graph *g)
 static uint64_t key_of(const Args &a, int alg)
 {
     uint64_t k = 1469598103934665603ull ^ (uint64_t)alg;
-    const void *ptrs[] = {a.row, a.col, a.trow, a.tcol, a.label, a.sigma, a.bm, a.queue, a.heavy, a.stamp, a.ctl, a.wrows};
+    const void *ptrs[] = {a.row, a.col, a.trow, a.tcol, a.label, a.sigma, a.bm, a.queue, a.heavy, a.ctl, a.wrows};
     for (const void *p : ptrs) k = (k ^ (uint64_t)(uintptr_t)p) * 1099511628211ull;
     return k;
 }
@@ -744,7 +748,6 @@ static mg_status frontier_run_impl(mg_graph *g, int alg, int32_t src, const int3
     MG_CUDA(cudaMemsetAsync(a.label, 0x64, n * 4, s));
     MG_CUDA(cudaMemsetAsync(a.bm, 0, 3 * (size_t)a.words * 4, s));
     MG_CUDA(cudaMemsetAsync(a.visited, 0, (size_t)a.words * 4, s));
-    if (alg == ALG_SSSP) MG_CUDA(cudaMemsetAsync(a.stamp, 0xff, n * 4, s));
     if (alg == ALG_BC) MG_CUDA(cudaMemsetAsync(a.sigma, 0, n * 8, s));
     int max_iter = opt.max_iter > 0 ? opt.max_iter : (alg == ALG_SSSP ? 4 * g->nv + 16 : g->nv + 2);
     int alpha = opt.alpha > 0 ? opt.alpha : 15, beta = opt.beta > 0 ? opt.beta : 18;
@@ -759,6 +762,7 @@ static mg_status frontier_run_impl(mg_graph *g, int alg, int32_t src, const int3
     Profiler &P = g->prof;
     const int sp = P.slot(alg == ALG_SSSP ? "sssp_push" : alg == ALG_BC ? "bc_push" : "bfs_push");
     const int sl = P.slot(alg == ALG_SSSP ? "sssp_pull" : alg == ALG_BC ? "bc_pull" : "bfs_pull");
+    const int sc = P.slot("frontier_compact");
     const int sd = P.slot("frontier_decide");
     BodyFn body = [&](cudaStream_t st, cudaGraphConditionalHandle h, int use_cond) -> mg_status {
         P.begin(sp);
@@ -774,6 +778,9 @@ static mg_status frontier_run_impl(mg_graph *g, int alg, int32_t src, const int3
         case ALG_SSSP: k_pull<ALG_SSSP><<<grid, THREADS, 0, st>>>(a); break;
         default: k_pull<ALG_BC><<<grid, THREADS, 0, st>>>(a); break;
         }
+        P.end();
+        P.begin(sc);
+        k_compact<<<grid, THREADS, 0, st>>>(a);
         P.end();
         P.begin(sd);
         k_decide<<<1, 32, 0, st>>>(a, h, use_cond);

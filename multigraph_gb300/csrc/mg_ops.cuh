@@ -53,14 +53,18 @@ struct Sssp {
         if (data < acc) acc = data;
     }
     __device__ static __forceinline__ bool update_condition(int32_t old, int32_t acc, int32_t) { return acc < old; }
-    // atomicMin on the distance, then an iteration stamp so a destination is
-    // enqueued once per iteration (the reference's atomicMax on vfc)
-    __device__ static __forceinline__ bool fused_update_condition(int32_t *loc, int32_t data, int32_t iter,
-                                                                  int32_t *stamp)
+    // atomicMin on the distance, then the destination's bit in the next
+    // frontier bitmap so it is enqueued once per iteration (the reference
+    // stamps vfc with atomicMax for the same purpose)
+    __device__ static __forceinline__ bool fused_update_condition(int32_t *loc, int32_t data, uint32_t *next_bm,
+                                                                  int32_t v)
     {
         if (data < *loc) {
             int32_t old = atomicMin(loc, data);
-            if (data < old && atomicMax(stamp, iter) < iter) return true;
+            if (data < old) {
+                uint32_t bit = 1u << (v & 31);
+                return (atomicOr(&next_bm[v >> 5], bit) & bit) == 0;
+            }
         }
         return false;
     }
