@@ -25,7 +25,7 @@ LIB = os.path.join(PKG, "libmg.so")
 BIN = os.path.join(PKG, "bin")
 
 GENCODE = "-gencode=arch=compute_103a,code=sm_103a"
-CU_SOURCES = ["mg_device.cu", "mg_frontier.cu", "mg_pr.cu", "mg_cc.cu", "mg_tune.cu", "mg_noalloc.cu"]
+CU_SOURCES = ["mg_device.cu", "mg_frontier.cu", "mg_pr.cu", "mg_cc.cu", "mg_tune.cu", "mg_noalloc.cu", "mg_bcb.cu"]
 CPP_SOURCES = ["mg_host.cpp"]
 CLI_NAMES = ["BFS", "SSSP", "BC", "CC", "DATA_DRIVEN_PR", "TOPOLOGY_DRIVEN_PR"]
 

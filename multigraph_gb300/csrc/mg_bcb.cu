@@ -1,0 +1,661 @@
+// mg_bcb.cu -- batched multi-source Brandes BC: 32 sources per traversal,
+// one lane of a warp per source.
+//
+// The reference runs one BC source per program invocation (main.cu:52-86:
+// MultiGraph_V_E_V forward, then MultiGraph_V_E_V_pull backward over the
+// archived levels, process2.cu:263-325).  Here a group of up to 32 sources
+// is traversed together, level-synchronously:
+//
+//   vis[v]   bit s set once v has been reached from source s
+//   fm[v]    bit s set when v is on source s's current frontier
+//   sig[v*32+s]  FP64 path count of v from source s
+//   q[v*32+s]    (1 + delta_s[v]) / sig_s[v]   (FP32, backward)
+//   archive  (vertex, mask) entries, grouped by level: entry (v, M) at
+//            level d means v is at distance d from exactly the sources in M
+//
+// Forward level d -> d+1 (five launches, looped by a CUDA-graph WHILE node):
+//   k_bb_mark     sparse levels only: frontier entries scan their out-edges
+//                 and collect the distinct candidate destinations (a vertex
+//                 not yet reached by some source of the entry's mask)
+//   k_bb_pull     each candidate row (sparse) or every row that some source
+//                 has not reached (dense) scans its in-edges; a warp loads 32
+//                 column ids and their frontier masks at once, keeps the
+//                 lanes that hit (ballot), and lane s adds sig[u*32+s] for
+//                 each hit of source s.  Rows above heavy_deg go in 2048-edge
+//                 chunks whose partials land in hpart.
+//   k_bb_heavy    folds the chunk partials of heavy rows in chunk order
+//   k_bb_compact  archives the new frontier (one atomic per warp), sums its
+//                 out-degrees for the direction switch, clears the old
+//                 frontier's masks
+//   k_bb_decide   next level, sparse/dense choice (Beamer: frontier
+//                 out-edges x alpha against m), loop condition
+// Backward level L (four launches): the level-L masks are scattered into a
+// dense array, every level-L entry sums q over successors whose level-(L+1)
+// mask shares the source, and lane s finishes
+//   delta_s[u] = sig_s[u] * sum,  q_s[u] = (1 + delta_s[u]) / sig_s[u]
+// with the per-vertex score bc[u] += sum of delta_s[u] over the entry's
+// sources (u excluded as its own source).
+//
+// Every sum runs in a fixed order (the warp's edge order, then chunk order),
+// so results do not depend on scheduling; path counts are integers in FP64
+// and exact up to 2^53.  The column stream and the frontier-mask gathers are
+// shared by the 32 sources of a group, which is where the batch gains over
+// one traversal per source.
+
+#include "mg_device.cuh"
+
+#include <algorithm>
+#include <cstring>
+#include <vector>
+
+namespace {
+
+constexpr int W = 32;                 // sources per group (one per lane)
+constexpr int THREADS = 256;
+constexpr int32_t MARK_HEAVY = 2048;  // frontier entries above this out-degree are marked by the whole grid
+
+struct BbCtl {
+    int32_t more;
+    int32_t d;          // forward level being expanded
+    int32_t cur;        // fm buffer holding level d
+    int32_t dense;      // this level pulls over every row
+    int32_t ncand;      // sparse: candidate rows (atomic)
+    int32_t nnew;       // entries archived at level d+1 (atomic)
+    int32_t nfh;        // heavy frontier entries at level d
+    int32_t nfh_build;  // heavy entries of level d+1 (atomic)
+    int32_t nlevels;    // levels 0..nlevels-1 archived (set when the forward sweep ends)
+    int32_t L;          // backward level
+    int32_t status;     // 1: level cap reached
+    int32_t dirmode;    // MG_DIR_*
+    int32_t alpha;
+    int32_t max_levels;
+    uint32_t gmask;     // lanes holding a source
+    int32_t dense_levels;
+    unsigned long long nfe;      // out-edges of level d+1 (atomic)
+    unsigned long long nfe_cur;  // out-edges of level d
+};
+
+struct BbArgs {
+    int32_t n;
+    int32_t m;
+    const int32_t *row, *col;    // out-edges
+    const int32_t *trow, *tcol;  // in-edges
+    const int32_t *hchunk;       // (row, begin, end) of the heavy in-rows
+    int32_t nhchunks;
+    const int32_t *hrows, *hrow_chunk;
+    int32_t nhrows;
+    int32_t heavy_deg;
+    uint32_t *vis;
+    uint32_t *fm0, *fm1;
+    uint32_t *cbm;               // candidate bitmap (sparse levels)
+    int32_t *cand;
+    int32_t *arch;
+    uint32_t *amask;
+    size_t cap;                  // archive capacity (32 n)
+    int32_t *off;                // level offsets into the archive
+    double *sig;
+    float *q;
+    double *hpart;               // per chunk x 32 lanes (backward reuses it as float)
+    uint32_t *hmask;
+    double *bc;                  // score accumulator (all groups)
+    int32_t *fheavy;
+    const int32_t *src;          // the group's sources (engine ids), W entries
+    BbCtl *ctl;
+};
+
+__device__ __forceinline__ uint32_t *fm_of(const BbArgs &a, int i) { return i ? a.fm1 : a.fm0; }
+
+__device__ __forceinline__ unsigned long long warp_sum_u64(unsigned long long x)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+    return x;
+}
+
+// ---------------------------------------------------------------------------
+// forward
+// ---------------------------------------------------------------------------
+__global__ void k_bb_init(BbArgs a, int32_t nsrc, int32_t dirmode, int32_t alpha, int32_t max_levels)
+{
+    const int lane = threadIdx.x;
+    const bool valid = lane < nsrc;
+    const int32_t v = valid ? a.src[lane] : -1 - lane;
+    const uint32_t same = __match_any_sync(0xffffffffu, v);
+    const bool leader = valid && lane == __ffs(same) - 1;
+    if (valid) a.sig[(size_t)v * W + lane] = 1.0;
+    const uint32_t leaders = __ballot_sync(0xffffffffu, leader);
+    unsigned long long deg = 0;
+    int heavy = 0;
+    if (leader) {
+        const int pos = __popc(leaders & ((1u << lane) - 1u));
+        a.vis[v] = same;
+        a.fm0[v] = same;
+        a.arch[pos] = v;
+        a.amask[pos] = same;
+        const int32_t d = a.row[v + 1] - a.row[v];
+        deg = (unsigned long long)d;
+        heavy = d > MARK_HEAVY;
+    }
+    const uint32_t hv = __ballot_sync(0xffffffffu, heavy);
+    if (heavy) a.fheavy[__popc(hv & ((1u << lane) - 1u))] = v;
+    deg = warp_sum_u64(deg);
+    if (lane == 0) {
+        BbCtl c;
+        memset(&c, 0, sizeof(c));
+        const int cnt = __popc(leaders);
+        c.more = cnt > 0;
+        c.d = 0;
+        c.cur = 0;
+        c.dirmode = dirmode;
+        c.alpha = alpha;
+        c.max_levels = max_levels;
+        c.gmask = nsrc >= 32 ? 0xffffffffu : ((1u << nsrc) - 1u);
+        c.nfh = __popc(hv);
+        c.nfe_cur = deg;
+        c.dense = dirmode == MG_DIR_PULL;
+        c.dense_levels = c.dense;
+        a.off[0] = 0;
+        a.off[1] = cnt;
+        *a.ctl = c;
+    }
+}
+
+__device__ __forceinline__ void mark_edge_block(const BbArgs &a, int32_t p, int32_t e, uint32_t f)
+{
+    bool pred = false;
+    int32_t v = 0;
+    if (p < e) {
+        v = __ldg(&a.col[p]);
+        pred = (f & ~a.vis[v]) != 0 && mgd::bm_set(a.cbm, v);
+    }
+    int slot = mgd::warp_append(&a.ctl->ncand, pred);
+    if (pred) a.cand[slot] = v;
+}
+
+__global__ void __launch_bounds__(THREADS) k_bb_mark(BbArgs a)
+{
+    const BbCtl c = *a.ctl;
+    if (c.more == 0 || c.dense) return;
+    const int lane = mgd::lane();
+    const int gwarp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int nwarps = (gridDim.x * blockDim.x) >> 5;
+    const int32_t b0 = a.off[c.d], b1 = a.off[c.d + 1];
+    for (int32_t i = b0 + gwarp; i < b1; i += nwarps) {
+        const int32_t u = a.arch[i];
+        const uint32_t f = a.amask[i];
+        const int32_t b = a.row[u], e = a.row[u + 1];
+        if (e - b > MARK_HEAVY) continue;
+        for (int32_t base = b; base < e; base += 32) mark_edge_block(a, base + lane, e, f);
+    }
+    // heavy frontier entries: every warp of the grid takes 32-edge slices
+    const uint32_t *fcur = fm_of(a, c.cur);
+    for (int32_t h = 0; h < c.nfh; h++) {
+        const int32_t u = a.fheavy[h];
+        const uint32_t f = fcur[u];
+        const int32_t b = a.row[u], e = a.row[u + 1];
+        for (int32_t base = b + gwarp * 32; base < e; base += nwarps * 32) mark_edge_block(a, base + lane, e, f);
+    }
+}
+
+// One row's in-edges [b, e) against the frontier masks: lane s returns the
+// sum of sig over in-neighbours on source s's frontier; *hit gets the union
+// of the masks that hit (restricted to `want`).
+__device__ __forceinline__ double pull_span(const BbArgs &a, const uint32_t *fcur, int32_t b, int32_t e,
+                                            uint32_t want, uint32_t &hit)
+{
+    const int lane = mgd::lane();
+    double acc = 0.0;
+    uint32_t newm = 0;
+    for (int32_t base = b; base < e; base += 32) {
+        const int32_t p = base + lane;
+        int32_t u = 0;
+        uint32_t f = 0;
+        if (p < e) {
+            u = __ldg(&a.tcol[p]);
+            f = fcur[u] & want;
+        }
+        unsigned hits = __ballot_sync(0xffffffffu, f != 0);
+        while (hits) {
+            const int j = __ffs(hits) - 1;
+            hits &= hits - 1;
+            const int32_t uj = __shfl_sync(0xffffffffu, u, j);
+            const uint32_t fj = __shfl_sync(0xffffffffu, f, j);
+            newm |= fj;
+            if ((fj >> lane) & 1u) acc += a.sig[(size_t)uj * W + lane];
+        }
+    }
+    hit = newm;
+    return acc;
+}
+
+__device__ __forceinline__ void settle_row(const BbArgs &a, uint32_t *fnext, int32_t v, uint32_t newm, double acc)
+{
+    const int lane = mgd::lane();
+    if ((newm >> lane) & 1u) a.sig[(size_t)v * W + lane] = acc;
+    if (lane == 0) {
+        a.vis[v] |= newm;
+        fnext[v] = newm;
+    }
+}
+
+__global__ void __launch_bounds__(THREADS) k_bb_pull(BbArgs a)
+{
+    const BbCtl c = *a.ctl;
+    if (c.more == 0) return;
+    const int lane = mgd::lane();
+    const int gwarp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int nwarps = (gridDim.x * blockDim.x) >> 5;
+    const uint32_t *fcur = fm_of(a, c.cur);
+    uint32_t *fnext = fm_of(a, c.cur ^ 1);
+    const int32_t nrows = c.dense ? a.n : c.ncand;
+    for (int32_t i = gwarp; i < nrows; i += nwarps) {
+        const int32_t v = c.dense ? i : a.cand[i];
+        const uint32_t want = ~a.vis[v] & c.gmask;
+        if (want == 0) continue;
+        const int32_t b = a.trow[v], e = a.trow[v + 1];
+        if (e - b > a.heavy_deg) continue;  // chunk path below
+        uint32_t newm;
+        const double acc = pull_span(a, fcur, b, e, want, newm);
+        if (newm) settle_row(a, fnext, v, newm, acc);
+    }
+    for (int32_t ch = gwarp; ch < a.nhchunks; ch += nwarps) {
+        const int32_t v = a.hchunk[3 * ch], b = a.hchunk[3 * ch + 1], e = a.hchunk[3 * ch + 2];
+        uint32_t want = ~a.vis[v] & c.gmask;
+        if (!c.dense && !mgd::bm_test(a.cbm, v)) want = 0;
+        uint32_t newm = 0;
+        double acc = 0.0;
+        if (want) acc = pull_span(a, fcur, b, e, want, newm);
+        if (newm) a.hpart[(size_t)ch * W + lane] = acc;
+        if (lane == 0) a.hmask[ch] = newm;
+    }
+}
+
+__global__ void __launch_bounds__(THREADS) k_bb_heavy(BbArgs a)
+{
+    const BbCtl c = *a.ctl;
+    if (c.more == 0) return;
+    const int lane = mgd::lane();
+    const int gwarp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int nwarps = (gridDim.x * blockDim.x) >> 5;
+    uint32_t *fnext = fm_of(a, c.cur ^ 1);
+    for (int32_t i = gwarp; i < a.nhrows; i += nwarps) {
+        const int32_t v = a.hrows[i], k0 = a.hrow_chunk[i], k1 = a.hrow_chunk[i + 1];
+        uint32_t newm = 0;
+        double acc = 0.0;
+        for (int32_t k = k0; k < k1; k++) {
+            const uint32_t hm = a.hmask[k];
+            newm |= hm;
+            if ((hm >> lane) & 1u) acc += a.hpart[(size_t)k * W + lane];
+        }
+        if (newm) settle_row(a, fnext, v, newm, acc);
+    }
+}
+
+__global__ void __launch_bounds__(THREADS) k_bb_compact(BbArgs a)
+{
+    BbCtl *cp = a.ctl;
+    const BbCtl c = *cp;
+    if (c.more == 0) return;
+    const int lane = mgd::lane();
+    const int gtid = blockIdx.x * blockDim.x + threadIdx.x;
+    const int gwarp = gtid >> 5;
+    const int nwarps = (gridDim.x * blockDim.x) >> 5;
+    uint32_t *fcur = fm_of(a, c.cur);
+    const uint32_t *fnext = fm_of(a, c.cur ^ 1);
+    // the old frontier's masks (every reader of level d has finished)
+    for (int32_t i = a.off[c.d] + gtid; i < a.off[c.d + 1]; i += gridDim.x * blockDim.x) fcur[a.arch[i]] = 0;
+    const int32_t base_out = a.off[c.d + 1];
+    const int32_t nrows = c.dense ? a.n : c.ncand;
+    for (int32_t base = gwarp * 32; base < nrows; base += nwarps * 32) {
+        const int32_t i = base + lane;
+        int32_t v = -1;
+        uint32_t msk = 0;
+        if (i < nrows) {
+            v = c.dense ? i : a.cand[i];
+            if (!c.dense) atomicAnd(&a.cbm[v >> 5], ~(1u << (v & 31)));
+            msk = fnext[v];
+        }
+        const bool pred = msk != 0;
+        int32_t deg = 0;
+        if (pred) deg = a.row[v + 1] - a.row[v];
+        const int slot = mgd::warp_append(&cp->nnew, pred);
+        if (pred) {
+            const size_t at = (size_t)base_out + (size_t)slot;
+            if (at < a.cap) {
+                a.arch[at] = v;
+                a.amask[at] = msk;
+            } else {
+                cp->status = 2;
+            }
+            if (deg > MARK_HEAVY) a.fheavy[atomicAdd(&cp->nfh_build, 1)] = v;
+        }
+        const unsigned long long s = warp_sum_u64((unsigned long long)deg);
+        if (lane == 0 && s) atomicAdd(&cp->nfe, s);
+    }
+}
+
+__global__ void k_bb_decide(BbArgs a, cudaGraphConditionalHandle h, int use_cond)
+{
+    if (threadIdx.x != 0) return;
+    BbCtl *cp = a.ctl;
+    BbCtl c = *cp;
+    if (c.more) {
+        const int32_t nnew = c.nnew;
+        a.off[c.d + 2] = a.off[c.d + 1] + nnew;
+        if (nnew == 0 || c.status) {
+            c.more = 0;
+            c.nlevels = c.d + 1;
+        } else if (c.d + 2 >= c.max_levels) {
+            c.more = 0;
+            c.status = 1;
+            c.nlevels = c.d + 2;
+        } else {
+            c.d += 1;
+            c.cur ^= 1;
+            c.nfe_cur = c.nfe;
+            c.nfh = c.nfh_build;
+            if (c.dirmode == MG_DIR_PUSH) c.dense = 0;
+            else if (c.dirmode == MG_DIR_PULL) c.dense = 1;
+            else c.dense = c.nfe_cur * (unsigned long long)c.alpha > (unsigned long long)a.m;
+            c.dense_levels += c.dense;
+        }
+        c.nfe = 0;
+        c.nnew = 0;
+        c.ncand = 0;
+        c.nfh_build = 0;
+        *cp = c;
+    }
+    if (use_cond) cudaGraphSetConditional(h, c.more ? 1u : 0u);
+}
+
+// ---------------------------------------------------------------------------
+// backward
+// ---------------------------------------------------------------------------
+__global__ void k_bbb_init(BbArgs a)
+{
+    if (threadIdx.x != 0) return;
+    BbCtl *cp = a.ctl;
+    cp->L = cp->nlevels - 1;
+    cp->more = cp->status == 0 && cp->L >= 1;
+}
+
+// level-L masks into fm[L & 1] (zero before this launch)
+__global__ void __launch_bounds__(THREADS) k_bbb_scatter(BbArgs a)
+{
+    const BbCtl c = *a.ctl;
+    if (c.more == 0) return;
+    uint32_t *cur = fm_of(a, c.L & 1);
+    for (int32_t i = a.off[c.L] + blockIdx.x * blockDim.x + threadIdx.x; i < a.off[c.L + 1];
+         i += gridDim.x * blockDim.x)
+        cur[a.arch[i]] = a.amask[i];
+}
+
+// successors' q summed for the sources in `want`: out-edges [b, e)
+__device__ __forceinline__ float back_span(const BbArgs &a, const uint32_t *nxt, const int32_t *col, int32_t b,
+                                           int32_t e, uint32_t want)
+{
+    const int lane = mgd::lane();
+    float acc = 0.0f;
+    for (int32_t base = b; base < e; base += 32) {
+        const int32_t p = base + lane;
+        int32_t v = 0;
+        uint32_t f = 0;
+        if (p < e) {
+            v = __ldg(&col[p]);
+            f = nxt[v] & want;
+        }
+        unsigned hits = __ballot_sync(0xffffffffu, f != 0);
+        while (hits) {
+            const int j = __ffs(hits) - 1;
+            hits &= hits - 1;
+            const int32_t vj = __shfl_sync(0xffffffffu, v, j);
+            const uint32_t fj = __shfl_sync(0xffffffffu, f, j);
+            if ((fj >> lane) & 1u) acc += a.q[(size_t)vj * W + lane];
+        }
+    }
+    return acc;
+}
+
+__device__ __forceinline__ void back_finish(const BbArgs &a, int32_t u, uint32_t msk, float s)
+{
+    const int lane = mgd::lane();
+    double contrib = 0.0;
+    if ((msk >> lane) & 1u) {
+        const double sg = a.sig[(size_t)u * W + lane];
+        const float dv = (float)(sg * (double)s);
+        a.q[(size_t)u * W + lane] = (float)((1.0 + (double)dv) / sg);
+        if (a.src[lane] != u) contrib = (double)dv;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) contrib += __shfl_xor_sync(0xffffffffu, contrib, o);
+    if (lane == 0) a.bc[u] += contrib;
+}
+
+__global__ void __launch_bounds__(THREADS) k_bbb_pull(BbArgs a)
+{
+    const BbCtl c = *a.ctl;
+    if (c.more == 0) return;
+    const int lane = mgd::lane();
+    const int gwarp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int nwarps = (gridDim.x * blockDim.x) >> 5;
+    const uint32_t *cur = fm_of(a, c.L & 1);
+    const uint32_t *nxt = fm_of(a, (c.L + 1) & 1);
+    for (int32_t i = a.off[c.L] + gwarp; i < a.off[c.L + 1]; i += nwarps) {
+        const int32_t u = a.arch[i];
+        const uint32_t msk = a.amask[i];
+        const int32_t b = a.row[u], e = a.row[u + 1];
+        if (e - b > a.heavy_deg) continue;  // chunk path below
+        const float s = back_span(a, nxt, a.col, b, e, msk);
+        back_finish(a, u, msk, s);
+    }
+    // heavy rows: the in-row chunks double as out-row chunks (symmetric graphs)
+    float *hp = reinterpret_cast<float *>(a.hpart);
+    for (int32_t ch = gwarp; ch < a.nhchunks; ch += nwarps) {
+        const int32_t u = a.hchunk[3 * ch];
+        const uint32_t msk = cur[u];
+        if (msk == 0) continue;
+        hp[(size_t)ch * W + lane] = back_span(a, nxt, a.tcol, a.hchunk[3 * ch + 1], a.hchunk[3 * ch + 2], msk);
+    }
+}
+
+__global__ void __launch_bounds__(THREADS) k_bbb_heavy(BbArgs a)
+{
+    const BbCtl c = *a.ctl;
+    if (c.more == 0) return;
+    const int lane = mgd::lane();
+    const int gtid = blockIdx.x * blockDim.x + threadIdx.x;
+    const int gwarp = gtid >> 5;
+    const int nwarps = (gridDim.x * blockDim.x) >> 5;
+    const uint32_t *cur = fm_of(a, c.L & 1);
+    uint32_t *nxt = fm_of(a, (c.L + 1) & 1);
+    const float *hp = reinterpret_cast<const float *>(a.hpart);
+    for (int32_t i = gwarp; i < a.nhrows; i += nwarps) {
+        const int32_t u = a.hrows[i];
+        const uint32_t msk = cur[u];
+        if (msk == 0) continue;
+        float s = 0.0f;
+        for (int32_t k = a.hrow_chunk[i]; k < a.hrow_chunk[i + 1]; k++) s += hp[(size_t)k * W + lane];
+        back_finish(a, u, msk, s);
+    }
+    // level L+1 is no longer read: clear its masks for level L-1
+    for (int32_t i = a.off[c.L + 1] + gtid; i < a.off[c.L + 2]; i += gridDim.x * blockDim.x) nxt[a.arch[i]] = 0;
+}
+
+__global__ void k_bbb_decide(BbArgs a, cudaGraphConditionalHandle h, int use_cond)
+{
+    if (threadIdx.x != 0) return;
+    BbCtl *cp = a.ctl;
+    int more = cp->more;
+    if (more) {
+        cp->L -= 1;
+        more = cp->L >= 1;
+        cp->more = more;
+    }
+    if (use_cond) cudaGraphSetConditional(h, more ? 1u : 0u);
+}
+
+__global__ void k_bb_to_float(int32_t n, const double *bc, float *out)
+{
+    for (int32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x) out[v] = (float)bc[v];
+}
+
+}  // namespace
+
+struct BcWS {
+    mgi::DevBuf vis, fm, cbm, cand, arch, amask, off, sig, q, hpart, hmask, bc, bcf, fheavy, src, ctl;
+    mgi::LoopGraph fwd, bwd;
+};
+
+namespace mgi {
+
+void free_bc_ws(mg_graph *g)
+{
+    if (!g->bws) return;
+    BcWS *w = g->bws;
+    DevBuf *bufs[] = {&w->vis, &w->fm, &w->cbm, &w->cand, &w->arch, &w->amask, &w->off, &w->sig,
+                      &w->q, &w->hpart, &w->hmask, &w->bc, &w->bcf, &w->fheavy, &w->src, &w->ctl};
+    for (DevBuf *b : bufs) dev_free(*b);
+    w->fwd.destroy();
+    w->bwd.destroy();
+    delete w;
+    g->bws = nullptr;
+}
+
+// Batched BC over engine-id sources; the float scores (engine order) are
+// left in the workspace and returned through *bc_dev.
+mg_status bc_batched(mg_graph *g, const int32_t *src_engine, int32_t nsrc, const mg_opts &opt, mg_run_info *info,
+                     const float **bc_dev)
+{
+    if (!g->symmetric) return fail(MG_ERR_UNSUPPORTED, "batched BC needs a structurally symmetric graph");
+    if (!g->bws) g->bws = new BcWS();
+    BcWS *w = g->bws;
+    const size_t n = (size_t)std::max(g->nv, 1);
+    const size_t words = (n + 31) / 32;
+    const size_t cap = n * W;
+    const size_t nch = (size_t)std::max(g->nhchunks, 1);
+    MG_TRY(dev_alloc(w->vis, n * 4));
+    MG_TRY(dev_alloc(w->fm, 2 * n * 4));
+    MG_TRY(dev_alloc(w->cbm, words * 4));
+    MG_TRY(dev_alloc(w->cand, n * 4));
+    MG_TRY(dev_alloc(w->arch, cap * 4));
+    MG_TRY(dev_alloc(w->amask, cap * 4));
+    MG_TRY(dev_alloc(w->off, (n + 4) * 4));
+    MG_TRY(dev_alloc(w->sig, cap * 8));
+    MG_TRY(dev_alloc(w->q, cap * 4));
+    MG_TRY(dev_alloc(w->hpart, nch * W * 8));
+    MG_TRY(dev_alloc(w->hmask, nch * 4));
+    MG_TRY(dev_alloc(w->bc, n * 8));
+    MG_TRY(dev_alloc(w->bcf, n * 4));
+    MG_TRY(dev_alloc(w->fheavy, n * 4));
+    MG_TRY(dev_alloc(w->src, W * 4));
+    MG_TRY(dev_alloc(w->ctl, sizeof(BbCtl)));
+
+    BbArgs a;
+    std::memset(&a, 0, sizeof(a));
+    a.n = g->nv;
+    a.m = g->ne;
+    a.row = g->row.as<int32_t>(); a.col = g->col.as<int32_t>();
+    a.trow = g->trow; a.tcol = g->tcol;
+    a.hchunk = g->hchunk.as<int32_t>(); a.nhchunks = g->nhchunks;
+    a.hrows = g->hrows.as<int32_t>(); a.hrow_chunk = g->hrow_chunk.as<int32_t>(); a.nhrows = g->nhrows;
+    a.heavy_deg = g->heavy_deg;
+    a.vis = w->vis.as<uint32_t>();
+    a.fm0 = w->fm.as<uint32_t>(); a.fm1 = a.fm0 + n;
+    a.cbm = w->cbm.as<uint32_t>();
+    a.cand = w->cand.as<int32_t>();
+    a.arch = w->arch.as<int32_t>();
+    a.amask = w->amask.as<uint32_t>();
+    a.cap = cap;
+    a.off = w->off.as<int32_t>();
+    a.sig = w->sig.as<double>();
+    a.q = w->q.as<float>();
+    a.hpart = w->hpart.as<double>();
+    a.hmask = w->hmask.as<uint32_t>();
+    a.bc = w->bc.as<double>();
+    a.fheavy = w->fheavy.as<int32_t>();
+    a.src = w->src.as<int32_t>();
+    a.ctl = w->ctl.as<BbCtl>();
+
+    cudaStream_t s = g->stream;
+    MG_CUDA(cudaMemsetAsync(a.bc, 0, n * 8, s));
+    MG_CUDA(cudaMemsetAsync(a.cbm, 0, words * 4, s));
+    const int grid = launch_grid(g, THREADS, 8);
+    const int alpha = opt.alpha > 0 ? opt.alpha : 15;
+    const int max_levels = g->nv + 2;
+    Profiler &P = g->prof;
+    const int s_mark = P.slot("bcb_mark"), s_pull = P.slot("bcb_pull"), s_heavy = P.slot("bcb_heavy");
+    const int s_comp = P.slot("bcb_compact"), s_dec = P.slot("bcb_decide");
+    const int s_bsc = P.slot("bcb_back_scatter"), s_bp = P.slot("bcb_back"), s_bh = P.slot("bcb_back_heavy");
+    const int s_bd = P.slot("bcb_back_decide");
+    BodyFn fwd = [&](cudaStream_t st, cudaGraphConditionalHandle h, int use_cond) -> mg_status {
+        P.begin(s_mark);
+        k_bb_mark<<<grid, THREADS, 0, st>>>(a);
+        P.end();
+        P.begin(s_pull);
+        k_bb_pull<<<grid, THREADS, 0, st>>>(a);
+        P.end();
+        P.begin(s_heavy);
+        k_bb_heavy<<<grid, THREADS, 0, st>>>(a);
+        P.end();
+        P.begin(s_comp);
+        k_bb_compact<<<grid, THREADS, 0, st>>>(a);
+        P.end();
+        P.begin(s_dec);
+        k_bb_decide<<<1, 32, 0, st>>>(a, h, use_cond);
+        P.end();
+        MG_CUDA(cudaGetLastError());
+        return MG_OK;
+    };
+    BodyFn bwd = [&](cudaStream_t st, cudaGraphConditionalHandle h, int use_cond) -> mg_status {
+        P.begin(s_bsc);
+        k_bbb_scatter<<<grid, THREADS, 0, st>>>(a);
+        P.end();
+        P.begin(s_bp);
+        k_bbb_pull<<<grid, THREADS, 0, st>>>(a);
+        P.end();
+        P.begin(s_bh);
+        k_bbb_heavy<<<grid, THREADS, 0, st>>>(a);
+        P.end();
+        P.begin(s_bd);
+        k_bbb_decide<<<1, 32, 0, st>>>(a, h, use_cond);
+        P.end();
+        MG_CUDA(cudaGetLastError());
+        return MG_OK;
+    };
+    uint64_t key = 0x6263622d66776400ull;
+    const void *ptrs[] = {a.row, a.col, a.trow, a.tcol, a.vis, a.fm0, a.arch, a.sig, a.q, a.hpart, a.bc, a.ctl};
+    for (const void *p : ptrs) key = (key ^ (uint64_t)(uintptr_t)p) * 1099511628211ull;
+    key ^= (uint64_t)grid << 48;
+    const int mode = opt.profile ? MG_EXEC_HOST : opt.exec;
+    int32_t levels = 0, dense_levels = 0;
+    for (int32_t g0 = 0; g0 < nsrc; g0 += W) {
+        const int32_t cnt = std::min<int32_t>(W, nsrc - g0);
+        MG_CUDA(cudaMemcpyAsync(w->src.p, src_engine + g0, (size_t)cnt * 4, cudaMemcpyHostToDevice, s));
+        MG_CUDA(cudaMemsetAsync(a.vis, 0, n * 4, s));
+        MG_CUDA(cudaMemsetAsync(a.fm0, 0, 2 * n * 4, s));
+        k_bb_init<<<1, 32, 0, s>>>(a, cnt, opt.direction, alpha, max_levels);
+        MG_CUDA(cudaGetLastError());
+        MG_TRY(run_loop(mode, opt.profile != 0, s, w->fwd, key, fwd, &a.ctl->more, g->pinned_flag, max_levels + 2));
+        k_bbb_init<<<1, 32, 0, s>>>(a);
+        MG_CUDA(cudaGetLastError());
+        MG_TRY(run_loop(mode, opt.profile != 0, s, w->bwd, key ^ 0x5a5a, bwd, &a.ctl->more, g->pinned_flag,
+                        max_levels + 2));
+        BbCtl hc;
+        MG_CUDA(cudaMemcpyAsync(&hc, a.ctl, sizeof(hc), cudaMemcpyDeviceToHost, s));
+        MG_CUDA(cudaStreamSynchronize(s));
+        if (hc.status == 1) return fail(MG_ERR_ITER_LIMIT, "batched BC: level cap %d reached", max_levels);
+        if (hc.status != 0) return fail(MG_ERR_CUDA, "batched BC: level archive overflow");
+        levels += hc.nlevels;
+        dense_levels += hc.dense_levels;
+    }
+    k_bb_to_float<<<grid, THREADS, 0, s>>>(g->nv, a.bc, w->bcf.as<float>());
+    MG_CUDA(cudaGetLastError());
+    if (info) {
+        info->iterations = levels;
+        info->pull_iterations = dense_levels;
+    }
+    *bc_dev = w->bcf.as<float>();
+    return MG_OK;
+}
+
+}  // namespace mgi

@@ -129,8 +129,6 @@ void free_cc_ws(mg_graph *g)
     g->cws = nullptr;
 }
 
-void free_bc_ws(mg_graph *g) { (void)g; }
-
 mg_status cc_run(mg_graph *g, mg_run_info *info)
 {
     if (!g->cws) g->cws = new CcWS();

@@ -170,6 +170,10 @@ mg_status cc_to_caller(mg_graph *g, const int32_t *parent, const void **out);
 // per-edge 4-byte payloads between caller CSR order and engine CSR order
 mg_status edges_to_engine(mg_graph *g, const void *src_caller, void *dst_engine);
 mg_status edges_to_caller(mg_graph *g, const void *src_engine, void *dst_caller);
+// batched multi-source BC over engine-id sources (symmetric graphs); the
+// float scores in engine order stay in the graph's BC workspace
+mg_status bc_batched(mg_graph *g, const int32_t *src_engine, int32_t nsrc, const mg_opts &opt, mg_run_info *info,
+                     const float **bc_dev);
 }  // namespace mgi
 
 // ---------------------------------------------------------------------------

@@ -924,6 +924,20 @@ mg_status mg_bc_multi(mg_graph *g, const int32_t *sources, int32_t nsrc, const m
     if (nsrc < 0 || (nsrc > 0 && !sources)) return fail(MG_ERR_INVALID, "invalid sources");
     for (int32_t i = 0; i < nsrc; i++)
         if (sources[i] < 0 || sources[i] >= g->nv) return fail(MG_ERR_RANGE, "source %d out of range", sources[i]);
+    if (g->symmetric) {
+        // 32 sources per traversal (mg_bcb.cu)
+        std::vector<int32_t> eng((size_t)nsrc);
+        for (int32_t i = 0; i < nsrc; i++) eng[(size_t)i] = to_engine(g, sources[i]);
+        const float *bcd = nullptr;
+        MG_TRY(bc_batched(g, eng.data(), nsrc, opt, info, &bcd));
+        MG_TRY(publish(g, MG_RES_BC, bcd, 4));
+        mg_run_info keep;
+        if (info) keep = *info;
+        MG_TRY(end_run(g, opt, info));
+        if (info) { info->iterations = keep.iterations; info->pull_iterations = keep.pull_iterations; }
+        return copy_out(g, bc_out, g->res[MG_RES_BC], (size_t)g->nv * 4);
+    }
+    // directed graphs: one forward/backward traversal per source
     MG_TRY(ensure_ws(g, ALG_BC));
     FrontierWS *w = g->fws;
     MG_TRY(dev_alloc(w->bc, (size_t)std::max(g->nv, 1) * 4));

@@ -33,6 +33,50 @@ def test_bc_multi_sources():
     g.free()
 
 
+@pytest.mark.parametrize("direction", [mg.DIR_AUTO, mg.DIR_PUSH, mg.DIR_PULL])
+def test_bc_multi_groups_heavy_rows(direction):
+    # 70 sources = three groups of 32 (the last partial), duplicates
+    # included; scale 13 has rows above the 512 in-degree chunk threshold
+    h = mg.HostGraph.rmat(13, 16, seed=9)
+    g, og = _pair(h)
+    rng = np.random.default_rng(3)
+    src = rng.integers(0, og.nv, 70)
+    src[5] = src[6] = src[40]
+    bc, info = g.bc_multi(src, direction=direction)
+    ref = O.bc_multi_f64(og, src)
+    err = float(np.max(np.abs(bc.astype(np.float64) - ref)) / np.max(np.abs(ref)))
+    assert err < 1e-5, err
+    g.free()
+
+
+def test_bc_multi_matches_single_source_sum():
+    # the batched scores equal the sum of single-source deltas
+    h = mg.HostGraph.rmat(10, 8, seed=12)
+    g, og = _pair(h)
+    src = [0, 3, 3, 77, og.nv - 1]
+    bc, _ = g.bc_multi(src, exec=mg.EXEC_HOST)
+    acc = np.zeros(og.nv, np.float64)
+    for s in src:
+        (_, _, dl), _ = g.bc(s)
+        d = dl.astype(np.float64)
+        d[s] = 0.0
+        acc += d
+    err = float(np.max(np.abs(bc - acc)) / np.max(np.abs(acc)))
+    assert err < 1e-5, err
+    g.free()
+
+
+def test_bc_multi_unreachable_and_empty():
+    h = mg.HostGraph.from_entries(6, [0, 1, 3, 4], [1, 2, 4, 5])
+    g, og = _pair(h)
+    bc, _ = g.bc_multi([0, 5])
+    ref = O.bc_multi_f64(og, [0, 5])
+    assert np.allclose(bc, ref, rtol=1e-6, atol=0)
+    bc0, _ = g.bc_multi([])
+    assert not np.any(bc0)
+    g.free()
+
+
 def test_bc_multi_lattice():
     h = mg.HostGraph.lattice(40, 30, 0.05, seed=2)
     g, og = _pair(h)
