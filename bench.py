@@ -9,7 +9,10 @@ per processing run / time), two runs per step.  One JSON line on rank 0:
 value (inputs resident in HBM), e2e (through the C ABI with pinned host CSR
 copied in and results copied out every step), roofline of the dominant
 kernel (the PageRank pull sweep), cpu_baseline (the oracle's restatement of
-validate.cu's CPU algorithms on this host), clocks sampled during the run.
+validate.cu's CPU algorithms on this host), clocks sampled during the run,
+and batched_vs_plain: multi-source BC, personalised PageRank and the
+64-graph BFS+CC batch against one plain call per instance, plus the
+PageRank adjoint's forward / forward+backward times (skip with --no-batch).
 
 --impl reference times the reference's CPU implementation of the path (the
 oracle port of validate.cu: Bellman-Ford SSSP and the PageRank recurrence)
@@ -44,6 +47,10 @@ def parse():
     p.add_argument("--impl", default="mg", choices=["mg", "reference"])
     p.add_argument("--scale", type=int, default=SCALE)
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-batch", action="store_true", help="skip the batched-vs-plain and adjoint comparisons")
+    p.add_argument("--exec", default="graph", choices=["graph", "host"],
+                   help="iteration loops as CUDA graphs with a device-side WHILE node (default) or host-driven "
+                        "(every kernel a separate launch, as a profiler's launch list needs)")
     return p.parse_args()
 
 
@@ -142,6 +149,90 @@ def cpu_oracle_run(rp, col, wt, counts=None):
     return t1 - t0, sweeps, t2 - t1, iters
 
 
+def batch_report(mg, device):
+    """Batched against plain launches (outside the timed region; device time
+    of each call from its own cudaEvents):
+      bc_256   : 256-source BC on R-MAT scale 20 (mg_bc_multi) vs 256 mg_bc
+      ppr_256  : 256 one-hot personalised PageRanks (mg_ppr_batch) vs 256
+                 single-seed runs
+      graphs_64: BFS + CC on 64 R-MAT graphs, scales 10-18, edge factor
+                 8-32 (mg_batch_*) vs one graph per call
+      adjoint  : weighted PageRank on R-MAT scale 21 with FP32 weights in
+                 (0, 1], forward alone vs forward + backward
+    Each entry carries the agreement of the two results."""
+    import numpy as np
+    out = {}
+    h = mg.HostGraph.rmat(20, EDGE_FACTOR, seed=20)
+    g = mg.Graph(h, device)
+    rng = np.random.default_rng(20)
+    src = rng.integers(0, g.nv, 256).astype(np.int32)
+    g.bc_multi(src[:32], out=False)
+    bcb, ib = g.bc_multi(src)
+    _, ib2 = g.bc_multi(src, out=False)
+    tb = min(ib.device_ms, ib2.device_ms)
+    acc = np.zeros(g.nv, np.float64)
+    tp = 0.0
+    for s_ in src:
+        (_, _, dl), i1 = g.bc(int(s_))
+        tp += i1.device_ms
+        d = dl.astype(np.float64)
+        d[int(s_)] = 0.0
+        acc += d
+    out["bc_256"] = {"graph": f"rmat20_ef16 n={g.nv} m={g.ne}", "batched_ms": tb, "plain_ms": tp,
+                     "speedup": tp / tb, "batched_gteps": 256 * 2 * g.ne / tb / 1e6,
+                     "max_rel_diff": float(np.max(np.abs(bcb - acc)) / max(np.max(np.abs(acc)), 1e-30))}
+    seeds = src
+    g.ppr_batch(seeds[:8], out=False, tol=TOL)
+    xb, pb = g.ppr_batch(seeds, tol=TOL)
+    tb = pb.device_ms
+    tp, diff = 0.0, 0.0
+    for i, s_ in enumerate(seeds):
+        x1, p1 = g.ppr_batch([int(s_)], tol=TOL)
+        tp += p1.device_ms
+        diff = max(diff, float(np.max(np.abs(x1[0] - xb[i]))))
+    out["ppr_256"] = {"graph": f"rmat20_ef16 n={g.nv} m={g.ne}", "batched_ms": tb, "plain_ms": tp,
+                      "speedup": tp / tb, "sweeps": pb.iterations, "max_abs_diff": diff}
+    g.free()
+    rng = np.random.default_rng(64)
+    hs = [mg.HostGraph.rmat(int(sc), int(ef), seed=int(i) + 1) for i, (sc, ef) in
+          enumerate(zip(rng.integers(10, 19, 64), rng.integers(8, 33, 64)))]
+    b = mg.Batch(hs, device)
+    srcs = [0] * len(hs)
+    b.bfs(srcs)
+    b.cc()
+    lb, i1 = b.bfs(srcs)
+    cb, i2 = b.cc()
+    tb = i1.device_ms + i2.device_ms
+    tp, same = 0.0, True
+    for k, hh in enumerate(hs):
+        gg = mg.Graph(hh, device)
+        gg.bfs(0, out=False)
+        lv, j1 = gg.bfs(0)
+        lab, j2 = gg.cc()
+        tp += j1.device_ms + j2.device_ms
+        same = same and bool(np.array_equal(lv, lb[k]) and np.array_equal(lab, cb[k]))
+        gg.free()
+    b.free()
+    out["graphs_64"] = {"graphs": "64 R-MAT, scales U{10..18}, edge factor U{8..32}",
+                        "edges": int(sum(hh.ne for hh in hs)), "batched_ms": tb, "plain_ms": tp,
+                        "speedup": tp / tb, "bit_exact": same}
+    h = mg.HostGraph.rmat(21, EDGE_FACTOR, seed=21)
+    g = mg.Graph(h, device)
+    rng = np.random.default_rng(21)
+    w = rng.uniform(0.0, 1.0, g.ne)
+    w = np.where(w == 0.0, 1.0, w).astype(np.float32)
+    g.set_float_weights(w)
+    gv = rng.standard_normal(g.nv).astype(np.float32)
+    g.wpagerank(out=False, tol=TOL)
+    _, fi = g.wpagerank(out=False, tol=TOL)
+    _, bi = g.wpagerank_backward(gv, out=False, tol=TOL)
+    out["adjoint"] = {"graph": f"rmat21_ef16 n={g.nv} m={g.ne}", "forward_ms": fi.device_ms,
+                      "backward_ms": bi.device_ms, "forward_backward_ms": fi.device_ms + bi.device_ms,
+                      "forward_sweeps": fi.iterations, "backward_sweeps": bi.iterations}
+    g.free()
+    return out
+
+
 def reference_arm(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -197,7 +288,7 @@ def main():
     g = mg.Graph(h, local)
     n, m = g.nv, g.ne
     stream = torch.cuda.ExternalStream(g.stream(), device=torch.device("cuda", local))
-    opts = mg.default_opts(tol=TOL, damping=DAMPING)
+    opts = mg.default_opts(tol=TOL, damping=DAMPING, exec=mg.EXEC_HOST if args.exec == "host" else mg.EXEC_GRAPH)
 
     def step(out=False):
         _, si = g.sssp(0, opts, out=out)
@@ -218,8 +309,9 @@ def main():
     launches = 0
     for _ in range(args.steps):
         si, pi = step()
-        # SSSP: init + (push, pull, decide) per iteration; PageRank: 2 inits + (sweep, apply) per sweep
-        launches += 1 + 3 * si.iterations + 2 + 2 * pi.iterations
+        # SSSP: init + (push, pull, compact, decide) per iteration + id mapping;
+        # PageRank: 2 inits + (sweep, apply) per sweep + id mapping
+        launches += 2 + 4 * si.iterations + 3 + 2 * pi.iterations
     e1.record(stream)
     torch.cuda.synchronize()
     if dist:
@@ -252,6 +344,7 @@ def main():
 
     if rank != 0:
         return 0
+    batched = None if (args.no_batch or world > 1) else batch_report(mg, local)
     peak, peak_kind = peaks()
     sweep = kt.get("pr_pull", [1, 0.0])
     avg_ms = sweep[1] / max(sweep[0], 1)
@@ -290,6 +383,7 @@ def main():
         "clocks": clk,
         "gpu_launches": launches,
         "kernel_ms": {k: {"launches": v[0], "total_ms": round(v[1], 4)} for k, v in kt.items()},
+        "batched_vs_plain": batched,
     }
     print(json.dumps(line), flush=True)
     if dist:

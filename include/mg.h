@@ -230,6 +230,7 @@ mg_status mg_wpagerank(mg_graph *dg, const mg_opts *o, float *x_out, mg_run_info
 /* Backward of L = sum_i g_i x_i through mg_wpagerank's fixed point.
  * lambda = g + d P lambda (transposed fixed point), then per edge
  * grad_w[e] = d x_u / S_u * (lambda_v - sum_k P_uk lambda_k).
+ * The lambda iteration stops when its L1 change is <= tol * |g|_1.
  * Uses the x of the last mg_wpagerank on this graph.  No reference counterpart. */
 mg_status mg_wpagerank_backward(mg_graph *dg, const float *g_host, const mg_opts *o, float *grad_w_out,
                                 float *lambda_out, mg_run_info *info);

@@ -331,31 +331,123 @@ static void build_layout(const mg_host_graph &h, HostLayout &L)
     }
 }
 
-// new row i' of the engine CSR = caller row new2old[i'] (same entry order);
-// column ids mapped through old2new when map_ids
-__global__ void k_relabel_edges(int32_t n, const int32_t *new2old, const int32_t *old2new, const int32_t *o_row,
-                                const uint32_t *src, const int32_t *row_new, uint32_t *dst, int map_ids)
+// Engine row i of the relabeled CSR is caller row new2old[i] with the same
+// entry order, so engine position p (in row r, offset p - row_new[r])
+// corresponds to caller position o_row[new2old[r]] + p - row_new[r].
+//
+// pos_row[k] = engine row of position min(32k, m-1), built once per upload.
+// A warp handles 32 consecutive positions [32c, 32c+32): their rows lie in
+// [pos_row[c], pos_row[c+1]], so when that span is under 32 rows each lane
+// finds its row in one coalesced load of the span's row starts and five
+// shuffles; wider spans (runs of empty rows) fall back to a binary search.
+// Four such 32-position steps are interleaved per warp for memory-level
+// parallelism.
+__device__ __forceinline__ int32_t row_of_position(const int32_t *row_new, int32_t p, int32_t lo, int32_t hi)
+{
+    // last r in [lo, hi] with row_new[r] <= p
+    while (lo < hi) {
+        const int32_t mid = (lo + hi + 1) >> 1;
+        if (__ldg(&row_new[mid]) <= p) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
+
+__global__ void k_pos_rows(int32_t n, int32_t m, const int32_t *row_new, int32_t *pos_row)
+{
+    const int32_t nk = m / 32 + 2;
+    for (int32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < nk; k += gridDim.x * blockDim.x) {
+        const int32_t p = (int32_t)min((int64_t)k * 32, (int64_t)m - 1);
+        pos_row[k] = row_of_position(row_new, p, 0, n - 1);
+    }
+}
+
+constexpr int RELABEL_ILP = 4;
+
+// caller position of this lane's position 32c + lane (-1 past the end)
+__device__ __forceinline__ void caller_positions(int32_t n, int32_t m, const int32_t *new2old, const int32_t *o_row,
+                                                 const int32_t *row_new, const int32_t *pos_row, int32_t c0,
+                                                 int32_t (&q)[RELABEL_ILP])
 {
     const int lane = threadIdx.x & 31;
-    for (int32_t i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < n; i += (gridDim.x * blockDim.x) >> 5) {
-        const int32_t u = new2old[i];
-        const int32_t b = o_row[u], len = o_row[u + 1] - b, o = row_new[i];
-        for (int32_t j = lane; j < len; j += 32) {
-            uint32_t x = src[b + j];
-            dst[o + j] = map_ids ? (uint32_t)old2new[x] : x;
+    int32_t ra[RELABEL_ILP], rb[RELABEL_ILP], w[RELABEL_ILP], rr[RELABEL_ILP], st[RELABEL_ILP];
+    const int32_t nsteps = (m + 31) / 32;
+#pragma unroll
+    for (int j = 0; j < RELABEL_ILP; j++) {
+        const int32_t c = min(c0 + j, nsteps - 1);
+        ra[j] = __ldg(&pos_row[c]);
+        rb[j] = __ldg(&pos_row[c + 1]);
+    }
+#pragma unroll
+    for (int j = 0; j < RELABEL_ILP; j++)
+        w[j] = (ra[j] + lane <= rb[j]) ? __ldg(&row_new[ra[j] + lane]) : 0x7fffffff;
+#pragma unroll
+    for (int j = 0; j < RELABEL_ILP; j++) {
+        const int32_t p = (c0 + j) * 32 + lane;
+        if (rb[j] - ra[j] < 32) {
+            const int o = mgd::owner_lane(w[j], p);
+            rr[j] = ra[j] + o;
+            st[j] = __shfl_sync(0xffffffffu, w[j], o);
+        } else {
+            rr[j] = row_of_position(row_new, min(p, m - 1), ra[j], rb[j]);
+            st[j] = __ldg(&row_new[rr[j]]);
+        }
+    }
+#pragma unroll
+    for (int j = 0; j < RELABEL_ILP; j++) rr[j] = __ldg(&new2old[rr[j]]);
+#pragma unroll
+    for (int j = 0; j < RELABEL_ILP; j++) {
+        const int32_t p = (c0 + j) * 32 + lane;
+        q[j] = (c0 + j < nsteps && p < m) ? __ldg(&o_row[rr[j]]) + (p - st[j]) : -1;
+    }
+}
+
+// caller CSR -> engine CSR for up to two 4-byte edge arrays; the first is
+// mapped through old2new when map_ids (column ids)
+__global__ void k_relabel_edges(int32_t n, int32_t m, const int32_t *new2old, const int32_t *old2new,
+                                const int32_t *o_row, const int32_t *row_new, const int32_t *pos_row,
+                                const uint32_t *src0, uint32_t *dst0, const uint32_t *src1, uint32_t *dst1,
+                                int map_ids)
+{
+    const int lane = threadIdx.x & 31;
+    const int32_t nsteps = (m + 31) / 32;
+    const int32_t gwarp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int32_t nwarps = (gridDim.x * blockDim.x) >> 5;
+    for (int32_t c0 = gwarp * RELABEL_ILP; c0 < nsteps; c0 += nwarps * RELABEL_ILP) {
+        int32_t q[RELABEL_ILP];
+        caller_positions(n, m, new2old, o_row, row_new, pos_row, c0, q);
+        uint32_t x[RELABEL_ILP], y[RELABEL_ILP];
+#pragma unroll
+        for (int j = 0; j < RELABEL_ILP; j++) {
+            x[j] = q[j] >= 0 ? __ldg(&src0[q[j]]) : 0u;
+            y[j] = (q[j] >= 0 && dst1) ? __ldg(&src1[q[j]]) : 0u;
+        }
+#pragma unroll
+        for (int j = 0; j < RELABEL_ILP; j++)
+            if (q[j] >= 0 && map_ids) x[j] = (uint32_t)__ldg(&old2new[x[j]]);
+#pragma unroll
+        for (int j = 0; j < RELABEL_ILP; j++) {
+            if (q[j] < 0) continue;
+            const int32_t p = (c0 + j) * 32 + lane;
+            dst0[p] = x[j];
+            if (dst1) dst1[p] = y[j];
         }
     }
 }
 
 // inverse of k_relabel_edges for per-edge payloads (engine order -> caller order)
-__global__ void k_unrelabel_edges(int32_t n, const int32_t *new2old, const int32_t *o_row, const uint32_t *src,
-                                  const int32_t *row_new, uint32_t *dst)
+__global__ void k_unrelabel_edges(int32_t n, int32_t m, const int32_t *new2old, const int32_t *o_row,
+                                  const int32_t *row_new, const int32_t *pos_row, const uint32_t *src, uint32_t *dst)
 {
     const int lane = threadIdx.x & 31;
-    for (int32_t i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < n; i += (gridDim.x * blockDim.x) >> 5) {
-        const int32_t u = new2old[i];
-        const int32_t b = o_row[u], len = o_row[u + 1] - b, o = row_new[i];
-        for (int32_t j = lane; j < len; j += 32) dst[b + j] = src[o + j];
+    const int32_t nsteps = (m + 31) / 32;
+    const int32_t gwarp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int32_t nwarps = (gridDim.x * blockDim.x) >> 5;
+    for (int32_t c0 = gwarp * RELABEL_ILP; c0 < nsteps; c0 += nwarps * RELABEL_ILP) {
+        int32_t q[RELABEL_ILP];
+        caller_positions(n, m, new2old, o_row, row_new, pos_row, c0, q);
+#pragma unroll
+        for (int j = 0; j < RELABEL_ILP; j++)
+            if (q[j] >= 0) dst[q[j]] = __ldg(&src[(c0 + j) * 32 + lane]);
     }
 }
 
@@ -387,13 +479,15 @@ __global__ void k_cc_label_old(int32_t n, const int32_t *parent, const int32_t *
 
 static mg_status relabel_device(mg_graph *g)
 {
+    if (g->ne == 0) return MG_OK;
     const int grid = g->num_sms * 8;
-    k_relabel_edges<<<grid, 256, 0, g->stream>>>(g->nv, g->new2old.as<int32_t>(), g->old2new.as<int32_t>(),
-                                                 g->o_row.as<int32_t>(), g->o_col.as<uint32_t>(), g->row.as<int32_t>(),
-                                                 g->col.as<uint32_t>(), 1);
-    k_relabel_edges<<<grid, 256, 0, g->stream>>>(g->nv, g->new2old.as<int32_t>(), g->old2new.as<int32_t>(),
-                                                 g->o_row.as<int32_t>(), g->o_wt.as<uint32_t>(), g->row.as<int32_t>(),
-                                                 g->wt.as<uint32_t>(), 0);
+    MG_TRY(dev_alloc(g->pos_row, ((size_t)g->ne / 32 + 2) * 4));
+    k_pos_rows<<<grid, 256, 0, g->stream>>>(g->nv, g->ne, g->row.as<int32_t>(), g->pos_row.as<int32_t>());
+    k_relabel_edges<<<grid, 256, 0, g->stream>>>(g->nv, g->ne, g->new2old.as<int32_t>(), g->old2new.as<int32_t>(),
+                                                 g->o_row.as<int32_t>(), g->row.as<int32_t>(),
+                                                 g->pos_row.as<int32_t>(), g->o_col.as<uint32_t>(),
+                                                 g->col.as<uint32_t>(), g->o_wt.as<uint32_t>(), g->wt.as<uint32_t>(),
+                                                 1);
     MG_CUDA(cudaGetLastError());
     return MG_OK;
 }
@@ -454,9 +548,11 @@ mg_status edges_to_engine(mg_graph *g, const void *src_caller, void *dst_engine)
         MG_CUDA(cudaMemcpyAsync(dst_engine, src_caller, (size_t)g->ne * 4, cudaMemcpyDeviceToDevice, g->stream));
         return MG_OK;
     }
-    k_relabel_edges<<<g->num_sms * 8, 256, 0, g->stream>>>(g->nv, g->new2old.as<int32_t>(), nullptr,
-                                                           g->o_row.as<int32_t>(), (const uint32_t *)src_caller,
-                                                           g->row.as<int32_t>(), (uint32_t *)dst_engine, 0);
+    if (g->ne == 0) return MG_OK;
+    k_relabel_edges<<<g->num_sms * 8, 256, 0, g->stream>>>(g->nv, g->ne, g->new2old.as<int32_t>(), nullptr,
+                                                           g->o_row.as<int32_t>(), g->row.as<int32_t>(),
+                                                           g->pos_row.as<int32_t>(), (const uint32_t *)src_caller,
+                                                           (uint32_t *)dst_engine, nullptr, nullptr, 0);
     MG_CUDA(cudaGetLastError());
     return MG_OK;
 }
@@ -467,8 +563,10 @@ mg_status edges_to_caller(mg_graph *g, const void *src_engine, void *dst_caller)
         MG_CUDA(cudaMemcpyAsync(dst_caller, src_engine, (size_t)g->ne * 4, cudaMemcpyDeviceToDevice, g->stream));
         return MG_OK;
     }
-    k_unrelabel_edges<<<g->num_sms * 8, 256, 0, g->stream>>>(g->nv, g->new2old.as<int32_t>(), g->o_row.as<int32_t>(),
-                                                             (const uint32_t *)src_engine, g->row.as<int32_t>(),
+    if (g->ne == 0) return MG_OK;
+    k_unrelabel_edges<<<g->num_sms * 8, 256, 0, g->stream>>>(g->nv, g->ne, g->new2old.as<int32_t>(),
+                                                             g->o_row.as<int32_t>(), g->row.as<int32_t>(),
+                                                             g->pos_row.as<int32_t>(), (const uint32_t *)src_engine,
                                                              (uint32_t *)dst_caller);
     MG_CUDA(cudaGetLastError());
     return MG_OK;
@@ -568,7 +666,7 @@ static void destroy_graph(mg_graph *g)
     DevBuf *bufs[] = {&g->row, &g->col, &g->wt, &g->trow_own, &g->tcol_own, &g->twt_own,
                       &g->hchunk, &g->hrows, &g->hrow_chunk, &g->fw, &g->o_fw, &g->ppr_hchunk, &g->ppr_hrows,
                       &g->ppr_hrow_chunk, &g->o_row, &g->o_col, &g->o_wt, &g->old2new, &g->new2old,
-                      &g->wrows, &g->trows};
+                      &g->wrows, &g->trows, &g->pos_row};
     for (DevBuf *b : bufs) dev_free(*b);
     for (DevBuf &b : g->res_out) dev_free(b);
     if (g->pinned_flag) cudaFreeHost(g->pinned_flag);
@@ -652,6 +750,7 @@ mg_status mg_graph_reload(mg_graph *g, const mg_host_graph *h)
         build_layout(*h, L);
         MG_TRY(upload_arrays(g, h, L, false));
     }
+    g->fw_version += 1;  // quantities derived from the float weights are stale
     return MG_OK;
 }
 
@@ -684,6 +783,7 @@ mg_status mg_graph_set_float_weights(mg_graph *g, const float *w)
     }
     MG_CUDA(cudaStreamSynchronize(g->stream));
     g->has_fw = true;
+    g->fw_version += 1;
     return MG_OK;
 }
 

@@ -126,12 +126,14 @@ struct mg_graph {
     // float edge weights for weighted PageRank (CSR order)
     mgi::DevBuf fw;
     bool has_fw = false;
+    uint64_t fw_version = 0;       // bumped whenever fw or the CSR changes
     // hub-first relabeling: the engines run on ids ordered by descending
     // log2 degree; results are mapped back before they leave the library
     bool relabeled = false;
     mgi::DevBuf o_row, o_col, o_wt;        // the CSR in the caller's ids (as uploaded)
     mgi::DevBuf o_fw;                      // float weights in caller CSR order
     mgi::DevBuf old2new, new2old;          // int32 [nv]
+    mgi::DevBuf pos_row;                   // int32 [ne/32 + 2]: engine row of position 32k
     std::vector<int32_t> h_old2new;        // host copy for mapping sources
     mgi::DevBuf res_out[8];                // results in the caller's ids
     // per-algorithm workspaces

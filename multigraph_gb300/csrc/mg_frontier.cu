@@ -758,7 +758,7 @@ static mg_status frontier_run_impl(mg_graph *g, int alg, int32_t src, const int3
     default: k_init<ALG_BC><<<1, 32, 0, s>>>(a, src, srcs_dev, nsrc, opt.direction, alpha, beta, max_iter); break;
     }
     MG_CUDA(cudaGetLastError());
-    const int grid = launch_grid(g, THREADS, 4);
+    const int grid = launch_grid(g, THREADS, 8);
     Profiler &P = g->prof;
     const int sp = P.slot(alg == ALG_SSSP ? "sssp_push" : alg == ALG_BC ? "bc_push" : "bfs_push");
     const int sl = P.slot(alg == ALG_SSSP ? "sssp_pull" : alg == ALG_BC ? "bc_pull" : "bfs_pull");
@@ -829,7 +829,7 @@ mg_status bc_backward(mg_graph *g, int32_t src, const mg_opts &opt, float *bcacc
     float *q = w->q.as<float>(), *delta = w->delta.as<float>();
     BCtl *bc = w->bctl.as<BCtl>();
     int32_t *hl = w->bheavy.as<int32_t>();
-    const int grid = launch_grid(g, THREADS, 4);
+    const int grid = launch_grid(g, THREADS, 8);
     k_bc_q_init<<<grid, THREADS, 0, s>>>(g->nv, a.sigma, a.label, q, delta);
     k_bc_back_init<<<1, 32, 0, s>>>(a.ctl, bc, src);
     MG_CUDA(cudaGetLastError());

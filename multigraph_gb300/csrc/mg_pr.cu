@@ -588,6 +588,7 @@ __global__ void k_ppr_store(int32_t n, const float *X, int32_t nseed, int32_t s0
 struct PrWS {
     mgi::DevBuf x0, x1, c0, c1, active, hpart, bpart, ctl, S, wT, gvec, grad, lam_keep, xkeep;
     mgi::DevBuf wT_caller, gvec_caller, grad_caller;  // caller-order staging of a relabeled graph
+    uint64_t wT_version = 0;  // fw_version that S and wT were derived from (0: none)
     mgi::LoopGraph lg[6];
 };
 
@@ -714,22 +715,27 @@ static mg_status pr_setup(mg_graph *g, PArgs &a, bool weighted_or_adj)
     return MG_OK;
 }
 
-// transposed float weights: wT[pos of (v,u) in row v] = w[pos of (u,v) in row u]
-__global__ void k_transpose_weights(int32_t n, const int32_t *row, const int32_t *col, const float *w, float *wT)
+// transposed float weights: wT[pos of (v,u) in row v] = w[pos of (u,v) in row u].
+// One thread per edge: the owner row u of position p by binary search over
+// the row offsets, then u among row v's (ascending) columns.
+__global__ void k_transpose_weights(int32_t n, int32_t m, const int32_t *row, const int32_t *col, const float *w,
+                                    float *wT)
 {
-    for (int32_t u = blockIdx.x * blockDim.x + threadIdx.x; u < n; u += gridDim.x * blockDim.x) {
-        for (int32_t p = row[u]; p < row[u + 1]; p++) {
-            int32_t v = col[p];
-            // binary search u in row v (columns ascending)
-            int32_t lo = row[v], hi = row[v + 1] - 1, q = -1;
-            while (lo <= hi) {
-                int32_t mid = (lo + hi) >> 1;
-                int32_t cm = col[mid];
-                if (cm == u) { q = mid; break; }
-                if (cm < u) lo = mid + 1; else hi = mid - 1;
-            }
-            if (q >= 0) wT[q] = w[p];
+    for (int32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < m; p += gridDim.x * blockDim.x) {
+        int32_t lo = 0, hi = n - 1;  // last u with row[u] <= p
+        while (lo < hi) {
+            const int32_t mid = (lo + hi + 1) >> 1;
+            if (__ldg(&row[mid]) <= p) lo = mid; else hi = mid - 1;
         }
+        const int32_t u = lo, v = __ldg(&col[p]);
+        int32_t a = __ldg(&row[v]), b = __ldg(&row[v + 1]) - 1, q = -1;
+        while (a <= b) {
+            const int32_t mid = (a + b) >> 1;
+            const int32_t cm = __ldg(&col[mid]);
+            if (cm == u) { q = mid; break; }
+            if (cm < u) a = mid + 1; else b = mid - 1;
+        }
+        if (q >= 0) wT[q] = __ldg(&w[p]);
     }
 }
 
@@ -792,17 +798,24 @@ mg_status mg_wpagerank(mg_graph *g, const mg_opts *o, float *x_out, mg_run_info 
     const size_t n = (size_t)std::max(g->nv, 1), m = (size_t)std::max(g->ne, 1);
     MG_TRY(dev_alloc(w->wT, m * 4 + 16));  // 16 bytes of tail padding for aligned staging
     MG_TRY(dev_alloc(w->xkeep, n * 4));
-    k_row_sums<<<grid, THREADS, 0, s>>>(g->nv, g->row.as<int32_t>(), g->fw.as<float>(), a.S);
-    if (g->relabeled) {
-        // transposed weights are located in the caller's CSR (ascending
-        // columns), then carried to engine order like the column ids
-        MG_TRY(dev_alloc(w->wT_caller, m * 4 + 16));
-        k_transpose_weights<<<grid, THREADS, 0, s>>>(g->nv, g->o_row.as<int32_t>(), g->o_col.as<int32_t>(),
-                                                      g->o_fw.as<float>(), w->wT_caller.as<float>());
-        MG_TRY(edges_to_engine(g, w->wT_caller.p, w->wT.p));
-    } else {
-        k_transpose_weights<<<grid, THREADS, 0, s>>>(g->nv, g->row.as<int32_t>(), g->col.as<int32_t>(),
-                                                      g->fw.as<float>(), w->wT.as<float>());
+    if (w->wT_version != g->fw_version) {
+        // out-weight sums and transposed weights, once per set of weights
+        const int egrid = launch_grid(g, THREADS, 16);
+        k_row_sums<<<grid, THREADS, 0, s>>>(g->nv, g->row.as<int32_t>(), g->fw.as<float>(), a.S);
+        if (g->relabeled) {
+            // transposed weights are located in the caller's CSR (ascending
+            // columns), then carried to engine order like the column ids
+            MG_TRY(dev_alloc(w->wT_caller, m * 4 + 16));
+            k_transpose_weights<<<egrid, THREADS, 0, s>>>(g->nv, g->ne, g->o_row.as<int32_t>(),
+                                                          g->o_col.as<int32_t>(), g->o_fw.as<float>(),
+                                                          w->wT_caller.as<float>());
+            MG_TRY(edges_to_engine(g, w->wT_caller.p, w->wT.p));
+        } else {
+            k_transpose_weights<<<egrid, THREADS, 0, s>>>(g->nv, g->ne, g->row.as<int32_t>(), g->col.as<int32_t>(),
+                                                          g->fw.as<float>(), w->wT.as<float>());
+        }
+        MG_CUDA(cudaGetLastError());
+        w->wT_version = g->fw_version;
     }
     a.pw = w->wT.as<float>();
     float d = opt.damping > 0 ? opt.damping : 0.85f;
@@ -850,11 +863,17 @@ mg_status mg_wpagerank_backward(mg_graph *g, const float *g_host, const mg_opts 
     float tol = opt.tol > 0 ? opt.tol : 1e-6f;
     int max_iter = opt.max_iter > 0 ? opt.max_iter : 10000;
     // initial mean of lambda = mean of g (for dangling rows)
-    std::vector<float> gh(g_host, g_host + g->nv);
-    double gm = 0.0;
-    for (float v : gh) gm += v;
+    // and the stopping threshold, relative to |g|_1: lambda scales with g,
+    // and an absolute L1 threshold would sit below FP32 resolution for
+    // large n
+    double gm = 0.0, g1 = 0.0;
+    for (int32_t i = 0; i < g->nv; i++) {
+        gm += g_host[i];
+        g1 += std::fabs((double)g_host[i]);
+    }
     gm = g->nv ? gm / g->nv : 0.0;
-    k_pr_ctl_init<<<1, 32, 0, s>>>(a.ctl, g->nv, max_iter, d, tol, 0.0, gm);
+    const float tol_abs = (float)(tol * std::max(g1, 1e-30));
+    k_pr_ctl_init<<<1, 32, 0, s>>>(a.ctl, g->nv, max_iter, d, tol_abs, 0.0, gm);
     k_pr_init<V_ADJ><<<grid, THREADS, 0, s>>>(a, 0.0f);
     int cur = 0;
     MG_TRY(pr_loop<V_ADJ>(g, a, opt, "wpr_adjoint", info, &cur));
