@@ -5,14 +5,23 @@
 // (pointer jumping, process.cu:940-967,1012-1049) driven by main.cu:113-119,
 // which return to the host after every hooking and jumping round.
 //
-// Here one pass over the edges does the whole job: every edge unions its two
-// endpoints in a lock-free union-find whose links always go from the larger
-// root to the smaller one (parent[x] <= x), with path halving in find; a
-// final pass compresses every vertex to its root.  The root of a component
-// is therefore its minimum vertex id, which is exactly the canonical label
-// the reference's validator derives (validate.cu:234-242,263-273).  Union
+// Here the edges are hooked in a lock-free union-find whose links always go
+// from the larger root to the smaller one (parent[x] <= x), with path halving
+// in find; a final pass compresses every vertex to its root.  The root of a
+// component is therefore its minimum vertex id, which is exactly the
+// canonical label the reference's validator derives
+// (validate.cu:234-242,263-273), whatever order the unions run in.  Union
 // retries only when another thread changed the same root, so every loop is
 // lock-free and bounded by the number of successful links.
+//
+// Symmetric graphs skip most of the edges (neighbour sampling, as in
+// Sutton et al., "Optimizing Parallel Graph Connectivity Computation via
+// Subgraph Sampling", IPDPS 2018): every vertex first links to its first
+// SAMPLE_ROUNDS neighbours, the trees are compressed, the most frequent root
+// among 1024 sampled vertices is taken as the giant component, and only rows
+// whose vertex is outside it hook their remaining edges (in both
+// directions, so an edge with one end in the giant component is hooked from
+// the other end).  General graphs hook every in-edge once.
 //
 // Multi-graph batches: the graphs are laid out as one disjoint union (vertex
 // ids offset per graph), so one multi-source BFS and one CC pass cover the
@@ -55,29 +64,81 @@ __device__ __forceinline__ void cc_union(int32_t *parent, int32_t a, int32_t b)
     }
 }
 
+constexpr int SAMPLE_ROUNDS = 2;
+constexpr int MODE_SAMPLES = 1024;
+
 __global__ void k_cc_init(int32_t n, const int32_t *row, const int32_t *col, int32_t *parent)
 {
     for (int32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x) {
         int32_t p = mgops::Cc::initialize(v);
-        // first (smallest) neighbour below v starts the tree (columns ascend)
+        // the first neighbour below v starts the tree (a valid link: parent < v)
         if (row[v + 1] > row[v]) p = min(p, col[row[v]]);
         parent[v] = p;
     }
 }
 
+// link every vertex to its r-th neighbour
+__global__ void k_cc_sample(int32_t n, const int32_t *row, const int32_t *col, int32_t r, int32_t *parent);
+
+// the most frequent root among MODE_SAMPLES vertices (ties: smallest id);
+// one block of MODE_SAMPLES threads
+__global__ void __launch_bounds__(MODE_SAMPLES) k_cc_mode(int32_t n, const int32_t *parent, int32_t *giant)
+{
+    __shared__ int32_t s_val[MODE_SAMPLES];
+    __shared__ int32_t s_best[MODE_SAMPLES / 32], s_cnt[MODE_SAMPLES / 32];
+    const int t = threadIdx.x;
+    // spread the samples over the id range (hub-first ids put hubs first)
+    const int32_t v = (int32_t)(((int64_t)t * n) / MODE_SAMPLES + (((int64_t)t * 7919) % max(n / MODE_SAMPLES, 1)));
+    s_val[t] = parent[min(max(v, 0), n - 1)];
+    __syncthreads();
+    const int32_t mine = s_val[t];
+    int cnt = 0;
+    for (int i = 0; i < MODE_SAMPLES; i++) cnt += (s_val[i] == mine);
+    // block argmax of (cnt, -value)
+    int32_t bv = mine;
+    int bc = cnt;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const int32_t ov = __shfl_xor_sync(0xffffffffu, bv, o);
+        const int oc = __shfl_xor_sync(0xffffffffu, bc, o);
+        if (oc > bc || (oc == bc && ov < bv)) { bv = ov; bc = oc; }
+    }
+    if ((t & 31) == 0) { s_best[t >> 5] = bv; s_cnt[t >> 5] = bc; }
+    __syncthreads();
+    if (t == 0) {
+        for (int w = 1; w < MODE_SAMPLES / 32; w++)
+            if (s_cnt[w] > bc || (s_cnt[w] == bc && s_best[w] < bv)) { bv = s_best[w]; bc = s_cnt[w]; }
+        *giant = bv;
+    }
+}
+
+__global__ void k_cc_sample(int32_t n, const int32_t *row, const int32_t *col, int32_t r, int32_t *parent)
+{
+    for (int32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x) {
+        const int32_t b = row[v];
+        if (row[v + 1] - b > r) {
+            const int32_t u = col[b + r];
+            if (u != v) cc_union(parent, v, u);
+        }
+    }
+}
+
 // per-edge union over the degree-binned rows (bins_reduce interface;
-// the reduction value is unused)
+// the reduction value is unused).  giant >= 0: rows whose vertex points at
+// the giant root are skipped and the others hook every entry; giant < 0:
+// every row, each undirected edge once when symmetric.
 struct HookOp {
     using T = int;
     static constexpr bool kRowAware = true;  // the union needs the row (source vertex)
     static constexpr bool kWeights = false;
     int32_t *parent;
     int symmetric;
+    int32_t giant;
     __device__ int identity() const { return 0; }
-    __device__ bool skip(int32_t) const { return false; }
+    __device__ bool skip(int32_t v) const { return giant >= 0 && parent[v] == giant; }
     __device__ int edge(int32_t, int32_t src, int32_t dst, int32_t) const
     {
-        if (src != dst && (!symmetric || dst < src)) cc_union(parent, src, dst);
+        if (src != dst && (giant >= 0 || !symmetric || dst < src)) cc_union(parent, src, dst);
         return 0;
     }
     __device__ int combine(int, int) const { return 0; }
@@ -90,17 +151,21 @@ struct HookOp {
 __global__ void __launch_bounds__(THREADS) k_cc_hook(int32_t n, const int32_t *prow, const int32_t *pcol,
                                                      const int32_t *wrows, int32_t nwrows, const int32_t *trows,
                                                      int32_t ntrows, const int32_t *hchunk, int32_t nhchunks,
-                                                     int32_t heavy_deg, int symmetric, int32_t *parent)
+                                                     int symmetric, const int32_t *giant_p, int32_t *parent)
 {
-    HookOp op{parent, symmetric};
-    (void)heavy_deg;
+    const int32_t giant = giant_p ? *giant_p : -1;
+    HookOp op{parent, symmetric, giant};
     mgd::bins_reduce(op, prow, pcol, nullptr, wrows, nwrows, trows, ntrows);
+    __shared__ int s_skip;
     for (int32_t ch = blockIdx.x; ch < nhchunks; ch += gridDim.x) {
         int32_t u = hchunk[3 * ch], b = hchunk[3 * ch + 1], e = hchunk[3 * ch + 2];
-        for (int32_t p = b + threadIdx.x; p < e; p += blockDim.x) {
-            int32_t dst = pcol[p];
-            if (u != dst && (!symmetric || dst < u)) cc_union(parent, u, dst);
-        }
+        // one thread decides for the block (parent[u] may change meanwhile)
+        if (threadIdx.x == 0) s_skip = op.skip(u);
+        __syncthreads();
+        const bool skip = s_skip;
+        __syncthreads();
+        if (skip) continue;
+        for (int32_t p = b + threadIdx.x; p < e; p += blockDim.x) op.edge(p, u, pcol[p], 0);
     }
 }
 
@@ -116,7 +181,7 @@ __global__ void k_cc_compress(int32_t n, int32_t *parent)
 }  // namespace
 
 struct CcWS {
-    mgi::DevBuf parent;
+    mgi::DevBuf parent, giant;
 };
 
 namespace mgi {
@@ -125,6 +190,7 @@ void free_cc_ws(mg_graph *g)
 {
     if (!g->cws) return;
     dev_free(g->cws->parent);
+    dev_free(g->cws->giant);
     delete g->cws;
     g->cws = nullptr;
 }
@@ -133,18 +199,36 @@ mg_status cc_run(mg_graph *g, mg_run_info *info)
 {
     if (!g->cws) g->cws = new CcWS();
     MG_TRY(dev_alloc(g->cws->parent, (size_t)std::max(g->nv, 1) * 4));
+    MG_TRY(dev_alloc(g->cws->giant, 4));
     int32_t *parent = g->cws->parent.as<int32_t>();
+    int32_t *giant = g->cws->giant.as<int32_t>();
     cudaStream_t s = g->stream;
+    if (g->nv == 0) return MG_OK;
     const int grid = launch_grid(g, THREADS, 8);
     Profiler &P = g->prof;
-    int si = P.slot("cc_init"), sh = P.slot("cc_hook"), sc = P.slot("cc_compress");
+    const int si = P.slot("cc_init"), sh = P.slot("cc_hook"), sc = P.slot("cc_compress");
+    const bool sample = g->symmetric;
     P.begin(si);
     k_cc_init<<<grid, THREADS, 0, s>>>(g->nv, g->trow, g->tcol, parent);
     P.end();
+    if (sample) {
+        const int ss = P.slot("cc_sample"), sm = P.slot("cc_mode");
+        for (int r = 1; r < SAMPLE_ROUNDS + 1; r++) {  // neighbour 0 is linked by k_cc_init
+            P.begin(ss);
+            k_cc_sample<<<grid, THREADS, 0, s>>>(g->nv, g->trow, g->tcol, r, parent);
+            P.end();
+        }
+        P.begin(sc);
+        k_cc_compress<<<grid, THREADS, 0, s>>>(g->nv, parent);
+        P.end();
+        P.begin(sm);
+        k_cc_mode<<<1, MODE_SAMPLES, 0, s>>>(g->nv, parent, giant);
+        P.end();
+    }
     P.begin(sh);
     k_cc_hook<<<grid, THREADS, 0, s>>>(g->nv, g->trow, g->tcol, g->wrows.as<int32_t>(), g->nwrows,
                                        g->trows.as<int32_t>(), g->ntrows, g->hchunk.as<int32_t>(), g->nhchunks,
-                                       g->heavy_deg, g->symmetric ? 1 : 0, parent);
+                                       g->symmetric ? 1 : 0, sample ? giant : nullptr, parent);
     P.end();
     P.begin(sc);
     k_cc_compress<<<grid, THREADS, 0, s>>>(g->nv, parent);

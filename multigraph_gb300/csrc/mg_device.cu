@@ -463,11 +463,27 @@ __global__ void k_to_caller(int32_t n, int32_t rows, const int32_t *old2new, con
     }
 }
 
-// CC labels: minimum caller id of every engine-space root, then per vertex
+// CC labels: minimum caller id of every engine-space root, then per vertex.
+// Most vertices share one root (the giant component), so a warp whose 32
+// vertices have the same root reduces first and issues one atomic.
 __global__ void k_cc_min_old(int32_t n, const int32_t *parent, const int32_t *new2old, int32_t *minold)
 {
-    for (int32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x)
-        atomicMin(&minold[parent[v]], new2old[v]);
+    const int lane = threadIdx.x & 31;
+    for (int32_t base = blockIdx.x * blockDim.x + (threadIdx.x & ~31); base < n; base += gridDim.x * blockDim.x) {
+        const int32_t v = base + lane;
+        const bool ok = v < n;
+        const int32_t key = ok ? parent[v] : -1 - lane;
+        int32_t val = ok ? new2old[v] : 0x7fffffff;
+        int same = 0;
+        __match_all_sync(0xffffffffu, key, &same);
+        if (same) {
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) val = min(val, __shfl_xor_sync(0xffffffffu, val, o));
+            if (lane == 0 && val < __ldcg(&minold[key])) atomicMin(&minold[key], val);
+        } else if (ok && val < __ldcg(&minold[key])) {
+            atomicMin(&minold[key], val);
+        }
+    }
 }
 
 __global__ void k_cc_label_old(int32_t n, const int32_t *parent, const int32_t *old2new, const int32_t *minold,
