@@ -159,6 +159,10 @@ def batch_report(mg, device):
                  8-32 (mg_batch_*) vs one graph per call
       adjoint  : weighted PageRank on R-MAT scale 21 with FP32 weights in
                  (0, 1], forward alone vs forward + backward
+      lattice_bc_64: 64-source BC on the 4096 x 4096 lattice with 5 %
+                 diagonal shortcuts; the plain figure is 64 x the mean of
+                 two timed single-source runs (a full plain sweep takes
+                 about 15 s)
     Each entry carries the agreement of the two results."""
     import numpy as np
     out = {}
@@ -229,6 +233,20 @@ def batch_report(mg, device):
     out["adjoint"] = {"graph": f"rmat21_ef16 n={g.nv} m={g.ne}", "forward_ms": fi.device_ms,
                       "backward_ms": bi.device_ms, "forward_backward_ms": fi.device_ms + bi.device_ms,
                       "forward_sweeps": fi.iterations, "backward_sweeps": bi.iterations}
+    g.free()
+    h = mg.HostGraph.lattice(4096, 4096, 0.05, seed=3)
+    g = mg.Graph(h, device)
+    rng = np.random.default_rng(64)
+    ls = rng.integers(0, g.nv, 64).astype(np.int32)
+    _, lb = g.bc_multi(ls, out=False)
+    t1 = []
+    for s_ in ls[:2]:
+        _, i1 = g.bc(int(s_), out=False)
+        t1.append(i1.device_ms)
+    plain = 64 * float(np.mean(t1))
+    out["lattice_bc_64"] = {"graph": f"lattice4096x4096 +5% shortcuts n={g.nv} m={g.ne}",
+                            "batched_ms": lb.device_ms, "plain_ms_estimated": plain,
+                            "speedup": plain / lb.device_ms, "levels_per_group": lb.iterations / 2}
     g.free()
     return out
 

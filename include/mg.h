@@ -93,6 +93,17 @@ void mg_host_graph_free(mg_host_graph *g);
  * entry) or "pattern" when with_weights == 0. */
 mg_status mg_write_mtx(const mg_host_graph *g, const char *path, int32_t with_weights);
 
+/* Binary CSR cache: the loader's output (row offsets, column ids, weights,
+ * start_p, tra) in one file, so a graph parsed once from MTX reloads at
+ * disk speed.  Layout: a 40-byte header (magic "MGCSR001", nv, ne,
+ * start_p, tra, flags, FNV-1a 64 checksum of the arrays, little-endian),
+ * then csc_v[nv+1], csc_e[ne], csc_ev[ne] as int32.  mg_load_csr checks
+ * the header, the file size, the checksum and the CSR invariants
+ * (MG_ERR_PARSE on any mismatch).  No reference counterpart (the reference
+ * re-parses the MTX text on every run, read_input.cu:24-97). */
+mg_status mg_save_csr(const mg_host_graph *g, const char *path);
+mg_status mg_load_csr(const char *path, mg_host_graph **out);
+
 /* Synthetic inputs (no reference counterpart; the reference reads files).
  * R-MAT (Chakrabarti, Zhan, Faloutsos 2004): edge_factor * 2^scale draws,
  * quadrant probabilities a, b, c, 1-a-b-c; symmetrised, self-loops and

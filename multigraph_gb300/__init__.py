@@ -86,6 +86,8 @@ def _load_lib():
         "mg_host_graph_pin": ([vp], i32),
         "mg_host_graph_free": ([vp], None),
         "mg_write_mtx": ([vp, C.c_char_p, i32], i32),
+        "mg_save_csr": ([vp, C.c_char_p], i32),
+        "mg_load_csr": ([C.c_char_p, P(vp)], i32),
         "mg_gen_rmat": ([i32, i32, C.c_double, C.c_double, C.c_double, u64, i32, i32, i32, P(vp)], i32),
         "mg_gen_lattice": ([i32, i32, C.c_double, u64, P(vp)], i32),
         "mg_graph_upload": ([vp, i32, P(vp)], i32),
@@ -135,6 +137,7 @@ lib = _LazyLib()
 EXPORTED = [
     "mg_status_string", "mg_last_error", "mg_version", "mg_load_mtx", "mg_host_graph_from_entries",
     "mg_host_graph_from_csr", "mg_host_graph_view", "mg_host_graph_pin", "mg_host_graph_free", "mg_write_mtx",
+    "mg_save_csr", "mg_load_csr",
     "mg_gen_rmat", "mg_gen_lattice", "mg_graph_upload", "mg_graph_reload", "mg_graph_free", "mg_graph_info",
     "mg_graph_stream", "mg_graph_set_float_weights", "mg_opts_default", "mg_result_device", "mg_bfs", "mg_sssp",
     "mg_cc", "mg_bc", "mg_bc_multi", "mg_pagerank", "mg_ppr_batch", "mg_wpagerank", "mg_wpagerank_backward",
@@ -265,6 +268,16 @@ class HostGraph:
 
     def write_mtx(self, path: str, with_weights: bool = True):
         _check(lib.mg_write_mtx(self._h, path.encode(), int(with_weights)), "mg_write_mtx")
+
+    def save_csr(self, path: str):
+        """Binary CSR cache (mg_save_csr)."""
+        _check(lib.mg_save_csr(self._h, path.encode()), "mg_save_csr")
+
+    @classmethod
+    def load_csr(cls, path: str) -> "HostGraph":
+        h = C.c_void_p()
+        _check(lib.mg_load_csr(path.encode(), C.byref(h)), "mg_load_csr")
+        return cls(h)
 
     def free(self):
         if self._h:

@@ -17,7 +17,9 @@
 // validate.cu:6) is a small sequential CPU recomputation in this file; set
 // MG_VALIDATE=0 to skip it.  Environment options: MG_EXEC=host|graph,
 // MG_DIRECTION=auto|push|pull, MG_WEIGHT_SEED (pattern-file weights),
-// MG_TUNE_CACHE=<file> (use the autotuner), MG_JSON=1 (extra JSON line).
+// MG_TUNE_CACHE=<file> (use the autotuner), MG_JSON=1 (extra JSON line),
+// MG_CSR_SAVE=<file.mgcsr> (write the loaded CSR as a binary cache).  A
+// `.mgcsr` input file is read with mg_load_csr instead of the MTX parser.
 
 #include "mg.h"
 
@@ -151,11 +153,23 @@ int main(int argc, char **argv)
     uint64_t seed = std::strtoull(env("MG_WEIGHT_SEED", "1"), nullptr, 10);
     if (alg == CC || alg == PR_T || alg == PR_D) source = 0;  // main.cu:579,614 use source 0
 
+    // a binary CSR cache (mg_save_csr) loads without parsing; its source
+    // argument is already a loader (compacted) vertex id
+    const std::string fname(file);
+    const bool binary = fname.size() > 6 && fname.compare(fname.size() - 6, 6, ".mgcsr") == 0;
     mg_host_graph *hg = nullptr;
-    mg_status s = mg_load_mtx(file, source, flags, seed, 0, &hg);
+    mg_status s = binary ? mg_load_csr(file, &hg) : mg_load_mtx(file, source, flags, seed, 0, &hg);
     if (s != MG_OK) return die(s, "load");
+    if (!binary && std::getenv("MG_CSR_SAVE")) {
+        s = mg_save_csr(hg, std::getenv("MG_CSR_SAVE"));
+        if (s != MG_OK) return die(s, "save");
+    }
     mg_csr_view view;
     mg_host_graph_view(hg, &view);
+    if (binary && alg != CC && alg != PR_T && alg != PR_D) {
+        if (source < 0 || source >= view.nv) return die(MG_ERR_RANGE, "source");
+        view.start_p = source;
+    }
     mg_graph *dg = nullptr;
     s = mg_graph_upload(hg, 0, &dg);
     if (s != MG_OK) return die(s, "upload");

@@ -606,6 +606,125 @@ mg_status mg_write_mtx(const mg_host_graph *g, const char *path, int32_t with_we
     return ok ? MG_OK : fail(MG_ERR_IO, "write failed on %s", path);
 }
 
+// ---------------------------------------------------------------------------
+// binary CSR cache
+// ---------------------------------------------------------------------------
+namespace {
+
+const char CSR_MAGIC[8] = {'M', 'G', 'C', 'S', 'R', '0', '0', '1'};
+
+struct CsrHeader {
+    char magic[8];
+    int32_t nv, ne, start_p, tra;
+    uint32_t flags;  // bit 0: weights present (always set by mg_save_csr)
+    uint32_t pad;
+    uint64_t checksum;
+};
+static_assert(sizeof(CsrHeader) == 40, "header layout");
+
+uint64_t fnv1a(uint64_t h, const void *data, size_t bytes)
+{
+    const unsigned char *p = static_cast<const unsigned char *>(data);
+    for (size_t i = 0; i < bytes; i++) h = (h ^ p[i]) * 1099511628211ull;
+    return h;
+}
+
+uint64_t csr_checksum(const mg_host_graph &g)
+{
+    uint64_t h = 1469598103934665603ull;
+    h = fnv1a(h, g.v.data(), g.v.size() * 4);
+    h = fnv1a(h, g.e.data(), g.e.size() * 4);
+    h = fnv1a(h, g.ev.data(), g.ev.size() * 4);
+    return h;
+}
+
+bool little_endian()
+{
+    const uint32_t x = 1;
+    unsigned char c;
+    std::memcpy(&c, &x, 1);
+    return c == 1;
+}
+
+}  // namespace
+
+mg_status mg_save_csr(const mg_host_graph *g, const char *path)
+{
+    clear_error();
+    if (!g || !path) return fail(MG_ERR_INVALID, "null argument");
+    if (!little_endian()) return fail(MG_ERR_UNSUPPORTED, "binary CSR files are little-endian");
+    CsrHeader hd;
+    std::memset(&hd, 0, sizeof(hd));
+    std::memcpy(hd.magic, CSR_MAGIC, 8);
+    hd.nv = g->nv;
+    hd.ne = g->ne;
+    hd.start_p = g->start_p;
+    hd.tra = g->tra;
+    hd.flags = 1;
+    hd.checksum = csr_checksum(*g);
+    FILE *f = std::fopen(path, "wb");
+    if (!f) return fail(MG_ERR_IO, "cannot open %s for writing", path);
+    bool ok = std::fwrite(&hd, sizeof(hd), 1, f) == 1;
+    ok = ok && std::fwrite(g->v.data(), 4, g->v.size(), f) == g->v.size();
+    if (g->ne > 0) {
+        ok = ok && std::fwrite(g->e.data(), 4, g->e.size(), f) == g->e.size();
+        ok = ok && std::fwrite(g->ev.data(), 4, g->ev.size(), f) == g->ev.size();
+    }
+    ok = (std::fclose(f) == 0) && ok;
+    return ok ? MG_OK : fail(MG_ERR_IO, "write failed on %s", path);
+}
+
+mg_status mg_load_csr(const char *path, mg_host_graph **out)
+{
+    clear_error();
+    if (!path || !out) return fail(MG_ERR_INVALID, "null argument");
+    *out = nullptr;
+    if (!little_endian()) return fail(MG_ERR_UNSUPPORTED, "binary CSR files are little-endian");
+    FILE *f = std::fopen(path, "rb");
+    if (!f) return fail(MG_ERR_IO, "cannot open %s", path);
+    std::unique_ptr<FILE, int (*)(FILE *)> guard(f, std::fclose);
+    CsrHeader hd;
+    if (std::fread(&hd, sizeof(hd), 1, f) != 1) return fail(MG_ERR_PARSE, "%s: truncated header", path);
+    if (std::memcmp(hd.magic, CSR_MAGIC, 8) != 0) return fail(MG_ERR_PARSE, "%s: not a binary CSR file", path);
+    if (hd.nv < 0 || hd.ne < 0 || hd.flags != 1 || (hd.nv == 0 && hd.ne != 0))
+        return fail(MG_ERR_PARSE, "%s: bad header (nv %d, ne %d, flags %u)", path, hd.nv, hd.ne, hd.flags);
+    if (std::fseek(f, 0, SEEK_END) != 0) return fail(MG_ERR_IO, "%s: seek failed", path);
+    const long long size = std::ftell(f);
+    const long long want = (long long)sizeof(hd) + 4ll * ((long long)hd.nv + 1) + 8ll * hd.ne;
+    if (size != want) return fail(MG_ERR_PARSE, "%s: size %lld, header implies %lld", path, size, want);
+    std::fseek(f, (long)sizeof(hd), SEEK_SET);
+    if (inject_alloc_failure()) return fail(MG_ERR_OOM, "host allocation failed (injected)");
+    std::unique_ptr<mg_host_graph> g(new mg_host_graph());
+    g->nv = hd.nv;
+    g->ne = hd.ne;
+    g->start_p = hd.start_p;
+    g->tra = hd.tra;
+    try {
+        g->v.resize((size_t)hd.nv + 1);
+        g->e.resize((size_t)hd.ne);
+        g->ev.resize((size_t)hd.ne);
+    } catch (const std::bad_alloc &) {
+        return fail(MG_ERR_OOM, "host allocation failed");
+    }
+    bool ok = std::fread(g->v.data(), 4, g->v.size(), f) == g->v.size();
+    if (hd.ne > 0) {
+        ok = ok && std::fread(g->e.data(), 4, g->e.size(), f) == g->e.size();
+        ok = ok && std::fread(g->ev.data(), 4, g->ev.size(), f) == g->ev.size();
+    }
+    if (!ok) return fail(MG_ERR_PARSE, "%s: truncated arrays", path);
+    if (csr_checksum(*g) != hd.checksum) return fail(MG_ERR_PARSE, "%s: checksum mismatch", path);
+    if (g->v[0] != 0 || g->v[(size_t)hd.nv] != hd.ne) return fail(MG_ERR_PARSE, "%s: bad row offsets", path);
+    for (int32_t u = 0; u < hd.nv; u++)
+        if (g->v[(size_t)u + 1] < g->v[(size_t)u]) return fail(MG_ERR_PARSE, "%s: row offsets decrease at %d", path, u);
+    for (int32_t p = 0; p < hd.ne; p++)
+        if (g->e[(size_t)p] < 0 || g->e[(size_t)p] >= hd.nv)
+            return fail(MG_ERR_PARSE, "%s: column id out of range at entry %d", path, p);
+    if (hd.nv > 0 && (hd.start_p < 0 || hd.start_p >= hd.nv))
+        return fail(MG_ERR_PARSE, "%s: start_p %d out of range", path, hd.start_p);
+    *out = g.release();
+    return MG_OK;
+}
+
 void mg_host_graph_free(mg_host_graph *g);  // defined with the CUDA parts (unpins)
 
 // ---------------------------------------------------------------------------

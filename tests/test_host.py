@@ -145,6 +145,39 @@ def test_write_mtx_round_trip():
     assert np.array_equal(o.csc_e, h.arrays()[1])
 
 
+def test_binary_csr_cache_round_trip_and_corruption():
+    tmp = tempfile.mkdtemp()
+    src = _write(tmp, "s.mtx", "%%MatrixMarket matrix coordinate integer symmetric\n6 6 4\n2 1 5\n3 2 7\n5 4 1\n6 5 9\n")
+    for h in (mg.HostGraph.rmat(10, 8, seed=5), mg.HostGraph.load_mtx(src, 3, mg.LOAD_SYM)):
+        p = os.path.join(tmp, "g.mgcsr")
+        h.save_csr(p)
+        back = mg.HostGraph.load_csr(p)
+        assert (back.nv, back.ne, back.view().start_p, back.view().tra) == \
+            (h.nv, h.ne, h.view().start_p, h.view().tra)
+        for x, y in zip(h.arrays(), back.arrays()):
+            assert np.array_equal(x, y)
+    raw = bytearray(open(p, "rb").read())
+    bad = []
+    flip = bytearray(raw)
+    flip[-5] ^= 0x40                                   # a weight bit: checksum
+    bad.append(("flip.mgcsr", flip))
+    bad.append(("trunc.mgcsr", raw[:-4]))              # size check
+    magic = bytearray(raw)
+    magic[0:8] = b"NOTACSR!"
+    bad.append(("magic.mgcsr", magic))
+    bad.append(("short.mgcsr", raw[:20]))              # header cut
+    for name, data in bad:
+        q = os.path.join(tmp, name)
+        with open(q, "wb") as f:
+            f.write(data)
+        with pytest.raises(mg.MGError) as e:
+            mg.HostGraph.load_csr(q)
+        assert e.value.status == mg.MG_ERR_PARSE, name
+    with pytest.raises(mg.MGError) as e:
+        mg.HostGraph.load_csr(os.path.join(tmp, "missing.mgcsr"))
+    assert e.value.status == mg.MG_ERR_IO
+
+
 # --------------------------------------------------------------------------
 # failure injection (host side): the k-th allocation fails
 # --------------------------------------------------------------------------
