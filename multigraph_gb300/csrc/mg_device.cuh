@@ -229,6 +229,59 @@ struct WarpStage {
     __device__ __forceinline__ void push(int32_t v) { buf[atomicAdd(cnt, 1)] = v; }
 };
 
+// Grid-wide barrier for persistent kernels launched cooperatively (every
+// block resident).  Two levels so that no counter sees more than a few
+// dozen arrivals: block b arrives on counter 2 + (b % GRID_SYNC_GROUPS); the
+// last arrival of a group arrives on bar[0]; the last of those resets
+// bar[0] and bumps the generation bar[1], on which every other block waits.
+// bar holds 2 + GRID_SYNC_GROUPS words, zero before the launch.  The fences
+// on both sides order every block's writes before the barrier against every
+// block's reads after it.  The wait is bounded: after GRID_SYNC_LIMIT cycles
+// (about 2 s) the block sets *err and the barrier returns false, so a broken
+// launch ends with an error status instead of a hang; callers return at
+// once on false.
+constexpr long long GRID_SYNC_LIMIT = 4000000000ll;
+constexpr unsigned GRID_SYNC_GROUPS = 32;
+
+__device__ __forceinline__ bool grid_sync(unsigned *bar, int *err)
+{
+    __shared__ int s_ok;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        volatile unsigned *gen = bar + 1;
+        const unsigned g0 = *gen;
+        const unsigned grp = blockIdx.x % GRID_SYNC_GROUPS;
+        const unsigned ngroups = min(gridDim.x, GRID_SYNC_GROUPS);
+        const unsigned in_grp = (gridDim.x - grp + GRID_SYNC_GROUPS - 1) / GRID_SYNC_GROUPS;
+        __threadfence();
+        int ok = 1;
+        bool last = false;
+        if (atomicAdd(&bar[2 + grp], 1u) == in_grp - 1) {
+            atomicExch(&bar[2 + grp], 0u);
+            last = atomicAdd(&bar[0], 1u) == ngroups - 1;
+        }
+        if (last) {
+            atomicExch(&bar[0], 0u);
+            __threadfence();
+            atomicAdd(&bar[1], 1u);
+        } else {
+            const long long t0 = clock64();
+            while (*gen == g0) {
+                if (clock64() - t0 > GRID_SYNC_LIMIT) {
+                    ok = 0;
+                    atomicExch(err, 1);
+                    break;
+                }
+                __nanosleep(32);
+            }
+        }
+        __threadfence();
+        s_ok = ok && *(volatile int *)err == 0;
+    }
+    __syncthreads();
+    return s_ok != 0;
+}
+
 __device__ __forceinline__ bool bm_test(const uint32_t *bm, int v) { return (bm[v >> 5] >> (v & 31)) & 1u; }
 __device__ __forceinline__ bool bm_set(uint32_t *bm, int v)  // returns true if this call set it
 {

@@ -5,23 +5,27 @@
 // process_f1 / make_frontier / phase1 / phase11 / phase2 and the sampling
 // heuristic, and MultiGraph_V_E_V_pull (process2.cu:263-325).
 //
-// One iteration is three launches, all with a fixed persistent grid so the
-// loop can live inside a CUDA graph with a device-side WHILE node:
-//   k_push   frontier queue -> neighbours (warp load-balanced search over the
+// The loop lives inside a CUDA graph with a device-side WHILE node; one
+// pass of its body is four launches with fixed grids:
+//   k_sparse_levels  (cooperative, persistent) every consecutive push level:
+//            frontier queue -> neighbours (warp load-balanced search over the
 //            degrees of 32 queue entries; vertices above PUSH_HEAVY split over
 //            the whole grid), claims / relaxes destinations with the
 //            operator hooks, appends the next queue with warp-aggregated
-//            atomics and sets the next-frontier bitmap;
+//            atomics and sets the next-frontier bitmap; grid barriers
+//            between levels, block 0 runs the end-of-level decision;
 //   k_pull   (when the frontier is dense) every unvisited vertex scans its
 //            in-edges against the frontier bitmap (BFS stops at the first
 //            parent; SSSP/BC reduce over all in-edges), light rows in
 //            degree bins (warp / thread per row), heavy rows in 2048-edge
 //            chunks;
+//   k_compact (after a pull) next queue from the next-frontier bitmap;
 //   k_decide 1 warp: next size, direction switch (frontier edges against
 //            unvisited edges, Beamer), iteration cap, loop condition.
-// Only one of k_push / k_pull does work in an iteration; the other returns
-// at once.  Frontier bitmaps are triple-buffered: the active kernel clears
-// the buffer the next iteration will write.
+// The push phase returns as soon as the switch picks pull; k_pull /
+// k_compact / k_decide then run one dense level and the body repeats.
+// Frontier bitmaps are triple-buffered: the active kernel clears the buffer
+// the next iteration will write.
 
 #include "mg_device.cuh"
 #include "mg_ops.cuh"
@@ -35,6 +39,9 @@ constexpr int ALG_BFS = 0, ALG_SSSP = 1, ALG_BC = 2;
 constexpr int MODE_PUSH = 0, MODE_PULL = 1;
 constexpr int32_t PUSH_HEAVY = 4096;
 constexpr int THREADS = 256;
+constexpr int PTHREADS = 1024;  // persistent kernels: 2 CTAs of 1024 per SM (fewer barrier arrivals)
+// grid barrier words (2 + GRID_SYNC_GROUPS) + the error flag, rounded up
+constexpr size_t BAR_BYTES = 4 * (2 + mgd::GRID_SYNC_GROUPS + 1 + 7);
 
 struct FCtl {
     int32_t more;       // continue flag (host loop readback)
@@ -77,9 +84,24 @@ struct Args {
     int32_t *heavy;      // 2 * n (parity)
     int32_t *lvl_off;
     FCtl *ctl;
+    unsigned *bar;       // grid barrier of the persistent push kernel (2 words)
+    int *bar_err;        // set when a grid barrier wait times out
 };
 
 __device__ __forceinline__ uint32_t *bm_buf(const Args &a, int idx) { return a.bm + (size_t)idx * a.words; }
+
+// The loop state as the persistent kernel re-reads it after every grid
+// barrier: through L2, never from a stale L1 line.
+static_assert(sizeof(FCtl) % 8 == 0, "FCtl is copied as 8-byte words");
+__device__ __forceinline__ FCtl load_ctl(const FCtl *p)
+{
+    FCtl c;
+    const int2 *s = reinterpret_cast<const int2 *>(p);
+    int2 *d = reinterpret_cast<int2 *>(&c);
+#pragma unroll
+    for (int i = 0; i < (int)(sizeof(FCtl) / 8); i++) d[i] = __ldcg(s + i);
+    return c;
+}
 
 // warp-wide: add v (64-bit) from every lane to *dst with one atomic
 __device__ __forceinline__ void warp_add64(long long *dst, long long v)
@@ -92,21 +114,20 @@ __device__ __forceinline__ void warp_add64(long long *dst, long long v)
 // record a newly reached vertex in the next frontier (push sweeps; all lanes
 // call).  SSSP has already set the vertex's bit when it claimed it.
 template <int ALG>
-__device__ __forceinline__ void emit_next(const Args &a, const FCtl &c, int nextbuf, bool found, int32_t v)
+__device__ __forceinline__ void emit_next(const Args &a, const FCtl &c, int nextbuf, bool found, int32_t v,
+                                          long long &dsum)
 {
     int slot = mgd::warp_append(&a.ctl->nq, found);
-    long long d = 0;
     if (found) {
         a.queue[c.nqoff + slot] = v;
         if (ALG != ALG_SSSP) mgd::bm_set(bm_buf(a, nextbuf), v);
         int32_t dg = a.row[v + 1] - a.row[v];
-        d = dg;
+        dsum += dg;
         if (dg > PUSH_HEAVY) {
             int h = atomicAdd(&a.ctl->nhcur, 1);
             a.heavy[(size_t)(c.hpar ^ 1) * a.n + h] = v;
         }
     }
-    warp_add64(&a.ctl->nf_edges, d);
 }
 
 // ----------------------------------------------------------------------------
@@ -133,11 +154,13 @@ __device__ __forceinline__ bool push_edge(const Args &a, int it1, int32_t v, int
     }
 }
 
+// One push level.  Queue entries, heavy entries and the frontier's labels /
+// path counts were written by other blocks in the previous level, so they
+// are loaded through L2 (__ldcg): the persistent kernel runs many levels in
+// one launch.
 template <int ALG>
-__global__ void __launch_bounds__(THREADS) k_push(Args a)
+__device__ __forceinline__ void push_level(const Args &a, const FCtl &c)
 {
-    const FCtl c = *a.ctl;
-    if (c.mode != MODE_PUSH || c.more == 0) return;
     const int it1 = c.iter + 1;
     const int nextbuf = (c.cur + 1) % 3, sparebuf = (c.cur + 2) % 3;
     // clear the buffer the next iteration writes
@@ -148,13 +171,13 @@ __global__ void __launch_bounds__(THREADS) k_push(Args a)
     const int lane = mgd::lane();
     const int gwarp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int nwarps = (gridDim.x * blockDim.x) >> 5;
-    long long scanned = 0;
+    long long scanned = 0, dsum = 0;
     // heavy frontier vertices: every thread of the grid strides over their edges
     for (int h = 0; h < c.hcur; h++) {
-        int32_t u = a.heavy[(size_t)c.hpar * a.n + h];
+        int32_t u = __ldcg(&a.heavy[(size_t)c.hpar * a.n + h]);
         int32_t b = a.row[u], e = a.row[u + 1];
-        int32_t pi = a.label[u];
-        double pd = (ALG == ALG_BC) ? a.sigma[u] : 0.0;
+        int32_t pi = __ldcg(&a.label[u]);
+        double pd = (ALG == ALG_BC) ? __ldcg(&a.sigma[u]) : 0.0;
         int32_t span = e - b;
         int32_t rounds = (span + gridDim.x * blockDim.x - 1) / (gridDim.x * blockDim.x);
         for (int r = 0; r < rounds; r++) {
@@ -165,21 +188,28 @@ __global__ void __launch_bounds__(THREADS) k_push(Args a)
                 v = a.col[k];
                 found = push_edge<ALG>(a, it1, v, pi, pd, (ALG == ALG_SSSP) ? a.wt[k] : 0, bm_buf(a, nextbuf));
             }
-            emit_next<ALG>(a, c, nextbuf, found, v);
+            emit_next<ALG>(a, c, nextbuf, found, v, dsum);
         }
         scanned += (threadIdx.x == 0 && blockIdx.x == 0) ? span : 0;
     }
-    // light frontier vertices: 32 per warp, load-balanced over their edges
-    for (int base = gwarp * 32; base < c.qsize; base += nwarps * 32) {
+    // light frontier vertices: vpw per warp (32, or fewer when the frontier
+    // would leave warps idle), load-balanced over their edges
+    int vpw = 32;
+    if (c.qsize < nwarps * 32) {
+        const int want = max(1, c.qsize / nwarps);
+        vpw = 1;
+        while (vpw * 2 <= want) vpw *= 2;
+    }
+    for (int base = gwarp * vpw; base < c.qsize; base += nwarps * vpw) {
         int32_t u = -1, start = 0, deg = 0, pi = 0;
         double pd = 0.0;
-        if (base + lane < c.qsize) {
-            u = a.queue[c.qoff + base + lane];
+        if (lane < vpw && base + lane < c.qsize) {
+            u = __ldcg(&a.queue[c.qoff + base + lane]);
             start = a.row[u];
             deg = a.row[u + 1] - start;
             if (deg > PUSH_HEAVY) deg = 0;
-            pi = a.label[u];
-            if (ALG == ALG_BC) pd = a.sigma[u];
+            pi = __ldcg(&a.label[u]);
+            if (ALG == ALG_BC) pd = __ldcg(&a.sigma[u]);
         }
         int incl = mgd::warp_scan_incl(deg);
         int excl = incl - deg;
@@ -198,9 +228,10 @@ __global__ void __launch_bounds__(THREADS) k_push(Args a)
                 v = a.col[e];
                 found = push_edge<ALG>(a, it1, v, opi, opd, (ALG == ALG_SSSP) ? a.wt[e] : 0, bm_buf(a, nextbuf));
             }
-            emit_next<ALG>(a, c, nextbuf, found, v);
+            emit_next<ALG>(a, c, nextbuf, found, v, dsum);
         }
     }
+    warp_add64(&a.ctl->nf_edges, dsum);
     if (lane == 0 && scanned) atomicAdd((unsigned long long *)&a.ctl->scanned, (unsigned long long)scanned);
 }
 
@@ -421,53 +452,109 @@ __global__ void __launch_bounds__(THREADS) k_compact(Args a)
 // ----------------------------------------------------------------------------
 // decide: 1 thread
 // ----------------------------------------------------------------------------
-__global__ void k_decide(Args a, cudaGraphConditionalHandle h, int use_cond)
+__device__ __forceinline__ void store_ctl(FCtl *p, const FCtl &c)
 {
-    FCtl *c = a.ctl;
-    if (threadIdx.x != 0) return;
-    int more = c->more;
+    int2 *d = reinterpret_cast<int2 *>(p);
+    const int2 *s = reinterpret_cast<const int2 *>(&c);
+#pragma unroll
+    for (int i = 0; i < (int)(sizeof(FCtl) / 8); i++) d[i] = s[i];
+}
+
+// End of a level (one thread, no other thread touching the loop state):
+// next queue slice, direction switch, caps.  Works on a register copy (one
+// batch of parallel loads, one batch of stores).  Returns the continue flag.
+__device__ __forceinline__ int decide_step(const Args &a)
+{
+    FCtl c = load_ctl(a.ctl);
+    int more = c.more;
     if (more) {
-        int32_t nq = c->nq;
-        if (c->mode == MODE_PULL) c->pull_iters++;
-        c->iter += 1;
-        if (c->archive && c->iter + 1 < a.n + 3) {
-            a.lvl_off[c->iter + 1] = c->nqoff + nq;
-            if (nq > 0) c->nlevels = c->iter + 1;
+        const int32_t nq = c.nq;
+        if (c.mode == MODE_PULL) c.pull_iters++;
+        c.iter += 1;
+        if (c.archive && c.iter + 1 < a.n + 3) {
+            a.lvl_off[c.iter + 1] = c.nqoff + nq;
+            if (nq > 0) c.nlevels = c.iter + 1;
         }
-        c->qoff = c->nqoff;
-        c->qsize = nq;
-        c->nqoff = c->archive ? (c->qoff + nq) : (c->qoff == 0 ? a.n : 0);
-        c->nq = 0;
-        c->hcur = c->nhcur;
-        c->nhcur = 0;
-        c->hpar ^= 1;
-        c->cur = (c->cur + 1) % 3;
-        long long nfe = c->nf_edges;
-        c->visited_edges += nfe;
-        c->nf_edges = 0;
+        c.qoff = c.nqoff;
+        c.qsize = nq;
+        c.nqoff = c.archive ? (c.qoff + nq) : (c.qoff == 0 ? a.n : 0);
+        c.nq = 0;
+        c.hcur = c.nhcur;
+        c.nhcur = 0;
+        c.hpar ^= 1;
+        c.cur = (c.cur + 1) % 3;
+        const long long nfe = c.nf_edges;
+        c.visited_edges += nfe;
+        c.nf_edges = 0;
         if (nq == 0) {
             more = 0;
         } else {
-            if (c->dirmode == MG_DIR_PUSH) c->mode = MODE_PUSH;
-            else if (c->dirmode == MG_DIR_PULL) c->mode = MODE_PULL;
-            else if (c->archive) {
+            if (c.dirmode == MG_DIR_PUSH) c.mode = MODE_PUSH;
+            else if (c.dirmode == MG_DIR_PULL) c.mode = MODE_PULL;
+            else if (c.archive) {
                 // Beamer: push -> pull when frontier edges exceed unvisited
                 // edges / alpha; pull -> push when the frontier is below n / beta
-                long long unvisited = (long long)a.m - c->visited_edges;
-                if (c->mode == MODE_PUSH) {
-                    if (nfe * (long long)c->alpha > unvisited && nq > 64) c->mode = MODE_PULL;
+                const long long unvisited = (long long)a.m - c.visited_edges;
+                if (c.mode == MODE_PUSH) {
+                    if (nfe * (long long)c.alpha > unvisited && nq > 64) c.mode = MODE_PULL;
                 } else {
-                    if ((long long)nq * c->beta < a.n) c->mode = MODE_PUSH;
+                    if ((long long)nq * c.beta < a.n) c.mode = MODE_PUSH;
                 }
             } else {
                 // SSSP: pull when the frontier's edges are a large share of m
-                c->mode = (nfe * (long long)c->alpha > (long long)a.m) ? MODE_PULL : MODE_PUSH;
+                c.mode = (nfe * (long long)c.alpha > (long long)a.m) ? MODE_PULL : MODE_PUSH;
             }
-            if (c->iter >= c->max_iter) { c->status = 1; more = 0; }
+            if (c.iter >= c.max_iter) { c.status = 1; more = 0; }
         }
-        c->more = more;
+        c.more = more;
+        store_ctl(a.ctl, c);
     }
+    return more;
+}
+
+__global__ void k_decide(Args a, cudaGraphConditionalHandle h, int use_cond)
+{
+    if (threadIdx.x != 0) return;
+    const int more = decide_step(a);
     if (use_cond) cudaGraphSetConditional(h, more ? 1u : 0u);
+}
+
+// Persistent push phase: consecutive push levels in one cooperative launch,
+// separated by grid barriers (push level | barrier | block 0 decides |
+// barrier), until the traversal ends or the direction switch picks pull.
+// High-diameter graphs (lattices, road networks) spend thousands of levels
+// here, each a few microseconds instead of a round of kernel launches.  A
+// barrier timeout sets status 3 and ends the traversal.
+// Every block reads the loop state once per level: one warp loads it
+// (one L2 request per block instead of one per warp) and shares it.
+__device__ __forceinline__ FCtl block_load_ctl(const FCtl *p)
+{
+    __shared__ int2 s_c[sizeof(FCtl) / 8];
+    if (threadIdx.x < sizeof(FCtl) / 8) s_c[threadIdx.x] = __ldcg(reinterpret_cast<const int2 *>(p) + threadIdx.x);
+    __syncthreads();
+    FCtl c;
+    int2 *d = reinterpret_cast<int2 *>(&c);
+#pragma unroll
+    for (int i = 0; i < (int)(sizeof(FCtl) / 8); i++) d[i] = s_c[i];
+    __syncthreads();
+    return c;
+}
+
+template <int ALG>
+__global__ void __launch_bounds__(PTHREADS, 2) k_sparse_levels(Args a)
+{
+    for (int32_t lv = 0; lv <= a.n + 2; lv++) {
+        const FCtl c = block_load_ctl(a.ctl);
+        if (c.more == 0 || c.mode != MODE_PUSH) return;
+        push_level<ALG>(a, c);
+        if (!mgd::grid_sync(a.bar, a.bar_err)) break;
+        if (blockIdx.x == 0 && threadIdx.x == 0) decide_step(a);
+        if (!mgd::grid_sync(a.bar, a.bar_err)) break;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0 && *(volatile int *)a.bar_err) {
+        a.ctl->status = 3;
+        a.ctl->more = 0;
+    }
 }
 
 // ----------------------------------------------------------------------------
@@ -515,10 +602,9 @@ __global__ void k_init(Args a, int32_t src, const int32_t *srcs, int32_t nsrc, i
 // process_fbc :5-132 in one pull form over the archived level lists)
 // ----------------------------------------------------------------------------
 struct BCtl {
-    int32_t more;
-    int32_t L;       // level whose predecessors are being finalised
-    int32_t nheavy;
-    int32_t src;     // source of this sweep (excluded from the BC sum)
+    int32_t L0;       // deepest level; levels L0 .. 1 finalise their predecessors
+    int32_t src;      // source of this sweep (excluded from the BC sum)
+    int32_t hcnt[2];  // heavy entries listed at a level, by level parity
 };
 
 __global__ void k_bc_q_init(int32_t n, const double *sigma, const int32_t *label, float *q, float *delta)
@@ -538,24 +624,32 @@ __device__ __forceinline__ void bc_finish_vertex(int32_t v, float s, const doubl
     if (bc && v != src) bc[v] += dv;
 }
 
-__global__ void __launch_bounds__(THREADS) k_bc_back(Args a, BCtl *bc_ctl, float *q, float *delta, float *bcacc,
-                                                     int32_t *heavy_list)
+// Level L-1 entries pull (1+delta)/sigma from their level-L successors.
+// q of the successors was written by other blocks in the previous level,
+// so it is loaded through L2 (the persistent kernel runs every level in one
+// launch).  Entries above PUSH_HEAVY are listed for bc_back_heavy_level.
+__device__ __forceinline__ void bc_back_level(const Args &a, int32_t L, int32_t src, int32_t *hcount, float *q,
+                                              float *delta, float *bcacc, int32_t *heavy_list)
 {
-    const BCtl bctl = *bc_ctl;
-    if (bctl.more == 0) return;
-    const int32_t L = bctl.L, src = bctl.src;
     const int32_t b0 = a.lvl_off[L - 1], b1 = a.lvl_off[L];
     const int lane = mgd::lane();
     const int gwarp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int nwarps = (gridDim.x * blockDim.x) >> 5;
-    for (int base = b0 + gwarp * 32; base < b1; base += nwarps * 32) {
+    // vpw entries per warp: 32, or fewer when the level would leave warps idle
+    int vpw = 32;
+    if (b1 - b0 < nwarps * 32) {
+        const int want = max(1, (b1 - b0) / nwarps);
+        vpw = 1;
+        while (vpw * 2 <= want) vpw *= 2;
+    }
+    for (int base = b0 + gwarp * vpw; base < b1; base += nwarps * vpw) {
         int32_t v = -1, start = 0, deg = 0;
-        if (base + lane < b1) {
+        if (lane < vpw && base + lane < b1) {
             v = a.queue[base + lane];
             start = a.row[v];
             deg = a.row[v + 1] - start;
             if (deg > PUSH_HEAVY) {
-                int h = atomicAdd(&bc_ctl->nheavy, 1);
+                int h = atomicAdd(hcount, 1);
                 heavy_list[h] = v;
                 deg = 0;
                 v = -1;
@@ -573,7 +667,7 @@ __global__ void __launch_bounds__(THREADS) k_bc_back(Args a, BCtl *bc_ctl, float
             float t = 0.0f;
             if (k < total) {
                 int32_t w = a.col[e];
-                if (a.label[w] == L) t = q[w];
+                if (a.label[w] == L) t = __ldcg(&q[w]);
             } else {
                 own = -1;
             }
@@ -598,20 +692,18 @@ __global__ void __launch_bounds__(THREADS) k_bc_back(Args a, BCtl *bc_ctl, float
     }
 }
 
-__global__ void __launch_bounds__(THREADS) k_bc_back_heavy(Args a, BCtl *bc_ctl, float *q, float *delta,
-                                                           float *bcacc, const int32_t *heavy_list)
+// heavy entries of the level: a CTA each, fixed-order block sum
+__device__ __forceinline__ void bc_back_heavy_level(const Args &a, int32_t L, int32_t src, int32_t nheavy, float *q,
+                                                    float *delta, float *bcacc, const int32_t *heavy_list)
 {
-    const BCtl bctl = *bc_ctl;
-    if (bctl.more == 0) return;
-    const int32_t L = bctl.L, src = bctl.src;
-    __shared__ float s_part[THREADS / 32];
-    for (int32_t h = blockIdx.x; h < bctl.nheavy; h += gridDim.x) {
-        int32_t v = heavy_list[h];
+    __shared__ float s_part[32];
+    for (int32_t h = blockIdx.x; h < nheavy; h += gridDim.x) {
+        int32_t v = __ldcg(&heavy_list[h]);
         int32_t b = a.row[v], e = a.row[v + 1];
         float acc = 0.0f;
         for (int32_t p = b + threadIdx.x; p < e; p += blockDim.x) {
             int32_t w = a.col[p];
-            if (a.label[w] == L) acc += q[w];
+            if (a.label[w] == L) acc += __ldcg(&q[w]);
         }
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
@@ -619,33 +711,48 @@ __global__ void __launch_bounds__(THREADS) k_bc_back_heavy(Args a, BCtl *bc_ctl,
         __syncthreads();
         if (threadIdx.x == 0) {
             float s = 0.0f;
-            for (int w = 0; w < THREADS / 32; w++) s += s_part[w];
+            for (int w = 0; w < (int)(blockDim.x >> 5); w++) s += s_part[w];
             bc_finish_vertex(v, s, a.sigma, delta, q, bcacc, src);
         }
         __syncthreads();
     }
 }
 
-__global__ void k_bc_back_decide(BCtl *bc_ctl, cudaGraphConditionalHandle h, int use_cond)
+// Persistent backward sweep: every level in one cooperative launch, two
+// grid barriers per level (light entries | barrier | heavy entries |
+// barrier).  Every block walks L = L0 .. 1 itself; the heavy-entry counter
+// alternates with the level's parity, and block 0 clears the one the next
+// level will use while the current level runs (its last readers finished
+// before the previous barrier).  A barrier timeout sets the error flag; the
+// host reads it and fails the run.
+__global__ void __launch_bounds__(PTHREADS, 2) k_bc_back_levels(Args a, BCtl *bc_ctl, float *q, float *delta,
+                                                                float *bcacc, int32_t *heavy_list)
 {
-    if (threadIdx.x != 0) return;
-    int more = bc_ctl->more;
-    if (more) {
-        bc_ctl->L -= 1;
-        bc_ctl->nheavy = 0;
-        if (bc_ctl->L < 1) more = 0;
-        bc_ctl->more = more;
+    __shared__ int4 s_b;
+    __shared__ int s_nheavy;
+    if (threadIdx.x == 0) s_b = __ldcg(reinterpret_cast<const int4 *>(bc_ctl));
+    __syncthreads();
+    const int32_t L0 = s_b.x, src = s_b.y;
+    for (int32_t L = L0; L >= 1; L--) {
+        const int par = L & 1;
+        if (blockIdx.x == 0 && threadIdx.x == 0) bc_ctl->hcnt[par ^ 1] = 0;
+        bc_back_level(a, L, src, &bc_ctl->hcnt[par], q, delta, bcacc, heavy_list);
+        if (!mgd::grid_sync(a.bar, a.bar_err)) return;
+        if (threadIdx.x == 0) s_nheavy = __ldcg(&bc_ctl->hcnt[par]);
+        __syncthreads();
+        const int32_t nheavy = s_nheavy;
+        bc_back_heavy_level(a, L, src, nheavy, q, delta, bcacc, heavy_list);
+        if (!mgd::grid_sync(a.bar, a.bar_err)) return;
     }
-    if (use_cond) cudaGraphSetConditional(h, more ? 1u : 0u);
 }
 
 __global__ void k_bc_back_init(const FCtl *fc, BCtl *bc_ctl, int32_t src)
 {
     if (threadIdx.x != 0) return;
     bc_ctl->src = src;
-    bc_ctl->L = fc->nlevels - 1;
-    bc_ctl->nheavy = 0;
-    bc_ctl->more = bc_ctl->L >= 1 ? 1 : 0;
+    bc_ctl->L0 = fc->nlevels - 1;
+    bc_ctl->hcnt[0] = 0;
+    bc_ctl->hcnt[1] = 0;
 }
 
 }  // namespace
@@ -656,8 +763,10 @@ __global__ void k_bc_back_init(const FCtl *fc, BCtl *bc_ctl, int32_t src)
 struct FrontierWS {
     mgi::DevBuf label, sigma, bm, visited, queue, heavy, lvl_off, ctl;
     mgi::DevBuf q, delta, bc, bctl, bheavy, srcbuf;
+    mgi::DevBuf bar;        // grid barrier words + error flag of the persistent kernels
+    int coop_grid[3] = {0, 0, 0};  // resident blocks of k_sparse_levels<ALG> on this device
+    int coop_back = 0;             // resident blocks of k_bc_back_levels
     mgi::LoopGraph lg[3];
-    mgi::LoopGraph lg_back;
 };
 
 namespace mgi {
@@ -667,10 +776,9 @@ void free_frontier_ws(mg_graph *g)
     if (!g->fws) return;
     FrontierWS *w = g->fws;
     DevBuf *bufs[] = {&w->label, &w->sigma, &w->bm, &w->visited, &w->queue, &w->heavy,
-                      &w->lvl_off, &w->ctl, &w->q, &w->delta, &w->bc, &w->bctl, &w->bheavy, &w->srcbuf};
+                      &w->lvl_off, &w->ctl, &w->q, &w->delta, &w->bc, &w->bctl, &w->bheavy, &w->srcbuf, &w->bar};
     for (DevBuf *b : bufs) dev_free(*b);
     for (auto &l : w->lg) l.destroy();
-    w->lg_back.destroy();
     delete w;
     g->fws = nullptr;
 }
@@ -688,7 +796,36 @@ static mg_status ensure_ws(mg_graph *g, int alg)
     MG_TRY(dev_alloc(w->heavy, 2 * n * 4));
     MG_TRY(dev_alloc(w->ctl, sizeof(FCtl)));
     MG_TRY(dev_alloc(w->lvl_off, (n + 3) * 4));
+    MG_TRY(dev_alloc(w->bar, BAR_BYTES));
     if (alg == ALG_BC) MG_TRY(dev_alloc(w->sigma, n * 8));
+    if (w->coop_grid[alg] == 0) {
+        int per_sm = 0;
+        switch (alg) {
+        case ALG_BFS: MG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_sparse_levels<ALG_BFS>, PTHREADS, 0)); break;
+        case ALG_SSSP: MG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_sparse_levels<ALG_SSSP>, PTHREADS, 0)); break;
+        default: MG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_sparse_levels<ALG_BC>, PTHREADS, 0)); break;
+        }
+        if (per_sm < 1) return fail(MG_ERR_CUDA, "persistent push kernel does not fit on an SM");
+        w->coop_grid[alg] = std::min(per_sm, 2) * g->num_sms;
+    }
+    return MG_OK;
+}
+
+// cooperative launch (all blocks resident) of the persistent push phase
+template <int ALG>
+static mg_status launch_sparse_levels(const Args &a, int grid, cudaStream_t st)
+{
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)grid);
+    cfg.blockDim = dim3(PTHREADS);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    MG_CUDA(cudaLaunchKernelEx(&cfg, k_sparse_levels<ALG>, a));
     return MG_OK;
 }
 
@@ -714,6 +851,8 @@ static Args make_args(mg_graph *g)
     a.heavy = w->heavy.as<int32_t>();
     a.lvl_off = w->lvl_off.as<int32_t>();
     a.ctl = w->ctl.as<FCtl>();
+    a.bar = w->bar.as<unsigned>();
+    a.bar_err = reinterpret_cast<int *>(w->bar.as<unsigned>() + 2 + mgd::GRID_SYNC_GROUPS);
     return a;
 }
 
@@ -748,6 +887,7 @@ static mg_status frontier_run_impl(mg_graph *g, int alg, int32_t src, const int3
     MG_CUDA(cudaMemsetAsync(a.label, 0x64, n * 4, s));
     MG_CUDA(cudaMemsetAsync(a.bm, 0, 3 * (size_t)a.words * 4, s));
     MG_CUDA(cudaMemsetAsync(a.visited, 0, (size_t)a.words * 4, s));
+    MG_CUDA(cudaMemsetAsync(w->bar.p, 0, BAR_BYTES, s));
     if (alg == ALG_BC) MG_CUDA(cudaMemsetAsync(a.sigma, 0, n * 8, s));
     int max_iter = opt.max_iter > 0 ? opt.max_iter : (alg == ALG_SSSP ? 4 * g->nv + 16 : g->nv + 2);
     int alpha = opt.alpha > 0 ? opt.alpha : 15, beta = opt.beta > 0 ? opt.beta : 18;
@@ -767,9 +907,9 @@ static mg_status frontier_run_impl(mg_graph *g, int alg, int32_t src, const int3
     BodyFn body = [&](cudaStream_t st, cudaGraphConditionalHandle h, int use_cond) -> mg_status {
         P.begin(sp);
         switch (alg) {
-        case ALG_BFS: k_push<ALG_BFS><<<grid, THREADS, 0, st>>>(a); break;
-        case ALG_SSSP: k_push<ALG_SSSP><<<grid, THREADS, 0, st>>>(a); break;
-        default: k_push<ALG_BC><<<grid, THREADS, 0, st>>>(a); break;
+        case ALG_BFS: MG_TRY(launch_sparse_levels<ALG_BFS>(a, w->coop_grid[alg], st)); break;
+        case ALG_SSSP: MG_TRY(launch_sparse_levels<ALG_SSSP>(a, w->coop_grid[alg], st)); break;
+        default: MG_TRY(launch_sparse_levels<ALG_BC>(a, w->coop_grid[alg], st)); break;
         }
         P.end();
         P.begin(sl);
@@ -799,6 +939,7 @@ static mg_status frontier_run_impl(mg_graph *g, int alg, int32_t src, const int3
         info->pull_iterations = hc.pull_iters;
         info->edges_scanned = hc.scanned;
     }
+    if (hc.status == 3) return fail(MG_ERR_CUDA, "grid barrier of the persistent push kernel timed out");
     if (hc.status != 0) return fail(MG_ERR_ITER_LIMIT, "iteration cap %d reached", max_iter);
     return MG_OK;
 }
@@ -830,28 +971,37 @@ mg_status bc_backward(mg_graph *g, int32_t src, const mg_opts &opt, float *bcacc
     BCtl *bc = w->bctl.as<BCtl>();
     int32_t *hl = w->bheavy.as<int32_t>();
     const int grid = launch_grid(g, THREADS, 8);
+    if (w->coop_back == 0) {
+        int per_sm = 0;
+        MG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_bc_back_levels, PTHREADS, 0));
+        if (per_sm < 1) return fail(MG_ERR_CUDA, "persistent backward kernel does not fit on an SM");
+        w->coop_back = std::min(per_sm, 2) * g->num_sms;
+    }
     k_bc_q_init<<<grid, THREADS, 0, s>>>(g->nv, a.sigma, a.label, q, delta);
     k_bc_back_init<<<1, 32, 0, s>>>(a.ctl, bc, src);
+    MG_CUDA(cudaMemsetAsync(w->bar.p, 0, BAR_BYTES, s));
     MG_CUDA(cudaGetLastError());
+    // every level in one cooperative launch
     Profiler &P = g->prof;
-    const int sb = P.slot("bc_back"), sh = P.slot("bc_back_heavy"), sd = P.slot("bc_back_decide");
-    BodyFn body = [&](cudaStream_t st, cudaGraphConditionalHandle h, int use_cond) -> mg_status {
-        P.begin(sb);
-        k_bc_back<<<grid, THREADS, 0, st>>>(a, bc, q, delta, bcacc, hl);
-        P.end();
-        P.begin(sh);
-        k_bc_back_heavy<<<grid, THREADS, 0, st>>>(a, bc, q, delta, bcacc, hl);
-        P.end();
-        P.begin(sd);
-        k_bc_back_decide<<<1, 32, 0, st>>>(bc, h, use_cond);
-        P.end();
-        MG_CUDA(cudaGetLastError());
-        return MG_OK;
-    };
-    // the graph bakes in the bc accumulator (null for single-source runs)
-    uint64_t key = key_of(a, 7) ^ ((uint64_t)(uintptr_t)bcacc * 31) ^ ((uint64_t)(uintptr_t)q * 17);
-    return run_loop(opt.profile ? MG_EXEC_HOST : opt.exec, opt.profile != 0, s, w->lg_back, key, body, &bc->more,
-                    g->pinned_flag, g->nv + 4);
+    const int sb = P.slot("bc_back");
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)w->coop_back);
+    cfg.blockDim = dim3(PTHREADS);
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    P.begin(sb);
+    MG_CUDA(cudaLaunchKernelEx(&cfg, k_bc_back_levels, a, bc, q, delta, bcacc, hl));
+    P.end();
+    int err = 0;
+    MG_CUDA(cudaMemcpyAsync(&err, a.bar_err, 4, cudaMemcpyDeviceToHost, s));
+    MG_CUDA(cudaStreamSynchronize(s));
+    if (err) return fail(MG_ERR_CUDA, "grid barrier of the persistent backward kernel timed out");
+    (void)opt;
+    return MG_OK;
 }
 
 }  // namespace mgi
