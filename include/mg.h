@@ -128,8 +128,18 @@ typedef struct mg_graph mg_graph;
  * src<dst edge list for CC) on `device`. */
 mg_status mg_graph_upload(const mg_host_graph *g, int32_t device, mg_graph **out);
 /* Re-copy a host CSR of the same nv/ne into an existing device graph (the
- * allocation is reused; no device allocation happens). */
+ * allocation is reused when the degrees are unchanged; a graph whose row
+ * offsets differ is laid out again).  Equivalent to mg_graph_stage followed
+ * by mg_graph_commit. */
 mg_status mg_graph_reload(mg_graph *dg, const mg_host_graph *g);
+/* Double-buffered input: mg_graph_stage starts copying g (same nv/ne) into
+ * the device graph's staging buffers on the graph's copy stream and returns
+ * at once, so the copy overlaps runs still working on the current graph;
+ * g must stay alive and unchanged until mg_graph_commit.  mg_graph_commit
+ * makes later runs wait for the copy and rebuilds the device CSR from it on
+ * the graph's stream.  No reference counterpart. */
+mg_status mg_graph_stage(mg_graph *dg, const mg_host_graph *g);
+mg_status mg_graph_commit(mg_graph *dg);
 /* Replaces release_MultiGraph (release_structure.cu:4). */
 void mg_graph_free(mg_graph *dg);
 mg_status mg_graph_info(const mg_graph *dg, int32_t *nv, int32_t *ne);

@@ -92,6 +92,8 @@ def _load_lib():
         "mg_gen_lattice": ([i32, i32, C.c_double, u64, P(vp)], i32),
         "mg_graph_upload": ([vp, i32, P(vp)], i32),
         "mg_graph_reload": ([vp, vp], i32),
+        "mg_graph_stage": ([vp, vp], i32),
+        "mg_graph_commit": ([vp], i32),
         "mg_graph_free": ([vp], None),
         "mg_graph_info": ([vp, P(i32), P(i32)], i32),
         "mg_graph_stream": ([vp], vp),
@@ -138,7 +140,8 @@ EXPORTED = [
     "mg_status_string", "mg_last_error", "mg_version", "mg_load_mtx", "mg_host_graph_from_entries",
     "mg_host_graph_from_csr", "mg_host_graph_view", "mg_host_graph_pin", "mg_host_graph_free", "mg_write_mtx",
     "mg_save_csr", "mg_load_csr",
-    "mg_gen_rmat", "mg_gen_lattice", "mg_graph_upload", "mg_graph_reload", "mg_graph_free", "mg_graph_info",
+    "mg_gen_rmat", "mg_gen_lattice", "mg_graph_upload", "mg_graph_reload", "mg_graph_stage", "mg_graph_commit",
+    "mg_graph_free", "mg_graph_info",
     "mg_graph_stream", "mg_graph_set_float_weights", "mg_opts_default", "mg_result_device", "mg_bfs", "mg_sssp",
     "mg_cc", "mg_bc", "mg_bc_multi", "mg_pagerank", "mg_ppr_batch", "mg_wpagerank", "mg_wpagerank_backward",
     "mg_batch_create", "mg_batch_free", "mg_batch_bfs", "mg_batch_cc", "mg_autotune", "mg_pagerank_noalloc",
@@ -304,6 +307,17 @@ class Graph:
 
     def reload(self, host: HostGraph):
         _check(lib.mg_graph_reload(self._h, host._h), "mg_graph_reload")
+
+    def stage(self, host: HostGraph):
+        """Start copying `host` into the staging buffers (overlaps running work);
+        keep `host` alive until commit()."""
+        self._staged = host
+        _check(lib.mg_graph_stage(self._h, host._h), "mg_graph_stage")
+
+    def commit(self):
+        """Rebuild the device CSR from the staged copy (after the runs before it)."""
+        _check(lib.mg_graph_commit(self._h), "mg_graph_commit")
+        self._staged = None
 
     def stream(self) -> int:
         return lib.mg_graph_stream(self._h) or 0

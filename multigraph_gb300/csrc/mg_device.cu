@@ -366,7 +366,7 @@ constexpr int RELABEL_ILP = 4;
 // caller position of this lane's position 32c + lane (-1 past the end)
 __device__ __forceinline__ void caller_positions(int32_t n, int32_t m, const int32_t *new2old, const int32_t *o_row,
                                                  const int32_t *row_new, const int32_t *pos_row, int32_t c0,
-                                                 int32_t (&q)[RELABEL_ILP])
+                                                 int32_t (&q)[RELABEL_ILP], int32_t (&crow)[RELABEL_ILP])
 {
     const int lane = threadIdx.x & 31;
     int32_t ra[RELABEL_ILP], rb[RELABEL_ILP], w[RELABEL_ILP], rr[RELABEL_ILP], st[RELABEL_ILP];
@@ -395,31 +395,74 @@ __device__ __forceinline__ void caller_positions(int32_t n, int32_t m, const int
 #pragma unroll
     for (int j = 0; j < RELABEL_ILP; j++) rr[j] = __ldg(&new2old[rr[j]]);
 #pragma unroll
+    for (int j = 0; j < RELABEL_ILP; j++) crow[j] = rr[j];
+#pragma unroll
     for (int j = 0; j < RELABEL_ILP; j++) {
         const int32_t p = (c0 + j) * 32 + lane;
         q[j] = (c0 + j < nsteps && p < m) ? __ldg(&o_row[rr[j]]) + (p - st[j]) : -1;
     }
 }
 
+// Symmetry checksum of an edge (u -> v, weight w): the hash of the
+// undirected pair (min, max, w), added to sums[0] when u < v and to sums[1]
+// when u > v.  A graph whose every edge has a reverse edge of the same
+// weight gives equal sums; a missing reverse edge or a different weight
+// makes them differ except with probability about 2^-64.
+__device__ __forceinline__ unsigned long long pair_hash(uint32_t a, uint32_t b, uint32_t w)
+{
+    unsigned long long z = ((unsigned long long)a << 32 | b) + 0x9E3779B97F4A7C15ull * (w + 1ull);
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+
+__device__ __forceinline__ void sym_add(unsigned long long &s_lo, unsigned long long &s_hi, int32_t u, int32_t v,
+                                        uint32_t w)
+{
+    if (u < v) s_lo += pair_hash((uint32_t)u, (uint32_t)v, w);
+    else if (u > v) s_hi += pair_hash((uint32_t)v, (uint32_t)u, w);
+}
+
+__device__ __forceinline__ void sym_flush(unsigned long long *sums, unsigned long long s_lo, unsigned long long s_hi)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        s_lo += __shfl_xor_sync(0xffffffffu, s_lo, o);
+        s_hi += __shfl_xor_sync(0xffffffffu, s_hi, o);
+    }
+    if ((threadIdx.x & 31) == 0 && (s_lo | s_hi)) {
+        atomicAdd(&sums[0], s_lo);
+        atomicAdd(&sums[1], s_hi);
+    }
+}
+
 // caller CSR -> engine CSR for up to two 4-byte edge arrays; the first is
-// mapped through old2new when map_ids (column ids)
+// mapped through old2new when map_ids (column ids).  With sums, the
+// symmetry checksum of (caller row, caller column, second array) is formed
+// on the way.
 __global__ void k_relabel_edges(int32_t n, int32_t m, const int32_t *new2old, const int32_t *old2new,
                                 const int32_t *o_row, const int32_t *row_new, const int32_t *pos_row,
                                 const uint32_t *src0, uint32_t *dst0, const uint32_t *src1, uint32_t *dst1,
-                                int map_ids)
+                                int map_ids, unsigned long long *sums)
 {
     const int lane = threadIdx.x & 31;
     const int32_t nsteps = (m + 31) / 32;
     const int32_t gwarp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int32_t nwarps = (gridDim.x * blockDim.x) >> 5;
+    unsigned long long s_lo = 0, s_hi = 0;
     for (int32_t c0 = gwarp * RELABEL_ILP; c0 < nsteps; c0 += nwarps * RELABEL_ILP) {
-        int32_t q[RELABEL_ILP];
-        caller_positions(n, m, new2old, o_row, row_new, pos_row, c0, q);
+        int32_t q[RELABEL_ILP], u[RELABEL_ILP];
+        caller_positions(n, m, new2old, o_row, row_new, pos_row, c0, q, u);
         uint32_t x[RELABEL_ILP], y[RELABEL_ILP];
 #pragma unroll
         for (int j = 0; j < RELABEL_ILP; j++) {
             x[j] = q[j] >= 0 ? __ldg(&src0[q[j]]) : 0u;
             y[j] = (q[j] >= 0 && dst1) ? __ldg(&src1[q[j]]) : 0u;
+        }
+        if (sums) {
+#pragma unroll
+            for (int j = 0; j < RELABEL_ILP; j++)
+                if (q[j] >= 0) sym_add(s_lo, s_hi, u[j], (int32_t)x[j], y[j]);
         }
 #pragma unroll
         for (int j = 0; j < RELABEL_ILP; j++)
@@ -432,6 +475,22 @@ __global__ void k_relabel_edges(int32_t n, int32_t m, const int32_t *new2old, co
             if (dst1) dst1[p] = y[j];
         }
     }
+    if (sums) sym_flush(sums, s_lo, s_hi);
+}
+
+// symmetry checksum of a CSR without relabeling (rows below the hub
+// threshold, so a thread per row)
+__global__ void k_sym_check(int32_t n, const int32_t *row, const int32_t *col, const int32_t *wt,
+                            unsigned long long *sums)
+{
+    unsigned long long s_lo = 0, s_hi = 0;
+    const int32_t stride = gridDim.x * blockDim.x;
+    for (int32_t base = blockIdx.x * blockDim.x + (threadIdx.x & ~31); base < n; base += stride) {
+        const int32_t u = base + (threadIdx.x & 31);
+        if (u < n)
+            for (int32_t p = row[u]; p < row[u + 1]; p++) sym_add(s_lo, s_hi, u, col[p], (uint32_t)wt[p]);
+    }
+    sym_flush(sums, s_lo, s_hi);
 }
 
 // inverse of k_relabel_edges for per-edge payloads (engine order -> caller order)
@@ -443,8 +502,8 @@ __global__ void k_unrelabel_edges(int32_t n, int32_t m, const int32_t *new2old, 
     const int32_t gwarp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int32_t nwarps = (gridDim.x * blockDim.x) >> 5;
     for (int32_t c0 = gwarp * RELABEL_ILP; c0 < nsteps; c0 += nwarps * RELABEL_ILP) {
-        int32_t q[RELABEL_ILP];
-        caller_positions(n, m, new2old, o_row, row_new, pos_row, c0, q);
+        int32_t q[RELABEL_ILP], crow[RELABEL_ILP];
+        caller_positions(n, m, new2old, o_row, row_new, pos_row, c0, q, crow);
 #pragma unroll
         for (int j = 0; j < RELABEL_ILP; j++)
             if (q[j] >= 0) dst[q[j]] = __ldg(&src[(c0 + j) * 32 + lane]);
@@ -493,7 +552,7 @@ __global__ void k_cc_label_old(int32_t n, const int32_t *parent, const int32_t *
         out[v] = minold[parent[old2new[v]]];
 }
 
-static mg_status relabel_device(mg_graph *g)
+static mg_status relabel_device(mg_graph *g, unsigned long long *sym_sums = nullptr)
 {
     if (g->ne == 0) return MG_OK;
     const int grid = g->num_sms * 8;
@@ -503,7 +562,7 @@ static mg_status relabel_device(mg_graph *g)
                                                  g->o_row.as<int32_t>(), g->row.as<int32_t>(),
                                                  g->pos_row.as<int32_t>(), g->o_col.as<uint32_t>(),
                                                  g->col.as<uint32_t>(), g->o_wt.as<uint32_t>(), g->wt.as<uint32_t>(),
-                                                 1);
+                                                 1, sym_sums);
     MG_CUDA(cudaGetLastError());
     return MG_OK;
 }
@@ -568,7 +627,7 @@ mg_status edges_to_engine(mg_graph *g, const void *src_caller, void *dst_engine)
     k_relabel_edges<<<g->num_sms * 8, 256, 0, g->stream>>>(g->nv, g->ne, g->new2old.as<int32_t>(), nullptr,
                                                            g->o_row.as<int32_t>(), g->row.as<int32_t>(),
                                                            g->pos_row.as<int32_t>(), (const uint32_t *)src_caller,
-                                                           (uint32_t *)dst_engine, nullptr, nullptr, 0);
+                                                           (uint32_t *)dst_engine, nullptr, nullptr, 0, nullptr);
     MG_CUDA(cudaGetLastError());
     return MG_OK;
 }
@@ -682,12 +741,19 @@ static void destroy_graph(mg_graph *g)
     DevBuf *bufs[] = {&g->row, &g->col, &g->wt, &g->trow_own, &g->tcol_own, &g->twt_own,
                       &g->hchunk, &g->hrows, &g->hrow_chunk, &g->fw, &g->o_fw, &g->ppr_hchunk, &g->ppr_hrows,
                       &g->ppr_hrow_chunk, &g->o_row, &g->o_col, &g->o_wt, &g->old2new, &g->new2old,
-                      &g->wrows, &g->trows, &g->pos_row};
+                      &g->wrows, &g->trows, &g->pos_row, &g->sym_sums};
     for (DevBuf *b : bufs) dev_free(*b);
     for (DevBuf &b : g->res_out) dev_free(b);
     if (g->pinned_flag) cudaFreeHost(g->pinned_flag);
+    if (g->sym_host) cudaFreeHost(g->sym_host);
     if (g->ev0) cudaEventDestroy(g->ev0);
     if (g->ev1) cudaEventDestroy(g->ev1);
+    if (g->ev_staged) cudaEventDestroy(g->ev_staged);
+    if (g->ev_consumed) cudaEventDestroy(g->ev_consumed);
+    if (g->copy_stream) {
+        cudaStreamSynchronize(g->copy_stream);
+        cudaStreamDestroy(g->copy_stream);
+    }
     if (g->stream) cudaStreamDestroy(g->stream);
     delete g;
 }
@@ -727,47 +793,101 @@ mg_status mg_graph_upload(const mg_host_graph *h, int32_t device, mg_graph **out
     g->ne = h->ne;
     MG_CUDA(cudaDeviceGetAttribute(&g->num_sms, cudaDevAttrMultiProcessorCount, device));
     MG_CUDA(cudaStreamCreateWithFlags(&g->stream, cudaStreamNonBlocking));
+    MG_CUDA(cudaStreamCreateWithFlags(&g->copy_stream, cudaStreamNonBlocking));
     MG_CUDA(cudaEventCreate(&g->ev0));
     MG_CUDA(cudaEventCreate(&g->ev1));
+    MG_CUDA(cudaEventCreateWithFlags(&g->ev_staged, cudaEventDisableTiming));
+    MG_CUDA(cudaEventCreateWithFlags(&g->ev_consumed, cudaEventDisableTiming));
     MG_CUDA(cudaMallocHost(&g->pinned_flag, 64));
+    MG_CUDA(cudaMallocHost(&g->sym_host, 16));
     HostLayout L;
     build_layout(*h, L);
     MG_TRY(upload_arrays(g.get(), h, L, true));
+    g->h_row = h->v;
+    MG_CUDA(cudaEventRecord(g->ev_consumed, g->stream));
     *out = g.release();
+    return MG_OK;
+}
+
+mg_status mg_graph_stage(mg_graph *g, const mg_host_graph *h)
+{
+    clear_error();
+    if (!g || !h) return fail(MG_ERR_INVALID, "null argument");
+    if (h->nv != g->nv || h->ne != g->ne) return fail(MG_ERR_INVALID, "staging needs the same nv/ne");
+    MG_CUDA(cudaSetDevice(g->device));
+    const size_t n = (size_t)h->nv, m = (size_t)h->ne;
+    // caller-order buffers: the relabel source of a relabeled graph, plain
+    // staging buffers otherwise
+    MG_TRY(dev_alloc(g->o_row, (n + 1) * 4));
+    MG_TRY(dev_alloc(g->o_col, std::max<size_t>(m, 4) * 4 + COL_PAD));
+    MG_TRY(dev_alloc(g->o_wt, std::max<size_t>(m, 4) * 4 + COL_PAD));
+    cudaStream_t cs = g->copy_stream;
+    MG_CUDA(cudaStreamWaitEvent(cs, g->ev_consumed, 0));  // the last commit has read them
+    MG_CUDA(cudaMemcpyAsync(g->o_row.p, h->v.data(), (n + 1) * 4, cudaMemcpyHostToDevice, cs));
+    if (m) {
+        MG_CUDA(cudaMemcpyAsync(g->o_col.p, h->e.data(), m * 4, cudaMemcpyHostToDevice, cs));
+        MG_CUDA(cudaMemcpyAsync(g->o_wt.p, h->ev.data(), m * 4, cudaMemcpyHostToDevice, cs));
+    }
+    MG_CUDA(cudaEventRecord(g->ev_staged, cs));
+    g->staged_h = h;
+    return MG_OK;
+}
+
+mg_status mg_graph_commit(mg_graph *g)
+{
+    clear_error();
+    if (!g) return fail(MG_ERR_INVALID, "null argument");
+    if (!g->staged_h) return fail(MG_ERR_INVALID, "nothing staged (mg_graph_stage)");
+    MG_CUDA(cudaSetDevice(g->device));
+    const mg_host_graph *h = g->staged_h;
+    g->staged_h = nullptr;
+    cudaStream_t s = g->stream;
+    MG_CUDA(cudaStreamWaitEvent(s, g->ev_staged, 0));
+    const size_t n = (size_t)h->nv, m = (size_t)h->ne;
+    const bool same_degrees = g->h_row.size() == n + 1 &&
+                              std::memcmp(g->h_row.data(), h->v.data(), (n + 1) * 4) == 0;
+    if (!same_degrees || !(g->symmetric && g->weights_symmetric)) {
+        // new degrees or a transposed copy to rebuild: lay the graph out again
+        HostLayout L;
+        build_layout(*h, L);
+        MG_TRY(upload_arrays(g, h, L, true));
+        g->h_row = h->v;
+    } else {
+        // the layout assumes symmetric edges and weights: check the staged
+        // input with the pair checksum (formed during the relabel pass) and
+        // lay it out again from the host when it is not
+        MG_TRY(dev_alloc(g->sym_sums, 16));
+        unsigned long long *sums = g->sym_sums.as<unsigned long long>();
+        MG_CUDA(cudaMemsetAsync(sums, 0, 16, s));
+        if (g->relabeled) {
+            MG_TRY(relabel_device(g, sums));  // engine CSR from the staged caller-order arrays
+        } else {
+            MG_CUDA(cudaMemcpyAsync(g->row.p, g->o_row.p, (n + 1) * 4, cudaMemcpyDeviceToDevice, s));
+            if (m) {
+                MG_CUDA(cudaMemcpyAsync(g->col.p, g->o_col.p, m * 4, cudaMemcpyDeviceToDevice, s));
+                MG_CUDA(cudaMemcpyAsync(g->wt.p, g->o_wt.p, m * 4, cudaMemcpyDeviceToDevice, s));
+            }
+            k_sym_check<<<g->num_sms * 8, 256, 0, s>>>(g->nv, g->row.as<int32_t>(), g->col.as<int32_t>(),
+                                                       g->wt.as<int32_t>(), sums);
+            MG_CUDA(cudaGetLastError());
+        }
+        MG_CUDA(cudaMemcpyAsync(g->sym_host, sums, 16, cudaMemcpyDeviceToHost, s));
+        MG_CUDA(cudaStreamSynchronize(s));
+        if (g->sym_host[0] != g->sym_host[1]) {
+            HostLayout L;
+            build_layout(*h, L);
+            MG_TRY(upload_arrays(g, h, L, true));
+        }
+    }
+    MG_CUDA(cudaEventRecord(g->ev_consumed, s));
+    g->fw_version += 1;  // quantities derived from the float weights are stale
     return MG_OK;
 }
 
 mg_status mg_graph_reload(mg_graph *g, const mg_host_graph *h)
 {
-    clear_error();
-    if (!g || !h) return fail(MG_ERR_INVALID, "null argument");
-    if (h->nv != g->nv || h->ne != g->ne) return fail(MG_ERR_INVALID, "reload needs the same nv/ne");
-    MG_CUDA(cudaSetDevice(g->device));
-    // Same degrees: the order, the index tables and the row offsets stay;
-    // the edge arrays are re-copied (and relabeled on the device).
-    const size_t n = (size_t)h->nv, m = (size_t)h->ne;
-    cudaStream_t s = g->stream;
-    if (g->relabeled) {
-        MG_CUDA(cudaMemcpyAsync(g->o_row.p, h->v.data(), (n + 1) * 4, cudaMemcpyHostToDevice, s));
-        if (m) {
-            MG_CUDA(cudaMemcpyAsync(g->o_col.p, h->e.data(), m * 4, cudaMemcpyHostToDevice, s));
-            MG_CUDA(cudaMemcpyAsync(g->o_wt.p, h->ev.data(), m * 4, cudaMemcpyHostToDevice, s));
-        }
-        MG_TRY(relabel_device(g));
-    } else {
-        MG_CUDA(cudaMemcpyAsync(g->row.p, h->v.data(), (n + 1) * 4, cudaMemcpyHostToDevice, s));
-        if (m) {
-            MG_CUDA(cudaMemcpyAsync(g->col.p, h->e.data(), m * 4, cudaMemcpyHostToDevice, s));
-            MG_CUDA(cudaMemcpyAsync(g->wt.p, h->ev.data(), m * 4, cudaMemcpyHostToDevice, s));
-        }
-    }
-    if (!(g->symmetric && g->weights_symmetric)) {
-        HostLayout L;
-        build_layout(*h, L);
-        MG_TRY(upload_arrays(g, h, L, false));
-    }
-    g->fw_version += 1;  // quantities derived from the float weights are stale
-    return MG_OK;
+    MG_TRY(mg_graph_stage(g, h));
+    return mg_graph_commit(g);
 }
 
 void mg_graph_free(mg_graph *g) { destroy_graph(g); }

@@ -99,6 +99,13 @@ struct mg_graph {
     int num_sms = 0;
     cudaStream_t stream = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    // double-buffered input (mg_graph_stage / mg_graph_commit)
+    cudaStream_t copy_stream = nullptr;
+    cudaEvent_t ev_staged = nullptr, ev_consumed = nullptr;
+    const mg_host_graph *staged_h = nullptr;
+    std::vector<int32_t> h_row;    // caller-order row offsets the layout was built from
+    mgi::DevBuf sym_sums;          // pair checksum of a committed input (2 x uint64)
+    unsigned long long *sym_host = nullptr;  // pinned readback of sym_sums
     int32_t nv = 0, ne = 0;
     bool symmetric = true;         // transpose == graph (pull uses the same arrays)
     bool weights_symmetric = true; // weight of (u,v) == weight of (v,u)

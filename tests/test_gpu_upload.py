@@ -1,0 +1,93 @@
+"""Re-uploading graphs on the GPU: mg_graph_reload with new weights, with a
+new structure of the same size, and the double-buffered mg_graph_stage /
+mg_graph_commit pair (runs before the commit still see the old graph)."""
+import numpy as np
+import pytest
+
+import multigraph_gb300 as mg
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+
+def _csr(rp, col, wt):
+    return mg.HostGraph.from_csr(rp, col, wt), O.csr_from_arrays(rp, col, wt)
+
+
+def _permuted(rp, col, wt, seed):
+    """Same n and m, vertices renamed (so the row degrees move)."""
+    n = len(rp) - 1
+    perm = np.random.default_rng(seed).permutation(n).astype(np.int32)
+    src = np.repeat(np.arange(n, dtype=np.int32), np.diff(rp))
+    s2, d2 = perm[src], perm[col]
+    order = np.lexsort((d2, s2))
+    rp2 = np.zeros(n + 1, np.int32)
+    rp2[1:] = np.cumsum(np.bincount(s2, minlength=n))
+    return rp2, d2[order].astype(np.int32), wt[order].astype(np.int32)
+
+
+def _check_all(g, og, src):
+    lv, _ = g.bfs(src)
+    assert np.array_equal(lv, O.bfs(og, src))
+    dist, _ = g.sssp(src)
+    assert np.array_equal(dist, O.sssp(og, src)[0])
+    lab, _ = g.cc()
+    assert np.array_equal(lab, O.cc_minlabel(og))
+    x, info = g.pagerank(mg.PR_TOPOLOGY, tol=1e-6)
+    ref, _ = O.pr_norm_f64(og, 0.85, 1e-6, info.iterations)
+    assert float(np.max(np.abs(x.astype(np.float64) - ref))) < 1e-6
+
+
+@pytest.mark.parametrize("kind", ["rmat", "lattice"])   # relabeled / not relabeled
+def test_reload_new_weights_and_new_structure(kind):
+    h0 = mg.HostGraph.rmat(11, 16, seed=31) if kind == "rmat" else mg.HostGraph.lattice(40, 33, 0.05, seed=4)
+    rp, col, wt = h0.arrays()
+    g = mg.Graph(h0)
+    _check_all(g, O.csr_from_arrays(rp, col, wt), 0)
+    # same structure, new weights
+    wt2 = (np.random.default_rng(1).integers(1, 64, len(wt))).astype(np.int32)
+    h1, og1 = _csr(rp, col, wt2)
+    g.reload(h1)
+    _check_all(g, og1, 0)
+    # same n and m, different degrees: laid out again
+    h2, og2 = _csr(*_permuted(rp, col, wt2, 2))
+    g.reload(h2)
+    _check_all(g, og2, 3)
+    g.free()
+
+
+def test_stage_overlaps_and_commit_switches():
+    h0 = mg.HostGraph.rmat(12, 16, seed=32)
+    rp, col, wt = h0.arrays()
+    og0 = O.csr_from_arrays(rp, col, wt)
+    wt2 = (np.random.default_rng(5).integers(1, 64, len(wt))).astype(np.int32)
+    h1, og1 = _csr(rp, col, wt2)
+    h1.pin()
+    g = mg.Graph(h0)
+    g.stage(h1)
+    d_old, _ = g.sssp(0)                        # still the uploaded graph
+    assert np.array_equal(d_old, O.sssp(og0, 0)[0])
+    g.commit()
+    d_new, _ = g.sssp(0)
+    assert np.array_equal(d_new, O.sssp(og1, 0)[0])
+    # a pipeline of alternating inputs
+    for k in range(4):
+        nxt = h0 if k % 2 == 0 else h1
+        g.stage(nxt)
+        g.commit()
+        d, _ = g.sssp(0)
+        assert np.array_equal(d, O.sssp(og0 if k % 2 == 0 else og1, 0)[0]), k
+    g.free()
+
+
+def test_stage_commit_errors():
+    h0 = mg.HostGraph.rmat(8, 8, seed=3)
+    g = mg.Graph(h0)
+    with pytest.raises(mg.MGError) as e:
+        g.commit()
+    assert e.value.status == mg.MG_ERR_INVALID
+    other = mg.HostGraph.rmat(9, 8, seed=3)
+    with pytest.raises(mg.MGError) as e:
+        g.stage(other)
+    assert e.value.status == mg.MG_ERR_INVALID
+    g.free()
