@@ -80,16 +80,27 @@ __global__ void k_cc_init(int32_t n, const int32_t *row, const int32_t *col, int
 // link every vertex to its r-th neighbour
 __global__ void k_cc_sample(int32_t n, const int32_t *row, const int32_t *col, int32_t r, int32_t *parent);
 
-// the most frequent root among MODE_SAMPLES vertices (ties: smallest id);
-// one block of MODE_SAMPLES threads
-__global__ void __launch_bounds__(MODE_SAMPLES) k_cc_mode(int32_t n, const int32_t *parent, int32_t *giant)
+// The most frequent root among MODE_SAMPLES vertices of one graph of a
+// batch (block b samples caller ids [voff[b], voff[b+1]), the whole id range
+// without voff; ties: smallest id) is marked in the giant-root bitmap.
+// Graphs of a batch share no edges, so skipping the rows of every marked
+// component stays exact: an edge leaving a marked component is hooked from
+// its unmarked end.  One block of MODE_SAMPLES threads per graph.
+__global__ void __launch_bounds__(MODE_SAMPLES) k_cc_mode(int32_t n, const int32_t *voff, const int32_t *old2new,
+                                                          const int32_t *parent, uint32_t *giant_bm)
 {
     __shared__ int32_t s_val[MODE_SAMPLES];
     __shared__ int32_t s_best[MODE_SAMPLES / 32], s_cnt[MODE_SAMPLES / 32];
     const int t = threadIdx.x;
-    // spread the samples over the id range (hub-first ids put hubs first)
-    const int32_t v = (int32_t)(((int64_t)t * n) / MODE_SAMPLES + (((int64_t)t * 7919) % max(n / MODE_SAMPLES, 1)));
-    s_val[t] = parent[min(max(v, 0), n - 1)];
+    const int32_t lo = voff ? voff[blockIdx.x] : 0, hi = voff ? voff[blockIdx.x + 1] : n;
+    const int32_t span = hi - lo;
+    if (span <= 0) return;  // block-uniform
+    // spread the samples over the id range
+    int32_t v = lo + (int32_t)(((int64_t)t * span) / MODE_SAMPLES +
+                               (((int64_t)t * 7919) % max(span / MODE_SAMPLES, 1)));
+    v = min(max(v, lo), hi - 1);
+    if (old2new) v = old2new[v];
+    s_val[t] = parent[v];
     __syncthreads();
     const int32_t mine = s_val[t];
     int cnt = 0;
@@ -108,7 +119,7 @@ __global__ void __launch_bounds__(MODE_SAMPLES) k_cc_mode(int32_t n, const int32
     if (t == 0) {
         for (int w = 1; w < MODE_SAMPLES / 32; w++)
             if (s_cnt[w] > bc || (s_cnt[w] == bc && s_best[w] < bv)) { bv = s_best[w]; bc = s_cnt[w]; }
-        *giant = bv;
+        mgd::bm_set(giant_bm, bv);
     }
 }
 
@@ -124,21 +135,21 @@ __global__ void k_cc_sample(int32_t n, const int32_t *row, const int32_t *col, i
 }
 
 // per-edge union over the degree-binned rows (bins_reduce interface;
-// the reduction value is unused).  giant >= 0: rows whose vertex points at
-// the giant root are skipped and the others hook every entry; giant < 0:
-// every row, each undirected edge once when symmetric.
+// the reduction value is unused).  With giant_bm: rows whose vertex points
+// at a marked giant root are skipped and the others hook every entry;
+// without: every row, each undirected edge once when symmetric.
 struct HookOp {
     using T = int;
     static constexpr bool kRowAware = true;  // the union needs the row (source vertex)
     static constexpr bool kWeights = false;
     int32_t *parent;
     int symmetric;
-    int32_t giant;
+    const uint32_t *giant_bm;
     __device__ int identity() const { return 0; }
-    __device__ bool skip(int32_t v) const { return giant >= 0 && parent[v] == giant; }
+    __device__ bool skip(int32_t v) const { return giant_bm && mgd::bm_test(giant_bm, parent[v]); }
     __device__ int edge(int32_t, int32_t src, int32_t dst, int32_t) const
     {
-        if (src != dst && (giant >= 0 || !symmetric || dst < src)) cc_union(parent, src, dst);
+        if (src != dst && (giant_bm || !symmetric || dst < src)) cc_union(parent, src, dst);
         return 0;
     }
     __device__ int combine(int, int) const { return 0; }
@@ -151,10 +162,9 @@ struct HookOp {
 __global__ void __launch_bounds__(THREADS) k_cc_hook(int32_t n, const int32_t *prow, const int32_t *pcol,
                                                      const int32_t *wrows, int32_t nwrows, const int32_t *trows,
                                                      int32_t ntrows, const int32_t *hchunk, int32_t nhchunks,
-                                                     int symmetric, const int32_t *giant_p, int32_t *parent)
+                                                     int symmetric, const uint32_t *giant_bm, int32_t *parent)
 {
-    const int32_t giant = giant_p ? *giant_p : -1;
-    HookOp op{parent, symmetric, giant};
+    HookOp op{parent, symmetric, giant_bm};
     mgd::bins_reduce(op, prow, pcol, nullptr, wrows, nwrows, trows, ntrows);
     __shared__ int s_skip;
     for (int32_t ch = blockIdx.x; ch < nhchunks; ch += gridDim.x) {
@@ -181,7 +191,7 @@ __global__ void k_cc_compress(int32_t n, int32_t *parent)
 }  // namespace
 
 struct CcWS {
-    mgi::DevBuf parent, giant;
+    mgi::DevBuf parent, giant, voff;
 };
 
 namespace mgi {
@@ -191,18 +201,30 @@ void free_cc_ws(mg_graph *g)
     if (!g->cws) return;
     dev_free(g->cws->parent);
     dev_free(g->cws->giant);
+    dev_free(g->cws->voff);
     delete g->cws;
     g->cws = nullptr;
 }
 
-mg_status cc_run(mg_graph *g, mg_run_info *info)
+// CC of the graph, or of a batch arena whose graphs occupy the caller-id
+// ranges voff[0..ngraphs] (one giant component per graph)
+mg_status cc_run(mg_graph *g, mg_run_info *info, const std::vector<int32_t> *voff = nullptr)
 {
     if (!g->cws) g->cws = new CcWS();
+    const size_t words = ((size_t)std::max(g->nv, 1) + 31) / 32;
     MG_TRY(dev_alloc(g->cws->parent, (size_t)std::max(g->nv, 1) * 4));
-    MG_TRY(dev_alloc(g->cws->giant, 4));
+    MG_TRY(dev_alloc(g->cws->giant, words * 4));
     int32_t *parent = g->cws->parent.as<int32_t>();
-    int32_t *giant = g->cws->giant.as<int32_t>();
+    uint32_t *giant = g->cws->giant.as<uint32_t>();
     cudaStream_t s = g->stream;
+    int ngraphs = 1;
+    const int32_t *voff_dev = nullptr;
+    if (voff && voff->size() > 2) {
+        ngraphs = (int)voff->size() - 1;
+        MG_TRY(dev_alloc(g->cws->voff, voff->size() * 4));
+        MG_CUDA(cudaMemcpyAsync(g->cws->voff.p, voff->data(), voff->size() * 4, cudaMemcpyHostToDevice, s));
+        voff_dev = g->cws->voff.as<int32_t>();
+    }
     if (g->nv == 0) return MG_OK;
     const int grid = launch_grid(g, THREADS, 8);
     Profiler &P = g->prof;
@@ -221,8 +243,10 @@ mg_status cc_run(mg_graph *g, mg_run_info *info)
         P.begin(sc);
         k_cc_compress<<<grid, THREADS, 0, s>>>(g->nv, parent);
         P.end();
+        MG_CUDA(cudaMemsetAsync(giant, 0, words * 4, s));
         P.begin(sm);
-        k_cc_mode<<<1, MODE_SAMPLES, 0, s>>>(g->nv, parent, giant);
+        k_cc_mode<<<ngraphs, MODE_SAMPLES, 0, s>>>(g->nv, voff_dev, g->relabeled ? g->old2new.as<int32_t>() : nullptr,
+                                                    parent, giant);
         P.end();
     }
     P.begin(sh);
@@ -339,7 +363,7 @@ mg_status mg_batch_cc(mg_batch *b, const mg_opts *o, int32_t *labels_out, mg_run
     mg_graph *g = b->dg;
     mg_opts opt;
     MG_TRY(begin_run(g, o, opt, info));
-    MG_TRY(cc_run(g, info));
+    MG_TRY(cc_run(g, info, &b->voff));
     MG_TRY(cc_to_caller(g, g->cws->parent.as<int32_t>(), &g->res[MG_RES_LABEL]));
     MG_TRY(end_run(g, opt, info));
     if (!labels_out) return MG_OK;
