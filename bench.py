@@ -308,6 +308,9 @@ def main():
     n, m = g.nv, g.ne
     stream = torch.cuda.ExternalStream(g.stream(), device=torch.device("cuda", local))
     opts = mg.default_opts(tol=TOL, damping=DAMPING, exec=mg.EXEC_HOST if args.exec == "host" else mg.EXEC_GRAPH)
+    # the autotuner picks the pull layout's heavy-row threshold and chunk
+    # size (it re-bins this graph; outside the timed region)
+    g.autotune(mg.ALGO_PR, 0)
 
     def step(out=False):
         _, si = g.sssp(0, opts, out=out)

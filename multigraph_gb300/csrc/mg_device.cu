@@ -230,6 +230,8 @@ struct HostLayout {
     bool symmetric = true, wsym = true;
     std::vector<int32_t> hchunk, hrows, hrow_chunk;
     std::vector<int32_t> wrows, trows;  // degree bins (engine ids)
+    std::vector<int32_t> prow;          // pull-side row offsets (engine order)
+    int32_t heavy = 0, chunk = 0;
     int32_t n_dangling = 0, min_weight = 0;
     // hub-first relabeling (engine id = rank by descending log2 out-degree)
     bool relabel = false;
@@ -263,7 +265,37 @@ static void hub_first_order(const mg_host_graph &h, std::vector<int32_t> &new2ol
     }
 }
 
-static void build_layout(const mg_host_graph &h, HostLayout &L)
+// Degree bins and heavy chunks of the pull rows (row offsets prow, engine
+// order): rows above `heavy` in-edges are cut into `chunk`-edge pieces,
+// rows of 33..heavy go to the warp bin, the rest to the thread bin.
+static void build_bins(const std::vector<int32_t> &prow, int32_t n, int32_t heavy, int32_t chunk, HostLayout &L)
+{
+    L.hchunk.clear();
+    L.hrows.clear();
+    L.hrow_chunk.assign(1, 0);
+    L.wrows.clear();
+    L.trows.clear();
+    for (int32_t v = 0; v < n; v++) {
+        int32_t d = prow[v + 1] - prow[v];
+        if (d > heavy) {
+            L.hrows.push_back(v);
+            for (int32_t b = prow[v]; b < prow[v + 1]; b += chunk) {
+                L.hchunk.push_back(v);
+                L.hchunk.push_back(b);
+                L.hchunk.push_back(std::min(prow[v + 1], b + chunk));
+            }
+            L.hrow_chunk.push_back((int32_t)(L.hchunk.size() / 3));
+        } else if (d > 32) {
+            L.wrows.push_back(v);
+        } else {
+            L.trows.push_back(v);
+        }
+    }
+    L.heavy = heavy;
+    L.chunk = chunk;
+}
+
+static void build_layout(const mg_host_graph &h, HostLayout &L, int32_t heavy = HEAVY_DEG, int32_t chunk = HCHUNK)
 {
     const int32_t n = h.nv, m = h.ne;
     bool skewed = false;
@@ -308,27 +340,8 @@ static void build_layout(const mg_host_graph &h, HostLayout &L)
     L.n_dangling = 0;
     for (int32_t v = 0; v < n; v++) L.n_dangling += (h.v[v + 1] == h.v[v]);
     L.min_weight = m ? *std::min_element(h.ev.begin(), h.ev.end()) : 0;
-    // heavy rows and chunks
-    L.hrow_chunk.push_back(0);
-    for (int32_t v = 0; v < n; v++) {
-        int32_t d = prow[v + 1] - prow[v];
-        if (d > HEAVY_DEG) {
-            L.hrows.push_back(v);
-            for (int32_t b = prow[v]; b < prow[v + 1]; b += HCHUNK) {
-                L.hchunk.push_back(v);
-                L.hchunk.push_back(b);
-                L.hchunk.push_back(std::min(prow[v + 1], b + HCHUNK));
-            }
-            L.hrow_chunk.push_back((int32_t)(L.hchunk.size() / 3));
-        }
-    }
-    // degree bins for the row-reduction kernels
-    for (int32_t v = 0; v < n; v++) {
-        int32_t d = prow[v + 1] - prow[v];
-        if (d > HEAVY_DEG) continue;
-        if (d > 32) L.wrows.push_back(v);
-        else L.trows.push_back(v);
-    }
+    L.prow = prow;
+    build_bins(prow, n, heavy, chunk, L);
 }
 
 // Engine row i of the relabeled CSR is caller row new2old[i] with the same
@@ -567,7 +580,25 @@ static mg_status relabel_device(mg_graph *g, unsigned long long *sym_sums = null
     return MG_OK;
 }
 
+static mg_status upload_bins(mg_graph *g, const HostLayout &L);
+
 namespace mgi {
+
+mg_status rebin(mg_graph *g, int32_t heavy, int32_t chunk)
+{
+    if (heavy < 32 || chunk < 256 || chunk % 256 != 0) return fail(MG_ERR_INVALID, "bad bin parameters %d/%d", heavy, chunk);
+    if (heavy == g->heavy_deg && chunk == g->hchunk_size) return MG_OK;
+    MG_CUDA(cudaStreamSynchronize(g->stream));
+    HostLayout L;
+    build_bins(g->h_prow, g->nv, heavy, chunk, L);
+    MG_TRY(upload_bins(g, L));
+    // captured loops and per-chunk buffers follow the old bins
+    free_frontier_ws(g);
+    free_pr_ws(g);
+    free_cc_ws(g);
+    free_bc_ws(g);
+    return MG_OK;
+}
 
 int32_t to_engine(const mg_graph *g, int32_t v) { return g->relabeled ? g->h_old2new[v] : v; }
 
@@ -649,6 +680,34 @@ mg_status edges_to_caller(mg_graph *g, const void *src_engine, void *dst_caller)
 
 }  // namespace mgi
 
+// degree bins and heavy chunks to the device (buffers grow when needed)
+static mg_status upload_bins(mg_graph *g, const HostLayout &L)
+{
+    cudaStream_t s = g->stream;
+    MG_TRY(dev_alloc(g->hchunk, std::max<size_t>(L.hchunk.size(), 3) * 4));
+    MG_TRY(dev_alloc(g->hrows, std::max<size_t>(L.hrows.size(), 1) * 4));
+    MG_TRY(dev_alloc(g->hrow_chunk, L.hrow_chunk.size() * 4));
+    MG_TRY(dev_alloc(g->wrows, std::max<size_t>(L.wrows.size(), 1) * 4));
+    MG_TRY(dev_alloc(g->trows, std::max<size_t>(L.trows.size(), 1) * 4));
+    if (!L.hchunk.empty())
+        MG_CUDA(cudaMemcpyAsync(g->hchunk.p, L.hchunk.data(), L.hchunk.size() * 4, cudaMemcpyHostToDevice, s));
+    if (!L.hrows.empty())
+        MG_CUDA(cudaMemcpyAsync(g->hrows.p, L.hrows.data(), L.hrows.size() * 4, cudaMemcpyHostToDevice, s));
+    MG_CUDA(cudaMemcpyAsync(g->hrow_chunk.p, L.hrow_chunk.data(), L.hrow_chunk.size() * 4, cudaMemcpyHostToDevice, s));
+    if (!L.wrows.empty())
+        MG_CUDA(cudaMemcpyAsync(g->wrows.p, L.wrows.data(), L.wrows.size() * 4, cudaMemcpyHostToDevice, s));
+    if (!L.trows.empty())
+        MG_CUDA(cudaMemcpyAsync(g->trows.p, L.trows.data(), L.trows.size() * 4, cudaMemcpyHostToDevice, s));
+    MG_CUDA(cudaStreamSynchronize(s));
+    g->nwrows = (int32_t)L.wrows.size();
+    g->ntrows = (int32_t)L.trows.size();
+    g->nhchunks = (int32_t)(L.hchunk.size() / 3);
+    g->nhrows = (int32_t)L.hrows.size();
+    g->heavy_deg = L.heavy;
+    g->hchunk_size = L.chunk;
+    return MG_OK;
+}
+
 static mg_status upload_arrays(mg_graph *g, const mg_host_graph *h, const HostLayout &L, bool alloc)
 {
     const size_t n = (size_t)h->nv, m = (size_t)h->ne;
@@ -668,11 +727,6 @@ static mg_status upload_arrays(mg_graph *g, const mg_host_graph *h, const HostLa
             MG_TRY(dev_alloc(g->tcol_own, std::max<size_t>(m, 4) * 4 + COL_PAD));
             MG_TRY(dev_alloc(g->twt_own, std::max<size_t>(m, 4) * 4 + COL_PAD));
         }
-        MG_TRY(dev_alloc(g->hchunk, std::max<size_t>(L.hchunk.size(), 3) * 4));
-        MG_TRY(dev_alloc(g->hrows, std::max<size_t>(L.hrows.size(), 1) * 4));
-        MG_TRY(dev_alloc(g->hrow_chunk, L.hrow_chunk.size() * 4));
-        MG_TRY(dev_alloc(g->wrows, std::max<size_t>(L.wrows.size(), 1) * 4));
-        MG_TRY(dev_alloc(g->trows, std::max<size_t>(L.trows.size(), 1) * 4));
     }
     cudaStream_t s = g->stream;
     g->relabeled = L.relabel;
@@ -705,21 +759,8 @@ static mg_status upload_arrays(mg_graph *g, const mg_host_graph *h, const HostLa
     } else {
         g->trow = g->row.as<int32_t>(); g->tcol = g->col.as<int32_t>(); g->twt = g->wt.as<int32_t>();
     }
-    if (!L.hchunk.empty())
-        MG_CUDA(cudaMemcpyAsync(g->hchunk.p, L.hchunk.data(), L.hchunk.size() * 4, cudaMemcpyHostToDevice, s));
-    if (!L.hrows.empty())
-        MG_CUDA(cudaMemcpyAsync(g->hrows.p, L.hrows.data(), L.hrows.size() * 4, cudaMemcpyHostToDevice, s));
-    MG_CUDA(cudaMemcpyAsync(g->hrow_chunk.p, L.hrow_chunk.data(), L.hrow_chunk.size() * 4, cudaMemcpyHostToDevice, s));
-    if (!L.wrows.empty())
-        MG_CUDA(cudaMemcpyAsync(g->wrows.p, L.wrows.data(), L.wrows.size() * 4, cudaMemcpyHostToDevice, s));
-    if (!L.trows.empty())
-        MG_CUDA(cudaMemcpyAsync(g->trows.p, L.trows.data(), L.trows.size() * 4, cudaMemcpyHostToDevice, s));
-    g->nwrows = (int32_t)L.wrows.size();
-    g->ntrows = (int32_t)L.trows.size();
-    MG_CUDA(cudaStreamSynchronize(s));
-    g->nhchunks = (int32_t)(L.hchunk.size() / 3);
-    g->nhrows = (int32_t)L.hrows.size();
-    g->heavy_deg = HEAVY_DEG;
+    MG_TRY(upload_bins(g, L));
+    g->h_prow = L.prow;
     g->symmetric = L.symmetric;
     g->weights_symmetric = L.wsym;
     g->n_dangling = L.n_dangling;
@@ -847,9 +888,10 @@ mg_status mg_graph_commit(mg_graph *g)
     const bool same_degrees = g->h_row.size() == n + 1 &&
                               std::memcmp(g->h_row.data(), h->v.data(), (n + 1) * 4) == 0;
     if (!same_degrees || !(g->symmetric && g->weights_symmetric)) {
-        // new degrees or a transposed copy to rebuild: lay the graph out again
+        // new degrees or a transposed copy to rebuild: lay the graph out
+        // again (with the graph's current, possibly tuned, bin parameters)
         HostLayout L;
-        build_layout(*h, L);
+        build_layout(*h, L, g->heavy_deg, g->hchunk_size);
         MG_TRY(upload_arrays(g, h, L, true));
         g->h_row = h->v;
     } else {
@@ -875,7 +917,7 @@ mg_status mg_graph_commit(mg_graph *g)
         MG_CUDA(cudaStreamSynchronize(s));
         if (g->sym_host[0] != g->sym_host[1]) {
             HostLayout L;
-            build_layout(*h, L);
+            build_layout(*h, L, g->heavy_deg, g->hchunk_size);
             MG_TRY(upload_arrays(g, h, L, true));
         }
     }

@@ -223,22 +223,25 @@ __global__ void __launch_bounds__(THREADS) k_pr_light(PArgs a)
     (void)nwarps;
     const int32_t *pwt = reinterpret_cast<const int32_t *>(a.pw);
     mgd::bins_reduce(op, a.prow, a.pcol, pwt, a.wrows, a.nwrows, a.trows, a.ntrows);
-    // heavy-row chunks of HCHUNK = 8 * THREADS edges, one per CTA: each
-    // thread issues its 8 column loads, then its 8 gathers
+    // heavy-row chunks, one per CTA, in batches of 8 * THREADS edges: each
+    // thread issues its 8 column loads, then its 8 gathers (one batch for
+    // the default 2048-edge chunks)
     __shared__ float s_part[THREADS / 32];
     for (int32_t ch = blockIdx.x; ch < a.nhchunks; ch += gridDim.x) {
         int32_t v = a.hchunk[3 * ch], b = a.hchunk[3 * ch + 1], e = a.hchunk[3 * ch + 2];
         float acc = 0.0f;
         if (!pr_row_skipped<V>(a, v)) {
-            int32_t u[8];
+            for (int32_t b0 = b; b0 < e; b0 += 8 * THREADS) {
+                int32_t u[8];
 #pragma unroll
-            for (int j = 0; j < 8; j++) {
-                int32_t p = b + threadIdx.x + j * THREADS;
-                u[j] = p < e ? __ldg(&a.pcol[p]) : -1;
+                for (int j = 0; j < 8; j++) {
+                    int32_t p = b0 + threadIdx.x + j * THREADS;
+                    u[j] = p < e ? __ldg(&a.pcol[p]) : -1;
+                }
+#pragma unroll
+                for (int j = 0; j < 8; j++)
+                    if (u[j] >= 0) acc += pr_gather<V>(a, c.cur, b0 + threadIdx.x + j * THREADS, u[j]);
             }
-#pragma unroll
-            for (int j = 0; j < 8; j++)
-                if (u[j] >= 0) acc += pr_gather<V>(a, c.cur, b + threadIdx.x + j * THREADS, u[j]);
         }
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);

@@ -1,14 +1,19 @@
-// mg_tune.cu -- autotuner for the sparse/dense (push/pull) switch.
+// mg_tune.cu -- autotuner for the sparse/dense (push/pull) switch and the
+// pull layout's chunk sizes.
 //
 // The reference decides between its sparse and dense paths with a runtime
 // sampler that times a pseudo iteration of each (process.cu:1115-1246,
 // pseudo_phase1/11/2 and pseudo_process_f1 with real side effects) and with
-// compile-time constants (common.h:10-52: DENSE_THRESHOLD, sampling factors).
-// Here the switch rule is fixed (Beamer's frontier-edges vs unvisited-edges
-// test for BFS/BC, frontier-edges vs m for SSSP) and its two thresholds are
-// tuned per graph: every candidate runs the real traversal in a CUDA graph,
-// the median of three timed runs decides, and the winner is cached in a text
-// file keyed by a graph signature (n, m and a log2 degree histogram).
+// compile-time constants (common.h:10-52: DENSE_THRESHOLD, sampling factors,
+// partition sizes).  Here the switch rule is fixed (Beamer's frontier-edges
+// vs unvisited-edges test for BFS/BC, frontier-edges vs m for SSSP) and its
+// two thresholds are tuned per graph; for PageRank the tuner picks the
+// heavy-row threshold and the chunk size of the pull layout (re-binned on
+// the device graph).  Every candidate runs the real algorithm in a CUDA
+// graph, the median of three timed runs decides, and the winner is cached
+// in a text file keyed by a graph signature (n, m and a log2 degree
+// histogram).  Cache lines: signature, algorithm, then alpha / beta /
+// direction, or heavy threshold / chunk edges / 0 for PageRank.
 
 #include "mg_device.cuh"
 
@@ -69,18 +74,53 @@ void cache_store(const char *path, uint64_t sig, int algo, const mg_opts &o, dou
     std::fclose(f);
 }
 
+// PageRank: heavy-row threshold x chunk size of the pull layout
+mg_status tune_pr_layout(mg_graph *g, const char *cache_path, uint64_t sig, const mg_opts &base)
+{
+    mg_opts cached = base;
+    if (cache_lookup(cache_path, sig, MG_ALGO_PR, &cached)) return mgi::rebin(g, cached.alpha, cached.beta);
+    struct Cand { int heavy, chunk; };
+    const Cand cands[] = {{256, 1024}, {256, 2048}, {512, 1024}, {512, 2048}, {512, 4096}, {1024, 2048},
+                          {1024, 4096}, {1024, 8192}, {2048, 4096}, {2048, 8192}};
+    double best_ms = 1e30;
+    Cand best = {512, 2048};
+    for (const Cand &c : cands) {
+        MG_TRY(mgi::rebin(g, c.heavy, c.chunk));
+        mg_opts o = base;
+        o.exec = MG_EXEC_GRAPH;
+        o.profile = 0;
+        std::vector<double> t;
+        for (int rep = 0; rep < 4; rep++) {
+            mg_run_info info;
+            MG_TRY(mg_pagerank(g, MG_PR_TOPOLOGY, &o, nullptr, &info));
+            if (rep > 0) t.push_back(info.device_ms);  // first run warms the graph
+        }
+        std::sort(t.begin(), t.end());
+        const double med = t[t.size() / 2];
+        if (med < best_ms) { best_ms = med; best = c; }
+    }
+    MG_TRY(mgi::rebin(g, best.heavy, best.chunk));
+    mg_opts rec = base;
+    rec.alpha = best.heavy;
+    rec.beta = best.chunk;
+    rec.direction = 0;
+    cache_store(cache_path, sig, MG_ALGO_PR, rec, best_ms);
+    return MG_OK;
+}
+
 }  // namespace
 
 extern "C" mg_status mg_autotune(mg_graph *g, int32_t algo, int32_t source, const char *cache_path, mg_opts *tuned)
 {
     mgi::clear_error();
     if (!g || !tuned) return mgi::fail(MG_ERR_INVALID, "null argument");
-    if (algo != MG_ALGO_BFS && algo != MG_ALGO_SSSP && algo != MG_ALGO_BC)
+    if (algo != MG_ALGO_BFS && algo != MG_ALGO_SSSP && algo != MG_ALGO_BC && algo != MG_ALGO_PR)
         return mgi::fail(MG_ERR_UNSUPPORTED, "nothing to tune for algorithm %d", algo);
-    if (source < 0 || source >= g->nv) return mgi::fail(MG_ERR_RANGE, "source out of range");
+    if (algo != MG_ALGO_PR && (source < 0 || source >= g->nv)) return mgi::fail(MG_ERR_RANGE, "source out of range");
     MG_CUDA(cudaSetDevice(g->device));
     mg_opts base = *tuned;
     uint64_t sig = graph_signature(g);
+    if (algo == MG_ALGO_PR) return tune_pr_layout(g, cache_path, sig, base);
     if (cache_lookup(cache_path, sig, algo, tuned)) return MG_OK;
 
     struct Cand { int alpha, beta, dir; };

@@ -1,0 +1,64 @@
+"""The autotuner (the reference's sampling heuristic, process.cu:1115-1246,
+and its compile-time thresholds, common.h:10-52): tuned switch thresholds
+and a tuned PageRank pull layout keep every result equal to the oracle, and
+the cache file is reused."""
+import os
+import tempfile
+
+import numpy as np
+import pytest
+
+import multigraph_gb300 as mg
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+
+def _pair(h):
+    rp, col, wt = h.arrays()
+    return mg.Graph(h), O.csr_from_arrays(rp, col, wt)
+
+
+def test_switch_thresholds_and_cache():
+    g, og = _pair(mg.HostGraph.rmat(11, 16, seed=41))
+    cache = os.path.join(tempfile.mkdtemp(), "tune.txt")
+    for algo in (mg.ALGO_BFS, mg.ALGO_SSSP, mg.ALGO_BC):
+        o = g.autotune(algo, 0, cache)
+        assert o.alpha > 0 and o.beta > 0
+        again = g.autotune(algo, 0, cache)             # from the cache file
+        assert (again.alpha, again.beta, again.direction) == (o.alpha, o.beta, o.direction)
+        lv, _ = g.bfs(0, o)
+        assert np.array_equal(lv, O.bfs(og, 0))
+        d, _ = g.sssp(0, o)
+        assert np.array_equal(d, O.sssp(og, 0)[0])
+    assert len(open(cache).read().splitlines()) == 3
+    g.free()
+
+
+def test_pagerank_layout_tuning_keeps_results():
+    g, og = _pair(mg.HostGraph.rmat(13, 16, seed=42))
+    cache = os.path.join(tempfile.mkdtemp(), "tune.txt")
+    g.autotune(mg.ALGO_PR, 0, cache)
+    line = open(cache).read().split()
+    heavy, chunk = int(line[2]), int(line[3])
+    assert heavy in (256, 512, 1024, 2048) and chunk in (1024, 2048, 4096, 8192)
+    x, info = g.pagerank(mg.PR_TOPOLOGY, tol=1e-6)
+    ref, _ = O.pr_norm_f64(og, 0.85, 1e-6, info.iterations)
+    assert float(np.max(np.abs(x.astype(np.float64) - ref))) < 1e-6
+    lv, _ = g.bfs(0)
+    assert np.array_equal(lv, O.bfs(og, 0))
+    d, _ = g.sssp(0)
+    assert np.array_equal(d, O.sssp(og, 0)[0])
+    lab, _ = g.cc()
+    assert np.array_equal(lab, O.cc_minlabel(og))
+    bc, _ = g.bc_multi([0, 5, 9])
+    ref_bc = O.bc_multi_f64(og, [0, 5, 9])
+    assert float(np.max(np.abs(bc - ref_bc)) / np.max(np.abs(ref_bc))) < 1e-5
+    # a second graph with the same signature takes the cached layout
+    g2, _ = _pair(mg.HostGraph.rmat(13, 16, seed=42))
+    g2.autotune(mg.ALGO_PR, 0, cache)
+    assert len(open(cache).read().splitlines()) == 1
+    x2, _ = g2.pagerank(mg.PR_TOPOLOGY, tol=1e-6)
+    assert np.array_equal(x, x2)
+    g.free()
+    g2.free()
