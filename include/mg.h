@@ -277,9 +277,10 @@ mg_status mg_batch_cc(mg_batch *b, const mg_opts *o, int32_t *labels_out, mg_run
 /* Times candidate switch thresholds on this graph for `algo` (MG_ALGO_BFS,
  * _SSSP, _BC), writes the best into *tuned and, when cache_path is non-NULL,
  * records it in that file keyed by a graph signature (reused on the next
- * call).  MG_ALGO_PR tunes the pull layout instead: the heavy-row threshold
- * and the chunk size of the degree bins, applied to the graph itself (every
- * pull kernel uses them; *tuned is left as passed, `source` is ignored). */
+ * call).  MG_ALGO_PR tunes the pull layout instead: the heavy-row threshold,
+ * the chunk size and the thread-bin cutoff of the degree bins, applied to
+ * the graph itself (every pull kernel uses them; *tuned is left as passed,
+ * `source` is ignored). */
 enum { MG_ALGO_BFS = 0, MG_ALGO_SSSP = 1, MG_ALGO_BC = 2, MG_ALGO_CC = 3, MG_ALGO_PR = 4 };
 mg_status mg_autotune(mg_graph *dg, int32_t algo, int32_t source, const char *cache_path, mg_opts *tuned);
 

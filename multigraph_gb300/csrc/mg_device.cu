@@ -25,6 +25,7 @@ namespace mgi {
 
 constexpr int32_t HEAVY_DEG = 512;                // pull rows above this take the CTA-chunk path
 constexpr int32_t HCHUNK = 2048;                  // = 8 edges x 256 threads of a chunk CTA
+constexpr int32_t TBIN = 32;                      // rows up to this in-degree take a thread each
 // column / weight arrays carry this many bytes of readable tail padding (the
 // pull kernels stage column ids with aligned 16-byte loads)
 constexpr size_t COL_PAD = 16;
@@ -231,7 +232,7 @@ struct HostLayout {
     std::vector<int32_t> hchunk, hrows, hrow_chunk;
     std::vector<int32_t> wrows, trows;  // degree bins (engine ids)
     std::vector<int32_t> prow;          // pull-side row offsets (engine order)
-    int32_t heavy = 0, chunk = 0;
+    int32_t heavy = 0, chunk = 0, tbin = 0;
     int32_t n_dangling = 0, min_weight = 0;
     // hub-first relabeling (engine id = rank by descending log2 out-degree)
     bool relabel = false;
@@ -267,8 +268,9 @@ static void hub_first_order(const mg_host_graph &h, std::vector<int32_t> &new2ol
 
 // Degree bins and heavy chunks of the pull rows (row offsets prow, engine
 // order): rows above `heavy` in-edges are cut into `chunk`-edge pieces,
-// rows of 33..heavy go to the warp bin, the rest to the thread bin.
-static void build_bins(const std::vector<int32_t> &prow, int32_t n, int32_t heavy, int32_t chunk, HostLayout &L)
+// rows of tbin+1..heavy go to the warp bin, the rest to the thread bin.
+static void build_bins(const std::vector<int32_t> &prow, int32_t n, int32_t heavy, int32_t chunk, int32_t tbin,
+                       HostLayout &L)
 {
     L.hchunk.clear();
     L.hrows.clear();
@@ -285,7 +287,7 @@ static void build_bins(const std::vector<int32_t> &prow, int32_t n, int32_t heav
                 L.hchunk.push_back(std::min(prow[v + 1], b + chunk));
             }
             L.hrow_chunk.push_back((int32_t)(L.hchunk.size() / 3));
-        } else if (d > 32) {
+        } else if (d > tbin) {
             L.wrows.push_back(v);
         } else {
             L.trows.push_back(v);
@@ -293,9 +295,11 @@ static void build_bins(const std::vector<int32_t> &prow, int32_t n, int32_t heav
     }
     L.heavy = heavy;
     L.chunk = chunk;
+    L.tbin = tbin;
 }
 
-static void build_layout(const mg_host_graph &h, HostLayout &L, int32_t heavy = HEAVY_DEG, int32_t chunk = HCHUNK)
+static void build_layout(const mg_host_graph &h, HostLayout &L, int32_t heavy = HEAVY_DEG, int32_t chunk = HCHUNK,
+                         int32_t tbin = TBIN)
 {
     const int32_t n = h.nv, m = h.ne;
     bool skewed = false;
@@ -341,7 +345,7 @@ static void build_layout(const mg_host_graph &h, HostLayout &L, int32_t heavy = 
     for (int32_t v = 0; v < n; v++) L.n_dangling += (h.v[v + 1] == h.v[v]);
     L.min_weight = m ? *std::min_element(h.ev.begin(), h.ev.end()) : 0;
     L.prow = prow;
-    build_bins(prow, n, heavy, chunk, L);
+    build_bins(prow, n, heavy, chunk, tbin, L);
 }
 
 // Engine row i of the relabeled CSR is caller row new2old[i] with the same
@@ -584,13 +588,14 @@ static mg_status upload_bins(mg_graph *g, const HostLayout &L);
 
 namespace mgi {
 
-mg_status rebin(mg_graph *g, int32_t heavy, int32_t chunk)
+mg_status rebin(mg_graph *g, int32_t heavy, int32_t chunk, int32_t tbin)
 {
-    if (heavy < 32 || chunk < 256 || chunk % 256 != 0) return fail(MG_ERR_INVALID, "bad bin parameters %d/%d", heavy, chunk);
-    if (heavy == g->heavy_deg && chunk == g->hchunk_size) return MG_OK;
+    if (tbin < 1 || heavy <= tbin || chunk < 256 || chunk % 256 != 0)
+        return fail(MG_ERR_INVALID, "bad bin parameters %d/%d/%d", heavy, chunk, tbin);
+    if (heavy == g->heavy_deg && chunk == g->hchunk_size && tbin == g->tbin) return MG_OK;
     MG_CUDA(cudaStreamSynchronize(g->stream));
     HostLayout L;
-    build_bins(g->h_prow, g->nv, heavy, chunk, L);
+    build_bins(g->h_prow, g->nv, heavy, chunk, tbin, L);
     MG_TRY(upload_bins(g, L));
     // captured loops and per-chunk buffers follow the old bins
     free_frontier_ws(g);
@@ -705,6 +710,7 @@ static mg_status upload_bins(mg_graph *g, const HostLayout &L)
     g->nhrows = (int32_t)L.hrows.size();
     g->heavy_deg = L.heavy;
     g->hchunk_size = L.chunk;
+    g->tbin = L.tbin;
     return MG_OK;
 }
 
@@ -891,7 +897,7 @@ mg_status mg_graph_commit(mg_graph *g)
         // new degrees or a transposed copy to rebuild: lay the graph out
         // again (with the graph's current, possibly tuned, bin parameters)
         HostLayout L;
-        build_layout(*h, L, g->heavy_deg, g->hchunk_size);
+        build_layout(*h, L, g->heavy_deg, g->hchunk_size, g->tbin);
         MG_TRY(upload_arrays(g, h, L, true));
         g->h_row = h->v;
     } else {
@@ -917,7 +923,7 @@ mg_status mg_graph_commit(mg_graph *g)
         MG_CUDA(cudaStreamSynchronize(s));
         if (g->sym_host[0] != g->sym_host[1]) {
             HostLayout L;
-            build_layout(*h, L, g->heavy_deg, g->hchunk_size);
+            build_layout(*h, L, g->heavy_deg, g->hchunk_size, g->tbin);
             MG_TRY(upload_arrays(g, h, L, true));
         }
     }

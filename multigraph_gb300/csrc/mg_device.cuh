@@ -126,6 +126,7 @@ struct mg_graph {
     int32_t nhrows = 0;
     int32_t heavy_deg = 0;         // rows with in-degree > heavy_deg are heavy
     int32_t hchunk_size = 0;       // edges per heavy chunk
+    int32_t tbin = 0;              // rows up to this in-degree are in the thread bin
     std::vector<int32_t> h_prow;   // pull-side row offsets (engine order), for re-binning
     int32_t n_dangling = 0;        // vertices with out-degree 0
     int32_t min_weight = 0;        // smallest integer edge weight
@@ -181,9 +182,10 @@ mg_status cc_to_caller(mg_graph *g, const int32_t *parent, const void **out);
 // per-edge 4-byte payloads between caller CSR order and engine CSR order
 mg_status edges_to_engine(mg_graph *g, const void *src_caller, void *dst_engine);
 mg_status edges_to_caller(mg_graph *g, const void *src_engine, void *dst_caller);
-// new degree bins / heavy chunks (heavy-row threshold, chunk edges) from the
+// new degree bins / heavy chunks (heavy-row threshold, chunk edges, thread
+// bin cutoff) from the
 // host copy of the pull-side row offsets; drops the algorithm workspaces
-mg_status rebin(mg_graph *g, int32_t heavy, int32_t chunk);
+mg_status rebin(mg_graph *g, int32_t heavy, int32_t chunk, int32_t tbin);
 // batched multi-source BC over engine-id sources (symmetric graphs); the
 // float scores in engine order stay in the graph's BC workspace
 mg_status bc_batched(mg_graph *g, const int32_t *src_engine, int32_t nsrc, const mg_opts &opt, mg_run_info *info,

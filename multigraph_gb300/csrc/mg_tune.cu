@@ -8,12 +8,13 @@
 // partition sizes).  Here the switch rule is fixed (Beamer's frontier-edges
 // vs unvisited-edges test for BFS/BC, frontier-edges vs m for SSSP) and its
 // two thresholds are tuned per graph; for PageRank the tuner picks the
-// heavy-row threshold and the chunk size of the pull layout (re-binned on
-// the device graph).  Every candidate runs the real algorithm in a CUDA
+// heavy-row threshold, the chunk size and the thread-bin cutoff of the pull
+// layout (re-binned on the device graph).  Every candidate runs the real algorithm in a CUDA
 // graph, the median of three timed runs decides, and the winner is cached
 // in a text file keyed by a graph signature (n, m and a log2 degree
 // histogram).  Cache lines: signature, algorithm, then alpha / beta /
-// direction, or heavy threshold / chunk edges / 0 for PageRank.
+// direction, or heavy threshold / chunk edges / thread-bin cutoff for
+// PageRank.
 
 #include "mg_device.cuh"
 
@@ -78,14 +79,18 @@ void cache_store(const char *path, uint64_t sig, int algo, const mg_opts &o, dou
 mg_status tune_pr_layout(mg_graph *g, const char *cache_path, uint64_t sig, const mg_opts &base)
 {
     mg_opts cached = base;
-    if (cache_lookup(cache_path, sig, MG_ALGO_PR, &cached)) return mgi::rebin(g, cached.alpha, cached.beta);
-    struct Cand { int heavy, chunk; };
-    const Cand cands[] = {{256, 1024}, {256, 2048}, {512, 1024}, {512, 2048}, {512, 4096}, {1024, 2048},
-                          {1024, 4096}, {1024, 8192}, {2048, 4096}, {2048, 8192}};
+    if (cache_lookup(cache_path, sig, MG_ALGO_PR, &cached))
+        return mgi::rebin(g, cached.alpha, cached.beta, cached.direction);
+    struct Cand { int heavy, chunk, tbin; };
+    std::vector<Cand> cands;
+    const int hc[][2] = {{256, 1024}, {256, 2048}, {512, 1024}, {512, 2048}, {512, 4096}, {1024, 2048},
+                         {1024, 4096}, {1024, 8192}, {2048, 4096}, {2048, 8192}};
+    for (int tb : {8, 16, 32})
+        for (const auto &p : hc) cands.push_back({p[0], p[1], tb});
     double best_ms = 1e30;
-    Cand best = {512, 2048};
+    Cand best = {512, 2048, 32};
     for (const Cand &c : cands) {
-        MG_TRY(mgi::rebin(g, c.heavy, c.chunk));
+        MG_TRY(mgi::rebin(g, c.heavy, c.chunk, c.tbin));
         mg_opts o = base;
         o.exec = MG_EXEC_GRAPH;
         o.profile = 0;
@@ -99,11 +104,11 @@ mg_status tune_pr_layout(mg_graph *g, const char *cache_path, uint64_t sig, cons
         const double med = t[t.size() / 2];
         if (med < best_ms) { best_ms = med; best = c; }
     }
-    MG_TRY(mgi::rebin(g, best.heavy, best.chunk));
+    MG_TRY(mgi::rebin(g, best.heavy, best.chunk, best.tbin));
     mg_opts rec = base;
     rec.alpha = best.heavy;
     rec.beta = best.chunk;
-    rec.direction = 0;
+    rec.direction = best.tbin;
     cache_store(cache_path, sig, MG_ALGO_PR, rec, best_ms);
     return MG_OK;
 }

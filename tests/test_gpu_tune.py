@@ -40,8 +40,8 @@ def test_pagerank_layout_tuning_keeps_results():
     cache = os.path.join(tempfile.mkdtemp(), "tune.txt")
     g.autotune(mg.ALGO_PR, 0, cache)
     line = open(cache).read().split()
-    heavy, chunk = int(line[2]), int(line[3])
-    assert heavy in (256, 512, 1024, 2048) and chunk in (1024, 2048, 4096, 8192)
+    heavy, chunk, tbin = int(line[2]), int(line[3]), int(line[4])
+    assert heavy in (256, 512, 1024, 2048) and chunk in (1024, 2048, 4096, 8192) and tbin in (8, 16, 32)
     x, info = g.pagerank(mg.PR_TOPOLOGY, tol=1e-6)
     ref, _ = O.pr_norm_f64(og, 0.85, 1e-6, info.iterations)
     assert float(np.max(np.abs(x.astype(np.float64) - ref))) < 1e-6
