@@ -253,6 +253,11 @@ struct PullOp;
 // SSSP: min over frontier in-neighbours of dist[u] + w (accumulate_nonAtomics
 // in row order), then one atomicMin + next-frontier bit on the row
 // (fused_update_condition)
+// With a dense frontier (all_in) every in-neighbour is relaxed without
+// the bitmap test: the row's minimum only gets smaller than the frontier-
+// restricted one, distances still converge to the same fixed point, and one
+// dependent load per edge goes away.  Unreached neighbours hold UNSET, whose
+// offer UNSET + w never beats the identity UNSET.
 template <>
 struct PullOp<ALG_SSSP> : PullEmit {
     using T = int32_t;
@@ -260,11 +265,13 @@ struct PullOp<ALG_SSSP> : PullEmit {
     static constexpr bool kWeights = true;
     const uint32_t *fb;
     int it1;
+    bool all_in;
     __device__ T identity() const { return mgops::Sssp::initialize(); }
     __device__ bool skip(int32_t) const { return false; }
     __device__ T edge(int32_t, int32_t, int32_t u, int32_t w) const
     {
-        return mgd::bm_test(fb, u) ? mgops::Sssp::get_partial_result(a.label[u], w) : mgops::UNSET;
+        if (!all_in && !mgd::bm_test(fb, u)) return mgops::UNSET;
+        return mgops::Sssp::get_partial_result(a.label[u], w);
     }
     __device__ T combine(T x, T y) const
     {
@@ -343,6 +350,7 @@ __global__ void __launch_bounds__(THREADS) k_pull(Args a)
     } else {
         // degree-binned rows; reached rows marked in the next-frontier bitmap
         PullOp<ALG> op{{a, bm_buf(a, nextbuf)}, fb, it1};
+        if constexpr (ALG == ALG_SSSP) op.all_in = (long long)c.qsize * 8 > a.n;
         mgd::bins_reduce(op, a.trow, a.tcol, a.twt, a.wrows, a.nwrows, a.trows, a.ntrows);
         (void)gwarp;
         (void)nwarps;
@@ -365,9 +373,10 @@ __global__ void __launch_bounds__(THREADS) k_pull(Args a)
         int32_t best = mgops::UNSET;
         double ssum = 0.0;
         int hit = 0;
+        const bool all_in = (ALG == ALG_SSSP) && (long long)c.qsize * 8 > a.n;  // as PullOp<ALG_SSSP>
         for (int32_t p = b + threadIdx.x; p < e; p += blockDim.x) {
             int32_t u = a.tcol[p];
-            if (mgd::bm_test(fb, u)) {
+            if (all_in || mgd::bm_test(fb, u)) {
                 hit = 1;
                 if (ALG == ALG_SSSP) mgops::Sssp::accumulate_nonAtomics(best, mgops::Sssp::get_partial_result(a.label[u], a.twt[p]), 0);
                 if (ALG == ALG_BC) ssum += a.sigma[u];
