@@ -5,15 +5,17 @@
 // (16-bit sparse-tile streams sp1/sp2, dense tiles, an intermediate buffer
 // i1 written and re-read every dense iteration, ~12.5 B/edge) sized for
 // Kepler's 48 KB shared memory.  On GB300 the whole pull-side gather vector
-// of these graphs (n*4 B, <= 67 MB) stays in the 126 MB L2, so the layout here
+// of these graphs (n*4 B, <= 67 MB) stays in the 129 MB L2, so the layout here
 // is the CSR itself, renumbered hub-first when the degrees are skewed (the
 // engine-order CSR is rebuilt on the device from the caller's CSR), plus
 // small index tables that balance the pull kernels:
-//   wrows / trows : degree bins -- rows of 33..512 in-edges (a warp each)
-//                   and rows of <= 32 in-edges (a thread each);
-//   hchunk        : rows with in-degree > heavy_deg split into HCHUNK-edge
-//                   chunks, processed by whole CTAs, combined in a fixed order.
-// A transposed copy is built only when the graph is not symmetric.
+//   wrows / trows : degree bins -- rows of tbin+1..heavy_deg in-edges (a warp
+//                   each) and rows of <= tbin in-edges (a thread each);
+//   hchunk        : rows with in-degree > heavy_deg split into chunk-edge
+//                   pieces, processed by whole CTAs, combined in a fixed order.
+// heavy_deg / chunk / tbin start at HEAVY_DEG / HCHUNK / TBIN and are
+// re-chosen per graph by mg_autotune(MG_ALGO_PR).  A transposed copy is
+// built only when the graph is not symmetric.
 
 #include "mg_device.cuh"
 
@@ -26,8 +28,9 @@ namespace mgi {
 constexpr int32_t HEAVY_DEG = 512;                // pull rows above this take the CTA-chunk path
 constexpr int32_t HCHUNK = 2048;                  // = 8 edges x 256 threads of a chunk CTA
 constexpr int32_t TBIN = 32;                      // rows up to this in-degree take a thread each
-// column / weight arrays carry this many bytes of readable tail padding (the
-// pull kernels stage column ids with aligned 16-byte loads)
+// column / weight arrays carry this many bytes of tail padding past m
+// entries (defensive: a kernel that rounds a last read up stays inside the
+// allocation)
 constexpr size_t COL_PAD = 16;
 
 mg_status dev_alloc(DevBuf &b, size_t bytes)

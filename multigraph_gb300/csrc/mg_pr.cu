@@ -6,11 +6,12 @@
 // _phase11 / _phase2.  The reference scatters pr/deg with FP32 atomicAdd into
 // an intermediate buffer and gathers it in shared memory (order-dependent
 // sums, ~12.5 B/edge).  Here every sweep is a pull (gather) over in-edges:
-//   k_pr_light  degree bins (mg_bins.cuh): a warp per row of 33..512 in-edges
-//               (lanes read one 128 B line of column ids per step, a fixed
-//               shuffle tree sums them), a thread per row of <= 32 in-edges;
-//               then rows above 512 in-edges in 2048-edge chunks, one CTA
-//               each, partial sums written per chunk;
+//   k_pr_light  degree bins (mg_bins.cuh): a warp per row of tbin+1..heavy
+//               in-edges (lanes read one 128 B line of column ids per step,
+//               a fixed shuffle tree sums them), a thread per row of <= tbin
+//               in-edges; then rows above heavy in-edges in chunks, one CTA
+//               each, partial sums written per chunk (tbin / heavy / chunk
+//               default to 32 / 512 / 2048, mg_autotune re-picks them);
 //   k_pr_apply  heavy rows summed chunk by chunk in order (warp per row),
 //               then the last block to finish sums every block's residual
 //               partials in slot order: convergence test, loop condition.
@@ -799,7 +800,7 @@ mg_status mg_wpagerank(mg_graph *g, const mg_opts *o, float *x_out, mg_run_info 
     cudaStream_t s = g->stream;
     const int grid = a.nblocks;
     const size_t n = (size_t)std::max(g->nv, 1), m = (size_t)std::max(g->ne, 1);
-    MG_TRY(dev_alloc(w->wT, m * 4 + 16));  // 16 bytes of tail padding for aligned staging
+    MG_TRY(dev_alloc(w->wT, m * 4 + 16));  // 16 bytes of tail padding, as the column arrays
     MG_TRY(dev_alloc(w->xkeep, n * 4));
     if (w->wT_version != g->fw_version) {
         // out-weight sums and transposed weights, once per set of weights
