@@ -255,9 +255,13 @@ struct WarpStage {
 // launch ends with an error status instead of a hang; callers return at
 // once on false.
 constexpr long long GRID_SYNC_LIMIT = 4000000000ll;
+constexpr long long GRID_SYNC_TEST_LIMIT = 20000000ll;  // ~10 ms: the injected-failure wait
 constexpr unsigned GRID_SYNC_GROUPS = 32;
 
-__device__ __forceinline__ bool grid_sync(unsigned *bar, int *err)
+// `never` (failure injection, MG_FAIL_BARRIER): no block counts as the last
+// arrival, so every block waits out GRID_SYNC_TEST_LIMIT and the barrier
+// fails the way a lost block would make it fail.
+__device__ __forceinline__ bool grid_sync(unsigned *bar, int *err, int never = 0)
 {
     __shared__ int s_ok;
     __syncthreads();
@@ -270,10 +274,11 @@ __device__ __forceinline__ bool grid_sync(unsigned *bar, int *err)
         __threadfence();
         int ok = 1;
         bool last = false;
-        if (atomicAdd(&bar[2 + grp], 1u) == in_grp - 1) {
+        if (atomicAdd(&bar[2 + grp], 1u) == in_grp - 1 && !never) {
             atomicExch(&bar[2 + grp], 0u);
             last = atomicAdd(&bar[0], 1u) == ngroups - 1;
         }
+        const long long limit = never ? GRID_SYNC_TEST_LIMIT : GRID_SYNC_LIMIT;
         if (last) {
             atomicExch(&bar[0], 0u);
             __threadfence();
@@ -281,7 +286,7 @@ __device__ __forceinline__ bool grid_sync(unsigned *bar, int *err)
         } else {
             const long long t0 = clock64();
             while (*gen == g0) {
-                if (clock64() - t0 > GRID_SYNC_LIMIT) {
+                if (clock64() - t0 > limit) {
                     ok = 0;
                     atomicExch(err, 1);
                     break;

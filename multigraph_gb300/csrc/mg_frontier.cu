@@ -31,6 +31,7 @@
 #include "mg_ops.cuh"
 
 #include <algorithm>
+#include <cstdlib>
 #include <cstring>
 
 namespace {
@@ -84,8 +85,9 @@ struct Args {
     int32_t *heavy;      // 2 * n (parity)
     int32_t *lvl_off;
     FCtl *ctl;
-    unsigned *bar;       // grid barrier of the persistent push kernel (2 words)
+    unsigned *bar;       // grid barrier words of the persistent kernels
     int *bar_err;        // set when a grid barrier wait times out
+    int bar_never;       // failure injection: barriers never complete (MG_FAIL_BARRIER)
 };
 
 __device__ __forceinline__ uint32_t *bm_buf(const Args &a, int idx) { return a.bm + (size_t)idx * a.words; }
@@ -556,9 +558,9 @@ __global__ void __launch_bounds__(PTHREADS, 2) k_sparse_levels(Args a)
         const FCtl c = block_load_ctl(a.ctl);
         if (c.more == 0 || c.mode != MODE_PUSH) return;
         push_level<ALG>(a, c);
-        if (!mgd::grid_sync(a.bar, a.bar_err)) break;
+        if (!mgd::grid_sync(a.bar, a.bar_err, a.bar_never)) break;
         if (blockIdx.x == 0 && threadIdx.x == 0) decide_step(a);
-        if (!mgd::grid_sync(a.bar, a.bar_err)) break;
+        if (!mgd::grid_sync(a.bar, a.bar_err, a.bar_never)) break;
     }
     if (blockIdx.x == 0 && threadIdx.x == 0 && *(volatile int *)a.bar_err) {
         a.ctl->status = 3;
@@ -746,12 +748,12 @@ __global__ void __launch_bounds__(PTHREADS, 2) k_bc_back_levels(Args a, BCtl *bc
         const int par = L & 1;
         if (blockIdx.x == 0 && threadIdx.x == 0) bc_ctl->hcnt[par ^ 1] = 0;
         bc_back_level(a, L, src, &bc_ctl->hcnt[par], q, delta, bcacc, heavy_list);
-        if (!mgd::grid_sync(a.bar, a.bar_err)) return;
+        if (!mgd::grid_sync(a.bar, a.bar_err, a.bar_never)) return;
         if (threadIdx.x == 0) s_nheavy = __ldcg(&bc_ctl->hcnt[par]);
         __syncthreads();
         const int32_t nheavy = s_nheavy;
         bc_back_heavy_level(a, L, src, nheavy, q, delta, bcacc, heavy_list);
-        if (!mgd::grid_sync(a.bar, a.bar_err)) return;
+        if (!mgd::grid_sync(a.bar, a.bar_err, a.bar_never)) return;
     }
 }
 
@@ -862,6 +864,10 @@ static Args make_args(mg_graph *g)
     a.ctl = w->ctl.as<FCtl>();
     a.bar = w->bar.as<unsigned>();
     a.bar_err = reinterpret_cast<int *>(w->bar.as<unsigned>() + 2 + mgd::GRID_SYNC_GROUPS);
+    // failure injection for tests: the persistent kernels' barriers never
+    // complete, their bounded waits run out and the run reports an error
+    const char *fb = std::getenv("MG_FAIL_BARRIER");
+    a.bar_never = (fb && fb[0] == '1') ? 1 : 0;
     return a;
 }
 
@@ -870,6 +876,7 @@ static uint64_t key_of(const Args &a, int alg)
     uint64_t k = 1469598103934665603ull ^ (uint64_t)alg;
     const void *ptrs[] = {a.row, a.col, a.trow, a.tcol, a.label, a.sigma, a.bm, a.queue, a.heavy, a.ctl, a.wrows};
     for (const void *p : ptrs) k = (k ^ (uint64_t)(uintptr_t)p) * 1099511628211ull;
+    k ^= (uint64_t)a.bar_never << 63;  // captured kernel arguments include the injection flag
     return k;
 }
 
