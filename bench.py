@@ -49,6 +49,8 @@ def parse():
     p.add_argument("--scale", type=int, default=SCALE)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-batch", action="store_true", help="skip the batched-vs-plain and adjoint comparisons")
+    p.add_argument("--batch-only", action="store_true",
+                   help="print only the batched-vs-plain comparison as one JSON line (for profiling the batched kernels)")
     p.add_argument("--exec", default="graph", choices=["graph", "host"],
                    help="iteration loops as CUDA graphs with a device-side WHILE node (default) or host-driven "
                         "(every kernel a separate launch, as a profiler's launch list needs)")
@@ -150,7 +152,7 @@ def cpu_oracle_run(rp, col, wt, counts=None):
     return t1 - t0, sweeps, t2 - t1, iters
 
 
-def batch_report(mg, device):
+def batch_report(mg, device, exec_mode=None):
     """Batched against plain launches (outside the timed region; device time
     of each call from its own cudaEvents):
       bc_256   : 256-source BC on R-MAT scale 20 (mg_bc_multi) vs 256 mg_bc
@@ -167,18 +169,19 @@ def batch_report(mg, device):
     Each entry carries the agreement of the two results."""
     import numpy as np
     out = {}
+    ex = {} if exec_mode is None else {"exec": exec_mode}
     h = mg.HostGraph.rmat(20, EDGE_FACTOR, seed=20)
     g = mg.Graph(h, device)
     rng = np.random.default_rng(20)
     src = rng.integers(0, g.nv, 256).astype(np.int32)
-    g.bc_multi(src[:32], out=False)
-    bcb, ib = g.bc_multi(src)
-    _, ib2 = g.bc_multi(src, out=False)
+    g.bc_multi(src[:32], out=False, **ex)
+    bcb, ib = g.bc_multi(src, **ex)
+    _, ib2 = g.bc_multi(src, out=False, **ex)
     tb = min(ib.device_ms, ib2.device_ms)
     acc = np.zeros(g.nv, np.float64)
     tp = 0.0
     for s_ in src:
-        (_, _, dl), i1 = g.bc(int(s_))
+        (_, _, dl), i1 = g.bc(int(s_), **ex)
         tp += i1.device_ms
         d = dl.astype(np.float64)
         d[int(s_)] = 0.0
@@ -301,6 +304,11 @@ def main():
     import __graft_entry__
     __graft_entry__.build()
     import multigraph_gb300 as mg
+    if args.batch_only:
+        if rank == 0:
+            print(json.dumps({"batched_vs_plain": batch_report(
+                mg, local, mg.EXEC_HOST if args.exec == "host" else None)}), flush=True)
+        return 0
 
     h = build_graph(args.scale)
     h.pin()
