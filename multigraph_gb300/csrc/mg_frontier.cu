@@ -12,8 +12,9 @@
 //            degrees of 32 queue entries; vertices above PUSH_HEAVY split over
 //            the whole grid), claims / relaxes destinations with the
 //            operator hooks, appends the next queue with warp-aggregated
-//            atomics and sets the next-frontier bitmap; grid barriers
-//            between levels, block 0 runs the end-of-level decision;
+//            atomics and sets the next-frontier bitmap; one grid barrier
+//            per level, after which every block takes the end-of-level
+//            decision itself from the level's counters;
 //   k_pull   (when the frontier is dense) every unvisited vertex scans its
 //            in-edges against the frontier bitmap (BFS stops at the first
 //            parent; SSSP/BC reduce over all in-edges), light rows in
@@ -88,6 +89,19 @@ struct Args {
     unsigned *bar;       // grid barrier words of the persistent kernels
     int *bar_err;        // set when a grid barrier wait times out
     int bar_never;       // failure injection: barriers never complete (MG_FAIL_BARRIER)
+    struct LevelCnt *cnt;  // persistent push phase: per-level counters, 4 rotating slots
+};
+
+// Counters one push level produces (next queue size, heavy entries, next
+// frontier's out-edges).  The persistent push phase keeps them in 4 slots
+// by level mod 4, so every block can read level L's counters after the one
+// barrier while level L+1 appends to the next slot; block 0 clears slot
+// L+2 during level L (its last readers finished before the barrier that
+// began level L).
+struct LevelCnt {
+    int32_t nq;
+    int32_t nhcur;
+    long long nfe;
 };
 
 __device__ __forceinline__ uint32_t *bm_buf(const Args &a, int idx) { return a.bm + (size_t)idx * a.words; }
@@ -117,16 +131,16 @@ __device__ __forceinline__ void warp_add64(long long *dst, long long v)
 // call).  SSSP has already set the vertex's bit when it claimed it.
 template <int ALG>
 __device__ __forceinline__ void emit_next(const Args &a, const FCtl &c, int nextbuf, bool found, int32_t v,
-                                          long long &dsum)
+                                          long long &dsum, int32_t *nq, int32_t *nhcur)
 {
-    int slot = mgd::warp_append(&a.ctl->nq, found);
+    int slot = mgd::warp_append(nq, found);
     if (found) {
         a.queue[c.nqoff + slot] = v;
         if (ALG != ALG_SSSP) mgd::bm_set(bm_buf(a, nextbuf), v);
         int32_t dg = a.row[v + 1] - a.row[v];
         dsum += dg;
         if (dg > PUSH_HEAVY) {
-            int h = atomicAdd(&a.ctl->nhcur, 1);
+            int h = atomicAdd(nhcur, 1);
             a.heavy[(size_t)(c.hpar ^ 1) * a.n + h] = v;
         }
     }
@@ -161,7 +175,7 @@ __device__ __forceinline__ bool push_edge(const Args &a, int it1, int32_t v, int
 // are loaded through L2 (__ldcg): the persistent kernel runs many levels in
 // one launch.
 template <int ALG>
-__device__ __forceinline__ void push_level(const Args &a, const FCtl &c)
+__device__ __forceinline__ void push_level(const Args &a, const FCtl &c, LevelCnt *lc)
 {
     const int it1 = c.iter + 1;
     const int nextbuf = (c.cur + 1) % 3, sparebuf = (c.cur + 2) % 3;
@@ -190,7 +204,7 @@ __device__ __forceinline__ void push_level(const Args &a, const FCtl &c)
                 v = a.col[k];
                 found = push_edge<ALG>(a, it1, v, pi, pd, (ALG == ALG_SSSP) ? a.wt[k] : 0, bm_buf(a, nextbuf));
             }
-            emit_next<ALG>(a, c, nextbuf, found, v, dsum);
+            emit_next<ALG>(a, c, nextbuf, found, v, dsum, &lc->nq, &lc->nhcur);
         }
         scanned += (threadIdx.x == 0 && blockIdx.x == 0) ? span : 0;
     }
@@ -230,10 +244,10 @@ __device__ __forceinline__ void push_level(const Args &a, const FCtl &c)
                 v = a.col[e];
                 found = push_edge<ALG>(a, it1, v, opi, opd, (ALG == ALG_SSSP) ? a.wt[e] : 0, bm_buf(a, nextbuf));
             }
-            emit_next<ALG>(a, c, nextbuf, found, v, dsum);
+            emit_next<ALG>(a, c, nextbuf, found, v, dsum, &lc->nq, &lc->nhcur);
         }
     }
-    warp_add64(&a.ctl->nf_edges, dsum);
+    warp_add64(&lc->nfe, dsum);
     if (lane == 0 && scanned) atomicAdd((unsigned long long *)&a.ctl->scanned, (unsigned long long)scanned);
 }
 
@@ -471,30 +485,28 @@ __device__ __forceinline__ void store_ctl(FCtl *p, const FCtl &c)
     for (int i = 0; i < (int)(sizeof(FCtl) / 8); i++) d[i] = s[i];
 }
 
-// End of a level (one thread, no other thread touching the loop state):
-// next queue slice, direction switch, caps.  Works on a register copy (one
-// batch of parallel loads, one batch of stores).  Returns the continue flag.
-__device__ __forceinline__ int decide_step(const Args &a)
+// The end-of-level decision on a copy of the loop state, given the level's
+// counters; block 0 (write_lvl) also records the level offset.
+__device__ __forceinline__ int decide_local(const Args &a, FCtl &c, int32_t nq, int32_t nhcur, long long nfe_in,
+                                            bool write_lvl)
 {
-    FCtl c = load_ctl(a.ctl);
     int more = c.more;
     if (more) {
-        const int32_t nq = c.nq;
         if (c.mode == MODE_PULL) c.pull_iters++;
         c.iter += 1;
         if (c.archive && c.iter + 1 < a.n + 3) {
-            a.lvl_off[c.iter + 1] = c.nqoff + nq;
+            if (write_lvl) a.lvl_off[c.iter + 1] = c.nqoff + nq;
             if (nq > 0) c.nlevels = c.iter + 1;
         }
         c.qoff = c.nqoff;
         c.qsize = nq;
         c.nqoff = c.archive ? (c.qoff + nq) : (c.qoff == 0 ? a.n : 0);
         c.nq = 0;
-        c.hcur = c.nhcur;
+        c.hcur = nhcur;
         c.nhcur = 0;
         c.hpar ^= 1;
         c.cur = (c.cur + 1) % 3;
-        const long long nfe = c.nf_edges;
+        const long long nfe = nfe_in;
         c.visited_edges += nfe;
         c.nf_edges = 0;
         if (nq == 0) {
@@ -518,8 +530,19 @@ __device__ __forceinline__ int decide_step(const Args &a)
             if (c.iter >= c.max_iter) { c.status = 1; more = 0; }
         }
         c.more = more;
-        store_ctl(a.ctl, c);
     }
+    return more;
+}
+
+// End of a level (one thread, no other thread touching the loop state):
+// next queue slice, direction switch, caps.  Works on a register copy (one
+// batch of parallel loads, one batch of stores).  Returns the continue flag.
+__device__ __forceinline__ int decide_step(const Args &a)
+{
+    FCtl c = load_ctl(a.ctl);
+    if (c.more == 0) return 0;
+    const int more = decide_local(a, c, c.nq, c.nhcur, c.nf_edges, true);
+    store_ctl(a.ctl, c);
     return more;
 }
 
@@ -531,8 +554,10 @@ __global__ void k_decide(Args a, cudaGraphConditionalHandle h, int use_cond)
 }
 
 // Persistent push phase: consecutive push levels in one cooperative launch,
-// separated by grid barriers (push level | barrier | block 0 decides |
-// barrier), until the traversal ends or the direction switch picks pull.
+// one grid barrier per level (push level | barrier | every block decides
+// from the level's counters on its own copy of the loop state, the same
+// inputs giving the same decision everywhere), until the traversal ends or
+// the direction switch picks pull; block 0 writes the loop state back.
 // High-diameter graphs (lattices, road networks) spend thousands of levels
 // here, each a few microseconds instead of a round of kernel launches.  A
 // barrier timeout sets status 3 and ends the traversal.
@@ -554,17 +579,49 @@ __device__ __forceinline__ FCtl block_load_ctl(const FCtl *p)
 template <int ALG>
 __global__ void __launch_bounds__(PTHREADS, 2) k_sparse_levels(Args a)
 {
-    for (int32_t lv = 0; lv <= a.n + 2; lv++) {
-        const FCtl c = block_load_ctl(a.ctl);
-        if (c.more == 0 || c.mode != MODE_PUSH) return;
-        push_level<ALG>(a, c);
-        if (!mgd::grid_sync(a.bar, a.bar_err, a.bar_never)) break;
-        if (blockIdx.x == 0 && threadIdx.x == 0) decide_step(a);
-        if (!mgd::grid_sync(a.bar, a.bar_err, a.bar_never)) break;
+    __shared__ FCtl s_c;
+    __shared__ int4 s_cnt;
+    {
+        const FCtl c0 = block_load_ctl(a.ctl);
+        if (threadIdx.x == 0) s_c = c0;
+        __syncthreads();
     }
-    if (blockIdx.x == 0 && threadIdx.x == 0 && *(volatile int *)a.bar_err) {
-        a.ctl->status = 3;
-        a.ctl->more = 0;
+    bool ran = false;
+    for (int32_t lv = 0; lv <= a.n + 2; lv++) {
+        if (s_c.more == 0 || s_c.mode != MODE_PUSH) break;
+        ran = true;
+        LevelCnt *lc = a.cnt + (lv & 3);
+        if (blockIdx.x == 0 && threadIdx.x == 0) {
+            LevelCnt *z = a.cnt + ((lv + 2) & 3);
+            z->nq = 0;
+            z->nhcur = 0;
+            z->nfe = 0;
+        }
+        push_level<ALG>(a, s_c, lc);
+        if (!mgd::grid_sync(a.bar, a.bar_err, a.bar_never)) break;
+        if (threadIdx.x == 0) {
+            s_cnt = __ldcg(reinterpret_cast<const int4 *>(lc));  // nq, nhcur, nfe (lo, hi)
+            FCtl c = s_c;
+            const long long nfe = (long long)(((unsigned long long)(unsigned)s_cnt.w << 32) | (unsigned)s_cnt.z);
+            decide_local(a, c, s_cnt.x, s_cnt.y, nfe, blockIdx.x == 0);
+            s_c = c;
+        }
+        __syncthreads();
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        FCtl c = s_c;
+        if (*(volatile int *)a.bar_err) {
+            c.status = 3;
+            c.more = 0;
+        }
+        if (ran || c.status) {
+            // the loop state back to global memory for the other kernels,
+            // all but the last word (the scanned-edges statistic, which the
+            // push levels add to atomically)
+            int2 *d = reinterpret_cast<int2 *>(a.ctl);
+            const int2 *src = reinterpret_cast<const int2 *>(&c);
+            for (int i = 0; i < (int)(sizeof(FCtl) / 8) - 1; i++) d[i] = src[i];
+        }
     }
 }
 
@@ -775,6 +832,7 @@ struct FrontierWS {
     mgi::DevBuf label, sigma, bm, visited, queue, heavy, lvl_off, ctl;
     mgi::DevBuf q, delta, bc, bctl, bheavy, srcbuf;
     mgi::DevBuf bar;        // grid barrier words + error flag of the persistent kernels
+    mgi::DevBuf cnt;        // LevelCnt[4] of the persistent push phase
     int coop_grid[3] = {0, 0, 0};  // resident blocks of k_sparse_levels<ALG> on this device
     int coop_back = 0;             // resident blocks of k_bc_back_levels
     mgi::LoopGraph lg[3];
@@ -787,7 +845,8 @@ void free_frontier_ws(mg_graph *g)
     if (!g->fws) return;
     FrontierWS *w = g->fws;
     DevBuf *bufs[] = {&w->label, &w->sigma, &w->bm, &w->visited, &w->queue, &w->heavy,
-                      &w->lvl_off, &w->ctl, &w->q, &w->delta, &w->bc, &w->bctl, &w->bheavy, &w->srcbuf, &w->bar};
+                      &w->lvl_off, &w->ctl, &w->q, &w->delta, &w->bc, &w->bctl, &w->bheavy, &w->srcbuf, &w->bar,
+                      &w->cnt};
     for (DevBuf *b : bufs) dev_free(*b);
     for (auto &l : w->lg) l.destroy();
     delete w;
@@ -808,6 +867,7 @@ static mg_status ensure_ws(mg_graph *g, int alg)
     MG_TRY(dev_alloc(w->ctl, sizeof(FCtl)));
     MG_TRY(dev_alloc(w->lvl_off, (n + 3) * 4));
     MG_TRY(dev_alloc(w->bar, BAR_BYTES));
+    MG_TRY(dev_alloc(w->cnt, 4 * sizeof(LevelCnt)));
     if (alg == ALG_BC) MG_TRY(dev_alloc(w->sigma, n * 8));
     if (w->coop_grid[alg] == 0) {
         int per_sm = 0;
@@ -863,6 +923,7 @@ static Args make_args(mg_graph *g)
     a.lvl_off = w->lvl_off.as<int32_t>();
     a.ctl = w->ctl.as<FCtl>();
     a.bar = w->bar.as<unsigned>();
+    a.cnt = w->cnt.as<LevelCnt>();
     a.bar_err = reinterpret_cast<int *>(w->bar.as<unsigned>() + 2 + mgd::GRID_SYNC_GROUPS);
     // failure injection for tests: the persistent kernels' barriers never
     // complete, their bounded waits run out and the run reports an error
@@ -921,6 +982,7 @@ static mg_status frontier_run_impl(mg_graph *g, int alg, int32_t src, const int3
     const int sc = P.slot("frontier_compact");
     const int sd = P.slot("frontier_decide");
     BodyFn body = [&](cudaStream_t st, cudaGraphConditionalHandle h, int use_cond) -> mg_status {
+        MG_CUDA(cudaMemsetAsync(a.cnt, 0, 4 * sizeof(LevelCnt), st));
         P.begin(sp);
         switch (alg) {
         case ALG_BFS: MG_TRY(launch_sparse_levels<ALG_BFS>(a, w->coop_grid[alg], st)); break;

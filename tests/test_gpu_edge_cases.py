@@ -87,3 +87,38 @@ def test_empty_graph_and_bad_sources():
             g.bc_multi([0, bad])
         assert e.value.status == mg.MG_ERR_RANGE
     g.free()
+
+
+def test_unsupported_and_directed_paths():
+    rng = np.random.default_rng(11)
+    s = rng.integers(0, 300, 2500)
+    d = (s + rng.integers(1, 30, 2500)) % 300
+    h = mg.HostGraph.from_entries(300, s, d, rng.integers(1, 64, 2500), flags=mg.LOAD_NSYM)
+    g, og = _pair(h)
+    # weighted PageRank needs float weights, then a symmetric structure
+    with pytest.raises(mg.MGError) as e:
+        g.wpagerank()
+    assert e.value.status == mg.MG_ERR_UNSUPPORTED
+    g.set_float_weights(np.ones(og.ne, np.float32))
+    with pytest.raises(mg.MGError) as e:
+        g.wpagerank()
+    assert e.value.status == mg.MG_ERR_UNSUPPORTED
+    # multi-source BC on a directed graph: one traversal per source, equal
+    # to the sum of the single-source deltas
+    srcs = [0, 5, 5, 120]
+    bc, _ = g.bc_multi(srcs)
+    acc = np.zeros(og.nv)
+    for x in srcs:
+        (_, _, dl), _ = g.bc(x)
+        dd = dl.astype(np.float64)
+        dd[x] = 0.0
+        acc += dd
+    assert np.allclose(bc, acc, rtol=1e-5, atol=1e-5)
+    # BFS / SSSP / CC on the directed graph against the oracle
+    lv, _ = g.bfs(5)
+    assert np.array_equal(lv, O.bfs(og, 5))
+    dist, _ = g.sssp(5)
+    assert np.array_equal(dist, O.sssp(og, 5)[0])
+    lab, _ = g.cc()
+    assert np.array_equal(lab, O.cc_minlabel(og))
+    g.free()
