@@ -786,9 +786,9 @@ __device__ __forceinline__ void bc_back_heavy_level(const Args &a, int32_t L, in
     }
 }
 
-// Persistent backward sweep: every level in one cooperative launch, two
-// grid barriers per level (light entries | barrier | heavy entries |
-// barrier).  Every block walks L = L0 .. 1 itself; the heavy-entry counter
+// Persistent backward sweep: every level in one cooperative launch, one or
+// two grid barriers per level (light entries | barrier | heavy entries |
+// barrier, the second half only when the level listed heavy entries).  Every block walks L = L0 .. 1 itself; the heavy-entry counter
 // alternates with the level's parity, and block 0 clears the one the next
 // level will use while the current level runs (its last readers finished
 // before the previous barrier).  A barrier timeout sets the error flag; the
@@ -809,6 +809,10 @@ __global__ void __launch_bounds__(PTHREADS, 2) k_bc_back_levels(Args a, BCtl *bc
         if (threadIdx.x == 0) s_nheavy = __ldcg(&bc_ctl->hcnt[par]);
         __syncthreads();
         const int32_t nheavy = s_nheavy;
+        // most levels list no heavy entry: every block sees the same count
+        // and skips the heavy phase and its barrier together (block 0's
+        // early clear of this counter then leaves it at the 0 it holds)
+        if (nheavy == 0) continue;
         bc_back_heavy_level(a, L, src, nheavy, q, delta, bcacc, heavy_list);
         if (!mgd::grid_sync(a.bar, a.bar_err, a.bar_never)) return;
     }
