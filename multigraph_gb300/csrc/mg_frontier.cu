@@ -710,6 +710,26 @@ __device__ __forceinline__ void bc_back_level(const Args &a, int32_t L, int32_t 
         vpw = 1;
         while (vpw * 2 <= want) vpw *= 2;
     }
+    if (vpw == 1) {
+        // one entry per warp: lanes stride its edges, a shuffle tree sums
+        for (int i = b0 + gwarp; i < b1; i += nwarps) {
+            const int32_t v = a.queue[i];
+            const int32_t b = a.row[v], e = a.row[v + 1];
+            if (e - b > PUSH_HEAVY) {
+                if (lane == 0) heavy_list[atomicAdd(hcount, 1)] = v;
+                continue;
+            }
+            float acc = 0.0f;
+            for (int32_t p = b + lane; p < e; p += 32) {
+                const int32_t w = a.col[p];
+                if (a.label[w] == L) acc += __ldcg(&q[w]);
+            }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+            if (lane == 0) bc_finish_vertex(v, acc, a.sigma, delta, q, bcacc, src);
+        }
+        return;
+    }
     for (int base = b0 + gwarp * vpw; base < b1; base += nwarps * vpw) {
         int32_t v = -1, start = 0, deg = 0;
         if (lane < vpw && base + lane < b1) {
