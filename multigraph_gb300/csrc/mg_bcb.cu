@@ -160,6 +160,17 @@ __global__ void k_bb_init(BbArgs a, int32_t nsrc, int32_t dirmode, int32_t alpha
     }
 }
 
+// items per warp: `cap`, or fewer (a power of two) when `count` items would
+// leave warps idle
+__device__ __forceinline__ int entries_per_warp(int32_t count, int nwarps, int cap)
+{
+    if (count >= nwarps * cap) return cap;
+    const int want = max(1, count / nwarps);
+    int v = 1;
+    while (v * 2 <= want && v * 2 <= cap) v *= 2;
+    return v;
+}
+
 __device__ __forceinline__ void mark_edge_block(const BbArgs &a, int32_t p, int32_t e, uint32_t f)
 {
     bool pred = false;
@@ -180,12 +191,30 @@ __global__ void __launch_bounds__(THREADS) k_bb_mark(BbArgs a)
     const int gwarp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int nwarps = (gridDim.x * blockDim.x) >> 5;
     const int32_t b0 = a.off[c.d], b1 = a.off[c.d + 1];
-    for (int32_t i = b0 + gwarp; i < b1; i += nwarps) {
-        const int32_t u = a.arch[i];
-        const uint32_t f = a.amask[i];
-        const int32_t b = a.row[u], e = a.row[u + 1];
-        if (e - b > MARK_HEAVY) continue;
-        for (int32_t base = b; base < e; base += 32) mark_edge_block(a, base + lane, e, f);
+    // up to 32 entries per warp (fewer when the level would leave warps
+    // idle), their out-edges spread over the lanes by a load-balanced search
+    const int vpw = entries_per_warp(b1 - b0, nwarps, 32);
+    for (int32_t base = b0 + gwarp * vpw; base < b1; base += nwarps * vpw) {
+        int32_t start = 0, deg = 0;
+        uint32_t f = 0;
+        if (lane < vpw && base + lane < b1) {
+            const int32_t u = a.arch[base + lane];
+            f = a.amask[base + lane];
+            start = a.row[u];
+            deg = a.row[u + 1] - start;
+            if (deg > MARK_HEAVY) deg = 0;  // the grid-wide loop below
+        }
+        const int incl = mgd::warp_scan_incl(deg);
+        const int excl = incl - deg;
+        const int total = __shfl_sync(0xffffffffu, incl, 31);
+        for (int k0 = 0; k0 < total; k0 += 32) {
+            const int k = k0 + lane;
+            const int kk = k < total ? k : total - 1;
+            const int own = mgd::owner_lane(excl, kk);
+            const int32_t p = __shfl_sync(0xffffffffu, start, own) + (kk - __shfl_sync(0xffffffffu, excl, own));
+            const uint32_t fo = __shfl_sync(0xffffffffu, f, own);
+            mark_edge_block(a, k < total ? p : 0, k < total ? p + 1 : 0, fo);
+        }
     }
     // heavy frontier entries: every warp of the grid takes 32-edge slices
     const uint32_t *fcur = fm_of(a, c.cur);
