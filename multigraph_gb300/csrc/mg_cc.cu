@@ -17,7 +17,7 @@
 // Symmetric graphs skip most of the edges (neighbour sampling, as in
 // Sutton et al., "Optimizing Parallel Graph Connectivity Computation via
 // Subgraph Sampling", IPDPS 2018): every vertex first links to its first
-// SAMPLE_ROUNDS neighbours, the trees are compressed, the most frequent root
+// SAMPLE_ROUNDS neighbours (the trees compressed after each round), the most frequent root
 // among 1024 sampled vertices is taken as the giant component, and only rows
 // whose vertex is outside it hook their remaining edges (in both
 // directions, so an edge with one end in the giant component is hooked from
@@ -67,12 +67,13 @@ __device__ __forceinline__ void cc_union(int32_t *parent, int32_t a, int32_t b)
 constexpr int SAMPLE_ROUNDS = 2;
 constexpr int MODE_SAMPLES = 1024;
 
-__global__ void k_cc_init(int32_t n, const int32_t *row, const int32_t *col, int32_t *parent)
+// link_first: the first neighbour below v starts the tree (a valid link:
+// parent < v); otherwise every vertex is its own tree
+__global__ void k_cc_init(int32_t n, const int32_t *row, const int32_t *col, int32_t *parent, int link_first)
 {
     for (int32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x) {
         int32_t p = mgops::Cc::initialize(v);
-        // the first neighbour below v starts the tree (a valid link: parent < v)
-        if (row[v + 1] > row[v]) p = min(p, col[row[v]]);
+        if (link_first && row[v + 1] > row[v]) p = min(p, col[row[v]]);
         parent[v] = p;
     }
 }
@@ -231,18 +232,21 @@ mg_status cc_run(mg_graph *g, mg_run_info *info, const std::vector<int32_t> *vof
     const int si = P.slot("cc_init"), sh = P.slot("cc_hook"), sc = P.slot("cc_compress");
     const bool sample = g->symmetric;
     P.begin(si);
-    k_cc_init<<<grid, THREADS, 0, s>>>(g->nv, g->trow, g->tcol, parent);
+    k_cc_init<<<grid, THREADS, 0, s>>>(g->nv, g->trow, g->tcol, parent, sample ? 0 : 1);
     P.end();
     if (sample) {
+        // singleton trees, then each sampling round links every vertex to
+        // its r-th neighbour and flattens the trees again, so no find walks
+        // a long chain (a lattice's first neighbours would chain rows)
         const int ss = P.slot("cc_sample"), sm = P.slot("cc_mode");
-        for (int r = 1; r < SAMPLE_ROUNDS + 1; r++) {  // neighbour 0 is linked by k_cc_init
+        for (int r = 0; r < SAMPLE_ROUNDS; r++) {
             P.begin(ss);
             k_cc_sample<<<grid, THREADS, 0, s>>>(g->nv, g->trow, g->tcol, r, parent);
             P.end();
+            P.begin(sc);
+            k_cc_compress<<<grid, THREADS, 0, s>>>(g->nv, parent);
+            P.end();
         }
-        P.begin(sc);
-        k_cc_compress<<<grid, THREADS, 0, s>>>(g->nv, parent);
-        P.end();
         MG_CUDA(cudaMemsetAsync(giant, 0, words * 4, s));
         P.begin(sm);
         k_cc_mode<<<ngraphs, MODE_SAMPLES, 0, s>>>(g->nv, voff_dev, g->relabeled ? g->old2new.as<int32_t>() : nullptr,
