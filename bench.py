@@ -408,7 +408,7 @@ def main():
         "config": {"workload": f"rmat{args.scale}_ef{EDGE_FACTOR}: SSSP(src 0) + PageRank(d=0.85, L1 tol 1e-6)",
                    "nv": n, "ne": m, "sssp_iterations": si.iterations, "pr_sweeps": pi.iterations,
                    "parallelism": f"replicas x{world}", "l2": "inputs (column ids + weights, 1 GB) exceed L2",
-                   "baseline_metric": "GTEPS & HBM GB/s vs peak (BASELINE.json)"},
+                   "metric_family": "GTEPS and HBM GB/s against the measured peak"},
         "e2e": {"value": e2e_val, "unit": "GTEPS", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": (achieved / peak) if achieved else None, "traffic": traffic,
