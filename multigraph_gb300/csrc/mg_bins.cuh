@@ -36,13 +36,15 @@ __device__ __forceinline__ typename Op::T warp_row(Op &op, const int32_t *__rest
     const int32_t b = prow[v], e = prow[v + 1];
     T acc0 = op.identity(), acc1 = op.identity();
     int32_t p = b + ln;
+    // the column / weight stream is read once per sweep: evict-first loads
+    // (__ldcs) keep L1 and L2 for the gathered vertex values
     for (; p + 32 < e; p += 64) {  // two independent loads in flight per lane
-        int32_t u0 = __ldg(&pcol[p]), u1 = __ldg(&pcol[p + 32]);
-        int32_t w0 = Op::kWeights ? __ldg(&pwt[p]) : 0, w1 = Op::kWeights ? __ldg(&pwt[p + 32]) : 0;
+        int32_t u0 = __ldcs(&pcol[p]), u1 = __ldcs(&pcol[p + 32]);
+        int32_t w0 = Op::kWeights ? __ldcs(&pwt[p]) : 0, w1 = Op::kWeights ? __ldcs(&pwt[p + 32]) : 0;
         acc0 = op.combine(acc0, op.edge(p, v, u0, w0));
         acc1 = op.combine(acc1, op.edge(p + 32, v, u1, w1));
     }
-    if (p < e) acc0 = op.combine(acc0, op.edge(p, v, __ldg(&pcol[p]), Op::kWeights ? __ldg(&pwt[p]) : 0));
+    if (p < e) acc0 = op.combine(acc0, op.edge(p, v, __ldcs(&pcol[p]), Op::kWeights ? __ldcs(&pwt[p]) : 0));
     return warp_combine(op, op.combine(acc0, acc1));
 }
 

@@ -237,7 +237,7 @@ __global__ void __launch_bounds__(THREADS) k_pr_light(PArgs a)
 #pragma unroll
                 for (int j = 0; j < 8; j++) {
                     int32_t p = b0 + threadIdx.x + j * THREADS;
-                    u[j] = p < e ? __ldg(&a.pcol[p]) : -1;
+                    u[j] = p < e ? __ldcs(&a.pcol[p]) : -1;  // streamed once: evict-first
                 }
 #pragma unroll
                 for (int j = 0; j < 8; j++)
