@@ -240,7 +240,7 @@ __device__ __forceinline__ double pull_span(const BbArgs &a, const uint32_t *fcu
         int32_t u = 0;
         uint32_t f = 0;
         if (p < e) {
-            u = __ldg(&a.tcol[p]);
+            u = __ldcs(&a.tcol[p]);
             f = fcur[u] & want;
         }
         unsigned hits = __ballot_sync(0xffffffffu, f != 0);
@@ -430,7 +430,7 @@ __device__ __forceinline__ float back_span(const BbArgs &a, const uint32_t *nxt,
         int32_t v = 0;
         uint32_t f = 0;
         if (p < e) {
-            v = __ldg(&col[p]);
+            v = __ldcs(&col[p]);
             f = nxt[v] & want;
         }
         unsigned hits = __ballot_sync(0xffffffffu, f != 0);

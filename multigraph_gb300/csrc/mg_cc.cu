@@ -176,7 +176,7 @@ __global__ void __launch_bounds__(THREADS) k_cc_hook(int32_t n, const int32_t *p
         const bool skip = s_skip;
         __syncthreads();
         if (skip) continue;
-        for (int32_t p = b + threadIdx.x; p < e; p += blockDim.x) op.edge(p, u, pcol[p], 0);
+        for (int32_t p = b + threadIdx.x; p < e; p += blockDim.x) op.edge(p, u, __ldcs(&pcol[p]), 0);
     }
 }
 

@@ -391,7 +391,7 @@ __global__ void __launch_bounds__(THREADS) k_pull(Args a)
         int hit = 0;
         const bool all_in = (ALG == ALG_SSSP) && (long long)c.qsize * 8 > a.n;  // as PullOp<ALG_SSSP>
         for (int32_t p = b + threadIdx.x; p < e; p += blockDim.x) {
-            int32_t u = a.tcol[p];
+            int32_t u = __ldcs(&a.tcol[p]);  // streamed once: evict-first
             if (all_in || mgd::bm_test(fb, u)) {
                 hit = 1;
                 if (ALG == ALG_SSSP) mgops::Sssp::accumulate_nonAtomics(best, mgops::Sssp::get_partial_result(a.label[u], a.twt[p]), 0);
