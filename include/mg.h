@@ -221,8 +221,10 @@ mg_status mg_cc(mg_graph *dg, const mg_opts *o, int32_t *label_out, mg_run_info 
 mg_status mg_bc(mg_graph *dg, int32_t source, const mg_opts *o, int32_t *level_out, double *sigma_out,
                 float *delta_out, mg_run_info *info);
 
-/* Multi-source BC scores bc[v] = sum_s delta_s[v] (v != s).  No reference
- * counterpart (the reference runs one source). */
+/* Multi-source BC scores bc[v] = sum_s delta_s[v] (v != s).  Symmetric
+ * graphs traverse 32 sources at a time (one lane per source; up to 2^26
+ * vertices, ~650 B of device memory per vertex), directed graphs one source
+ * at a time.  No reference counterpart (the reference runs one source). */
 mg_status mg_bc_multi(mg_graph *dg, const int32_t *sources, int32_t nsrc, const mg_opts *o,
                       float *bc_out, mg_run_info *info);
 

@@ -556,6 +556,9 @@ mg_status bc_batched(mg_graph *g, const int32_t *src_engine, int32_t nsrc, const
                      const float **bc_dev)
 {
     if (!g->symmetric) return fail(MG_ERR_UNSUPPORTED, "batched BC needs a structurally symmetric graph");
+    // archive positions (up to 32 entries per vertex) are int32
+    if ((int64_t)g->nv * W > (int64_t)INT32_MAX - 4)
+        return fail(MG_ERR_UNSUPPORTED, "batched BC takes graphs of up to %d vertices", (int)((INT32_MAX - 4) / W));
     if (!g->bws) g->bws = new BcWS();
     BcWS *w = g->bws;
     const size_t n = (size_t)std::max(g->nv, 1);
