@@ -20,6 +20,7 @@
 #include "mg_device.cuh"
 
 #include <algorithm>
+#include <utility>
 #include <cstring>
 #include <memory>
 
@@ -459,12 +460,15 @@ __device__ __forceinline__ void sym_flush(unsigned long long *sums, unsigned lon
 // caller CSR -> engine CSR for up to two 4-byte edge arrays; the first is
 // mapped through old2new when map_ids (column ids).  With sums, the
 // symmetry checksum of (caller row, caller column, second array) is formed
-// on the way.
+// on the way.  A non-zero *skip (caller row offsets that differ from the
+// layout's, found by k_rows_differ earlier on the stream) returns at once:
+// the positions would not match the staged arrays.
 __global__ void k_relabel_edges(int32_t n, int32_t m, const int32_t *new2old, const int32_t *old2new,
                                 const int32_t *o_row, const int32_t *row_new, const int32_t *pos_row,
                                 const uint32_t *src0, uint32_t *dst0, const uint32_t *src1, uint32_t *dst1,
-                                int map_ids, unsigned long long *sums)
+                                int map_ids, unsigned long long *sums, const unsigned long long *skip)
 {
+    if (skip && __ldcg(skip) != 0ull) return;
     const int lane = threadIdx.x & 31;
     const int32_t nsteps = (m + 31) / 32;
     const int32_t gwarp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -496,6 +500,16 @@ __global__ void k_relabel_edges(int32_t n, int32_t m, const int32_t *new2old, co
         }
     }
     if (sums) sym_flush(sums, s_lo, s_hi);
+}
+
+// *differ = 1 when the staged caller row offsets a differ from b (the
+// offsets the current layout was built from)
+__global__ void k_rows_differ(int32_t n1, const int32_t *a, const int32_t *b, unsigned long long *differ)
+{
+    int d = 0;
+    for (int32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n1; i += gridDim.x * blockDim.x)
+        d |= __ldcs(&a[i]) != __ldcs(&b[i]);
+    if (__syncthreads_or(d) && threadIdx.x == 0) *differ = 1ull;
 }
 
 // symmetry checksum of a CSR without relabeling (rows below the hub
@@ -572,17 +586,24 @@ __global__ void k_cc_label_old(int32_t n, const int32_t *parent, const int32_t *
         out[v] = minold[parent[old2new[v]]];
 }
 
-static mg_status relabel_device(mg_graph *g, unsigned long long *sym_sums = nullptr)
+// engine CSR (col, wt) from caller-order arrays with the current layout's
+// positions; the optional pair checksum and skip word as k_relabel_edges
+static mg_status relabel_device(mg_graph *g, const mgi::DevBuf &src_row, const mgi::DevBuf &src_col,
+                                const mgi::DevBuf &src_wt, unsigned long long *sym_sums = nullptr,
+                                const unsigned long long *skip = nullptr)
 {
     if (g->ne == 0) return MG_OK;
     const int grid = g->num_sms * 8;
-    MG_TRY(dev_alloc(g->pos_row, ((size_t)g->ne / 32 + 2) * 4));
-    k_pos_rows<<<grid, 256, 0, g->stream>>>(g->nv, g->ne, g->row.as<int32_t>(), g->pos_row.as<int32_t>());
+    if (!g->pos_valid) {  // once per layout
+        MG_TRY(dev_alloc(g->pos_row, ((size_t)g->ne / 32 + 2) * 4));
+        k_pos_rows<<<grid, 256, 0, g->stream>>>(g->nv, g->ne, g->row.as<int32_t>(), g->pos_row.as<int32_t>());
+        g->pos_valid = true;
+    }
     k_relabel_edges<<<grid, 256, 0, g->stream>>>(g->nv, g->ne, g->new2old.as<int32_t>(), g->old2new.as<int32_t>(),
-                                                 g->o_row.as<int32_t>(), g->row.as<int32_t>(),
-                                                 g->pos_row.as<int32_t>(), g->o_col.as<uint32_t>(),
-                                                 g->col.as<uint32_t>(), g->o_wt.as<uint32_t>(), g->wt.as<uint32_t>(),
-                                                 1, sym_sums);
+                                                 src_row.as<int32_t>(), g->row.as<int32_t>(),
+                                                 g->pos_row.as<int32_t>(), src_col.as<uint32_t>(),
+                                                 g->col.as<uint32_t>(), src_wt.as<uint32_t>(), g->wt.as<uint32_t>(),
+                                                 1, sym_sums, skip);
     MG_CUDA(cudaGetLastError());
     return MG_OK;
 }
@@ -666,7 +687,8 @@ mg_status edges_to_engine(mg_graph *g, const void *src_caller, void *dst_engine)
     k_relabel_edges<<<g->num_sms * 8, 256, 0, g->stream>>>(g->nv, g->ne, g->new2old.as<int32_t>(), nullptr,
                                                            g->o_row.as<int32_t>(), g->row.as<int32_t>(),
                                                            g->pos_row.as<int32_t>(), (const uint32_t *)src_caller,
-                                                           (uint32_t *)dst_engine, nullptr, nullptr, 0, nullptr);
+                                                           (uint32_t *)dst_engine, nullptr, nullptr, 0, nullptr,
+                                                           nullptr);
     MG_CUDA(cudaGetLastError());
     return MG_OK;
 }
@@ -750,7 +772,8 @@ static mg_status upload_arrays(mg_graph *g, const mg_host_graph *h, const HostLa
             MG_CUDA(cudaMemcpyAsync(g->o_wt.p, h->ev.data(), m * 4, cudaMemcpyHostToDevice, s));
         }
         g->nv = h->nv;
-        MG_TRY(relabel_device(g));
+        g->pos_valid = false;  // new engine row offsets
+        MG_TRY(relabel_device(g, g->o_row, g->o_col, g->o_wt));
     } else {
         MG_CUDA(cudaMemcpyAsync(g->row.p, h->v.data(), (n + 1) * 4, cudaMemcpyHostToDevice, s));
         if (m) {
@@ -791,7 +814,8 @@ static void destroy_graph(mg_graph *g)
     DevBuf *bufs[] = {&g->row, &g->col, &g->wt, &g->trow_own, &g->tcol_own, &g->twt_own,
                       &g->hchunk, &g->hrows, &g->hrow_chunk, &g->fw, &g->o_fw, &g->ppr_hchunk, &g->ppr_hrows,
                       &g->ppr_hrow_chunk, &g->o_row, &g->o_col, &g->o_wt, &g->old2new, &g->new2old,
-                      &g->wrows, &g->trows, &g->pos_row, &g->sym_sums};
+                      &g->wrows, &g->trows, &g->pos_row, &g->sym_sums, &g->s_row,
+                      &g->s_col, &g->s_wt};
     for (DevBuf *b : bufs) dev_free(*b);
     for (DevBuf &b : g->res_out) dev_free(b);
     if (g->pinned_flag) cudaFreeHost(g->pinned_flag);
@@ -849,11 +873,10 @@ mg_status mg_graph_upload(const mg_host_graph *h, int32_t device, mg_graph **out
     MG_CUDA(cudaEventCreateWithFlags(&g->ev_staged, cudaEventDisableTiming));
     MG_CUDA(cudaEventCreateWithFlags(&g->ev_consumed, cudaEventDisableTiming));
     MG_CUDA(cudaMallocHost(&g->pinned_flag, 64));
-    MG_CUDA(cudaMallocHost(&g->sym_host, 16));
+    MG_CUDA(cudaMallocHost(&g->sym_host, 24));
     HostLayout L;
     build_layout(*h, L);
     MG_TRY(upload_arrays(g.get(), h, L, true));
-    g->h_row = h->v;
     MG_CUDA(cudaEventRecord(g->ev_consumed, g->stream));
     *out = g.release();
     return MG_OK;
@@ -866,17 +889,17 @@ mg_status mg_graph_stage(mg_graph *g, const mg_host_graph *h)
     if (h->nv != g->nv || h->ne != g->ne) return fail(MG_ERR_INVALID, "staging needs the same nv/ne");
     MG_CUDA(cudaSetDevice(g->device));
     const size_t n = (size_t)h->nv, m = (size_t)h->ne;
-    // caller-order buffers: the relabel source of a relabeled graph, plain
-    // staging buffers otherwise
-    MG_TRY(dev_alloc(g->o_row, (n + 1) * 4));
-    MG_TRY(dev_alloc(g->o_col, std::max<size_t>(m, 4) * 4 + COL_PAD));
-    MG_TRY(dev_alloc(g->o_wt, std::max<size_t>(m, 4) * 4 + COL_PAD));
+    // staging buffers, separate from the current graph's caller-order
+    // arrays (o_*), which runs before the commit still read
+    MG_TRY(dev_alloc(g->s_row, (n + 1) * 4));
+    MG_TRY(dev_alloc(g->s_col, std::max<size_t>(m, 4) * 4 + COL_PAD));
+    MG_TRY(dev_alloc(g->s_wt, std::max<size_t>(m, 4) * 4 + COL_PAD));
     cudaStream_t cs = g->copy_stream;
     MG_CUDA(cudaStreamWaitEvent(cs, g->ev_consumed, 0));  // the last commit has read them
-    MG_CUDA(cudaMemcpyAsync(g->o_row.p, h->v.data(), (n + 1) * 4, cudaMemcpyHostToDevice, cs));
+    MG_CUDA(cudaMemcpyAsync(g->s_row.p, h->v.data(), (n + 1) * 4, cudaMemcpyHostToDevice, cs));
     if (m) {
-        MG_CUDA(cudaMemcpyAsync(g->o_col.p, h->e.data(), m * 4, cudaMemcpyHostToDevice, cs));
-        MG_CUDA(cudaMemcpyAsync(g->o_wt.p, h->ev.data(), m * 4, cudaMemcpyHostToDevice, cs));
+        MG_CUDA(cudaMemcpyAsync(g->s_col.p, h->e.data(), m * 4, cudaMemcpyHostToDevice, cs));
+        MG_CUDA(cudaMemcpyAsync(g->s_wt.p, h->ev.data(), m * 4, cudaMemcpyHostToDevice, cs));
     }
     MG_CUDA(cudaEventRecord(g->ev_staged, cs));
     g->staged_h = h;
@@ -894,40 +917,48 @@ mg_status mg_graph_commit(mg_graph *g)
     cudaStream_t s = g->stream;
     MG_CUDA(cudaStreamWaitEvent(s, g->ev_staged, 0));
     const size_t n = (size_t)h->nv, m = (size_t)h->ne;
-    const bool same_degrees = g->h_row.size() == n + 1 &&
-                              std::memcmp(g->h_row.data(), h->v.data(), (n + 1) * 4) == 0;
-    if (!same_degrees || !(g->symmetric && g->weights_symmetric)) {
-        // new degrees or a transposed copy to rebuild: lay the graph out
-        // again (with the graph's current, possibly tuned, bin parameters)
+    if (!(g->symmetric && g->weights_symmetric)) {
+        // a transposed copy to rebuild: lay the graph out again (with the
+        // graph's current, possibly tuned, bin parameters)
         HostLayout L;
         build_layout(*h, L, g->heavy_deg, g->hchunk_size, g->tbin);
         MG_TRY(upload_arrays(g, h, L, true));
-        g->h_row = h->v;
     } else {
-        // the layout assumes symmetric edges and weights: check the staged
-        // input with the pair checksum (formed during the relabel pass) and
-        // lay it out again from the host when it is not
-        MG_TRY(dev_alloc(g->sym_sums, 16));
+        // the layout assumes the caller row offsets it was built from and
+        // symmetric edges and weights: compare the offsets on the device,
+        // check the staged input with the pair checksum (formed during the
+        // relabel pass), read both back in one copy and lay the graph out
+        // again from the host when either fails
+        MG_TRY(dev_alloc(g->sym_sums, 24));
         unsigned long long *sums = g->sym_sums.as<unsigned long long>();
-        MG_CUDA(cudaMemsetAsync(sums, 0, 16, s));
+        MG_CUDA(cudaMemsetAsync(sums, 0, 24, s));
+        const int32_t *ref_row = g->relabeled ? g->o_row.as<int32_t>() : g->row.as<int32_t>();
+        k_rows_differ<<<g->num_sms * 4, 256, 0, s>>>((int32_t)n + 1, g->s_row.as<int32_t>(), ref_row, sums + 2);
+        MG_CUDA(cudaGetLastError());
         if (g->relabeled) {
-            MG_TRY(relabel_device(g, sums));  // engine CSR from the staged caller-order arrays
+            // engine CSR from the staged caller-order arrays
+            MG_TRY(relabel_device(g, g->s_row, g->s_col, g->s_wt, sums, sums + 2));
         } else {
-            MG_CUDA(cudaMemcpyAsync(g->row.p, g->o_row.p, (n + 1) * 4, cudaMemcpyDeviceToDevice, s));
+            MG_CUDA(cudaMemcpyAsync(g->row.p, g->s_row.p, (n + 1) * 4, cudaMemcpyDeviceToDevice, s));
             if (m) {
-                MG_CUDA(cudaMemcpyAsync(g->col.p, g->o_col.p, m * 4, cudaMemcpyDeviceToDevice, s));
-                MG_CUDA(cudaMemcpyAsync(g->wt.p, g->o_wt.p, m * 4, cudaMemcpyDeviceToDevice, s));
+                MG_CUDA(cudaMemcpyAsync(g->col.p, g->s_col.p, m * 4, cudaMemcpyDeviceToDevice, s));
+                MG_CUDA(cudaMemcpyAsync(g->wt.p, g->s_wt.p, m * 4, cudaMemcpyDeviceToDevice, s));
             }
             k_sym_check<<<g->num_sms * 8, 256, 0, s>>>(g->nv, g->row.as<int32_t>(), g->col.as<int32_t>(),
                                                        g->wt.as<int32_t>(), sums);
             MG_CUDA(cudaGetLastError());
         }
-        MG_CUDA(cudaMemcpyAsync(g->sym_host, sums, 16, cudaMemcpyDeviceToHost, s));
+        MG_CUDA(cudaMemcpyAsync(g->sym_host, sums, 24, cudaMemcpyDeviceToHost, s));
         MG_CUDA(cudaStreamSynchronize(s));
-        if (g->sym_host[0] != g->sym_host[1]) {
+        if (g->sym_host[2] != 0 || g->sym_host[0] != g->sym_host[1]) {
             HostLayout L;
             build_layout(*h, L, g->heavy_deg, g->hchunk_size, g->tbin);
             MG_TRY(upload_arrays(g, h, L, true));
+        } else if (g->relabeled) {
+            // the staged arrays are now the current graph's caller-order CSR
+            std::swap(g->o_row, g->s_row);
+            std::swap(g->o_col, g->s_col);
+            std::swap(g->o_wt, g->s_wt);
         }
     }
     MG_CUDA(cudaEventRecord(g->ev_consumed, s));

@@ -103,8 +103,8 @@ struct mg_graph {
     cudaStream_t copy_stream = nullptr;
     cudaEvent_t ev_staged = nullptr, ev_consumed = nullptr;
     const mg_host_graph *staged_h = nullptr;
-    std::vector<int32_t> h_row;    // caller-order row offsets the layout was built from
-    mgi::DevBuf sym_sums;          // pair checksum of a committed input (2 x uint64)
+    mgi::DevBuf s_row, s_col, s_wt; // staged next input (caller order); swapped with o_* on commit
+    mgi::DevBuf sym_sums;          // commit checks: pair checksum (2 x uint64), rows-differ word
     unsigned long long *sym_host = nullptr;  // pinned readback of sym_sums
     int32_t nv = 0, ne = 0;
     bool symmetric = true;         // transpose == graph (pull uses the same arrays)
@@ -144,6 +144,7 @@ struct mg_graph {
     mgi::DevBuf o_fw;                      // float weights in caller CSR order
     mgi::DevBuf old2new, new2old;          // int32 [nv]
     mgi::DevBuf pos_row;                   // int32 [ne/32 + 2]: engine row of position 32k
+    bool pos_valid = false;                // pos_row follows the current row offsets
     std::vector<int32_t> h_old2new;        // host copy for mapping sources
     mgi::DevBuf res_out[8];                // results in the caller's ids
     // per-algorithm workspaces

@@ -91,3 +91,35 @@ def test_stage_commit_errors():
         g.stage(other)
     assert e.value.status == mg.MG_ERR_INVALID
     g.free()
+
+
+def test_weighted_runs_between_stage_and_commit():
+    """Runs between mg_graph_stage and mg_graph_commit use the current
+    graph's caller-order arrays (the staged copy goes to separate buffers)."""
+    h0 = mg.HostGraph.rmat(11, 16, seed=33)
+    rp, col, wt = h0.arrays()
+    og0 = O.csr_from_arrays(rp, col, wt)
+    h1, og1 = _csr(*_permuted(rp, col, wt, 7))
+    rng = np.random.default_rng(9)
+    w0 = rng.uniform(0.05, 1.0, og0.ne).astype(np.float32)
+    w1 = rng.uniform(0.05, 1.0, og1.ne).astype(np.float32)
+    g = mg.Graph(h0)
+    g.stage(h1)
+    g.set_float_weights(w0)                     # weights of the current graph
+    x0, _ = g.wpagerank(tol=1e-7)
+    ref0 = O.wpr_f64(og0, w0.astype(np.float64), 0.85, 1e-13)[0]
+    assert float(np.max(np.abs(x0 - ref0))) < 1e-6
+    g.commit()
+    g.set_float_weights(w1)
+    x1, _ = g.wpagerank(tol=1e-7)
+    ref1 = O.wpr_f64(og1, w1.astype(np.float64), 0.85, 1e-13)[0]
+    assert float(np.max(np.abs(x1 - ref1))) < 1e-6
+    # the same structure again: the fast path (relabel only) then weights
+    g.stage(h1)
+    g.commit()
+    g.set_float_weights(w1)
+    x2, _ = g.wpagerank(tol=1e-7)
+    assert np.array_equal(x1, x2)
+    d, _ = g.sssp(5)
+    assert np.array_equal(d, O.sssp(og1, 5)[0])
+    g.free()
