@@ -36,6 +36,12 @@
 // with the per-vertex score bc[u] += sum of delta_s[u] over the entry's
 // sources (u excluded as its own source).
 //
+// On low-degree graphs (average degree <= 8) both pull kernels first give
+// each row / entry with at most 8 edges and at most 4 sources at this level
+// to one thread, which forms the same per-source sums in the same edge
+// order (a lattice level is mostly such rows, with one source each, so a
+// warp per row left 31 lanes idle); the rest go to the warp path above.
+//
 // Every sum runs in a fixed order (the warp's edge order, then chunk order),
 // so results do not depend on scheduling; path counts are integers in FP64
 // and exact up to 2^53.  The column stream and the frontier-mask gathers are
@@ -53,6 +59,12 @@ namespace {
 constexpr int W = 32;                 // sources per group (one per lane)
 constexpr int THREADS = 256;
 constexpr int32_t MARK_HEAVY = 2048;  // frontier entries above this out-degree are marked by the whole grid
+// rows with at most TDEG edges whose level touches at most TBITS sources are
+// handled by one thread (low-degree graphs: a lattice row has four or five
+// edges and usually one source per level); the rest by a warp, lane per source
+constexpr int TDEG = 8;
+constexpr int TBITS = 4;
+constexpr int TP_AVG_DEG = 8;  // graphs up to this average degree use the thread path
 
 struct BbCtl {
     int32_t more;
@@ -267,6 +279,37 @@ __device__ __forceinline__ void settle_row(const BbArgs &a, uint32_t *fnext, int
     }
 }
 
+// One thread, one row v with at most TDEG in-edges: per source s in the
+// sources that reach v at this level (at most TBITS of them, else false is
+// returned and the row goes to the warp path), the sum of sig over the
+// in-neighbours on s's frontier, in edge order as pull_span forms it.
+__device__ __forceinline__ bool pull_row_thread(const BbArgs &a, const uint32_t *fcur, uint32_t *fnext, int32_t v,
+                                                uint32_t want)
+{
+    const int32_t b = a.trow[v], e = a.trow[v + 1];
+    if (e - b > TDEG) return false;
+    uint32_t newm = 0;
+    for (int32_t p = b; p < e; p++) newm |= fcur[__ldg(&a.tcol[p])];
+    newm &= want;
+    if (__popc(newm) > TBITS) return false;
+    if (newm == 0) return true;
+    uint32_t mm = newm;
+    while (mm) {  // the row's edges again per source (L1 hits)
+        const int s = __ffs(mm) - 1;
+        mm &= mm - 1;
+        double acc = 0.0;
+        for (int32_t p = b; p < e; p++) {
+            const int32_t u = __ldg(&a.tcol[p]);
+            if ((fcur[u] >> s) & 1u) acc += a.sig[(size_t)u * W + s];
+        }
+        a.sig[(size_t)v * W + s] = acc;
+    }
+    a.vis[v] |= newm;
+    fnext[v] = newm;
+    return true;
+}
+
+template <bool TP>
 __global__ void __launch_bounds__(THREADS) k_bb_pull(BbArgs a)
 {
     const BbCtl c = *a.ctl;
@@ -277,15 +320,44 @@ __global__ void __launch_bounds__(THREADS) k_bb_pull(BbArgs a)
     const uint32_t *fcur = fm_of(a, c.cur);
     uint32_t *fnext = fm_of(a, c.cur ^ 1);
     const int32_t nrows = c.dense ? a.n : c.ncand;
-    for (int32_t i = gwarp; i < nrows; i += nwarps) {
-        const int32_t v = c.dense ? i : a.cand[i];
-        const uint32_t want = ~a.vis[v] & c.gmask;
-        if (want == 0) continue;
-        const int32_t b = a.trow[v], e = a.trow[v + 1];
-        if (e - b > a.heavy_deg) continue;  // chunk path below
-        uint32_t newm;
-        const double acc = pull_span(a, fcur, b, e, want, newm);
-        if (newm) settle_row(a, fnext, v, newm, acc);
+    if constexpr (TP) {
+        // up to 32 rows per warp, one per lane; rows the thread path
+        // declines are then pulled by the whole warp, one at a time
+        const int vpw = entries_per_warp(nrows, nwarps, 32);
+        for (int32_t base = gwarp * vpw; base < nrows; base += nwarps * vpw) {
+            const int32_t i = base + lane;
+            int32_t v = 0;
+            uint32_t want = 0;
+            bool deferred = false;
+            if (lane < vpw && i < nrows) {
+                v = c.dense ? i : a.cand[i];
+                want = ~a.vis[v] & c.gmask;
+                if (want) deferred = !pull_row_thread(a, fcur, fnext, v, want);
+            }
+            unsigned dm = __ballot_sync(0xffffffffu, deferred);
+            while (dm) {
+                const int j = __ffs(dm) - 1;
+                dm &= dm - 1;
+                const int32_t vj = __shfl_sync(0xffffffffu, v, j);
+                const uint32_t wj = __shfl_sync(0xffffffffu, want, j);
+                const int32_t b = a.trow[vj], e = a.trow[vj + 1];
+                if (e - b > a.heavy_deg) continue;  // chunk path below
+                uint32_t newm;
+                const double acc = pull_span(a, fcur, b, e, wj, newm);
+                if (newm) settle_row(a, fnext, vj, newm, acc);
+            }
+        }
+    } else {
+        for (int32_t i = gwarp; i < nrows; i += nwarps) {  // a warp per row
+            const int32_t v = c.dense ? i : a.cand[i];
+            const uint32_t want = ~a.vis[v] & c.gmask;
+            if (want == 0) continue;
+            const int32_t b = a.trow[v], e = a.trow[v + 1];
+            if (e - b > a.heavy_deg) continue;  // chunk path below
+            uint32_t newm;
+            const double acc = pull_span(a, fcur, b, e, want, newm);
+            if (newm) settle_row(a, fnext, v, newm, acc);
+        }
     }
     for (int32_t ch = gwarp; ch < a.nhchunks; ch += nwarps) {
         const int32_t v = a.hchunk[3 * ch], b = a.hchunk[3 * ch + 1], e = a.hchunk[3 * ch + 2];
@@ -460,6 +532,35 @@ __device__ __forceinline__ void back_finish(const BbArgs &a, int32_t u, uint32_t
     if (lane == 0) a.bc[u] += contrib;
 }
 
+// One thread, one level-L entry (u, msk) with at most TDEG out-edges and
+// at most TBITS sources: back_span and back_finish for each source of the
+// entry in turn (the same sums in the same edge order; the entry's score
+// contributions are added in source order).
+__device__ __forceinline__ bool back_entry_thread(const BbArgs &a, const uint32_t *nxt, int32_t u, uint32_t msk)
+{
+    if (__popc(msk) > TBITS) return false;
+    const int32_t b = a.row[u], e = a.row[u + 1];
+    if (e - b > TDEG) return false;
+    double contrib = 0.0;
+    uint32_t mm = msk;
+    while (mm) {
+        const int s = __ffs(mm) - 1;
+        mm &= mm - 1;
+        float acc = 0.0f;
+        for (int32_t p = b; p < e; p++) {
+            const int32_t v = __ldg(&a.col[p]);
+            if ((nxt[v] >> s) & 1u) acc += a.q[(size_t)v * W + s];
+        }
+        const double sg = a.sig[(size_t)u * W + s];
+        const float dv = (float)(sg * (double)acc);
+        a.q[(size_t)u * W + s] = (float)((1.0 + (double)dv) / sg);
+        if (a.src[s] != u) contrib += (double)dv;
+    }
+    a.bc[u] += contrib;
+    return true;
+}
+
+template <bool TP>
 __global__ void __launch_bounds__(THREADS) k_bbb_pull(BbArgs a)
 {
     const BbCtl c = *a.ctl;
@@ -469,13 +570,42 @@ __global__ void __launch_bounds__(THREADS) k_bbb_pull(BbArgs a)
     const int nwarps = (gridDim.x * blockDim.x) >> 5;
     const uint32_t *cur = fm_of(a, c.L & 1);
     const uint32_t *nxt = fm_of(a, (c.L + 1) & 1);
-    for (int32_t i = a.off[c.L] + gwarp; i < a.off[c.L + 1]; i += nwarps) {
-        const int32_t u = a.arch[i];
-        const uint32_t msk = a.amask[i];
-        const int32_t b = a.row[u], e = a.row[u + 1];
-        if (e - b > a.heavy_deg) continue;  // chunk path below
-        const float s = back_span(a, nxt, a.col, b, e, msk);
-        back_finish(a, u, msk, s);
+    if constexpr (TP) {
+        const int32_t lo = a.off[c.L], hi = a.off[c.L + 1];
+        // up to 32 entries per warp, one per lane; entries the thread path
+        // declines are then handled by the whole warp (lane per source)
+        const int vpw = entries_per_warp(hi - lo, nwarps, 32);
+        for (int32_t base = lo + gwarp * vpw; base < hi; base += nwarps * vpw) {
+            const int32_t i = base + lane;
+            int32_t u = 0;
+            uint32_t msk = 0;
+            bool deferred = false;
+            if (lane < vpw && i < hi) {
+                u = a.arch[i];
+                msk = a.amask[i];
+                deferred = !back_entry_thread(a, nxt, u, msk);
+            }
+            unsigned dm = __ballot_sync(0xffffffffu, deferred);
+            while (dm) {
+                const int j = __ffs(dm) - 1;
+                dm &= dm - 1;
+                const int32_t uj = __shfl_sync(0xffffffffu, u, j);
+                const uint32_t mj = __shfl_sync(0xffffffffu, msk, j);
+                const int32_t b = a.row[uj], e = a.row[uj + 1];
+                if (e - b > a.heavy_deg) continue;  // chunk path below
+                const float sj = back_span(a, nxt, a.col, b, e, mj);
+                back_finish(a, uj, mj, sj);
+            }
+        }
+    } else {
+        for (int32_t i = a.off[c.L] + gwarp; i < a.off[c.L + 1]; i += nwarps) {  // a warp per entry
+            const int32_t u = a.arch[i];
+            const uint32_t msk = a.amask[i];
+            const int32_t b = a.row[u], e = a.row[u + 1];
+            if (e - b > a.heavy_deg) continue;  // chunk path below
+            const float s = back_span(a, nxt, a.col, b, e, msk);
+            back_finish(a, u, msk, s);
+        }
     }
     // heavy rows: the in-row chunks double as out-row chunks (symmetric graphs)
     float *hp = reinterpret_cast<float *>(a.hpart);
@@ -612,6 +742,19 @@ mg_status bc_batched(mg_graph *g, const int32_t *src_engine, int32_t nsrc, const
     MG_CUDA(cudaMemsetAsync(a.bc, 0, n * 8, s));
     MG_CUDA(cudaMemsetAsync(a.cbm, 0, words * 4, s));
     const int grid = launch_grid(g, THREADS, 8);
+    // Low-degree graphs (average degree <= TP_AVG_DEG, e.g. lattices: a row
+    // of four or five edges, usually one source per level) take the pull
+    // kernels with the thread path; their grids are what stays resident
+    // (the thread path costs registers), so no CTA waits for a second wave.
+    // Denser graphs keep one warp per row at eight CTAs per SM.
+    const bool tp = (int64_t)g->ne <= (int64_t)TP_AVG_DEG * g->nv;
+    int occ_f = 8, occ_b = 8;
+    if (tp) {
+        MG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_f, k_bb_pull<true>, THREADS, 0));
+        MG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_b, k_bbb_pull<true>, THREADS, 0));
+    }
+    const int grid_f = launch_grid(g, THREADS, std::max(1, std::min(8, occ_f)));
+    const int grid_b = launch_grid(g, THREADS, std::max(1, std::min(8, occ_b)));
     const int alpha = opt.alpha > 0 ? opt.alpha : 15;
     const int max_levels = g->nv + 2;
     Profiler &P = g->prof;
@@ -624,7 +767,8 @@ mg_status bc_batched(mg_graph *g, const int32_t *src_engine, int32_t nsrc, const
         k_bb_mark<<<grid, THREADS, 0, st>>>(a);
         P.end();
         P.begin(s_pull);
-        k_bb_pull<<<grid, THREADS, 0, st>>>(a);
+        if (tp) k_bb_pull<true><<<grid_f, THREADS, 0, st>>>(a);
+        else k_bb_pull<false><<<grid_f, THREADS, 0, st>>>(a);
         P.end();
         P.begin(s_heavy);
         k_bb_heavy<<<grid, THREADS, 0, st>>>(a);
@@ -643,7 +787,8 @@ mg_status bc_batched(mg_graph *g, const int32_t *src_engine, int32_t nsrc, const
         k_bbb_scatter<<<grid, THREADS, 0, st>>>(a);
         P.end();
         P.begin(s_bp);
-        k_bbb_pull<<<grid, THREADS, 0, st>>>(a);
+        if (tp) k_bbb_pull<true><<<grid_b, THREADS, 0, st>>>(a);
+        else k_bbb_pull<false><<<grid_b, THREADS, 0, st>>>(a);
         P.end();
         P.begin(s_bh);
         k_bbb_heavy<<<grid, THREADS, 0, st>>>(a);
@@ -657,7 +802,7 @@ mg_status bc_batched(mg_graph *g, const int32_t *src_engine, int32_t nsrc, const
     uint64_t key = 0x6263622d66776400ull;
     const void *ptrs[] = {a.row, a.col, a.trow, a.tcol, a.vis, a.fm0, a.arch, a.sig, a.q, a.hpart, a.bc, a.ctl};
     for (const void *p : ptrs) key = (key ^ (uint64_t)(uintptr_t)p) * 1099511628211ull;
-    key ^= (uint64_t)grid << 48;
+    key ^= (uint64_t)grid << 48 ^ (uint64_t)grid_f << 32 ^ (uint64_t)grid_b << 16;
     const int mode = opt.profile ? MG_EXEC_HOST : opt.exec;
     int32_t levels = 0, dense_levels = 0;
     for (int32_t g0 = 0; g0 < nsrc; g0 += W) {

@@ -172,3 +172,33 @@ def test_multi_graph_batch():
         assert np.array_equal(lv, O.bfs(og, s))
         assert np.array_equal(lab, O.cc_minlabel(og))
     b.free()
+
+
+@pytest.mark.parametrize("exec_mode", [None, mg.EXEC_HOST])
+def test_bc_multi_low_degree_mixed_paths(exec_mode):
+    """A low-degree graph (thread-per-row path) with rows above the
+    thread path's degree limit, a heavy row, and clustered sources whose
+    levels carry many sources at once (both declined to the warp path)."""
+    h0 = mg.HostGraph.lattice(30, 30, 0.05, seed=8)
+    rp, col, _ = h0.arrays()
+    n = len(rp) - 1
+    src = np.repeat(np.arange(n, dtype=np.int64), np.diff(rp))
+    rng = np.random.default_rng(8)
+    extra_s, extra_d = [], []
+    for hub, deg in ((5, 12), (450, 20), (899, 600)):   # deg 12 / 20 rows, one heavy row
+        nb = rng.choice(n, deg, replace=False)
+        nb = nb[nb != hub]
+        extra_s += [hub] * len(nb)
+        extra_d += list(nb)
+    s_all = np.concatenate([src, np.array(extra_s), np.array(extra_d)])
+    d_all = np.concatenate([col.astype(np.int64), np.array(extra_d), np.array(extra_s)])
+    h = mg.HostGraph.from_entries(n, s_all, d_all)
+    g, og = _pair(h)
+    assert og.ne <= 8 * og.nv
+    sources = list(range(100, 140)) + [5, 450, 899, 7]   # 44 sources: two groups
+    kw = {} if exec_mode is None else {"exec": exec_mode}
+    bc, _ = g.bc_multi(sources, **kw)
+    ref = O.bc_multi_f64(og, sources)
+    err = float(np.max(np.abs(bc.astype(np.float64) - ref)) / np.max(np.abs(ref)))
+    assert err < 1e-5, err
+    g.free()
