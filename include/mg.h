@@ -135,9 +135,12 @@ mg_status mg_graph_reload(mg_graph *dg, const mg_host_graph *g);
 /* Double-buffered input: mg_graph_stage starts copying g (same nv/ne) into
  * the device graph's staging buffers on the graph's copy stream and returns
  * at once, so the copy overlaps runs still working on the current graph;
- * g must stay alive and unchanged until mg_graph_commit.  mg_graph_commit
- * makes later runs wait for the copy and rebuilds the device CSR from it on
- * the graph's stream.  No reference counterpart. */
+ * g must stay alive and unchanged until mg_graph_commit.  Runs (and
+ * mg_graph_set_float_weights) between the two calls use the current graph;
+ * the staged copy has buffers of its own.  mg_graph_commit makes later runs
+ * wait for the copy and rebuilds the device CSR from it on the graph's
+ * stream (row offsets compared on the device; a relabel pass when they
+ * match the layout's).  No reference counterpart. */
 mg_status mg_graph_stage(mg_graph *dg, const mg_host_graph *g);
 mg_status mg_graph_commit(mg_graph *dg);
 /* Replaces release_MultiGraph (release_structure.cu:4). */

@@ -13,7 +13,8 @@
 //   archive  (vertex, mask) entries, grouped by level: entry (v, M) at
 //            level d means v is at distance d from exactly the sources in M
 //
-// Forward level d -> d+1 (five launches, looped by a CUDA-graph WHILE node):
+// Forward level d -> d+1 (three launches, four with heavy rows, looped by a
+// CUDA-graph WHILE node):
 //   k_bb_mark     sparse levels only: frontier entries scan their out-edges
 //                 and collect the distinct candidate destinations (a vertex
 //                 not yet reached by some source of the entry's mask)
@@ -23,18 +24,20 @@
 //                 lanes that hit (ballot), and lane s adds sig[u*32+s] for
 //                 each hit of source s.  Rows above heavy_deg go in 2048-edge
 //                 chunks whose partials land in hpart.
-//   k_bb_heavy    folds the chunk partials of heavy rows in chunk order
+//   k_bb_heavy    (graphs with heavy rows) folds the chunk partials of heavy
+//                 rows in chunk order
 //   k_bb_compact  archives the new frontier (one atomic per warp), sums its
 //                 out-degrees for the direction switch, clears the old
-//                 frontier's masks
-//   k_bb_decide   next level, sparse/dense choice (Beamer: frontier
-//                 out-edges x alpha against m), loop condition
-// Backward level L (four launches): the level-L masks are scattered into a
-// dense array, every level-L entry sums q over successors whose level-(L+1)
-// mask shares the source, and lane s finishes
+//                 frontier's masks; the last block to finish decides the
+//                 next level (sparse/dense: Beamer, frontier out-edges x
+//                 alpha against m) and the loop condition
+// Backward level L (two launches, three with heavy rows): level l's masks
+// sit in a dense array fm[l % 3]; every level-L entry sums q over
+// successors whose level-(L+1) mask shares the source, and lane s finishes
 //   delta_s[u] = sig_s[u] * sum,  q_s[u] = (1 + delta_s[u]) / sig_s[u]
 // with the per-vertex score bc[u] += sum of delta_s[u] over the entry's
-// sources (u excluded as its own source).
+// sources (u excluded as its own source); k_bbb_next then clears level
+// L+1's masks, scatters level L-1's into the third buffer and steps L.
 //
 // On low-degree graphs (average degree <= 8) both pull kernels first give
 // each row / entry with at most 8 edges and at most 4 sources at this level
@@ -85,6 +88,7 @@ struct BbCtl {
     int32_t dense_levels;
     unsigned long long nfe;      // out-edges of level d+1 (atomic)
     unsigned long long nfe_cur;  // out-edges of level d
+    int32_t done;                // blocks finished (last-block-done step of the level's final kernel)
 };
 
 struct BbArgs {
@@ -98,7 +102,7 @@ struct BbArgs {
     int32_t nhrows;
     int32_t heavy_deg;
     uint32_t *vis;
-    uint32_t *fm0, *fm1;
+    uint32_t *fm0, *fm1, *fm2;   // frontier masks: forward fm0/fm1, backward level l in fm[l % 3]
     uint32_t *cbm;               // candidate bitmap (sparse levels)
     int32_t *cand;
     int32_t *arch;
@@ -116,6 +120,38 @@ struct BbArgs {
 };
 
 __device__ __forceinline__ uint32_t *fm_of(const BbArgs &a, int i) { return i ? a.fm1 : a.fm0; }
+__device__ __forceinline__ uint32_t *fmb_of(const BbArgs &a, int32_t l)
+{
+    const int32_t r = l % 3;
+    return r == 0 ? a.fm0 : (r == 1 ? a.fm1 : a.fm2);
+}
+
+// the control block as other blocks left it (L2, not a stale L1 line)
+__device__ __forceinline__ BbCtl load_ctl_l2(const BbCtl *cp)
+{
+    BbCtl c;
+    const int *src = reinterpret_cast<const int *>(cp);
+    int *dst = reinterpret_cast<int *>(&c);
+#pragma unroll
+    for (int k = 0; k < (int)(sizeof(BbCtl) / 4); k++) dst[k] = __ldcg(src + k);
+    return c;
+}
+
+// true in one thread of the last block of the grid to get here (every
+// block's earlier writes and atomics are visible to it)
+__device__ __forceinline__ bool last_block_done(int32_t *done)
+{
+    __shared__ int s_last;
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) s_last = atomicAdd(done, 1) == (int)gridDim.x - 1;
+    __syncthreads();
+    if (s_last && threadIdx.x == 0) {
+        __threadfence();
+        return true;
+    }
+    return false;
+}
 
 __device__ __forceinline__ unsigned long long warp_sum_u64(unsigned long long x)
 {
@@ -392,11 +428,16 @@ __global__ void __launch_bounds__(THREADS) k_bb_heavy(BbArgs a)
     }
 }
 
-__global__ void __launch_bounds__(THREADS) k_bb_compact(BbArgs a)
+// Archives level d+1 and, in the last block to finish, decides the next
+// level (Beamer's direction test, loop condition)
+__global__ void __launch_bounds__(THREADS) k_bb_compact(BbArgs a, cudaGraphConditionalHandle h, int use_cond)
 {
     BbCtl *cp = a.ctl;
     const BbCtl c = *cp;
-    if (c.more == 0) return;
+    if (c.more == 0) {
+        if (blockIdx.x == 0 && threadIdx.x == 0 && use_cond) cudaGraphSetConditional(h, 0u);
+        return;
+    }
     const int lane = mgd::lane();
     const int gtid = blockIdx.x * blockDim.x + threadIdx.x;
     const int gwarp = gtid >> 5;
@@ -433,62 +474,58 @@ __global__ void __launch_bounds__(THREADS) k_bb_compact(BbArgs a)
         const unsigned long long s = warp_sum_u64((unsigned long long)deg);
         if (lane == 0 && s) atomicAdd(&cp->nfe, s);
     }
-}
-
-__global__ void k_bb_decide(BbArgs a, cudaGraphConditionalHandle h, int use_cond)
-{
-    if (threadIdx.x != 0) return;
-    BbCtl *cp = a.ctl;
-    BbCtl c = *cp;
-    if (c.more) {
-        const int32_t nnew = c.nnew;
-        a.off[c.d + 2] = a.off[c.d + 1] + nnew;
-        if (nnew == 0 || c.status) {
-            c.more = 0;
-            c.nlevels = c.d + 1;
-        } else if (c.d + 2 >= c.max_levels) {
-            c.more = 0;
-            c.status = 1;
-            c.nlevels = c.d + 2;
-        } else {
-            c.d += 1;
-            c.cur ^= 1;
-            c.nfe_cur = c.nfe;
-            c.nfh = c.nfh_build;
-            if (c.dirmode == MG_DIR_PUSH) c.dense = 0;
-            else if (c.dirmode == MG_DIR_PULL) c.dense = 1;
-            else c.dense = c.nfe_cur * (unsigned long long)c.alpha > (unsigned long long)a.m;
-            c.dense_levels += c.dense;
-        }
-        c.nfe = 0;
-        c.nnew = 0;
-        c.ncand = 0;
-        c.nfh_build = 0;
-        *cp = c;
+    if (!last_block_done(&cp->done)) return;
+    BbCtl n = load_ctl_l2(cp);
+    const int32_t nnew = n.nnew;
+    a.off[n.d + 2] = a.off[n.d + 1] + nnew;
+    if (nnew == 0 || n.status) {
+        n.more = 0;
+        n.nlevels = n.d + 1;
+    } else if (n.d + 2 >= n.max_levels) {
+        n.more = 0;
+        n.status = 1;
+        n.nlevels = n.d + 2;
+    } else {
+        n.d += 1;
+        n.cur ^= 1;
+        n.nfe_cur = n.nfe;
+        n.nfh = n.nfh_build;
+        if (n.dirmode == MG_DIR_PUSH) n.dense = 0;
+        else if (n.dirmode == MG_DIR_PULL) n.dense = 1;
+        else n.dense = n.nfe_cur * (unsigned long long)n.alpha > (unsigned long long)a.m;
+        n.dense_levels += n.dense;
     }
-    if (use_cond) cudaGraphSetConditional(h, c.more ? 1u : 0u);
+    n.nfe = 0;
+    n.nnew = 0;
+    n.ncand = 0;
+    n.nfh_build = 0;
+    n.done = 0;
+    *cp = n;
+    if (use_cond) cudaGraphSetConditional(h, n.more ? 1u : 0u);
 }
 
 // ---------------------------------------------------------------------------
 // backward
 // ---------------------------------------------------------------------------
-__global__ void k_bbb_init(BbArgs a)
-{
-    if (threadIdx.x != 0) return;
-    BbCtl *cp = a.ctl;
-    cp->L = cp->nlevels - 1;
-    cp->more = cp->status == 0 && cp->L >= 1;
-}
-
-// level-L masks into fm[L & 1] (zero before this launch)
-__global__ void __launch_bounds__(THREADS) k_bbb_scatter(BbArgs a)
+// Backward start: L = deepest level; the masks of levels L and L-1 into
+// their buffers (all three are zero after the forward sweep).
+__global__ void k_bbb_start(BbArgs a)
 {
     const BbCtl c = *a.ctl;
-    if (c.more == 0) return;
-    uint32_t *cur = fm_of(a, c.L & 1);
-    for (int32_t i = a.off[c.L] + blockIdx.x * blockDim.x + threadIdx.x; i < a.off[c.L + 1];
-         i += gridDim.x * blockDim.x)
-        cur[a.arch[i]] = a.amask[i];
+    const int32_t L = c.nlevels - 1;
+    const bool run = c.status == 0 && L >= 1;
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        a.ctl->L = L;
+        a.ctl->more = run;
+        a.ctl->done = 0;
+    }
+    if (!run) return;
+    const int32_t stride = gridDim.x * blockDim.x;
+    for (int32_t l = L - 1; l <= L; l++) {
+        uint32_t *buf = fmb_of(a, l);
+        for (int32_t i = a.off[l] + blockIdx.x * blockDim.x + threadIdx.x; i < a.off[l + 1]; i += stride)
+            buf[a.arch[i]] = a.amask[i];
+    }
 }
 
 // successors' q summed for the sources in `want`: out-edges [b, e)
@@ -568,8 +605,8 @@ __global__ void __launch_bounds__(THREADS) k_bbb_pull(BbArgs a)
     const int lane = mgd::lane();
     const int gwarp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int nwarps = (gridDim.x * blockDim.x) >> 5;
-    const uint32_t *cur = fm_of(a, c.L & 1);
-    const uint32_t *nxt = fm_of(a, (c.L + 1) & 1);
+    const uint32_t *cur = fmb_of(a, c.L);
+    const uint32_t *nxt = fmb_of(a, c.L + 1);
     if constexpr (TP) {
         const int32_t lo = a.off[c.L], hi = a.off[c.L + 1];
         // up to 32 entries per warp, one per lane; entries the thread path
@@ -617,16 +654,15 @@ __global__ void __launch_bounds__(THREADS) k_bbb_pull(BbArgs a)
     }
 }
 
+// heavy rows: chunk partials folded in chunk order (graphs with heavy rows)
 __global__ void __launch_bounds__(THREADS) k_bbb_heavy(BbArgs a)
 {
     const BbCtl c = *a.ctl;
     if (c.more == 0) return;
     const int lane = mgd::lane();
-    const int gtid = blockIdx.x * blockDim.x + threadIdx.x;
-    const int gwarp = gtid >> 5;
+    const int gwarp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int nwarps = (gridDim.x * blockDim.x) >> 5;
-    const uint32_t *cur = fm_of(a, c.L & 1);
-    uint32_t *nxt = fm_of(a, (c.L + 1) & 1);
+    const uint32_t *cur = fmb_of(a, c.L);
     const float *hp = reinterpret_cast<const float *>(a.hpart);
     for (int32_t i = gwarp; i < a.nhrows; i += nwarps) {
         const int32_t u = a.hrows[i];
@@ -636,20 +672,33 @@ __global__ void __launch_bounds__(THREADS) k_bbb_heavy(BbArgs a)
         for (int32_t k = a.hrow_chunk[i]; k < a.hrow_chunk[i + 1]; k++) s += hp[(size_t)k * W + lane];
         back_finish(a, u, msk, s);
     }
-    // level L+1 is no longer read: clear its masks for level L-1
-    for (int32_t i = a.off[c.L + 1] + gtid; i < a.off[c.L + 2]; i += gridDim.x * blockDim.x) nxt[a.arch[i]] = 0;
 }
 
-__global__ void k_bbb_decide(BbArgs a, cudaGraphConditionalHandle h, int use_cond)
+// End of backward level L: level L+1's masks are no longer read (cleared),
+// level L-1's go into their buffer ((L-1) % 3, cleared at the end of level
+// L+1), and the last block to finish steps to L-1.
+__global__ void __launch_bounds__(THREADS) k_bbb_next(BbArgs a, cudaGraphConditionalHandle h, int use_cond)
 {
-    if (threadIdx.x != 0) return;
     BbCtl *cp = a.ctl;
-    int more = cp->more;
-    if (more) {
-        cp->L -= 1;
-        more = cp->L >= 1;
-        cp->more = more;
+    const BbCtl c = *cp;
+    if (c.more == 0) {
+        if (blockIdx.x == 0 && threadIdx.x == 0 && use_cond) cudaGraphSetConditional(h, 0u);
+        return;
     }
+    const int32_t stride = gridDim.x * blockDim.x;
+    const int32_t gtid = blockIdx.x * blockDim.x + threadIdx.x;
+    uint32_t *nxt = fmb_of(a, c.L + 1);
+    for (int32_t i = a.off[c.L + 1] + gtid; i < a.off[c.L + 2]; i += stride) nxt[a.arch[i]] = 0;
+    if (c.L >= 2) {
+        uint32_t *prv = fmb_of(a, c.L - 1);
+        for (int32_t i = a.off[c.L - 1] + gtid; i < a.off[c.L]; i += stride) prv[a.arch[i]] = a.amask[i];
+    }
+    if (!last_block_done(&cp->done)) return;
+    const int32_t L = __ldcg(&cp->L) - 1;
+    const int more = L >= 1;
+    cp->L = L;
+    cp->more = more;
+    cp->done = 0;
     if (use_cond) cudaGraphSetConditional(h, more ? 1u : 0u);
 }
 
@@ -696,7 +745,7 @@ mg_status bc_batched(mg_graph *g, const int32_t *src_engine, int32_t nsrc, const
     const size_t cap = n * W;
     const size_t nch = (size_t)std::max(g->nhchunks, 1);
     MG_TRY(dev_alloc(w->vis, n * 4));
-    MG_TRY(dev_alloc(w->fm, 2 * n * 4));
+    MG_TRY(dev_alloc(w->fm, 3 * n * 4));
     MG_TRY(dev_alloc(w->cbm, words * 4));
     MG_TRY(dev_alloc(w->cand, n * 4));
     MG_TRY(dev_alloc(w->arch, cap * 4));
@@ -722,7 +771,7 @@ mg_status bc_batched(mg_graph *g, const int32_t *src_engine, int32_t nsrc, const
     a.hrows = g->hrows.as<int32_t>(); a.hrow_chunk = g->hrow_chunk.as<int32_t>(); a.nhrows = g->nhrows;
     a.heavy_deg = g->heavy_deg;
     a.vis = w->vis.as<uint32_t>();
-    a.fm0 = w->fm.as<uint32_t>(); a.fm1 = a.fm0 + n;
+    a.fm0 = w->fm.as<uint32_t>(); a.fm1 = a.fm0 + n; a.fm2 = a.fm1 + n;
     a.cbm = w->cbm.as<uint32_t>();
     a.cand = w->cand.as<int32_t>();
     a.arch = w->arch.as<int32_t>();
@@ -757,11 +806,12 @@ mg_status bc_batched(mg_graph *g, const int32_t *src_engine, int32_t nsrc, const
     const int grid_b = launch_grid(g, THREADS, std::max(1, std::min(8, occ_b)));
     const int alpha = opt.alpha > 0 ? opt.alpha : 15;
     const int max_levels = g->nv + 2;
+    // heavy-row folds only on graphs that have heavy rows
+    const bool heavy = g->nhrows > 0;
     Profiler &P = g->prof;
     const int s_mark = P.slot("bcb_mark"), s_pull = P.slot("bcb_pull"), s_heavy = P.slot("bcb_heavy");
-    const int s_comp = P.slot("bcb_compact"), s_dec = P.slot("bcb_decide");
-    const int s_bsc = P.slot("bcb_back_scatter"), s_bp = P.slot("bcb_back"), s_bh = P.slot("bcb_back_heavy");
-    const int s_bd = P.slot("bcb_back_decide");
+    const int s_comp = P.slot("bcb_compact_decide");
+    const int s_bp = P.slot("bcb_back"), s_bh = P.slot("bcb_back_heavy"), s_bn = P.slot("bcb_back_next");
     BodyFn fwd = [&](cudaStream_t st, cudaGraphConditionalHandle h, int use_cond) -> mg_status {
         P.begin(s_mark);
         k_bb_mark<<<grid, THREADS, 0, st>>>(a);
@@ -770,31 +820,29 @@ mg_status bc_batched(mg_graph *g, const int32_t *src_engine, int32_t nsrc, const
         if (tp) k_bb_pull<true><<<grid_f, THREADS, 0, st>>>(a);
         else k_bb_pull<false><<<grid_f, THREADS, 0, st>>>(a);
         P.end();
-        P.begin(s_heavy);
-        k_bb_heavy<<<grid, THREADS, 0, st>>>(a);
-        P.end();
+        if (heavy) {
+            P.begin(s_heavy);
+            k_bb_heavy<<<grid, THREADS, 0, st>>>(a);
+            P.end();
+        }
         P.begin(s_comp);
-        k_bb_compact<<<grid, THREADS, 0, st>>>(a);
-        P.end();
-        P.begin(s_dec);
-        k_bb_decide<<<1, 32, 0, st>>>(a, h, use_cond);
+        k_bb_compact<<<grid, THREADS, 0, st>>>(a, h, use_cond);
         P.end();
         MG_CUDA(cudaGetLastError());
         return MG_OK;
     };
     BodyFn bwd = [&](cudaStream_t st, cudaGraphConditionalHandle h, int use_cond) -> mg_status {
-        P.begin(s_bsc);
-        k_bbb_scatter<<<grid, THREADS, 0, st>>>(a);
-        P.end();
         P.begin(s_bp);
         if (tp) k_bbb_pull<true><<<grid_b, THREADS, 0, st>>>(a);
         else k_bbb_pull<false><<<grid_b, THREADS, 0, st>>>(a);
         P.end();
-        P.begin(s_bh);
-        k_bbb_heavy<<<grid, THREADS, 0, st>>>(a);
-        P.end();
-        P.begin(s_bd);
-        k_bbb_decide<<<1, 32, 0, st>>>(a, h, use_cond);
+        if (heavy) {
+            P.begin(s_bh);
+            k_bbb_heavy<<<grid, THREADS, 0, st>>>(a);
+            P.end();
+        }
+        P.begin(s_bn);
+        k_bbb_next<<<grid, THREADS, 0, st>>>(a, h, use_cond);
         P.end();
         MG_CUDA(cudaGetLastError());
         return MG_OK;
@@ -802,18 +850,18 @@ mg_status bc_batched(mg_graph *g, const int32_t *src_engine, int32_t nsrc, const
     uint64_t key = 0x6263622d66776400ull;
     const void *ptrs[] = {a.row, a.col, a.trow, a.tcol, a.vis, a.fm0, a.arch, a.sig, a.q, a.hpart, a.bc, a.ctl};
     for (const void *p : ptrs) key = (key ^ (uint64_t)(uintptr_t)p) * 1099511628211ull;
-    key ^= (uint64_t)grid << 48 ^ (uint64_t)grid_f << 32 ^ (uint64_t)grid_b << 16;
+    key ^= (uint64_t)grid << 48 ^ (uint64_t)grid_f << 32 ^ (uint64_t)grid_b << 16 ^ (uint64_t)heavy;
     const int mode = opt.profile ? MG_EXEC_HOST : opt.exec;
     int32_t levels = 0, dense_levels = 0;
     for (int32_t g0 = 0; g0 < nsrc; g0 += W) {
         const int32_t cnt = std::min<int32_t>(W, nsrc - g0);
         MG_CUDA(cudaMemcpyAsync(w->src.p, src_engine + g0, (size_t)cnt * 4, cudaMemcpyHostToDevice, s));
         MG_CUDA(cudaMemsetAsync(a.vis, 0, n * 4, s));
-        MG_CUDA(cudaMemsetAsync(a.fm0, 0, 2 * n * 4, s));
+        MG_CUDA(cudaMemsetAsync(a.fm0, 0, 3 * n * 4, s));
         k_bb_init<<<1, 32, 0, s>>>(a, cnt, opt.direction, alpha, max_levels);
         MG_CUDA(cudaGetLastError());
         MG_TRY(run_loop(mode, opt.profile != 0, s, w->fwd, key, fwd, &a.ctl->more, g->pinned_flag, max_levels + 2));
-        k_bbb_init<<<1, 32, 0, s>>>(a);
+        k_bbb_start<<<grid, THREADS, 0, s>>>(a);
         MG_CUDA(cudaGetLastError());
         MG_TRY(run_loop(mode, opt.profile != 0, s, w->bwd, key ^ 0x5a5a, bwd, &a.ctl->more, g->pinned_flag,
                         max_levels + 2));
