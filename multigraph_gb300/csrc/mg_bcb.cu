@@ -8,8 +8,11 @@
 //
 //   vis[v]   bit s set once v has been reached from source s
 //   fm[v]    bit s set when v is on source s's current frontier
-//   sig[v*32+s]  FP64 path count of v from source s
-//   q[v*32+s]    (1 + delta_s[v]) / sig_s[v]   (FP32, backward)
+//   sig[v*32+s]  path count of v from source s (mgops::PathCount: FP64
+//                mantissa m and a 2^512 scale k; plain FP64 until a count
+//                reaches 2^512, then the run repeats in extended mode)
+//   q[v*32+s]    (1 + delta_s[v]) / m   (backward; FP32 with plain counts,
+//                FP64 with extended ones)
 //   archive  (vertex, mask) entries, grouped by level: entry (v, M) at
 //            level d means v is at distance d from exactly the sources in M
 //
@@ -52,8 +55,10 @@
 // one traversal per source.
 
 #include "mg_device.cuh"
+#include "mg_ops.cuh"
 
 #include <algorithm>
+#include <type_traits>
 #include <cstring>
 #include <vector>
 
@@ -89,6 +94,7 @@ struct BbCtl {
     unsigned long long nfe;      // out-edges of level d+1 (atomic)
     unsigned long long nfe_cur;  // out-edges of level d
     int32_t done;                // blocks finished (last-block-done step of the level's final kernel)
+    int32_t ovf;                 // a plain-mode path count reached 2^512 (ends the sweep)
 };
 
 struct BbArgs {
@@ -109,9 +115,10 @@ struct BbArgs {
     uint32_t *amask;
     size_t cap;                  // archive capacity (32 n)
     int32_t *off;                // level offsets into the archive
-    double *sig;
-    float *q;
-    double *hpart;               // per chunk x 32 lanes (backward reuses it as float)
+    mgops::PathCount *sig;
+    void *q;                     // float (plain counts) or double (extended) per (v, source)
+    mgops::PathCount *hpart;     // per chunk x 32 lanes (backward reuses it as double)
+    int32_t ext;                 // extended path counts
     uint32_t *hmask;
     double *bc;                  // score accumulator (all groups)
     int32_t *fheavy;
@@ -170,7 +177,7 @@ __global__ void k_bb_init(BbArgs a, int32_t nsrc, int32_t dirmode, int32_t alpha
     const int32_t v = valid ? a.src[lane] : -1 - lane;
     const uint32_t same = __match_any_sync(0xffffffffu, v);
     const bool leader = valid && lane == __ffs(same) - 1;
-    if (valid) a.sig[(size_t)v * W + lane] = 1.0;
+    if (valid) a.sig[(size_t)v * W + lane] = mgops::pc_one();
     const uint32_t leaders = __ballot_sync(0xffffffffu, leader);
     unsigned long long deg = 0;
     int heavy = 0;
@@ -277,11 +284,13 @@ __global__ void __launch_bounds__(THREADS) k_bb_mark(BbArgs a)
 // One row's in-edges [b, e) against the frontier masks: lane s returns the
 // sum of sig over in-neighbours on source s's frontier; *hit gets the union
 // of the masks that hit (restricted to `want`).
-__device__ __forceinline__ double pull_span(const BbArgs &a, const uint32_t *fcur, int32_t b, int32_t e,
-                                            uint32_t want, uint32_t &hit)
+template <bool EXT>
+__device__ __forceinline__ mgops::PathCount pull_span(const BbArgs &a, const uint32_t *fcur, int32_t b, int32_t e,
+                                                      uint32_t want, uint32_t &hit)
 {
     const int lane = mgd::lane();
-    double acc = 0.0;
+    mgops::PathCount acc = mgops::pc_zero();  // extended counts
+    double accp = 0.0;                        // plain counts
     uint32_t newm = 0;
     for (int32_t base = b; base < e; base += 32) {
         const int32_t p = base + lane;
@@ -298,17 +307,25 @@ __device__ __forceinline__ double pull_span(const BbArgs &a, const uint32_t *fcu
             const int32_t uj = __shfl_sync(0xffffffffu, u, j);
             const uint32_t fj = __shfl_sync(0xffffffffu, f, j);
             newm |= fj;
-            if ((fj >> lane) & 1u) acc += a.sig[(size_t)uj * W + lane];
+            if ((fj >> lane) & 1u) {
+                if (EXT) acc = mgops::pc_add(acc, a.sig[(size_t)uj * W + lane], true);
+                else accp += a.sig[(size_t)uj * W + lane].m;
+            }
         }
     }
     hit = newm;
+    if (!EXT) acc.m = accp;
     return acc;
 }
 
-__device__ __forceinline__ void settle_row(const BbArgs &a, uint32_t *fnext, int32_t v, uint32_t newm, double acc)
+__device__ __forceinline__ void settle_row(const BbArgs &a, uint32_t *fnext, int32_t v, uint32_t newm,
+                                           mgops::PathCount acc)
 {
     const int lane = mgd::lane();
-    if ((newm >> lane) & 1u) a.sig[(size_t)v * W + lane] = acc;
+    if ((newm >> lane) & 1u) {
+        a.sig[(size_t)v * W + lane] = acc;
+        if (!a.ext && acc.m >= mgops::PC_PLAIN_MAX) a.ctl->ovf = 1;
+    }
     if (lane == 0) {
         a.vis[v] |= newm;
         fnext[v] = newm;
@@ -333,19 +350,20 @@ __device__ __forceinline__ bool pull_row_thread(const BbArgs &a, const uint32_t 
     while (mm) {  // the row's edges again per source (L1 hits)
         const int s = __ffs(mm) - 1;
         mm &= mm - 1;
-        double acc = 0.0;
+        mgops::PathCount acc = mgops::pc_zero();
         for (int32_t p = b; p < e; p++) {
             const int32_t u = __ldg(&a.tcol[p]);
-            if ((fcur[u] >> s) & 1u) acc += a.sig[(size_t)u * W + s];
+            if ((fcur[u] >> s) & 1u) acc = mgops::pc_add(acc, a.sig[(size_t)u * W + s], a.ext != 0);
         }
         a.sig[(size_t)v * W + s] = acc;
+        if (!a.ext && acc.m >= mgops::PC_PLAIN_MAX) a.ctl->ovf = 1;
     }
     a.vis[v] |= newm;
     fnext[v] = newm;
     return true;
 }
 
-template <bool TP>
+template <bool TP, bool EXT>
 __global__ void __launch_bounds__(THREADS) k_bb_pull(BbArgs a)
 {
     const BbCtl c = *a.ctl;
@@ -379,7 +397,7 @@ __global__ void __launch_bounds__(THREADS) k_bb_pull(BbArgs a)
                 const int32_t b = a.trow[vj], e = a.trow[vj + 1];
                 if (e - b > a.heavy_deg) continue;  // chunk path below
                 uint32_t newm;
-                const double acc = pull_span(a, fcur, b, e, wj, newm);
+                const mgops::PathCount acc = pull_span<EXT>(a, fcur, b, e, wj, newm);
                 if (newm) settle_row(a, fnext, vj, newm, acc);
             }
         }
@@ -391,7 +409,7 @@ __global__ void __launch_bounds__(THREADS) k_bb_pull(BbArgs a)
             const int32_t b = a.trow[v], e = a.trow[v + 1];
             if (e - b > a.heavy_deg) continue;  // chunk path below
             uint32_t newm;
-            const double acc = pull_span(a, fcur, b, e, want, newm);
+            const mgops::PathCount acc = pull_span<EXT>(a, fcur, b, e, want, newm);
             if (newm) settle_row(a, fnext, v, newm, acc);
         }
     }
@@ -400,8 +418,8 @@ __global__ void __launch_bounds__(THREADS) k_bb_pull(BbArgs a)
         uint32_t want = ~a.vis[v] & c.gmask;
         if (!c.dense && !mgd::bm_test(a.cbm, v)) want = 0;
         uint32_t newm = 0;
-        double acc = 0.0;
-        if (want) acc = pull_span(a, fcur, b, e, want, newm);
+        mgops::PathCount acc = mgops::pc_zero();
+        if (want) acc = pull_span<EXT>(a, fcur, b, e, want, newm);
         if (newm) a.hpart[(size_t)ch * W + lane] = acc;
         if (lane == 0) a.hmask[ch] = newm;
     }
@@ -418,11 +436,11 @@ __global__ void __launch_bounds__(THREADS) k_bb_heavy(BbArgs a)
     for (int32_t i = gwarp; i < a.nhrows; i += nwarps) {
         const int32_t v = a.hrows[i], k0 = a.hrow_chunk[i], k1 = a.hrow_chunk[i + 1];
         uint32_t newm = 0;
-        double acc = 0.0;
+        mgops::PathCount acc = mgops::pc_zero();
         for (int32_t k = k0; k < k1; k++) {
             const uint32_t hm = a.hmask[k];
             newm |= hm;
-            if ((hm >> lane) & 1u) acc += a.hpart[(size_t)k * W + lane];
+            if ((hm >> lane) & 1u) acc = mgops::pc_add(acc, a.hpart[(size_t)k * W + lane], a.ext != 0);
         }
         if (newm) settle_row(a, fnext, v, newm, acc);
     }
@@ -478,7 +496,7 @@ __global__ void __launch_bounds__(THREADS) k_bb_compact(BbArgs a, cudaGraphCondi
     BbCtl n = load_ctl_l2(cp);
     const int32_t nnew = n.nnew;
     a.off[n.d + 2] = a.off[n.d + 1] + nnew;
-    if (nnew == 0 || n.status) {
+    if (nnew == 0 || n.status || n.ovf) {  // (a path-count overflow ends the sweep for a rerun)
         n.more = 0;
         n.nlevels = n.d + 1;
     } else if (n.d + 2 >= n.max_levels) {
@@ -513,7 +531,7 @@ __global__ void k_bbb_start(BbArgs a)
 {
     const BbCtl c = *a.ctl;
     const int32_t L = c.nlevels - 1;
-    const bool run = c.status == 0 && L >= 1;
+    const bool run = c.status == 0 && c.ovf == 0 && L >= 1;
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         a.ctl->L = L;
         a.ctl->more = run;
@@ -528,12 +546,32 @@ __global__ void k_bbb_start(BbArgs a)
     }
 }
 
-// successors' q summed for the sources in `want`: out-edges [b, e)
-__device__ __forceinline__ float back_span(const BbArgs &a, const uint32_t *nxt, const int32_t *col, int32_t b,
-                                           int32_t e, uint32_t want)
+template <bool EXT>
+using QT = typename std::conditional<EXT, double, float>::type;
+
+template <bool EXT>
+__device__ __forceinline__ QT<EXT> *q_of(const BbArgs &a)
+{
+    return reinterpret_cast<QT<EXT> *>(a.q);
+}
+
+// successor v's term for lane s of an entry whose count has scale ku
+template <bool EXT>
+__device__ __forceinline__ QT<EXT> back_term(const BbArgs &a, int32_t v, int s, int32_t ku)
+{
+    QT<EXT> t = q_of<EXT>(a)[(size_t)v * W + s];
+    if (EXT) t *= (QT<EXT>)mgops::pc_scale(ku - a.sig[(size_t)v * W + s].k);
+    return t;
+}
+
+// successors' q summed for the sources in `want`: out-edges [b, e); ku is
+// this lane's scale of the entry's path count
+template <bool EXT>
+__device__ __forceinline__ QT<EXT> back_span(const BbArgs &a, const uint32_t *nxt, const int32_t *col, int32_t b,
+                                             int32_t e, uint32_t want, int32_t ku)
 {
     const int lane = mgd::lane();
-    float acc = 0.0f;
+    QT<EXT> acc = 0;
     for (int32_t base = b; base < e; base += 32) {
         const int32_t p = base + lane;
         int32_t v = 0;
@@ -548,20 +586,29 @@ __device__ __forceinline__ float back_span(const BbArgs &a, const uint32_t *nxt,
             hits &= hits - 1;
             const int32_t vj = __shfl_sync(0xffffffffu, v, j);
             const uint32_t fj = __shfl_sync(0xffffffffu, f, j);
-            if ((fj >> lane) & 1u) acc += a.q[(size_t)vj * W + lane];
+            if ((fj >> lane) & 1u) acc += back_term<EXT>(a, vj, lane, ku);
         }
     }
     return acc;
 }
 
-__device__ __forceinline__ void back_finish(const BbArgs &a, int32_t u, uint32_t msk, float s)
+// lane's scale of u's path count (0 in plain mode)
+template <bool EXT>
+__device__ __forceinline__ int32_t lane_scale(const BbArgs &a, int32_t u, uint32_t msk)
+{
+    const int lane = mgd::lane();
+    return (EXT && ((msk >> lane) & 1u)) ? a.sig[(size_t)u * W + lane].k : 0;
+}
+
+template <bool EXT>
+__device__ __forceinline__ void back_finish(const BbArgs &a, int32_t u, uint32_t msk, QT<EXT> s)
 {
     const int lane = mgd::lane();
     double contrib = 0.0;
     if ((msk >> lane) & 1u) {
-        const double sg = a.sig[(size_t)u * W + lane];
+        const double sg = a.sig[(size_t)u * W + lane].m;
         const float dv = (float)(sg * (double)s);
-        a.q[(size_t)u * W + lane] = (float)((1.0 + (double)dv) / sg);
+        q_of<EXT>(a)[(size_t)u * W + lane] = (QT<EXT>)((1.0 + (double)dv) / sg);
         if (a.src[lane] != u) contrib = (double)dv;
     }
 #pragma unroll
@@ -573,6 +620,7 @@ __device__ __forceinline__ void back_finish(const BbArgs &a, int32_t u, uint32_t
 // at most TBITS sources: back_span and back_finish for each source of the
 // entry in turn (the same sums in the same edge order; the entry's score
 // contributions are added in source order).
+template <bool EXT>
 __device__ __forceinline__ bool back_entry_thread(const BbArgs &a, const uint32_t *nxt, int32_t u, uint32_t msk)
 {
     if (__popc(msk) > TBITS) return false;
@@ -583,21 +631,21 @@ __device__ __forceinline__ bool back_entry_thread(const BbArgs &a, const uint32_
     while (mm) {
         const int s = __ffs(mm) - 1;
         mm &= mm - 1;
-        float acc = 0.0f;
+        const mgops::PathCount su = a.sig[(size_t)u * W + s];
+        QT<EXT> acc = 0;
         for (int32_t p = b; p < e; p++) {
             const int32_t v = __ldg(&a.col[p]);
-            if ((nxt[v] >> s) & 1u) acc += a.q[(size_t)v * W + s];
+            if ((nxt[v] >> s) & 1u) acc += back_term<EXT>(a, v, s, su.k);
         }
-        const double sg = a.sig[(size_t)u * W + s];
-        const float dv = (float)(sg * (double)acc);
-        a.q[(size_t)u * W + s] = (float)((1.0 + (double)dv) / sg);
+        const float dv = (float)(su.m * (double)acc);
+        q_of<EXT>(a)[(size_t)u * W + s] = (QT<EXT>)((1.0 + (double)dv) / su.m);
         if (a.src[s] != u) contrib += (double)dv;
     }
     a.bc[u] += contrib;
     return true;
 }
 
-template <bool TP>
+template <bool TP, bool EXT>
 __global__ void __launch_bounds__(THREADS) k_bbb_pull(BbArgs a)
 {
     const BbCtl c = *a.ctl;
@@ -620,7 +668,7 @@ __global__ void __launch_bounds__(THREADS) k_bbb_pull(BbArgs a)
             if (lane < vpw && i < hi) {
                 u = a.arch[i];
                 msk = a.amask[i];
-                deferred = !back_entry_thread(a, nxt, u, msk);
+                deferred = !back_entry_thread<EXT>(a, nxt, u, msk);
             }
             unsigned dm = __ballot_sync(0xffffffffu, deferred);
             while (dm) {
@@ -630,8 +678,8 @@ __global__ void __launch_bounds__(THREADS) k_bbb_pull(BbArgs a)
                 const uint32_t mj = __shfl_sync(0xffffffffu, msk, j);
                 const int32_t b = a.row[uj], e = a.row[uj + 1];
                 if (e - b > a.heavy_deg) continue;  // chunk path below
-                const float sj = back_span(a, nxt, a.col, b, e, mj);
-                back_finish(a, uj, mj, sj);
+                const QT<EXT> sj = back_span<EXT>(a, nxt, a.col, b, e, mj, lane_scale<EXT>(a, uj, mj));
+                back_finish<EXT>(a, uj, mj, sj);
             }
         }
     } else {
@@ -640,22 +688,24 @@ __global__ void __launch_bounds__(THREADS) k_bbb_pull(BbArgs a)
             const uint32_t msk = a.amask[i];
             const int32_t b = a.row[u], e = a.row[u + 1];
             if (e - b > a.heavy_deg) continue;  // chunk path below
-            const float s = back_span(a, nxt, a.col, b, e, msk);
-            back_finish(a, u, msk, s);
+            const QT<EXT> s = back_span<EXT>(a, nxt, a.col, b, e, msk, lane_scale<EXT>(a, u, msk));
+            back_finish<EXT>(a, u, msk, s);
         }
     }
     // heavy rows: the in-row chunks double as out-row chunks (symmetric graphs)
-    float *hp = reinterpret_cast<float *>(a.hpart);
+    QT<EXT> *hp = reinterpret_cast<QT<EXT> *>(a.hpart);
     for (int32_t ch = gwarp; ch < a.nhchunks; ch += nwarps) {
         const int32_t u = a.hchunk[3 * ch];
         const uint32_t msk = cur[u];
         if (msk == 0) continue;
-        hp[(size_t)ch * W + lane] = back_span(a, nxt, a.tcol, a.hchunk[3 * ch + 1], a.hchunk[3 * ch + 2], msk);
+        hp[(size_t)ch * W + lane] = back_span<EXT>(a, nxt, a.tcol, a.hchunk[3 * ch + 1], a.hchunk[3 * ch + 2], msk,
+                                                   lane_scale<EXT>(a, u, msk));
     }
 }
 
 // heavy rows: chunk partials folded in chunk order (graphs with heavy rows)
-__global__ void __launch_bounds__(THREADS) k_bbb_heavy(BbArgs a)
+template <bool EXT>
+__global__ void __launch_bounds__(THREADS, 8) k_bbb_heavy(BbArgs a)
 {
     const BbCtl c = *a.ctl;
     if (c.more == 0) return;
@@ -663,14 +713,14 @@ __global__ void __launch_bounds__(THREADS) k_bbb_heavy(BbArgs a)
     const int gwarp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int nwarps = (gridDim.x * blockDim.x) >> 5;
     const uint32_t *cur = fmb_of(a, c.L);
-    const float *hp = reinterpret_cast<const float *>(a.hpart);
+    const QT<EXT> *hp = reinterpret_cast<const QT<EXT> *>(a.hpart);
     for (int32_t i = gwarp; i < a.nhrows; i += nwarps) {
         const int32_t u = a.hrows[i];
         const uint32_t msk = cur[u];
         if (msk == 0) continue;
-        float s = 0.0f;
+        QT<EXT> s = 0;
         for (int32_t k = a.hrow_chunk[i]; k < a.hrow_chunk[i + 1]; k++) s += hp[(size_t)k * W + lane];
-        back_finish(a, u, msk, s);
+        back_finish<EXT>(a, u, msk, s);
     }
 }
 
@@ -751,9 +801,9 @@ mg_status bc_batched(mg_graph *g, const int32_t *src_engine, int32_t nsrc, const
     MG_TRY(dev_alloc(w->arch, cap * 4));
     MG_TRY(dev_alloc(w->amask, cap * 4));
     MG_TRY(dev_alloc(w->off, (n + 4) * 4));
-    MG_TRY(dev_alloc(w->sig, cap * 8));
-    MG_TRY(dev_alloc(w->q, cap * 4));
-    MG_TRY(dev_alloc(w->hpart, nch * W * 8));
+    MG_TRY(dev_alloc(w->sig, cap * sizeof(mgops::PathCount)));
+    MG_TRY(dev_alloc(w->q, cap * 8));
+    MG_TRY(dev_alloc(w->hpart, nch * W * sizeof(mgops::PathCount)));
     MG_TRY(dev_alloc(w->hmask, nch * 4));
     MG_TRY(dev_alloc(w->bc, n * 8));
     MG_TRY(dev_alloc(w->bcf, n * 4));
@@ -778,9 +828,10 @@ mg_status bc_batched(mg_graph *g, const int32_t *src_engine, int32_t nsrc, const
     a.amask = w->amask.as<uint32_t>();
     a.cap = cap;
     a.off = w->off.as<int32_t>();
-    a.sig = w->sig.as<double>();
-    a.q = w->q.as<float>();
-    a.hpart = w->hpart.as<double>();
+    a.sig = w->sig.as<mgops::PathCount>();
+    a.q = w->q.p;
+    a.hpart = w->hpart.as<mgops::PathCount>();
+    a.ext = g->bc_ext ? 1 : 0;
     a.hmask = w->hmask.as<uint32_t>();
     a.bc = w->bc.as<double>();
     a.fheavy = w->fheavy.as<int32_t>();
@@ -799,8 +850,10 @@ mg_status bc_batched(mg_graph *g, const int32_t *src_engine, int32_t nsrc, const
     const bool tp = (int64_t)g->ne <= (int64_t)TP_AVG_DEG * g->nv;
     int occ_f = 8, occ_b = 8;
     if (tp) {
-        MG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_f, k_bb_pull<true>, THREADS, 0));
-        MG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_b, k_bbb_pull<true>, THREADS, 0));
+        if (a.ext) MG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_f, k_bb_pull<true, true>, THREADS, 0));
+        else MG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_f, k_bb_pull<true, false>, THREADS, 0));
+        if (a.ext) MG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_b, k_bbb_pull<true, true>, THREADS, 0));
+        else MG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_b, k_bbb_pull<true, false>, THREADS, 0));
     }
     const int grid_f = launch_grid(g, THREADS, std::max(1, std::min(8, occ_f)));
     const int grid_b = launch_grid(g, THREADS, std::max(1, std::min(8, occ_b)));
@@ -817,8 +870,13 @@ mg_status bc_batched(mg_graph *g, const int32_t *src_engine, int32_t nsrc, const
         k_bb_mark<<<grid, THREADS, 0, st>>>(a);
         P.end();
         P.begin(s_pull);
-        if (tp) k_bb_pull<true><<<grid_f, THREADS, 0, st>>>(a);
-        else k_bb_pull<false><<<grid_f, THREADS, 0, st>>>(a);
+        if (a.ext) {
+            if (tp) k_bb_pull<true, true><<<grid_f, THREADS, 0, st>>>(a);
+            else k_bb_pull<false, true><<<grid_f, THREADS, 0, st>>>(a);
+        } else {
+            if (tp) k_bb_pull<true, false><<<grid_f, THREADS, 0, st>>>(a);
+            else k_bb_pull<false, false><<<grid_f, THREADS, 0, st>>>(a);
+        }
         P.end();
         if (heavy) {
             P.begin(s_heavy);
@@ -833,12 +891,18 @@ mg_status bc_batched(mg_graph *g, const int32_t *src_engine, int32_t nsrc, const
     };
     BodyFn bwd = [&](cudaStream_t st, cudaGraphConditionalHandle h, int use_cond) -> mg_status {
         P.begin(s_bp);
-        if (tp) k_bbb_pull<true><<<grid_b, THREADS, 0, st>>>(a);
-        else k_bbb_pull<false><<<grid_b, THREADS, 0, st>>>(a);
+        if (a.ext) {
+            if (tp) k_bbb_pull<true, true><<<grid_b, THREADS, 0, st>>>(a);
+            else k_bbb_pull<false, true><<<grid_b, THREADS, 0, st>>>(a);
+        } else {
+            if (tp) k_bbb_pull<true, false><<<grid_b, THREADS, 0, st>>>(a);
+            else k_bbb_pull<false, false><<<grid_b, THREADS, 0, st>>>(a);
+        }
         P.end();
         if (heavy) {
             P.begin(s_bh);
-            k_bbb_heavy<<<grid, THREADS, 0, st>>>(a);
+            if (a.ext) k_bbb_heavy<true><<<grid, THREADS, 0, st>>>(a);
+            else k_bbb_heavy<false><<<grid, THREADS, 0, st>>>(a);
             P.end();
         }
         P.begin(s_bn);
@@ -850,7 +914,8 @@ mg_status bc_batched(mg_graph *g, const int32_t *src_engine, int32_t nsrc, const
     uint64_t key = 0x6263622d66776400ull;
     const void *ptrs[] = {a.row, a.col, a.trow, a.tcol, a.vis, a.fm0, a.arch, a.sig, a.q, a.hpart, a.bc, a.ctl};
     for (const void *p : ptrs) key = (key ^ (uint64_t)(uintptr_t)p) * 1099511628211ull;
-    key ^= (uint64_t)grid << 48 ^ (uint64_t)grid_f << 32 ^ (uint64_t)grid_b << 16 ^ (uint64_t)heavy;
+    key ^= (uint64_t)grid << 48 ^ (uint64_t)grid_f << 32 ^ (uint64_t)grid_b << 16 ^ (uint64_t)heavy ^
+           (uint64_t)a.ext << 1;
     const int mode = opt.profile ? MG_EXEC_HOST : opt.exec;
     int32_t levels = 0, dense_levels = 0;
     for (int32_t g0 = 0; g0 < nsrc; g0 += W) {
@@ -870,6 +935,12 @@ mg_status bc_batched(mg_graph *g, const int32_t *src_engine, int32_t nsrc, const
         MG_CUDA(cudaStreamSynchronize(s));
         if (hc.status == 1) return fail(MG_ERR_ITER_LIMIT, "batched BC: level cap %d reached", max_levels);
         if (hc.status != 0) return fail(MG_ERR_CUDA, "batched BC: level archive overflow");
+        if (hc.ovf && !g->bc_ext) {
+            // a path count passed FP64's comfortable range: this graph's BC
+            // runs use extended path counts from now on, starting over here
+            g->bc_ext = true;
+            return bc_batched(g, src_engine, nsrc, opt, info, bc_dev);
+        }
         levels += hc.nlevels;
         dense_levels += hc.dense_levels;
     }

@@ -16,12 +16,20 @@
 
 namespace mgd {
 
+// lane exchange of a row value (built-in types; composite value types
+// provide their own shfl_xor_val, found by argument-dependent lookup)
+template <class T>
+__device__ __forceinline__ T shfl_xor_val(T v, int o)
+{
+    return __shfl_xor_sync(0xffffffffu, v, o);
+}
+
 // warp-wide xor reduction tree (fixed order)
 template <class Op>
 __device__ __forceinline__ typename Op::T warp_combine(const Op &op, typename Op::T v)
 {
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v = op.combine(v, __shfl_xor_sync(0xffffffffu, v, o));
+    for (int o = 16; o > 0; o >>= 1) v = op.combine(v, shfl_xor_val(v, o));
     return v;
 }
 

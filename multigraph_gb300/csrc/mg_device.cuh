@@ -108,6 +108,7 @@ struct mg_graph {
     unsigned long long *sym_host = nullptr;  // pinned readback of sym_sums
     int32_t nv = 0, ne = 0;
     bool symmetric = true;         // transpose == graph (pull uses the same arrays)
+    bool bc_ext = false;           // BC path counts overflowed plain FP64 once: extended from then on
     bool weights_symmetric = true; // weight of (u,v) == weight of (v,u)
     // CSR (push side, out-edges)
     mgi::DevBuf row, col, wt;

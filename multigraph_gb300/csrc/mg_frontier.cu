@@ -32,6 +32,7 @@
 #include "mg_ops.cuh"
 
 #include <algorithm>
+#include <type_traits>
 #include <cstdlib>
 #include <cstring>
 
@@ -42,8 +43,10 @@ constexpr int MODE_PUSH = 0, MODE_PULL = 1;
 constexpr int32_t PUSH_HEAVY = 4096;
 constexpr int THREADS = 256;
 constexpr int PTHREADS = 1024;  // persistent kernels: 2 CTAs of 1024 per SM (fewer barrier arrivals)
-// grid barrier words (2 + GRID_SYNC_GROUPS) + the error flag, rounded up
+// grid barrier words (2 + GRID_SYNC_GROUPS), the barrier error flag, the BC
+// path-count overflow flag, rounded up
 constexpr size_t BAR_BYTES = 4 * (2 + mgd::GRID_SYNC_GROUPS + 1 + 7);
+constexpr int OVF_WORD = 2 + mgd::GRID_SYNC_GROUPS + 1;
 
 struct FCtl {
     int32_t more;       // continue flag (host loop readback)
@@ -78,7 +81,9 @@ struct Args {
     int32_t nhchunks;
     int32_t heavy_deg;
     int32_t *label;
-    double *sigma;
+    mgops::PathCount *sigma;
+    int32_t bc_ext;      // BC path counts in extended mode (mgops::PathCount)
+    int32_t *bc_ovf;     // set when a plain-mode path count reaches 2^512
     uint32_t *bm;        // 3 * words
     uint32_t *visited;
     int32_t words;
@@ -150,8 +155,8 @@ __device__ __forceinline__ void emit_next(const Args &a, const FCtl &c, int next
 // push: one edge (u -> v) with the source's payload
 // ----------------------------------------------------------------------------
 template <int ALG>
-__device__ __forceinline__ bool push_edge(const Args &a, int it1, int32_t v, int32_t payload_i, double payload_d,
-                                          int32_t w, uint32_t *next_bm)
+__device__ __forceinline__ bool push_edge(const Args &a, int it1, int32_t v, int32_t payload_i,
+                                          mgops::PathCount payload_d, int32_t w, uint32_t *next_bm)
 {
     if (ALG == ALG_BFS) {
         if (mgd::bm_test(a.visited, v)) return false;
@@ -164,7 +169,7 @@ __device__ __forceinline__ bool push_edge(const Args &a, int it1, int32_t v, int
     } else {
         bool on_level;
         bool claimed = mgops::BcForward::fused_update_condition(&a.label[v], it1, on_level);
-        if (on_level) mgops::BcForward::accumulate(&a.sigma[v], payload_d);
+        if (on_level) mgops::BcForward::accumulate(&a.sigma[v], payload_d, a.bc_ext != 0, a.bc_ovf);
         if (claimed) mgd::bm_set(a.visited, v);
         return claimed;
     }
@@ -193,7 +198,8 @@ __device__ __forceinline__ void push_level(const Args &a, const FCtl &c, LevelCn
         int32_t u = __ldcg(&a.heavy[(size_t)c.hpar * a.n + h]);
         int32_t b = a.row[u], e = a.row[u + 1];
         int32_t pi = __ldcg(&a.label[u]);
-        double pd = (ALG == ALG_BC) ? __ldcg(&a.sigma[u]) : 0.0;
+        const mgops::PathCount pd = (ALG == ALG_BC) ? mgops::pc_load_cg(&a.sigma[u]) : mgops::pc_zero();
+        if (ALG == ALG_BC && !a.bc_ext && pd.m >= mgops::PC_PLAIN_MAX) *a.bc_ovf = 1;
         int32_t span = e - b;
         int32_t rounds = (span + gridDim.x * blockDim.x - 1) / (gridDim.x * blockDim.x);
         for (int r = 0; r < rounds; r++) {
@@ -218,14 +224,17 @@ __device__ __forceinline__ void push_level(const Args &a, const FCtl &c, LevelCn
     }
     for (int base = gwarp * vpw; base < c.qsize; base += nwarps * vpw) {
         int32_t u = -1, start = 0, deg = 0, pi = 0;
-        double pd = 0.0;
+        mgops::PathCount pd = mgops::pc_zero();
         if (lane < vpw && base + lane < c.qsize) {
             u = __ldcg(&a.queue[c.qoff + base + lane]);
             start = a.row[u];
             deg = a.row[u + 1] - start;
             if (deg > PUSH_HEAVY) deg = 0;
             pi = __ldcg(&a.label[u]);
-            if (ALG == ALG_BC) pd = __ldcg(&a.sigma[u]);
+            if (ALG == ALG_BC) {
+                pd = mgops::pc_load_cg(&a.sigma[u]);
+                if (!a.bc_ext && pd.m >= mgops::PC_PLAIN_MAX) *a.bc_ovf = 1;
+            }
         }
         int incl = mgd::warp_scan_incl(deg);
         int excl = incl - deg;
@@ -237,7 +246,7 @@ __device__ __forceinline__ void push_level(const Args &a, const FCtl &c, LevelCn
             int own = mgd::owner_lane(excl, kk);
             int32_t e = __shfl_sync(0xffffffffu, start, own) + (kk - __shfl_sync(0xffffffffu, excl, own));
             int32_t opi = __shfl_sync(0xffffffffu, pi, own);
-            double opd = __shfl_sync(0xffffffffu, pd, own);
+            const mgops::PathCount opd = (ALG == ALG_BC) ? mgops::shfl_val(pd, own) : pd;
             bool found = false;
             int32_t v = 0;
             if (k < total) {
@@ -300,24 +309,28 @@ struct PullOp<ALG_SSSP> : PullEmit {
 // BC forward: unvisited rows sum the path counts of frontier in-neighbours
 template <>
 struct PullOp<ALG_BC> : PullEmit {
-    using T = double;
+    using T = mgops::PathCount;
     static constexpr bool kRowAware = true;  // visited rows are skipped
     static constexpr bool kWeights = false;
     const uint32_t *fb;
     int it1;
-    __device__ T identity() const { return 0.0; }
+    __device__ T identity() const { return mgops::pc_zero(); }
     __device__ bool skip(int32_t v) const { return mgd::bm_test(a.visited, v); }
-    __device__ T edge(int32_t, int32_t, int32_t u, int32_t) const { return mgd::bm_test(fb, u) ? a.sigma[u] : 0.0; }
+    __device__ T edge(int32_t, int32_t, int32_t u, int32_t) const
+    {
+        return mgd::bm_test(fb, u) ? a.sigma[u] : mgops::pc_zero();
+    }
     __device__ T combine(T x, T y) const
     {
-        mgops::BcForward::accumulate_nonAtomics(x, y);
+        mgops::BcForward::accumulate_nonAtomics(x, y, a.bc_ext != 0);
         return x;
     }
     __device__ void finish(int32_t v, T s)
     {
-        if (s > 0.0) {
+        if (s.m > 0.0) {
             a.label[v] = it1;
             a.sigma[v] = s;
+            if (!a.bc_ext && s.m >= mgops::PC_PLAIN_MAX) *a.bc_ovf = 1;
             mgd::bm_set(a.visited, v);
             mgd::bm_set(next_bm, v);
         }
@@ -374,7 +387,7 @@ __global__ void __launch_bounds__(THREADS) k_pull(Args a)
 
     // heavy rows: one CTA per 2048-edge chunk
     __shared__ int32_t s_min[THREADS / 32];
-    __shared__ double s_sum[THREADS / 32];
+    __shared__ mgops::PathCount s_sum[THREADS / 32];
     __shared__ int s_hit, s_skip;
     for (int32_t ch = blockIdx.x; ch < a.nhchunks; ch += gridDim.x) {
         int32_t v = a.hchunk[3 * ch], b = a.hchunk[3 * ch + 1], e = a.hchunk[3 * ch + 2];
@@ -387,7 +400,8 @@ __global__ void __launch_bounds__(THREADS) k_pull(Args a)
         __syncthreads();
         if (skip) continue;
         int32_t best = mgops::UNSET;
-        double ssum = 0.0;
+        mgops::PathCount ssum = mgops::pc_zero();
+        const bool ext = a.bc_ext != 0;
         int hit = 0;
         const bool all_in = (ALG == ALG_SSSP) && (long long)c.qsize * 8 > a.n;  // as PullOp<ALG_SSSP>
         for (int32_t p = b + threadIdx.x; p < e; p += blockDim.x) {
@@ -395,7 +409,7 @@ __global__ void __launch_bounds__(THREADS) k_pull(Args a)
             if (all_in || mgd::bm_test(fb, u)) {
                 hit = 1;
                 if (ALG == ALG_SSSP) mgops::Sssp::accumulate_nonAtomics(best, mgops::Sssp::get_partial_result(a.label[u], a.twt[p]), 0);
-                if (ALG == ALG_BC) ssum += a.sigma[u];
+                if (ALG == ALG_BC) ssum = mgops::pc_add(ssum, a.sigma[u], ext);
             }
         }
         if (threadIdx.x == 0) s_hit = 0;
@@ -404,14 +418,17 @@ __global__ void __launch_bounds__(THREADS) k_pull(Args a)
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) {
             best = min(best, __shfl_xor_sync(0xffffffffu, best, o));
-            ssum += __shfl_xor_sync(0xffffffffu, ssum, o);
+            if (ALG == ALG_BC) ssum = mgops::pc_add(ssum, mgops::shfl_xor_val(ssum, o), ext);
         }
         if (lane == 0) { s_min[threadIdx.x >> 5] = best; s_sum[threadIdx.x >> 5] = ssum; }
         __syncthreads();
         if (threadIdx.x == 0) {
             int32_t bm = mgops::UNSET;
-            double bs = 0.0;
-            for (int w = 0; w < THREADS / 32; w++) { bm = min(bm, s_min[w]); bs += s_sum[w]; }
+            mgops::PathCount bs = mgops::pc_zero();
+            for (int w = 0; w < THREADS / 32; w++) {
+                bm = min(bm, s_min[w]);
+                if (ALG == ALG_BC) bs = mgops::pc_add(bs, s_sum[w], ext);
+            }
             uint32_t *nb = bm_buf(a, nextbuf);
             if (s_hit) {
                 if (ALG == ALG_BFS) {
@@ -424,7 +441,7 @@ __global__ void __launch_bounds__(THREADS) k_pull(Args a)
                 } else {
                     bool on_level;
                     bool found = mgops::BcForward::fused_update_condition(&a.label[v], it1, on_level);
-                    if (on_level) mgops::BcForward::accumulate(&a.sigma[v], bs);
+                    if (on_level) mgops::BcForward::accumulate(&a.sigma[v], bs, ext, a.bc_ovf);
                     if (found) {
                         mgd::bm_set(a.visited, v);
                         mgd::bm_set(nb, v);
@@ -650,7 +667,7 @@ __global__ void k_init(Args a, int32_t src, const int32_t *srcs, int32_t nsrc, i
         int32_t s = srcs ? srcs[i] : src;
         if (!mgd::bm_set(a.visited, s)) continue;  // duplicate source
         a.label[s] = 0;
-        if (ALG == ALG_BC) a.sigma[s] = 1.0;
+        if (ALG == ALG_BC) a.sigma[s] = mgops::pc_one();
         mgd::bm_set(a.bm, s);  // buffer 0 is the current frontier
         a.queue[q++] = s;
         int32_t d = a.row[s + 1] - a.row[s];
@@ -667,7 +684,9 @@ __global__ void k_init(Args a, int32_t src, const int32_t *srcs, int32_t nsrc, i
 // ----------------------------------------------------------------------------
 // BC backward: delta[v] = sigma[v] * sum_{w succ, level[w] = L} q[w],
 // q[w] = (1 + delta[w]) / sigma[w]  (bc_phase1/2 of process2.cu:135-261 and
-// process_fbc :5-132 in one pull form over the archived level lists)
+// process_fbc :5-132 in one pull form over the archived level lists).
+// With path counts sigma = m * 2^(512 k), q is kept as (1 + delta) / m
+// (FP64) and a successor's term is scaled by 2^(512 (k_v - k_w)).
 // ----------------------------------------------------------------------------
 struct BCtl {
     int32_t L0;       // deepest level; levels L0 .. 1 finalise their predecessors
@@ -675,20 +694,39 @@ struct BCtl {
     int32_t hcnt[2];  // heavy entries listed at a level, by level parity
 };
 
-__global__ void k_bc_q_init(int32_t n, const double *sigma, const int32_t *label, float *q, float *delta)
+// q and the successor sums: FP32 with plain counts (below 2^100, so
+// (1 + delta) / sigma stays a normal FP32 number); FP64 with extended counts,
+// whose mantissas reach 2^512.
+template <bool EXT>
+using QT = typename std::conditional<EXT, double, float>::type;
+
+template <bool EXT>
+__global__ void k_bc_q_init(int32_t n, const mgops::PathCount *sigma, const int32_t *label, QT<EXT> *q, float *delta)
 {
     for (int32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x) {
         delta[v] = 0.0f;
-        q[v] = (label[v] != mgops::UNSET && sigma[v] > 0.0) ? (float)(1.0 / sigma[v]) : 0.0f;
+        const double m = sigma[v].m;
+        q[v] = (label[v] != mgops::UNSET && m > 0.0) ? (QT<EXT>)(1.0 / m) : (QT<EXT>)0;
     }
 }
 
-__device__ __forceinline__ void bc_finish_vertex(int32_t v, float s, const double *sigma, float *delta, float *q,
-                                                 float *bc, int32_t src)
+// successor w's term of a level-(L-1) entry with scale kv
+template <bool EXT>
+__device__ __forceinline__ QT<EXT> bc_succ_term(const Args &a, const QT<EXT> *q, int32_t w, int32_t kv)
 {
-    float dv = (float)(sigma[v] * (double)s);
+    QT<EXT> t = __ldcg(&q[w]);
+    if (EXT) t *= (QT<EXT>)mgops::pc_scale(kv - a.sigma[w].k);
+    return t;
+}
+
+template <bool EXT>
+__device__ __forceinline__ void bc_finish_vertex(int32_t v, QT<EXT> s, const mgops::PathCount *sigma, float *delta,
+                                                 QT<EXT> *q, float *bc, int32_t src)
+{
+    const double m = sigma[v].m;
+    const float dv = (float)(m * (double)s);
     delta[v] = dv;
-    q[v] = (float)((1.0 + (double)dv) / sigma[v]);
+    q[v] = (QT<EXT>)((1.0 + (double)dv) / m);
     if (bc && v != src) bc[v] += dv;
 }
 
@@ -696,7 +734,8 @@ __device__ __forceinline__ void bc_finish_vertex(int32_t v, float s, const doubl
 // q of the successors was written by other blocks in the previous level,
 // so it is loaded through L2 (the persistent kernel runs every level in one
 // launch).  Entries above PUSH_HEAVY are listed for bc_back_heavy_level.
-__device__ __forceinline__ void bc_back_level(const Args &a, int32_t L, int32_t src, int32_t *hcount, float *q,
+template <bool EXT>
+__device__ __forceinline__ void bc_back_level(const Args &a, int32_t L, int32_t src, int32_t *hcount, QT<EXT> *q,
                                               float *delta, float *bcacc, int32_t *heavy_list)
 {
     const int32_t b0 = a.lvl_off[L - 1], b1 = a.lvl_off[L];
@@ -719,23 +758,25 @@ __device__ __forceinline__ void bc_back_level(const Args &a, int32_t L, int32_t 
                 if (lane == 0) heavy_list[atomicAdd(hcount, 1)] = v;
                 continue;
             }
-            float acc = 0.0f;
+            const int32_t kv = EXT ? a.sigma[v].k : 0;
+            QT<EXT> acc = 0;
             for (int32_t p = b + lane; p < e; p += 32) {
                 const int32_t w = a.col[p];
-                if (a.label[w] == L) acc += __ldcg(&q[w]);
+                if (a.label[w] == L) acc += bc_succ_term<EXT>(a, q, w, kv);
             }
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-            if (lane == 0) bc_finish_vertex(v, acc, a.sigma, delta, q, bcacc, src);
+            if (lane == 0) bc_finish_vertex<EXT>(v, acc, a.sigma, delta, q, bcacc, src);
         }
         return;
     }
     for (int base = b0 + gwarp * vpw; base < b1; base += nwarps * vpw) {
-        int32_t v = -1, start = 0, deg = 0;
+        int32_t v = -1, start = 0, deg = 0, kv = 0;
         if (lane < vpw && base + lane < b1) {
             v = a.queue[base + lane];
             start = a.row[v];
             deg = a.row[v + 1] - start;
+            if (EXT) kv = a.sigma[v].k;
             if (deg > PUSH_HEAVY) {
                 int h = atomicAdd(hcount, 1);
                 heavy_list[h] = v;
@@ -746,23 +787,24 @@ __device__ __forceinline__ void bc_back_level(const Args &a, int32_t L, int32_t 
         int incl = mgd::warp_scan_incl(deg);
         int excl = incl - deg;
         int total = __shfl_sync(0xffffffffu, incl, 31);
-        float acc = 0.0f;
+        QT<EXT> acc = 0;
         for (int k0 = 0; k0 < total; k0 += 32) {
             int k = k0 + lane;
             int kk = k < total ? k : total - 1;
             int own = mgd::owner_lane(excl, kk);
             int32_t e = __shfl_sync(0xffffffffu, start, own) + (kk - __shfl_sync(0xffffffffu, excl, own));
-            float t = 0.0f;
+            const int32_t kown = __shfl_sync(0xffffffffu, kv, own);
+            QT<EXT> t = 0;
             if (k < total) {
                 int32_t w = a.col[e];
-                if (a.label[w] == L) t = __ldcg(&q[w]);
+                if (a.label[w] == L) t = bc_succ_term<EXT>(a, q, w, kown);
             } else {
                 own = -1;
             }
 #pragma unroll
             for (int o = 1; o < 32; o <<= 1) {
                 int oo = __shfl_down_sync(0xffffffffu, own, o);
-                float ot = __shfl_down_sync(0xffffffffu, t, o);
+                QT<EXT> ot = __shfl_down_sync(0xffffffffu, t, o);
                 if (lane + o < 32 && oo == own) t += ot;
             }
             int prev_own = __shfl_up_sync(0xffffffffu, own, 1);
@@ -772,35 +814,37 @@ __device__ __forceinline__ void bc_back_level(const Args &a, int32_t L, int32_t 
                 int hl = __ffs(heads) - 1;
                 heads &= heads - 1;
                 int ho = __shfl_sync(0xffffffffu, own, hl);
-                float ht = __shfl_sync(0xffffffffu, t, hl);
+                QT<EXT> ht = __shfl_sync(0xffffffffu, t, hl);
                 if (lane == ho) acc += ht;
             }
         }
-        if (v >= 0) bc_finish_vertex(v, acc, a.sigma, delta, q, bcacc, src);
+        if (v >= 0) bc_finish_vertex<EXT>(v, acc, a.sigma, delta, q, bcacc, src);
     }
 }
 
 // heavy entries of the level: a CTA each, fixed-order block sum
-__device__ __forceinline__ void bc_back_heavy_level(const Args &a, int32_t L, int32_t src, int32_t nheavy, float *q,
+template <bool EXT>
+__device__ __forceinline__ void bc_back_heavy_level(const Args &a, int32_t L, int32_t src, int32_t nheavy, QT<EXT> *q,
                                                     float *delta, float *bcacc, const int32_t *heavy_list)
 {
-    __shared__ float s_part[32];
+    __shared__ QT<EXT> s_part[32];
     for (int32_t h = blockIdx.x; h < nheavy; h += gridDim.x) {
         int32_t v = __ldcg(&heavy_list[h]);
         int32_t b = a.row[v], e = a.row[v + 1];
-        float acc = 0.0f;
+        const int32_t kv = EXT ? a.sigma[v].k : 0;
+        QT<EXT> acc = 0;
         for (int32_t p = b + threadIdx.x; p < e; p += blockDim.x) {
             int32_t w = a.col[p];
-            if (a.label[w] == L) acc += __ldcg(&q[w]);
+            if (a.label[w] == L) acc += bc_succ_term<EXT>(a, q, w, kv);
         }
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
         if ((threadIdx.x & 31) == 0) s_part[threadIdx.x >> 5] = acc;
         __syncthreads();
         if (threadIdx.x == 0) {
-            float s = 0.0f;
+            QT<EXT> s = 0;
             for (int w = 0; w < (int)(blockDim.x >> 5); w++) s += s_part[w];
-            bc_finish_vertex(v, s, a.sigma, delta, q, bcacc, src);
+            bc_finish_vertex<EXT>(v, s, a.sigma, delta, q, bcacc, src);
         }
         __syncthreads();
     }
@@ -813,7 +857,8 @@ __device__ __forceinline__ void bc_back_heavy_level(const Args &a, int32_t L, in
 // level will use while the current level runs (its last readers finished
 // before the previous barrier).  A barrier timeout sets the error flag; the
 // host reads it and fails the run.
-__global__ void __launch_bounds__(PTHREADS, 2) k_bc_back_levels(Args a, BCtl *bc_ctl, float *q, float *delta,
+template <bool EXT>
+__global__ void __launch_bounds__(PTHREADS, 2) k_bc_back_levels(Args a, BCtl *bc_ctl, QT<EXT> *q, float *delta,
                                                                 float *bcacc, int32_t *heavy_list)
 {
     __shared__ int4 s_b;
@@ -824,7 +869,7 @@ __global__ void __launch_bounds__(PTHREADS, 2) k_bc_back_levels(Args a, BCtl *bc
     for (int32_t L = L0; L >= 1; L--) {
         const int par = L & 1;
         if (blockIdx.x == 0 && threadIdx.x == 0) bc_ctl->hcnt[par ^ 1] = 0;
-        bc_back_level(a, L, src, &bc_ctl->hcnt[par], q, delta, bcacc, heavy_list);
+        bc_back_level<EXT>(a, L, src, &bc_ctl->hcnt[par], q, delta, bcacc, heavy_list);
         if (!mgd::grid_sync(a.bar, a.bar_err, a.bar_never)) return;
         if (threadIdx.x == 0) s_nheavy = __ldcg(&bc_ctl->hcnt[par]);
         __syncthreads();
@@ -833,9 +878,15 @@ __global__ void __launch_bounds__(PTHREADS, 2) k_bc_back_levels(Args a, BCtl *bc
         // and skips the heavy phase and its barrier together (block 0's
         // early clear of this counter then leaves it at the 0 it holds)
         if (nheavy == 0) continue;
-        bc_back_heavy_level(a, L, src, nheavy, q, delta, bcacc, heavy_list);
+        bc_back_heavy_level<EXT>(a, L, src, nheavy, q, delta, bcacc, heavy_list);
         if (!mgd::grid_sync(a.bar, a.bar_err, a.bar_never)) return;
     }
+}
+
+__global__ void k_pc_to_double(int32_t n, const mgops::PathCount *sigma, double *out)
+{
+    for (int32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x)
+        out[v] = mgops::pc_to_double(sigma[v]);
 }
 
 __global__ void k_bc_back_init(const FCtl *fc, BCtl *bc_ctl, int32_t src)
@@ -853,7 +904,7 @@ __global__ void k_bc_back_init(const FCtl *fc, BCtl *bc_ctl, int32_t src)
 // workspace
 // ----------------------------------------------------------------------------
 struct FrontierWS {
-    mgi::DevBuf label, sigma, bm, visited, queue, heavy, lvl_off, ctl;
+    mgi::DevBuf label, sigma, sigma_d, bm, visited, queue, heavy, lvl_off, ctl;
     mgi::DevBuf q, delta, bc, bctl, bheavy, srcbuf;
     mgi::DevBuf bar;        // grid barrier words + error flag of the persistent kernels
     mgi::DevBuf cnt;        // LevelCnt[4] of the persistent push phase
@@ -868,7 +919,7 @@ void free_frontier_ws(mg_graph *g)
 {
     if (!g->fws) return;
     FrontierWS *w = g->fws;
-    DevBuf *bufs[] = {&w->label, &w->sigma, &w->bm, &w->visited, &w->queue, &w->heavy,
+    DevBuf *bufs[] = {&w->label, &w->sigma, &w->sigma_d, &w->bm, &w->visited, &w->queue, &w->heavy,
                       &w->lvl_off, &w->ctl, &w->q, &w->delta, &w->bc, &w->bctl, &w->bheavy, &w->srcbuf, &w->bar,
                       &w->cnt};
     for (DevBuf *b : bufs) dev_free(*b);
@@ -892,7 +943,7 @@ static mg_status ensure_ws(mg_graph *g, int alg)
     MG_TRY(dev_alloc(w->lvl_off, (n + 3) * 4));
     MG_TRY(dev_alloc(w->bar, BAR_BYTES));
     MG_TRY(dev_alloc(w->cnt, 4 * sizeof(LevelCnt)));
-    if (alg == ALG_BC) MG_TRY(dev_alloc(w->sigma, n * 8));
+    if (alg == ALG_BC) MG_TRY(dev_alloc(w->sigma, n * sizeof(mgops::PathCount)));
     if (w->coop_grid[alg] == 0) {
         int per_sm = 0;
         switch (alg) {
@@ -938,7 +989,9 @@ static Args make_args(mg_graph *g)
     a.hchunk = g->hchunk.as<int32_t>(); a.nhchunks = g->nhchunks;
     a.heavy_deg = g->heavy_deg;
     a.label = w->label.as<int32_t>();
-    a.sigma = w->sigma.as<double>();
+    a.sigma = w->sigma.as<mgops::PathCount>();
+    a.bc_ext = g->bc_ext ? 1 : 0;
+    a.bc_ovf = reinterpret_cast<int32_t *>(w->bar.as<unsigned>() + OVF_WORD);
     a.bm = w->bm.as<uint32_t>();
     a.visited = w->visited.as<uint32_t>();
     a.words = (std::max(g->nv, 1) + 31) / 32;
@@ -962,6 +1015,7 @@ static uint64_t key_of(const Args &a, int alg)
     const void *ptrs[] = {a.row, a.col, a.trow, a.tcol, a.label, a.sigma, a.bm, a.queue, a.heavy, a.ctl, a.wrows};
     for (const void *p : ptrs) k = (k ^ (uint64_t)(uintptr_t)p) * 1099511628211ull;
     k ^= (uint64_t)a.bar_never << 63;  // captured kernel arguments include the injection flag
+    k ^= (uint64_t)a.bc_ext << 62;     // and the path-count mode
     return k;
 }
 
@@ -989,7 +1043,7 @@ static mg_status frontier_run_impl(mg_graph *g, int alg, int32_t src, const int3
     MG_CUDA(cudaMemsetAsync(a.bm, 0, 3 * (size_t)a.words * 4, s));
     MG_CUDA(cudaMemsetAsync(a.visited, 0, (size_t)a.words * 4, s));
     MG_CUDA(cudaMemsetAsync(w->bar.p, 0, BAR_BYTES, s));
-    if (alg == ALG_BC) MG_CUDA(cudaMemsetAsync(a.sigma, 0, n * 8, s));
+    if (alg == ALG_BC) MG_CUDA(cudaMemsetAsync(a.sigma, 0, n * sizeof(mgops::PathCount), s));
     int max_iter = opt.max_iter > 0 ? opt.max_iter : (alg == ALG_SSSP ? 4 * g->nv + 16 : g->nv + 2);
     int alpha = opt.alpha > 0 ? opt.alpha : 15, beta = opt.beta > 0 ? opt.beta : 18;
     if (alg == ALG_SSSP && opt.alpha <= 0) alpha = 4;
@@ -1034,8 +1088,16 @@ static mg_status frontier_run_impl(mg_graph *g, int alg, int32_t src, const int3
                     &a.ctl->more, g->pinned_flag, max_iter + 2));
     // status readback
     FCtl hc;
+    int32_t ovf = 0;
     MG_CUDA(cudaMemcpyAsync(&hc, a.ctl, sizeof(FCtl), cudaMemcpyDeviceToHost, s));
+    if (alg == ALG_BC) MG_CUDA(cudaMemcpyAsync(&ovf, a.bc_ovf, 4, cudaMemcpyDeviceToHost, s));
     MG_CUDA(cudaStreamSynchronize(s));
+    if (ovf && !g->bc_ext) {
+        // a path count passed FP64's comfortable range: this graph's BC runs
+        // use extended path counts from now on, starting with this one
+        g->bc_ext = true;
+        return frontier_run_impl(g, alg, src, srcs_host, nsrc, opt, info);
+    }
     if (info) {
         info->iterations = hc.iter;
         info->pull_iterations = hc.pull_iters;
@@ -1063,23 +1125,28 @@ mg_status bc_backward(mg_graph *g, int32_t src, const mg_opts &opt, float *bcacc
 {
     FrontierWS *w = g->fws;
     const size_t n = (size_t)std::max(g->nv, 1);
-    MG_TRY(dev_alloc(w->q, n * 4));
+    MG_TRY(dev_alloc(w->q, n * 8));
     MG_TRY(dev_alloc(w->delta, n * 4));
     MG_TRY(dev_alloc(w->bctl, sizeof(BCtl)));
     MG_TRY(dev_alloc(w->bheavy, n * 4));
     Args a = make_args(g);
     cudaStream_t s = g->stream;
-    float *q = w->q.as<float>(), *delta = w->delta.as<float>();
+    void *q = w->q.p;
+    float *delta = w->delta.as<float>();
     BCtl *bc = w->bctl.as<BCtl>();
     int32_t *hl = w->bheavy.as<int32_t>();
     const int grid = launch_grid(g, THREADS, 8);
     if (w->coop_back == 0) {
         int per_sm = 0;
-        MG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_bc_back_levels, PTHREADS, 0));
+        int per_sm_x = 0;
+        MG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_bc_back_levels<false>, PTHREADS, 0));
+        MG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_x, k_bc_back_levels<true>, PTHREADS, 0));
+        per_sm = std::min(per_sm, per_sm_x);
         if (per_sm < 1) return fail(MG_ERR_CUDA, "persistent backward kernel does not fit on an SM");
         w->coop_back = std::min(per_sm, 2) * g->num_sms;
     }
-    k_bc_q_init<<<grid, THREADS, 0, s>>>(g->nv, a.sigma, a.label, q, delta);
+    if (a.bc_ext) k_bc_q_init<true><<<grid, THREADS, 0, s>>>(g->nv, a.sigma, a.label, (double *)q, delta);
+    else k_bc_q_init<false><<<grid, THREADS, 0, s>>>(g->nv, a.sigma, a.label, (float *)q, delta);
     k_bc_back_init<<<1, 32, 0, s>>>(a.ctl, bc, src);
     MG_CUDA(cudaMemsetAsync(w->bar.p, 0, BAR_BYTES, s));
     MG_CUDA(cudaGetLastError());
@@ -1096,7 +1163,8 @@ mg_status bc_backward(mg_graph *g, int32_t src, const mg_opts &opt, float *bcacc
     cfg.attrs = attr;
     cfg.numAttrs = 1;
     P.begin(sb);
-    MG_CUDA(cudaLaunchKernelEx(&cfg, k_bc_back_levels, a, bc, q, delta, bcacc, hl));
+    if (a.bc_ext) MG_CUDA(cudaLaunchKernelEx(&cfg, k_bc_back_levels<true>, a, bc, (double *)q, delta, bcacc, hl));
+    else MG_CUDA(cudaLaunchKernelEx(&cfg, k_bc_back_levels<false>, a, bc, (float *)q, delta, bcacc, hl));
     P.end();
     int err = 0;
     MG_CUDA(cudaMemcpyAsync(&err, a.bar_err, 4, cudaMemcpyDeviceToHost, s));
@@ -1160,7 +1228,12 @@ mg_status mg_bc(mg_graph *g, int32_t source, const mg_opts *o, int32_t *level_ou
     MG_TRY(bc_backward(g, s, opt, nullptr));
     FrontierWS *w = g->fws;
     MG_TRY(publish(g, MG_RES_LEVEL, w->label.p, 4));
-    MG_TRY(publish(g, MG_RES_SIGMA, w->sigma.p, 8));
+    // path counts as FP64 values (infinity where a count exceeds the FP64 range)
+    MG_TRY(dev_alloc(w->sigma_d, (size_t)std::max(g->nv, 1) * 8));
+    k_pc_to_double<<<launch_grid(g, THREADS, 8), THREADS, 0, g->stream>>>(g->nv, w->sigma.as<mgops::PathCount>(),
+                                                                           w->sigma_d.as<double>());
+    MG_CUDA(cudaGetLastError());
+    MG_TRY(publish(g, MG_RES_SIGMA, w->sigma_d.p, 8));
     MG_TRY(publish(g, MG_RES_DELTA, w->delta.p, 4));
     MG_TRY(end_run(g, opt, info));
     MG_TRY(copy_out(g, level_out, g->res[MG_RES_LEVEL], (size_t)g->nv * 4));

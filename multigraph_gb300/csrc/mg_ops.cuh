@@ -70,13 +70,133 @@ struct Sssp {
     }
 };
 
+// Shortest-path counts.  The reference keeps them in int32, which wraps
+// after a few dozen levels of a lattice; FP64 alone overflows (past 1.8e308)
+// after about a thousand: the number of shortest paths to a point d steps
+// away grows like 2^d.  A PathCount is an FP64 mantissa m (0, or in
+// [1, 2^512)) with a scale k: sigma = m * 2^(512 k), exact to FP64 precision
+// at any depth.  Engines run in one of two modes:
+//   plain     k stays 0 and sums are plain FP64 adds (FP64 atomics in push
+//             sweeps); the backward sweep keeps (1 + delta) / sigma in FP32,
+//             so a count seen at or above PC_PLAIN_MAX = 2^90 (a summed row,
+//             an added contribution, or a frontier vertex's count read as a
+//             push payload) raises an overflow flag and the run is repeated
+//             in extended mode.  Counts one level past the last check stay
+//             below 2^90 * 2^31, so 1 / sigma stays a normal FP32 number;
+//   extended  every sum renormalises (m >= 2^512: m *= 2^-512, k += 1) and
+//             push sweeps add with a 16-byte compare-and-swap.
+struct __align__(16) PathCount {
+    double m;
+    int32_t k;
+    int32_t pad;
+};
+constexpr double PC_TOP = 0x1p512;   // m < PC_TOP
+constexpr double PC_DOWN = 0x1p-512;
+constexpr double PC_PLAIN_MAX = 0x1p90;  // plain-mode ceiling (see above)
+
+__device__ __forceinline__ PathCount pc_zero() { return PathCount{0.0, 0, 0}; }
+__device__ __forceinline__ PathCount pc_one() { return PathCount{1.0, 0, 0}; }
+
+// a + b; in plain mode k is 0 on both sides and no renormalisation happens
+__device__ __forceinline__ PathCount pc_add(PathCount a, PathCount b, bool ext)
+{
+    if (!ext) return PathCount{a.m + b.m, 0, 0};
+    if (b.m == 0.0) return a;
+    if (a.m == 0.0) return b;
+    if (a.k < b.k) {
+        const PathCount t = a;
+        a = b;
+        b = t;
+    }
+    const int32_t d = a.k - b.k;  // b is below a's ulp when d >= 2
+    double m = a.m + (d == 0 ? b.m : (d == 1 ? b.m * PC_DOWN : 0.0));
+    int32_t k = a.k;
+    if (m >= PC_TOP) {
+        m *= PC_DOWN;
+        k += 1;
+    }
+    return PathCount{m, k, 0};
+}
+
+// 2^(512 dk) for the exponent differences of neighbouring levels
+__device__ __forceinline__ double pc_scale(int32_t dk)
+{
+    return dk == 0 ? 1.0 : dk == -1 ? PC_DOWN : dk == 1 ? PC_TOP : dk < 0 ? 0.0 : __longlong_as_double(0x7ff0000000000000ll);
+}
+
+// FP64 value of a count (infinity past the FP64 range)
+__device__ __forceinline__ double pc_to_double(PathCount a)
+{
+    return a.k == 0 ? a.m : (a.k == 1 ? a.m * PC_TOP : (a.m == 0.0 ? 0.0 : __longlong_as_double(0x7ff0000000000000ll)));
+}
+
+// 16-byte load through L2 (counts written by other blocks in the same launch)
+__device__ __forceinline__ PathCount pc_load_cg(const PathCount *p)
+{
+    const longlong2 r = __ldcg(reinterpret_cast<const longlong2 *>(p));
+    PathCount c;
+    c.m = __longlong_as_double(r.x);
+    c.k = (int32_t)(r.y & 0xffffffffll);
+    c.pad = 0;
+    return c;
+}
+
+__device__ __forceinline__ PathCount shfl_xor_val(PathCount v, int o)
+{
+    v.m = __shfl_xor_sync(0xffffffffu, v.m, o);
+    v.k = __shfl_xor_sync(0xffffffffu, v.k, o);
+    return v;
+}
+
+__device__ __forceinline__ PathCount shfl_val(PathCount v, int src)
+{
+    v.m = __shfl_sync(0xffffffffu, v.m, src);
+    v.k = __shfl_sync(0xffffffffu, v.k, src);
+    return v;
+}
+
+// *loc += x.  Plain mode: one FP64 atomic add (no result awaited); *ovf is
+// set when x itself reaches PC_PLAIN_MAX.  Extended mode: compare-and-swap of
+// the 16-byte count;
+// every failed attempt means another thread's add went in, so the loop
+// ends after at most as many rounds as the vertex has in-edges.
+__device__ __forceinline__ void pc_atomic_add(PathCount *loc, PathCount x, bool ext, int32_t *ovf)
+{
+    if (!ext) {
+        atomicAdd(&loc->m, x.m);
+        if (x.m >= PC_PLAIN_MAX) *ovf = 1;
+        return;
+    }
+    unsigned __int128 *a = reinterpret_cast<unsigned __int128 *>(loc);
+    const longlong2 r = __ldcg(reinterpret_cast<const longlong2 *>(loc));
+    unsigned __int128 old = ((unsigned __int128)(unsigned long long)r.y << 64) | (unsigned long long)r.x;
+    while (true) {
+        PathCount o;
+        o.m = __longlong_as_double((long long)(unsigned long long)old);
+        o.k = (int32_t)(unsigned)(unsigned long long)(old >> 64);
+        o.pad = 0;
+        const PathCount n = pc_add(o, x, true);
+        const unsigned __int128 nv = ((unsigned __int128)(unsigned)n.k << 64) |
+                                     (unsigned long long)__double_as_longlong(n.m);
+        const unsigned __int128 prev = atomicCAS(a, old, nv);
+        if (prev == old) return;
+        old = prev;
+    }
+}
+
 // BC forward (levels + path counts): user_function.h:223-226, 247-251, 279-287, 310-317, 362-373, 409-417
-// Path counts are FP64 here (the reference uses int32).
+// Path counts are PathCounts here (the reference uses int32).
 struct BcForward {
     __device__ static __forceinline__ int32_t initialize() { return UNSET; }
     __device__ static __forceinline__ int32_t get_partial_result(int32_t src_level, int32_t) { return src_level + 1; }
-    __device__ static __forceinline__ void accumulate(double *sigma_loc, double sigma_src) { atomicAdd(sigma_loc, sigma_src); }
-    __device__ static __forceinline__ void accumulate_nonAtomics(double &acc, double sigma_src) { acc += sigma_src; }
+    __device__ static __forceinline__ void accumulate(PathCount *sigma_loc, PathCount sigma_src, bool ext, int32_t *ovf)
+    {
+        pc_atomic_add(sigma_loc, sigma_src, ext, ovf);
+    }
+    __device__ static __forceinline__ void accumulate_nonAtomics(PathCount &acc, PathCount sigma_src, bool ext)
+    {
+        acc = pc_add(acc, sigma_src, ext);
+    }
     // claim at level `iter` when unvisited; a destination already at `iter`
     // still collects the path count; true = newly discovered
     __device__ static __forceinline__ bool fused_update_condition(int32_t *level_loc, int32_t iter, bool &on_level)

@@ -280,6 +280,57 @@ void orc_bc_multi_f64(const orc_csr *g, const int32_t *src, int32_t nsrc, double
     free(lv); free(sg); free(dl);
 }
 
+/* The same Brandes sweeps (validate.cu:149-189 order) with long-double path
+ * counts and dependencies. */
+void orc_bc_ext(const orc_csr *g, int32_t src, int32_t *level, double *log2sigma, double *delta)
+{
+    int32_t nv = g->nv;
+    size_t cnt = (size_t)(nv > 0 ? nv : 1);
+    int32_t *q = (int32_t *)malloc(sizeof(int32_t) * cnt);
+    long double *sg = (long double *)malloc(sizeof(long double) * cnt);
+    long double *dl = (long double *)malloc(sizeof(long double) * cnt);
+    for (int32_t i = 0; i < nv; i++) { level[i] = ORC_IUNUSED; sg[i] = 0.0L; dl[i] = 0.0L; }
+    if (nv > 0) {
+        level[src] = 0; sg[src] = 1.0L; q[0] = src;
+        int32_t head = 0, tail = 1;
+        while (head != tail) {
+            int32_t u = q[head++];
+            for (int32_t j = g->csc_v[u]; j < g->csc_v[u + 1]; j++) {
+                int32_t k = g->csc_e[j];
+                if (level[k] == ORC_IUNUSED) { level[k] = level[u] + 1; q[tail++] = k; }
+                if (level[u] + 1 == level[k]) sg[k] += sg[u];
+            }
+        }
+        for (int32_t i = tail - 1; i >= 0; i--) {
+            int32_t w = q[i];
+            for (int32_t j = g->csc_v[w]; j < g->csc_v[w + 1]; j++) {
+                int32_t k = g->csc_e[j];
+                if (level[k] == level[w] - 1) dl[k] += (sg[k] / sg[w]) * (1.0L + dl[w]);
+            }
+        }
+    }
+    for (int32_t i = 0; i < nv; i++) {
+        log2sigma[i] = sg[i] > 0.0L ? (double)log2l(sg[i]) : -1.0;
+        delta[i] = (double)dl[i];
+    }
+    free(q); free(sg); free(dl);
+}
+
+void orc_bc_multi_ext(const orc_csr *g, const int32_t *src, int32_t nsrc, double *bc)
+{
+    int32_t nv = g->nv;
+    size_t cnt = (size_t)(nv > 0 ? nv : 1);
+    int32_t *lv = (int32_t *)malloc(sizeof(int32_t) * cnt);
+    double *ls = (double *)malloc(sizeof(double) * cnt);
+    double *dl = (double *)malloc(sizeof(double) * cnt);
+    for (int32_t i = 0; i < nv; i++) bc[i] = 0.0;
+    for (int32_t s = 0; s < nsrc; s++) {
+        orc_bc_ext(g, src[s], lv, ls, dl);
+        for (int32_t i = 0; i < nv; i++) if (i != src[s]) bc[i] += dl[i];
+    }
+    free(lv); free(ls); free(dl);
+}
+
 /* ------------------------------------------------------------------------ */
 /* validate.cu:223-308 -- CC                                                 */
 /* ------------------------------------------------------------------------ */

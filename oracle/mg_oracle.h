@@ -60,6 +60,12 @@ void orc_bc(const orc_csr *g, int32_t src, int32_t *level, int32_t *sigma, float
 void orc_bc_f64(const orc_csr *g, int32_t src, int32_t *level, double *sigma, double *delta);
 /* Multi-source BC scores: sum over sources of delta_s(v), v != s, FP64. */
 void orc_bc_multi_f64(const orc_csr *g, const int32_t *src, int32_t nsrc, double *bc);
+/* Brandes with long-double path counts (15-bit exponent on x86 and aarch64:
+ * counts up to ~1e4932, past the FP64 range that lattices with thousands of
+ * levels reach).  log2sigma[v] = log2 of the path count (-1 when unreached),
+ * delta in long double rounded to FP64. */
+void orc_bc_ext(const orc_csr *g, int32_t src, int32_t *level, double *log2sigma, double *delta);
+void orc_bc_multi_ext(const orc_csr *g, const int32_t *src, int32_t nsrc, double *bc);
 /* validate.cu:223-273 -- min-label propagation to the fixed point (labels = min id). */
 int  orc_cc_minlabel(const orc_csr *g, int32_t *label);
 /* validate.cu:234-242 / :263-273 -- relabel by first appearance, in place. */

@@ -66,6 +66,8 @@ def lib():
         L.orc_bc.argtypes = [C.c_void_p, C.c_int32, _i32p, _i32p, _f32p]
         L.orc_bc_f64.argtypes = [C.c_void_p, C.c_int32, _i32p, _f64p, _f64p]
         L.orc_bc_multi_f64.argtypes = [C.c_void_p, _i32p, C.c_int32, _f64p]
+        L.orc_bc_ext.argtypes = [C.c_void_p, C.c_int32, _i32p, _f64p, _f64p]
+        L.orc_bc_multi_ext.argtypes = [C.c_void_p, _i32p, C.c_int32, _f64p]
         L.orc_cc_minlabel.argtypes = [C.c_void_p, _i32p]
         L.orc_cc_minlabel.restype = C.c_int
         L.orc_cc_relabel.argtypes = [C.c_int32, _i32p]
@@ -165,6 +167,22 @@ def bc_f64(g: CSR, src: int):
     dl = np.empty(g.nv, dtype=np.float64)
     lib().orc_bc_f64(g._struct(), src, lv, sg, dl)
     return lv, sg, dl
+
+
+def bc_ext(g: CSR, src: int):
+    """Brandes with long-double path counts: (levels, log2 path counts, deltas)."""
+    lv = np.empty(g.nv, dtype=np.int32)
+    ls = np.empty(g.nv, dtype=np.float64)
+    dl = np.empty(g.nv, dtype=np.float64)
+    lib().orc_bc_ext(g._struct(), src, lv, ls, dl)
+    return lv, ls, dl
+
+
+def bc_multi_ext(g: CSR, sources) -> np.ndarray:
+    s = np.ascontiguousarray(sources, dtype=np.int32)
+    out = np.empty(g.nv, dtype=np.float64)
+    lib().orc_bc_multi_ext(g._struct(), s, len(s), out)
+    return out
 
 
 def bc_multi_f64(g: CSR, sources) -> np.ndarray:

@@ -240,3 +240,18 @@ def test_reference_validator_catches_planted_mistakes():
     d = O.sssp(orc, 0)[0]
     d[5] += 1
     assert "FAIL" in O.RefTool("SSSP").validate(p, 0, [d], tmp)
+
+
+def test_oracle_long_double_brandes_matches_fp64():
+    """The long-double Brandes of the oracle agrees with the FP64 one where
+    FP64 path counts are exact."""
+    from oracle import oracle as O
+    h = mg.HostGraph.lattice(30, 20, 0.05, seed=4)
+    rp, col, wt = h.arrays()
+    og = O.csr_from_arrays(rp, col, wt)
+    lv, sg, dl = O.bc_f64(og, 3)
+    lv2, ls, dl2 = O.bc_ext(og, 3)
+    assert np.array_equal(lv, lv2)
+    assert np.allclose(np.exp2(ls), sg, rtol=1e-12, atol=0)
+    assert np.allclose(dl2, dl, rtol=1e-12, atol=1e-12)
+    assert np.allclose(O.bc_multi_ext(og, [3, 9]), O.bc_multi_f64(og, [3, 9]), rtol=1e-12, atol=1e-12)
