@@ -230,7 +230,7 @@ mg_status mg_bc(mg_graph *dg, int32_t source, const mg_opts *o, int32_t *level_o
 
 /* Multi-source BC scores bc[v] = sum_s delta_s[v] (v != s).  Symmetric
  * graphs traverse 32 sources at a time (one lane per source; up to 2^26
- * vertices, ~650 B of device memory per vertex), directed graphs one source
+ * vertices, ~1 KB of device memory per vertex), directed graphs one source
  * at a time.  No reference counterpart (the reference runs one source). */
 mg_status mg_bc_multi(mg_graph *dg, const int32_t *sources, int32_t nsrc, const mg_opts *o,
                       float *bc_out, mg_run_info *info);

@@ -26,6 +26,7 @@ BIN = os.path.join(PKG, "bin")
 
 GENCODE = "-gencode=arch=compute_103a,code=sm_103a"
 CU_SOURCES = ["mg_device.cu", "mg_frontier.cu", "mg_pr.cu", "mg_cc.cu", "mg_tune.cu", "mg_noalloc.cu", "mg_bcb.cu"]
+CU_FLAGS = {}  # per-file extra nvcc flags
 CPP_SOURCES = ["mg_host.cpp"]
 CLI_NAMES = ["BFS", "SSSP", "BC", "CC", "DATA_DRIVEN_PR", "TOPOLOGY_DRIVEN_PR"]
 
@@ -70,7 +71,7 @@ def build(verbose: bool = False, ptxas_info: bool = False) -> str:
         objs.append(o)
         if _stale(o, [s] + hdrs):
             cmd = [nvcc, GENCODE, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
-                   "-I", INCLUDE, "-I", CSRC, "-c", s, "-o", o]
+                   "-I", INCLUDE, "-I", CSRC] + CU_FLAGS.get(src, []) + ["-c", s, "-o", o]
             if ptxas_info:
                 cmd.insert(3, "-Xptxas=-v")
             jobs.append(cmd)
