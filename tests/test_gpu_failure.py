@@ -55,4 +55,3 @@ def test_backward_barrier_timeout_is_reported_and_recoverable(path_graph):
     rlv, rsg, rdl = O.bc_f64(og, 3)
     assert np.array_equal(lv, rlv) and np.array_equal(sg, rsg)
     assert np.allclose(dl, rdl, rtol=1e-5, atol=1e-6)
-
