@@ -60,8 +60,20 @@ __global__ void k_bb_init(BbArgs a, int32_t nsrc, int32_t dirmode, int32_t alpha
 }
 
 
+// The kernels of one level run back to back with programmatic dependent
+// launch: each lets the next one launch as soon as all of its blocks are
+// running (griddepcontrol.launch_dependents) and starts by waiting for the
+// previous kernel to complete and flush (griddepcontrol.wait), so a level's
+// launch latencies overlap the previous kernel's tail.
+__device__ __forceinline__ void pdl_enter()
+{
+    cudaGridDependencySynchronize();
+    cudaTriggerProgrammaticLaunchCompletion();
+}
+
 __global__ void __launch_bounds__(THREADS) k_bb_mark(BbArgs a)
 {
+    pdl_enter();
     const BbCtl c = *a.ctl;
     if (c.more == 0 || c.dense) return;
     bb_mark_phase(a, c, a.off[c.d], a.off[c.d + 1], &a.ctl->k.ncand);
@@ -70,6 +82,7 @@ __global__ void __launch_bounds__(THREADS) k_bb_mark(BbArgs a)
 template <bool TP, bool EXT>
 __global__ void __launch_bounds__(THREADS) k_bb_pull(BbArgs a)
 {
+    pdl_enter();
     const BbCtl c = *a.ctl;
     if (c.more == 0) return;
     bb_pull_phase<TP, EXT>(a, c, c.dense ? a.n : c.k.ncand);
@@ -77,6 +90,7 @@ __global__ void __launch_bounds__(THREADS) k_bb_pull(BbArgs a)
 
 __global__ void __launch_bounds__(THREADS) k_bb_heavy(BbArgs a)
 {
+    pdl_enter();
     const BbCtl c = *a.ctl;
     if (c.more == 0) return;
     bb_heavy_phase(a, c);
@@ -86,6 +100,7 @@ __global__ void __launch_bounds__(THREADS) k_bb_heavy(BbArgs a)
 // level (Beamer's direction test, loop condition)
 __global__ void __launch_bounds__(THREADS) k_bb_compact(BbArgs a, cudaGraphConditionalHandle h, int use_cond)
 {
+    pdl_enter();
     BbCtl *cp = a.ctl;
     const BbCtl c = *cp;
     if (c.more == 0) {
@@ -123,6 +138,7 @@ __global__ void k_bbb_start(BbArgs a)
 template <bool TP, bool EXT>
 __global__ void __launch_bounds__(THREADS) k_bbb_pull(BbArgs a)
 {
+    pdl_enter();
     const BbCtl c = *a.ctl;
     if (c.more == 0) return;
     bbb_pull_phase<TP, EXT>(a, c.L);
@@ -131,6 +147,7 @@ __global__ void __launch_bounds__(THREADS) k_bbb_pull(BbArgs a)
 template <bool EXT>
 __global__ void __launch_bounds__(THREADS, 8) k_bbb_heavy(BbArgs a)
 {
+    pdl_enter();
     const BbCtl c = *a.ctl;
     if (c.more == 0) return;
     bbb_heavy_phase<EXT>(a, c.L);
@@ -140,6 +157,7 @@ __global__ void __launch_bounds__(THREADS, 8) k_bbb_heavy(BbArgs a)
 // finish steps to L-1
 __global__ void __launch_bounds__(THREADS) k_bbb_next(BbArgs a, cudaGraphConditionalHandle h, int use_cond)
 {
+    pdl_enter();
     BbCtl *cp = a.ctl;
     const BbCtl c = *cp;
     if (c.more == 0) {
@@ -172,6 +190,23 @@ struct BcWS {
 namespace mgi {
 
 using namespace mgbc;
+
+// launch with programmatic dependent launch on the previous kernel of the stream
+template <class K, class... Args>
+static mg_status launch_pdl(K kernel, int grid, cudaStream_t st, Args... args)
+{
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)grid);
+    cfg.blockDim = dim3(THREADS);
+    cfg.stream = st;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    MG_CUDA(cudaLaunchKernelEx(&cfg, kernel, args...));
+    return MG_OK;
+}
 
 void free_bc_ws(mg_graph *g)
 {
@@ -278,20 +313,20 @@ mg_status bc_batched(mg_graph *g, const int32_t *src_engine, int32_t nsrc, const
         P.end();
         P.begin(s_pull);
         if (a.ext) {
-            if (tp) k_bb_pull<true, true><<<grid_f, THREADS, 0, st>>>(a);
-            else k_bb_pull<false, true><<<grid_f, THREADS, 0, st>>>(a);
+            if (tp) MG_TRY(launch_pdl(k_bb_pull<true, true>, grid_f, st, a));
+            else MG_TRY(launch_pdl(k_bb_pull<false, true>, grid_f, st, a));
         } else {
-            if (tp) k_bb_pull<true, false><<<grid_f, THREADS, 0, st>>>(a);
-            else k_bb_pull<false, false><<<grid_f, THREADS, 0, st>>>(a);
+            if (tp) MG_TRY(launch_pdl(k_bb_pull<true, false>, grid_f, st, a));
+            else MG_TRY(launch_pdl(k_bb_pull<false, false>, grid_f, st, a));
         }
         P.end();
         if (heavy) {
             P.begin(s_heavy);
-            k_bb_heavy<<<grid, THREADS, 0, st>>>(a);
+            MG_TRY(launch_pdl(k_bb_heavy, grid, st, a));
             P.end();
         }
         P.begin(s_comp);
-        k_bb_compact<<<grid, THREADS, 0, st>>>(a, h, use_cond);
+        MG_TRY(launch_pdl(k_bb_compact, grid, st, a, h, use_cond));
         P.end();
         MG_CUDA(cudaGetLastError());
         return MG_OK;
@@ -308,12 +343,12 @@ mg_status bc_batched(mg_graph *g, const int32_t *src_engine, int32_t nsrc, const
         P.end();
         if (heavy) {
             P.begin(s_bh);
-            if (a.ext) k_bbb_heavy<true><<<grid, THREADS, 0, st>>>(a);
-            else k_bbb_heavy<false><<<grid, THREADS, 0, st>>>(a);
+            if (a.ext) MG_TRY(launch_pdl(k_bbb_heavy<true>, grid, st, a));
+            else MG_TRY(launch_pdl(k_bbb_heavy<false>, grid, st, a));
             P.end();
         }
         P.begin(s_bn);
-        k_bbb_next<<<grid, THREADS, 0, st>>>(a, h, use_cond);
+        MG_TRY(launch_pdl(k_bbb_next, grid, st, a, h, use_cond));
         P.end();
         MG_CUDA(cudaGetLastError());
         return MG_OK;
