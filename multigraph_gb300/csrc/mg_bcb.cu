@@ -61,15 +61,9 @@ __global__ void k_bb_init(BbArgs a, int32_t nsrc, int32_t dirmode, int32_t alpha
 
 
 // The kernels of one level run back to back with programmatic dependent
-// launch: each lets the next one launch as soon as all of its blocks are
-// running (griddepcontrol.launch_dependents) and starts by waiting for the
-// previous kernel to complete and flush (griddepcontrol.wait), so a level's
-// launch latencies overlap the previous kernel's tail.
-__device__ __forceinline__ void pdl_enter()
-{
-    cudaGridDependencySynchronize();
-    cudaTriggerProgrammaticLaunchCompletion();
-}
+// launch (mgi::launch_pdl / mgd::pdl_enter), so a level's launch latencies
+// overlap the previous kernel's tail.
+using mgd::pdl_enter;
 
 __global__ void __launch_bounds__(THREADS) k_bb_mark(BbArgs a)
 {
@@ -191,22 +185,6 @@ namespace mgi {
 
 using namespace mgbc;
 
-// launch with programmatic dependent launch on the previous kernel of the stream
-template <class K, class... Args>
-static mg_status launch_pdl(K kernel, int grid, cudaStream_t st, Args... args)
-{
-    cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3((unsigned)grid);
-    cfg.blockDim = dim3(THREADS);
-    cfg.stream = st;
-    cudaLaunchAttribute at[1];
-    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-    at[0].val.programmaticStreamSerializationAllowed = 1;
-    cfg.attrs = at;
-    cfg.numAttrs = 1;
-    MG_CUDA(cudaLaunchKernelEx(&cfg, kernel, args...));
-    return MG_OK;
-}
 
 void free_bc_ws(mg_graph *g)
 {
@@ -313,20 +291,20 @@ mg_status bc_batched(mg_graph *g, const int32_t *src_engine, int32_t nsrc, const
         P.end();
         P.begin(s_pull);
         if (a.ext) {
-            if (tp) MG_TRY(launch_pdl(k_bb_pull<true, true>, grid_f, st, a));
-            else MG_TRY(launch_pdl(k_bb_pull<false, true>, grid_f, st, a));
+            if (tp) MG_TRY(launch_pdl(k_bb_pull<true, true>, grid_f, THREADS, st, a));
+            else MG_TRY(launch_pdl(k_bb_pull<false, true>, grid_f, THREADS, st, a));
         } else {
-            if (tp) MG_TRY(launch_pdl(k_bb_pull<true, false>, grid_f, st, a));
-            else MG_TRY(launch_pdl(k_bb_pull<false, false>, grid_f, st, a));
+            if (tp) MG_TRY(launch_pdl(k_bb_pull<true, false>, grid_f, THREADS, st, a));
+            else MG_TRY(launch_pdl(k_bb_pull<false, false>, grid_f, THREADS, st, a));
         }
         P.end();
         if (heavy) {
             P.begin(s_heavy);
-            MG_TRY(launch_pdl(k_bb_heavy, grid, st, a));
+            MG_TRY(launch_pdl(k_bb_heavy, grid, THREADS, st, a));
             P.end();
         }
         P.begin(s_comp);
-        MG_TRY(launch_pdl(k_bb_compact, grid, st, a, h, use_cond));
+        MG_TRY(launch_pdl(k_bb_compact, grid, THREADS, st, a, h, use_cond));
         P.end();
         MG_CUDA(cudaGetLastError());
         return MG_OK;
@@ -343,12 +321,12 @@ mg_status bc_batched(mg_graph *g, const int32_t *src_engine, int32_t nsrc, const
         P.end();
         if (heavy) {
             P.begin(s_bh);
-            if (a.ext) MG_TRY(launch_pdl(k_bbb_heavy<true>, grid, st, a));
-            else MG_TRY(launch_pdl(k_bbb_heavy<false>, grid, st, a));
+            if (a.ext) MG_TRY(launch_pdl(k_bbb_heavy<true>, grid, THREADS, st, a));
+            else MG_TRY(launch_pdl(k_bbb_heavy<false>, grid, THREADS, st, a));
             P.end();
         }
         P.begin(s_bn);
-        MG_TRY(launch_pdl(k_bbb_next, grid, st, a, h, use_cond));
+        MG_TRY(launch_pdl(k_bbb_next, grid, THREADS, st, a, h, use_cond));
         P.end();
         MG_CUDA(cudaGetLastError());
         return MG_OK;

@@ -192,12 +192,42 @@ mg_status rebin(mg_graph *g, int32_t heavy, int32_t chunk, int32_t tbin);
 // float scores in engine order stay in the graph's BC workspace
 mg_status bc_batched(mg_graph *g, const int32_t *src_engine, int32_t nsrc, const mg_opts &opt, mg_run_info *info,
                      const float **bc_dev);
+
+// Launch with programmatic dependent launch on the stream's previous kernel:
+// the kernel may start while that one drains and must begin with
+// mgd::pdl_enter() (wait for its completion and memory flush).
+template <class K, class... Args>
+inline mg_status launch_pdl(K kernel, int grid, int block, cudaStream_t st, Args... args)
+{
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)grid);
+    cfg.blockDim = dim3((unsigned)block);
+    cfg.stream = st;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    MG_CUDA(cudaLaunchKernelEx(&cfg, kernel, args...));
+    return MG_OK;
+}
 }  // namespace mgi
 
 // ---------------------------------------------------------------------------
 // device helpers
 // ---------------------------------------------------------------------------
 namespace mgd {
+
+// First statement of a kernel launched with mgi::launch_pdl (a no-op under a
+// plain launch): wait for the previous kernel to complete and flush
+// (griddepcontrol.wait), then let the next one launch as soon as all of
+// this kernel's blocks are running (griddepcontrol.launch_dependents).
+__device__ __forceinline__ void pdl_enter()
+{
+    cudaGridDependencySynchronize();
+    cudaTriggerProgrammaticLaunchCompletion();
+}
+
 
 __device__ __forceinline__ int lane() { return threadIdx.x & 31; }
 
