@@ -350,9 +350,9 @@ def main():
     launches = 0
     for _ in range(args.steps):
         si, pi = step()
-        # SSSP: init + (push, pull, compact, decide) per iteration + id mapping;
+        # SSSP: init + (push, frontier min, pull, compact, decide) per iteration + id mapping;
         # PageRank: 2 inits + (sweep, apply) per sweep + id mapping
-        launches += 2 + 4 * si.iterations + 3 + 2 * pi.iterations
+        launches += 2 + 5 * si.iterations + 3 + 2 * pi.iterations
     e1.record(stream)
     torch.cuda.synchronize()
     if dist:

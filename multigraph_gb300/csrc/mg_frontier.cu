@@ -47,6 +47,7 @@ constexpr int PTHREADS = 1024;  // persistent kernels: 2 CTAs of 1024 per SM (fe
 // path-count overflow flag, rounded up
 constexpr size_t BAR_BYTES = 4 * (2 + mgd::GRID_SYNC_GROUPS + 1 + 7);
 constexpr int OVF_WORD = 2 + mgd::GRID_SYNC_GROUPS + 1;
+constexpr int FMIN_WORD = OVF_WORD + 1;  // SSSP: least distance on the current frontier (pull levels)
 
 struct FCtl {
     int32_t more;       // continue flag (host loop readback)
@@ -84,6 +85,8 @@ struct Args {
     mgops::PathCount *sigma;
     int32_t bc_ext;      // BC path counts in extended mode (mgops::PathCount)
     int32_t *bc_ovf;     // set when a plain-mode path count reaches 2^512
+    int32_t *fmin;       // SSSP pull levels: least distance on the frontier (k_fmin)
+    int32_t wmin;        // least edge weight
     uint32_t *bm;        // 3 * words
     uint32_t *visited;
     int32_t words;
@@ -283,16 +286,23 @@ struct PullOp;
 // restricted one, distances still converge to the same fixed point, and one
 // dependent load per edge goes away.  Unreached neighbours hold UNSET, whose
 // offer UNSET + w never beats the identity UNSET.
+//
+// A row whose distance is at most (least frontier distance + least weight)
+// cannot improve this level -- every offer is dist[u] + w from a frontier
+// vertex u, or from a vertex whose edges an earlier level already relaxed --
+// so it is skipped without reading its edges (`bound`).  On R-MAT the hubs
+// settle first, so the later pull levels read a fraction of the edges.
 template <>
 struct PullOp<ALG_SSSP> : PullEmit {
     using T = int32_t;
-    static constexpr bool kRowAware = false;
+    static constexpr bool kRowAware = true;
     static constexpr bool kWeights = true;
     const uint32_t *fb;
     int it1;
     bool all_in;
+    int32_t bound;
     __device__ T identity() const { return mgops::Sssp::initialize(); }
-    __device__ bool skip(int32_t) const { return false; }
+    __device__ bool skip(int32_t v) const { return a.label[v] <= bound; }
     __device__ T edge(int32_t, int32_t, int32_t u, int32_t w) const
     {
         if (!all_in && !mgd::bm_test(fb, u)) return mgops::UNSET;
@@ -337,6 +347,26 @@ struct PullOp<ALG_BC> : PullEmit {
     }
 };
 
+// SSSP pull levels: rows at or below this distance cannot improve
+__device__ __forceinline__ int32_t sssp_bound(const Args &a)
+{
+    const int32_t f = *a.fmin;
+    return f >= INT32_MAX - a.wmin ? INT32_MAX : f + a.wmin;
+}
+
+// least distance over the frontier queue (before an SSSP pull level)
+__global__ void __launch_bounds__(THREADS) k_fmin(Args a)
+{
+    const FCtl c = *a.ctl;
+    if (c.mode != MODE_PULL || c.more == 0) return;
+    int32_t mn = INT32_MAX;
+    for (int32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < c.qsize; i += gridDim.x * blockDim.x)
+        mn = min(mn, a.label[a.queue[c.qoff + i]]);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) mn = min(mn, __shfl_xor_sync(0xffffffffu, mn, o));
+    if (mgd::lane() == 0 && mn < INT32_MAX) atomicMin(a.fmin, mn);
+}
+
 template <int ALG>
 __global__ void __launch_bounds__(THREADS) k_pull(Args a)
 {
@@ -379,7 +409,10 @@ __global__ void __launch_bounds__(THREADS) k_pull(Args a)
     } else {
         // degree-binned rows; reached rows marked in the next-frontier bitmap
         PullOp<ALG> op{{a, bm_buf(a, nextbuf)}, fb, it1};
-        if constexpr (ALG == ALG_SSSP) op.all_in = (long long)c.qsize * 8 > a.n;
+        if constexpr (ALG == ALG_SSSP) {
+            op.all_in = (long long)c.qsize * 8 > a.n;
+            op.bound = sssp_bound(a);
+        }
         mgd::bins_reduce(op, a.trow, a.tcol, a.twt, a.wrows, a.nwrows, a.trows, a.ntrows);
         (void)gwarp;
         (void)nwarps;
@@ -394,7 +427,8 @@ __global__ void __launch_bounds__(THREADS) k_pull(Args a)
         // thread 0 decides for the block (the row may be claimed concurrently
         // by another chunk, so a per-thread test could diverge)
         if (threadIdx.x == 0)
-            s_skip = (ALG != ALG_SSSP) && mgd::bm_test(a.visited, v) && a.label[v] != it1;
+            s_skip = (ALG == ALG_SSSP) ? (a.label[v] <= sssp_bound(a))
+                                       : (mgd::bm_test(a.visited, v) && a.label[v] != it1);
         __syncthreads();
         const bool skip = s_skip;
         __syncthreads();
@@ -566,6 +600,7 @@ __device__ __forceinline__ int decide_step(const Args &a)
 __global__ void k_decide(Args a, cudaGraphConditionalHandle h, int use_cond)
 {
     if (threadIdx.x != 0) return;
+    *a.fmin = INT32_MAX;  // the next pull level's k_fmin starts from here
     const int more = decide_step(a);
     if (use_cond) cudaGraphSetConditional(h, more ? 1u : 0u);
 }
@@ -679,6 +714,7 @@ __global__ void k_init(Args a, int32_t src, const int32_t *srcs, int32_t nsrc, i
     c->nqoff = (ALG == ALG_SSSP) ? a.n : q;
     c->visited_edges = ve;
     if (ALG != ALG_SSSP) { a.lvl_off[0] = 0; a.lvl_off[1] = q; c->nlevels = 1; }
+    *a.fmin = INT32_MAX;
 }
 
 // ----------------------------------------------------------------------------
@@ -992,6 +1028,8 @@ static Args make_args(mg_graph *g)
     a.sigma = w->sigma.as<mgops::PathCount>();
     a.bc_ext = g->bc_ext ? 1 : 0;
     a.bc_ovf = reinterpret_cast<int32_t *>(w->bar.as<unsigned>() + OVF_WORD);
+    a.fmin = reinterpret_cast<int32_t *>(w->bar.as<unsigned>() + FMIN_WORD);
+    a.wmin = std::max(g->min_weight, 0);
     a.bm = w->bm.as<uint32_t>();
     a.visited = w->visited.as<uint32_t>();
     a.words = (std::max(g->nv, 1) + 31) / 32;
@@ -1058,6 +1096,7 @@ static mg_status frontier_run_impl(mg_graph *g, int alg, int32_t src, const int3
     const int sp = P.slot(alg == ALG_SSSP ? "sssp_push" : alg == ALG_BC ? "bc_push" : "bfs_push");
     const int sl = P.slot(alg == ALG_SSSP ? "sssp_pull" : alg == ALG_BC ? "bc_pull" : "bfs_pull");
     const int sc = P.slot("frontier_compact");
+    const int sf = P.slot("sssp_fmin");
     const int sd = P.slot("frontier_decide");
     BodyFn body = [&](cudaStream_t st, cudaGraphConditionalHandle h, int use_cond) -> mg_status {
         MG_CUDA(cudaMemsetAsync(a.cnt, 0, 4 * sizeof(LevelCnt), st));
@@ -1068,6 +1107,11 @@ static mg_status frontier_run_impl(mg_graph *g, int alg, int32_t src, const int3
         default: MG_TRY(launch_sparse_levels<ALG_BC>(a, w->coop_grid[alg], st)); break;
         }
         P.end();
+        if (alg == ALG_SSSP) {
+            P.begin(sf);
+            k_fmin<<<grid, THREADS, 0, st>>>(a);
+            P.end();
+        }
         P.begin(sl);
         switch (alg) {
         case ALG_BFS: k_pull<ALG_BFS><<<grid, THREADS, 0, st>>>(a); break;
