@@ -114,3 +114,23 @@ def test_pagerank_reference_forms(graphs):
             t = np.maximum(np.abs(ref), 1e-12)
             rel = float(np.max(np.abs(x - ref) / t))
             assert rel < 0.05, (name, variant, rel)  # validate.cu:93-100 (THR = 5%)
+
+
+@pytest.mark.parametrize("direction", [mg.DIR_AUTO, mg.DIR_PULL])
+@pytest.mark.parametrize("wmax", [0, 3, 64])
+def test_sssp_small_and_zero_weights(direction, wmax):
+    """The pull levels skip rows at or below (least frontier distance + least
+    weight); zero and tiny weights make that bound tight."""
+    h0 = mg.HostGraph.rmat(12, 16, seed=77)
+    rp, col, _ = h0.arrays()
+    # symmetric weights: one draw per undirected pair
+    src = np.repeat(np.arange(len(rp) - 1), np.diff(rp))
+    lo, hi = np.minimum(src, col), np.maximum(src, col)
+    w = ((lo.astype(np.int64) * 1000003 + hi * 7919 + wmax) % (wmax + 1)).astype(np.int32)
+    h = mg.HostGraph.from_csr(rp, col, w)
+    g = mg.Graph(h)
+    og = O.csr_from_arrays(rp, col, w)
+    for s in (0, 17, 1234):
+        d, _ = g.sssp(s, direction=direction)
+        assert np.array_equal(d, O.sssp(og, s)[0]), (wmax, s)
+    g.free()
