@@ -641,6 +641,11 @@ static uint64_t pkey(const PArgs &a, int v)
 
 // Runs sweeps of variant V until convergence; the result is x[ctl.cur]
 // (c[ctl.cur] for the adjoint).
+// apply CTAs per SM: more blocks shorten nothing (one heavy row per warp is
+// already in flight) but lengthen the last-block-done reduction and its
+// counter (R-MAT 22: 27 us per apply at 8, 20 us at 4)
+constexpr int APPLY_PER_SM = 4;
+
 template <int V>
 static mg_status pr_loop(mg_graph *g, PArgs &a, const mg_opts &opt, const char *name, mg_run_info *info,
                          int *final_cur)
@@ -651,7 +656,7 @@ static mg_status pr_loop(mg_graph *g, PArgs &a, const mg_opts &opt, const char *
     const int sl = P.slot(name);
     std::string hn = std::string(name) + "_apply";
     const int sh = P.slot(hn.c_str());
-    const int apply_grid = std::max(1, std::min(grid, (a.nhrows + 7) / 8));
+    const int apply_grid = std::max(1, std::min(std::min(grid, (a.nhrows + 7) / 8), g->num_sms * APPLY_PER_SM));
     BodyFn body = [&](cudaStream_t st, cudaGraphConditionalHandle h, int use_cond) -> mg_status {
         P.begin(sl);
         k_pr_light<V><<<grid, THREADS, 0, st>>>(a);
