@@ -221,7 +221,7 @@ mg_status mg_cc(mg_graph *dg, const mg_opts *o, int32_t *label_out, mg_run_info 
 /* Single-source Brandes: levels, sigma (FP64 path counts), delta (FP32).
  * Replaces the -DBC forward loop + MultiGraph_V_E_V_pull (process2.cu:263-325).
  * delta[v] is the raw dependency, including delta[source] as validate.cu:182-189.
- * Path counts that pass 2^512 (lattices after about a thousand levels) switch
+ * Path counts that pass 2^90 (lattices after a few hundred levels) switch
  * the graph's BC runs to extended counts (FP64 mantissa, 2^512 scale), so
  * delta stays exact to FP32 at any depth; sigma_out then holds +infinity for
  * counts beyond the FP64 range (the reference's int32 counts wrap). */

@@ -11,7 +11,8 @@
 //   fm[v]    bit s set when v is on source s's current frontier
 //   sig[v*32+s]  path count of v from source s (mgops::PathCount: FP64
 //                mantissa m and a 2^512 scale k; plain FP64 until a count
-//                reaches 2^512, then the run repeats in extended mode)
+//                reaches mgops::PC_PLAIN_MAX = 2^90, then the run repeats
+//                in extended mode)
 //   q[v*32+s]    (1 + delta_s[v]) / m   (backward; FP32 with plain counts,
 //                FP64 with extended ones)
 //   archive  (vertex, mask) entries, grouped by level: entry (v, M) at

@@ -84,7 +84,7 @@ struct Args {
     int32_t *label;
     mgops::PathCount *sigma;
     int32_t bc_ext;      // BC path counts in extended mode (mgops::PathCount)
-    int32_t *bc_ovf;     // set when a plain-mode path count reaches 2^512
+    int32_t *bc_ovf;     // set when a plain-mode path count reaches mgops::PC_PLAIN_MAX
     int32_t *fmin;       // SSSP pull levels: least distance on the frontier (k_fmin)
     int32_t wmin;        // least edge weight
     uint32_t *bm;        // 3 * words
