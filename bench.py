@@ -364,7 +364,7 @@ def main():
     # in and both results out.  Double-buffered: the next step's copy
     # (mg_graph_stage, copy stream) overlaps this step's runs, and
     # mg_graph_commit rebuilds the device CSR from it before the next step.
-    h2d = 4 * (n + 1) + 8 * m
+    h2d = h.stage_bytes()  # row offsets, column ids, weights (bytes: the pinned graph's weights fit)
     d2h = 8 * n
     torch.cuda.synchronize()
     t0 = time.perf_counter()

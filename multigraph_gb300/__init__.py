@@ -84,6 +84,7 @@ def _load_lib():
         "mg_host_graph_from_csr": ([i32, i32, vp, vp, vp, i32, P(vp)], i32),
         "mg_host_graph_view": ([vp, P(CsrView)], i32),
         "mg_host_graph_pin": ([vp], i32),
+        "mg_host_graph_stage_bytes": ([vp], i64),
         "mg_host_graph_free": ([vp], None),
         "mg_write_mtx": ([vp, C.c_char_p, i32], i32),
         "mg_save_csr": ([vp, C.c_char_p], i32),
@@ -138,7 +139,8 @@ lib = _LazyLib()
 # every symbol include/mg.h declares, in declaration order
 EXPORTED = [
     "mg_status_string", "mg_last_error", "mg_version", "mg_load_mtx", "mg_host_graph_from_entries",
-    "mg_host_graph_from_csr", "mg_host_graph_view", "mg_host_graph_pin", "mg_host_graph_free", "mg_write_mtx",
+    "mg_host_graph_from_csr", "mg_host_graph_view", "mg_host_graph_pin", "mg_host_graph_stage_bytes",
+    "mg_host_graph_free", "mg_write_mtx",
     "mg_save_csr", "mg_load_csr",
     "mg_gen_rmat", "mg_gen_lattice", "mg_graph_upload", "mg_graph_reload", "mg_graph_stage", "mg_graph_commit",
     "mg_graph_free", "mg_graph_info",
@@ -268,6 +270,10 @@ class HostGraph:
 
     def pin(self):
         _check(lib.mg_host_graph_pin(self._h), "mg_host_graph_pin")
+
+    def stage_bytes(self) -> int:
+        """Bytes Graph.stage copies to the device for this graph."""
+        return int(lib.mg_host_graph_stage_bytes(self._h))
 
     def write_mtx(self, path: str, with_weights: bool = True):
         _check(lib.mg_write_mtx(self._h, path.encode(), int(with_weights)), "mg_write_mtx")

@@ -255,3 +255,9 @@ def test_oracle_long_double_brandes_matches_fp64():
     assert np.allclose(np.exp2(ls), sg, rtol=1e-12, atol=0)
     assert np.allclose(dl2, dl, rtol=1e-12, atol=1e-12)
     assert np.allclose(O.bc_multi_ext(og, [3, 9]), O.bc_multi_f64(og, [3, 9]), rtol=1e-12, atol=1e-12)
+
+
+def test_stage_bytes_unpinned():
+    h = mg.HostGraph.rmat(8, 8, seed=1)
+    rp, col, _ = h.arrays()
+    assert h.stage_bytes() == 4 * len(rp) + 8 * len(col)
