@@ -26,7 +26,6 @@ import argparse
 import json
 import os
 import statistics
-import subprocess
 import sys
 import threading
 import time
@@ -67,72 +66,98 @@ def peaks():
 
 
 class ClockSampler:
-    """nvidia-smi clocks / throttle reasons sampled during the measurement."""
-    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,utilization.gpu,clocks_event_reasons.active,"
-              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
-              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+    """SM clock, power, utilisation and clock-event reasons of the GPU,
+    sampled every 100 ms during the measurement, in-process through NVML
+    (read-only queries).  A polling `nvidia-smi -lms` child was measured to
+    slow the end-to-end loop of each later process on the same GPU (31 ->
+    29 -> 24 -> 22 GTEPS over successive runs; steady without it), so the
+    sampler does not use one."""
+    # nvmlClocksEventReason* bits reported in "reasons"
+    REASONS = {0x4: "sw_power_cap", 0x8: "hw_slowdown", 0x20: "sw_thermal_slowdown", 0x40: "hw_thermal_slowdown"}
+    NVML_CLOCK_SM = 1
 
     def __init__(self, device: int):
         self.device = device
-        self.proc = None
-        self.lines = []
+        self.samples = []
+        self.lib = None
+        self.thread = None
+        self.running = False
+        try:
+            import ctypes
+            lib = ctypes.CDLL("libnvidia-ml.so.1")
+            if lib.nvmlInit_v2() != 0:
+                return
+            h = ctypes.c_void_p()
+            found = False
+            try:
+                import torch
+                uuid = str(torch.cuda.get_device_properties(device).uuid)
+                uuid = uuid if uuid.startswith("GPU-") else "GPU-" + uuid
+                found = lib.nvmlDeviceGetHandleByUUID(uuid.encode(), ctypes.byref(h)) == 0
+            except Exception:
+                found = False
+            if not found and lib.nvmlDeviceGetHandleByIndex_v2(device, ctypes.byref(h)) != 0:
+                return
+            self.reasons_fn = getattr(lib, "nvmlDeviceGetCurrentClocksEventReasons", None) or \
+                lib.nvmlDeviceGetCurrentClocksThrottleReasons
+            self.lib, self.h = lib, h
+        except (OSError, AttributeError):
+            self.lib = None
+
+    def _sample(self):
+        import ctypes
+        lib, h = self.lib, self.h
+        sm, mx, mw, reasons = ctypes.c_uint(), ctypes.c_uint(), ctypes.c_uint(), ctypes.c_ulonglong()
+        util = (ctypes.c_uint * 2)()  # nvmlUtilization_t {gpu, memory}
+        if (lib.nvmlDeviceGetClockInfo(h, self.NVML_CLOCK_SM, ctypes.byref(sm)) != 0
+                or lib.nvmlDeviceGetMaxClockInfo(h, self.NVML_CLOCK_SM, ctypes.byref(mx)) != 0
+                or lib.nvmlDeviceGetUtilizationRates(h, util) != 0
+                or self.reasons_fn(h, ctypes.byref(reasons)) != 0):
+            return None
+        if lib.nvmlDeviceGetPowerUsage(h, ctypes.byref(mw)) != 0:
+            mw.value = 0
+        return sm.value, mx.value, util[0], reasons.value, mw.value / 1000.0
+
+    def _loop(self):
+        while self.running:
+            smp = self._sample()
+            if smp:
+                self.samples.append(smp)
+            time.sleep(0.1)
 
     def start(self, keep=None):
         if keep:
-            self.lines = list(keep)
-        try:
-            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
-                                          "--format=csv,noheader,nounits", "-lms", "100"],
-                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
-            self.t = threading.Thread(target=self._read, daemon=True)
-            self.t.start()
-        except OSError:
-            self.proc = None
-
-    def _read(self):
-        for line in self.proc.stdout:
-            self.lines.append(line.strip())
+            self.samples = list(keep)
+        if self.lib is None:
+            return
+        self.running = True
+        self.thread = threading.Thread(target=self._loop, daemon=True)
+        self.thread.start()
 
     def pause(self):
         """Stop polling; returns the samples so far (start(keep=...) resumes)."""
-        if self.proc:
-            self.proc.terminate()
-            try:
-                self.proc.wait(timeout=5)
-            except subprocess.TimeoutExpired:
-                self.proc.kill()
-            self.t.join(timeout=5)
-            self.proc = None
-        return list(self.lines)
+        if self.thread:
+            self.running = False
+            self.thread.join(timeout=5)
+            self.thread = None
+        return list(self.samples)
 
     def stop(self):
-        if not self.proc:
-            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
-        self.proc.terminate()
-        try:
-            self.proc.wait(timeout=5)
-        except subprocess.TimeoutExpired:
-            self.proc.kill()
+        self.pause()
+        if self.lib is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["NVML unavailable"]}
+        self.lib.nvmlShutdown()
         sm, smax, reasons, load = [], None, set(), []
-        for ln in self.lines:
-            f = [x.strip() for x in ln.split(",")]
-            if len(f) < 10:
-                continue
-            try:
-                s, mx, util = float(f[1]), float(f[2]), float(f[4])
-            except ValueError:
-                continue
+        for s, mx, util, bits, _ in self.samples:
             smax = mx
             if util > 0:
                 load.append(s)
-                for name, val in zip(["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"],
-                                     f[6:10]):
-                    if val.lower().startswith("active"):
-                        reasons.add(name)
+                reasons.update(name for bit, name in self.REASONS.items() if bits & bit)
             sm.append(s)
         use = load if load else sm
         return {"sm_mhz": statistics.median(use) if use else None, "sm_max_mhz": smax,
-                "reasons": sorted(reasons), "samples": len(sm), "samples_under_load": len(load)}
+                "reasons": sorted(reasons), "samples": len(sm), "samples_under_load": len(load),
+                "source": "NVML"}
 
 
 def aggregate(ms_local, edges_per_step, steps, world, dist=None, device=None):
@@ -373,9 +398,8 @@ def main():
         dist.barrier()
     ms, value = aggregate(e0.elapsed_time(e1), 2 * m, args.steps, world, dist, torch.device("cuda", local))
     ms_per_step = ms / args.steps
-    # the clock sampler's nvidia-smi polling stalls the host-synchronised
-    # end-to-end loop: it runs around the device-timed region and the
-    # per-kernel timing pass, not around the end-to-end loop
+    # the clock sampler runs around the device-timed region and the
+    # per-kernel timing pass, not around the host-synchronised end-to-end loop
     clk_lines = clocks.pause()
 
     # ---- end to end through the C ABI: every step copies the pinned host CSR

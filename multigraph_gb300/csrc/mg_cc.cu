@@ -161,12 +161,12 @@ struct HookOp {
 // one pass over the pull-side arrays; symmetric graphs take each undirected
 // edge once (u > v), general graphs every entry
 __global__ void __launch_bounds__(THREADS) k_cc_hook(int32_t n, const int32_t *prow, const int32_t *pcol,
-                                                     const int32_t *wrows, int32_t nwrows, const int32_t *trows,
+                                                     const int32_t *wrows, int32_t nwrows, int32_t nwlong, const int32_t *trows,
                                                      int32_t ntrows, const int32_t *hchunk, int32_t nhchunks,
                                                      int symmetric, const uint32_t *giant_bm, int32_t *parent)
 {
     HookOp op{parent, symmetric, giant_bm};
-    mgd::bins_reduce(op, prow, pcol, nullptr, wrows, nwrows, trows, ntrows);
+    mgd::bins_reduce(op, prow, pcol, nullptr, wrows, nwrows, nwlong, trows, ntrows);
     __shared__ int s_skip;
     for (int32_t ch = blockIdx.x; ch < nhchunks; ch += gridDim.x) {
         int32_t u = hchunk[3 * ch], b = hchunk[3 * ch + 1], e = hchunk[3 * ch + 2];
@@ -254,7 +254,7 @@ mg_status cc_run(mg_graph *g, mg_run_info *info, const std::vector<int32_t> *vof
         P.end();
     }
     P.begin(sh);
-    k_cc_hook<<<grid, THREADS, 0, s>>>(g->nv, g->trow, g->tcol, g->wrows.as<int32_t>(), g->nwrows,
+    k_cc_hook<<<grid, THREADS, 0, s>>>(g->nv, g->trow, g->tcol, g->wrows.as<int32_t>(), g->nwrows, g->nwlong,
                                        g->trows.as<int32_t>(), g->ntrows, g->hchunk.as<int32_t>(), g->nhchunks,
                                        g->symmetric ? 1 : 0, sample ? giant : nullptr, parent);
     P.end();

@@ -235,6 +235,7 @@ struct HostLayout {
     bool symmetric = true, wsym = true;
     std::vector<int32_t> hchunk, hrows, hrow_chunk;
     std::vector<int32_t> wrows, trows;  // degree bins (engine ids)
+    int32_t nwlong = 0;                  // wrows[0, nwlong): rows of SUBWARP_MAX+ edges
     std::vector<int32_t> prow;          // pull-side row offsets (engine order)
     int32_t heavy = 0, chunk = 0, tbin = 0;
     int32_t n_dangling = 0, min_weight = 0;
@@ -297,6 +298,13 @@ static void build_bins(const std::vector<int32_t> &prow, int32_t n, int32_t heav
             L.trows.push_back(v);
         }
     }
+    // warp-bin rows of SUBWARP_MAX or more edges first (a warp each), the
+    // shorter ones after them (an 8-lane group each); order kept in each part
+    std::stable_partition(L.wrows.begin(), L.wrows.end(),
+                          [&](int32_t v) { return prow[v + 1] - prow[v] >= mgd::SUBWARP_MAX; });
+    L.nwlong = 0;
+    for (int32_t v : L.wrows)
+        if (prow[v + 1] - prow[v] >= mgd::SUBWARP_MAX) L.nwlong++;
     L.heavy = heavy;
     L.chunk = chunk;
     L.tbin = tbin;
@@ -738,6 +746,7 @@ static mg_status upload_bins(mg_graph *g, const HostLayout &L)
         MG_CUDA(cudaMemcpyAsync(g->trows.p, L.trows.data(), L.trows.size() * 4, cudaMemcpyHostToDevice, s));
     MG_CUDA(cudaStreamSynchronize(s));
     g->nwrows = (int32_t)L.wrows.size();
+    g->nwlong = L.nwlong;
     g->ntrows = (int32_t)L.trows.size();
     g->nhchunks = (int32_t)(L.hchunk.size() / 3);
     g->nhrows = (int32_t)L.hrows.size();

@@ -121,6 +121,7 @@ struct mg_graph {
     // thread rows (deg <= 32), in engine order
     mgi::DevBuf wrows, trows;
     int32_t nwrows = 0, ntrows = 0;
+    int32_t nwlong = 0;            // wrows[0, nwlong) have SUBWARP_MAX+ edges (a warp each)
     // heavy pull rows split into chunks: (row, begin, end) triplets
     mgi::DevBuf hchunk;            // int32 [3*nhchunks]
     int32_t nhchunks = 0;
@@ -219,6 +220,10 @@ inline mg_status launch_pdl(K kernel, int grid, int block, cudaStream_t st, Args
 // device helpers
 // ---------------------------------------------------------------------------
 namespace mgd {
+
+// warp-bin rows below this many edges are summed by an 8-lane group (four
+// rows per warp in flight, mg_bins.cuh), longer ones by a whole warp
+constexpr int32_t SUBWARP_MAX = 128;
 
 // First statement of a kernel launched with mgi::launch_pdl (a no-op under a
 // plain launch): wait for the previous kernel to complete and flush

@@ -77,7 +77,7 @@ struct Args {
     const int32_t *row, *col, *wt;     // push side
     const int32_t *trow, *tcol, *twt;  // pull side
     const int32_t *wrows, *trows;  // degree bins of the pull rows
-    int32_t nwrows, ntrows;
+    int32_t nwrows, ntrows, nwlong;
     const int32_t *hchunk;
     int32_t nhchunks;
     int32_t heavy_deg;
@@ -413,7 +413,7 @@ __global__ void __launch_bounds__(THREADS) k_pull(Args a)
             op.all_in = (long long)c.qsize * 8 > a.n;
             op.bound = sssp_bound(a);
         }
-        mgd::bins_reduce(op, a.trow, a.tcol, a.twt, a.wrows, a.nwrows, a.trows, a.ntrows);
+        mgd::bins_reduce(op, a.trow, a.tcol, a.twt, a.wrows, a.nwrows, a.nwlong, a.trows, a.ntrows);
         (void)gwarp;
         (void)nwarps;
     }
@@ -1020,7 +1020,7 @@ static Args make_args(mg_graph *g)
     a.m = g->ne;
     a.row = g->row.as<int32_t>(); a.col = g->col.as<int32_t>(); a.wt = g->wt.as<int32_t>();
     a.trow = g->trow; a.tcol = g->tcol; a.twt = g->twt;
-    a.wrows = g->wrows.as<int32_t>(); a.nwrows = g->nwrows;
+    a.wrows = g->wrows.as<int32_t>(); a.nwrows = g->nwrows; a.nwlong = g->nwlong;
     a.trows = g->trows.as<int32_t>(); a.ntrows = g->ntrows;
     a.hchunk = g->hchunk.as<int32_t>(); a.nhchunks = g->nhchunks;
     a.heavy_deg = g->heavy_deg;

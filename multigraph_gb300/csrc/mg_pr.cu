@@ -68,7 +68,7 @@ struct PArgs {
     const int32_t *outrow;   // push-side offsets (out-degrees)
     float *S;                // weighted: out-weight sums
     const int32_t *wrows, *trows;  // degree bins
-    int32_t nwrows, ntrows;
+    int32_t nwrows, ntrows, nwlong;
     const int32_t *hchunk;
     int32_t nhchunks;
     const int32_t *hrows;
@@ -223,7 +223,7 @@ __global__ void __launch_bounds__(THREADS) k_pr_light(PArgs a)
     (void)gwarp;
     (void)nwarps;
     const int32_t *pwt = reinterpret_cast<const int32_t *>(a.pw);
-    mgd::bins_reduce(op, a.prow, a.pcol, pwt, a.wrows, a.nwrows, a.trows, a.ntrows);
+    mgd::bins_reduce(op, a.prow, a.pcol, pwt, a.wrows, a.nwrows, a.nwlong, a.trows, a.ntrows);
     // heavy-row chunks, one per CTA, in batches of 8 * THREADS edges: each
     // thread issues its 8 column loads, then its 8 gathers (one batch for
     // the default 2048-edge chunks)
@@ -703,7 +703,7 @@ static mg_status pr_setup(mg_graph *g, PArgs &a, bool weighted_or_adj)
     a.prow = g->trow;
     a.pcol = g->tcol;
     a.outrow = g->row.as<int32_t>();
-    a.wrows = g->wrows.as<int32_t>(); a.nwrows = g->nwrows;
+    a.wrows = g->wrows.as<int32_t>(); a.nwrows = g->nwrows; a.nwlong = g->nwlong;
     a.trows = g->trows.as<int32_t>(); a.ntrows = g->ntrows;
     a.hchunk = g->hchunk.as<int32_t>(); a.nhchunks = g->nhchunks;
     a.hrows = g->hrows.as<int32_t>(); a.hrow_chunk = g->hrow_chunk.as<int32_t>(); a.nhrows = g->nhrows;
