@@ -425,10 +425,19 @@ __global__ void __launch_bounds__(THREADS) k_pull(Args a)
     for (int32_t ch = blockIdx.x; ch < a.nhchunks; ch += gridDim.x) {
         int32_t v = a.hchunk[3 * ch], b = a.hchunk[3 * ch + 1], e = a.hchunk[3 * ch + 2];
         // thread 0 decides for the block (the row may be claimed concurrently
-        // by another chunk, so a per-thread test could diverge)
-        if (threadIdx.x == 0)
-            s_skip = (ALG == ALG_SSSP) ? (a.label[v] <= sssp_bound(a))
-                                       : (mgd::bm_test(a.visited, v) && a.label[v] != it1);
+        // by another chunk, so a per-thread test could diverge).  BFS / BC
+        // skip only rows reached at an earlier level; the label is read from
+        // L2: hub-first ids put the heavy rows' labels in a few lines, and an
+        // L1 copy from an earlier chunk can predate this level's claim, which
+        // would drop this chunk's share of the row's path count
+        if (threadIdx.x == 0) {
+            if (ALG == ALG_SSSP) {
+                s_skip = a.label[v] <= sssp_bound(a);
+            } else {
+                const int32_t lv = __ldcg(&a.label[v]);
+                s_skip = lv != mgops::UNSET && lv != it1;
+            }
+        }
         __syncthreads();
         const bool skip = s_skip;
         __syncthreads();

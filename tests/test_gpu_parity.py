@@ -96,6 +96,32 @@ def test_bc_single(graphs, direction):
             assert rel < 1e-5, (name, s, rel)
 
 
+def test_bc_heavy_row_chunks_rmat20():
+    """Hub rows of R-MAT 20 are pulled in CTA-sized chunks that claim the row
+    concurrently; every chunk's share must reach the row's path count.  A
+    chunk that skipped a row another chunk had just claimed (stale label in
+    L1) left sigma short by that share on some runs, so each source runs
+    twice and sigma must match the oracle exactly."""
+    h = mg.HostGraph.rmat(20, 16, seed=20)
+    g = mg.Graph(h)
+    rp, col, wt = h.arrays()
+    og = O.csr_from_arrays(rp, col, wt)
+    src = np.random.default_rng(20).integers(0, g.nv, 32)
+    try:
+        for s in map(int, src):
+            rlv, rsg, rdl = O.bc_f64(og, s)
+            for _ in range(2):
+                (lv, sg, dl), _ = g.bc(s)
+                assert np.array_equal(lv, rlv), s
+                bad = np.nonzero(sg != rsg)[0]
+                assert len(bad) == 0, (s, bad[:4].tolist(), sg[bad[:4]].tolist(), rsg[bad[:4]].tolist())
+                den = np.maximum(np.abs(rdl), 1.0)
+                assert float(np.max(np.abs(dl.astype(np.float64) - rdl) / den)) < 1e-5, s
+    finally:
+        g.free()
+        h.free()
+
+
 @pytest.mark.parametrize("exec_mode", EXECS)
 def test_pagerank_normalised(graphs, exec_mode):
     for name, g, og, _ in graphs:
