@@ -7,7 +7,7 @@
  *    in device helpers that the loader and validator never call, so they are
  *    mapped to the *_sync forms purely to let the headers compile.
  * 2. verifyResults (validate.cu:22,28,197,200) reads the results through
- *    cudaMemcpyAsync.  The driver hands it host arrays, so the copy becomes a
+ *    cudaMemcpyAsync.  ref_driver.cu hands it host arrays, so the copy becomes a
  *    host memcpy and the reference validator runs on a machine with no GPU.
  */
 #pragma once

@@ -261,3 +261,32 @@ def test_stage_bytes_unpinned():
     h = mg.HostGraph.rmat(8, 8, seed=1)
     rp, col, _ = h.arrays()
     assert h.stage_bytes() == 4 * len(rp) + 8 * len(col)
+
+
+def test_bench_clock_summary_from_nvml_samples():
+    """bench.py's clock record: median SM clock over samples taken under
+    load, and the throttle reasons seen under load (NVML clock-event bits)."""
+    sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+    import bench
+
+    class FakeNvml:
+        shut = False
+
+        def nvmlShutdown(self):
+            FakeNvml.shut = True
+            return 0
+
+    c = bench.ClockSampler.__new__(bench.ClockSampler)
+    c.device, c.thread, c.running, c.lib = 0, None, False, FakeNvml()
+    # (sm MHz, max MHz, utilisation %, clock-event reason bits, W)
+    c.samples = [(2070, 2070, 0, 0x1, 90.0), (2070, 2070, 97, 0x4, 1390.0), (1995, 2070, 99, 0x4, 1400.0),
+                 (2070, 2070, 98, 0x0, 1200.0)]
+    r = c.stop()
+    assert FakeNvml.shut
+    assert r["sm_mhz"] == 2070 and r["sm_max_mhz"] == 2070
+    assert r["reasons"] == ["sw_power_cap"]
+    assert r["samples"] == 4 and r["samples_under_load"] == 3
+    c2 = bench.ClockSampler.__new__(bench.ClockSampler)
+    c2.device, c2.thread, c2.running, c2.lib, c2.samples = 0, None, False, None, []
+    c2.start()  # no NVML: nothing to poll
+    assert c2.stop()["reasons"] == ["NVML unavailable"]
