@@ -465,10 +465,25 @@ __device__ __forceinline__ void sym_flush(unsigned long long *sums, unsigned lon
     }
 }
 
+// least edge weight of a staged input, kept in sums[3] as w + 2^31 (so an
+// unsigned atomicMin orders signed weights); sums[3] starts at all ones
+__device__ __forceinline__ void wmin_flush(unsigned long long *enc, int32_t w)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) w = min(w, __shfl_xor_sync(0xffffffffu, w, o));
+    if ((threadIdx.x & 31) == 0 && w != INT32_MAX) atomicMin(enc, (unsigned long long)((long long)w - INT32_MIN));
+}
+
+static int32_t wmin_decode(unsigned long long enc)
+{
+    return enc == ~0ull ? 0 : (int32_t)((long long)enc + INT32_MIN);
+}
+
 // caller CSR -> engine CSR for up to two 4-byte edge arrays; the first is
 // mapped through old2new when map_ids (column ids).  With sums, the
 // symmetry checksum of (caller row, caller column, second array) is formed
-// on the way.  A non-zero *skip (caller row offsets that differ from the
+// on the way, and the least second-array value (the weights) in sums[3].
+// A non-zero *skip (caller row offsets that differ from the
 // layout's, found by k_rows_differ earlier on the stream) returns at once:
 // the positions would not match the staged arrays.
 __global__ void k_relabel_edges(int32_t n, int32_t m, const int32_t *new2old, const int32_t *old2new,
@@ -483,6 +498,7 @@ __global__ void k_relabel_edges(int32_t n, int32_t m, const int32_t *new2old, co
     const int32_t gwarp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int32_t nwarps = (gridDim.x * blockDim.x) >> 5;
     unsigned long long s_lo = 0, s_hi = 0;
+    int32_t wlo = INT32_MAX;
     for (int32_t c0 = gwarp * RELABEL_ILP; c0 < nsteps; c0 += nwarps * RELABEL_ILP) {
         int32_t q[RELABEL_ILP], u[RELABEL_ILP];
         caller_positions(n, m, new2old, o_row, row_new, pos_row, c0, q, u);
@@ -495,7 +511,10 @@ __global__ void k_relabel_edges(int32_t n, int32_t m, const int32_t *new2old, co
         if (sums) {
 #pragma unroll
             for (int j = 0; j < RELABEL_ILP; j++)
-                if (q[j] >= 0) sym_add(s_lo, s_hi, u[j], (int32_t)x[j], y[j]);
+                if (q[j] >= 0) {
+                    sym_add(s_lo, s_hi, u[j], (int32_t)x[j], y[j]);
+                    if (dst1) wlo = min(wlo, (int32_t)y[j]);
+                }
         }
 #pragma unroll
         for (int j = 0; j < RELABEL_ILP; j++)
@@ -508,7 +527,10 @@ __global__ void k_relabel_edges(int32_t n, int32_t m, const int32_t *new2old, co
             if (dst1) dst1[p] = y[j];
         }
     }
-    if (sums) sym_flush(sums, s_lo, s_hi);
+    if (sums) {
+        sym_flush(sums, s_lo, s_hi);
+        wmin_flush(&sums[3], wlo);
+    }
 }
 
 // staged byte weights -> int32 (graphs that are not relabeled)
@@ -529,18 +551,23 @@ __global__ void k_rows_differ(int32_t n1, const int32_t *a, const int32_t *b, un
 }
 
 // symmetry checksum of a CSR without relabeling (rows below the hub
-// threshold, so a thread per row)
+// threshold, so a thread per row), and its least weight in sums[3]
 __global__ void k_sym_check(int32_t n, const int32_t *row, const int32_t *col, const int32_t *wt,
                             unsigned long long *sums)
 {
     unsigned long long s_lo = 0, s_hi = 0;
+    int32_t wlo = INT32_MAX;
     const int32_t stride = gridDim.x * blockDim.x;
     for (int32_t base = blockIdx.x * blockDim.x + (threadIdx.x & ~31); base < n; base += stride) {
         const int32_t u = base + (threadIdx.x & 31);
         if (u < n)
-            for (int32_t p = row[u]; p < row[u + 1]; p++) sym_add(s_lo, s_hi, u, col[p], (uint32_t)wt[p]);
+            for (int32_t p = row[u]; p < row[u + 1]; p++) {
+                sym_add(s_lo, s_hi, u, col[p], (uint32_t)wt[p]);
+                wlo = min(wlo, wt[p]);
+            }
     }
     sym_flush(sums, s_lo, s_hi);
+    wmin_flush(&sums[3], wlo);
 }
 
 // inverse of k_relabel_edges for per-edge payloads (engine order -> caller order)
@@ -890,7 +917,7 @@ mg_status mg_graph_upload(const mg_host_graph *h, int32_t device, mg_graph **out
     MG_CUDA(cudaEventCreateWithFlags(&g->ev_staged, cudaEventDisableTiming));
     MG_CUDA(cudaEventCreateWithFlags(&g->ev_consumed, cudaEventDisableTiming));
     MG_CUDA(cudaMallocHost(&g->pinned_flag, 64));
-    MG_CUDA(cudaMallocHost(&g->sym_host, 24));
+    MG_CUDA(cudaMallocHost(&g->sym_host, 32));
     HostLayout L;
     build_layout(*h, L);
     MG_TRY(upload_arrays(g.get(), h, L, true));
@@ -929,6 +956,20 @@ mg_status mg_graph_stage(mg_graph *g, const mg_host_graph *h)
     return MG_OK;
 }
 
+// A commit that laid the graph out again may have changed the bins, the
+// chunk lists and the least weight that captured loops carry by value:
+// drop the workspaces (and with them the captured loops) so the next runs
+// rebuild them.
+static void drop_workspaces(mg_graph *g)
+{
+    free_frontier_ws(g);
+    free_pr_ws(g);
+    free_cc_ws(g);
+    free_bc_ws(g);
+    free_ppr_ws(g);
+    free_wpr_ws(g);
+}
+
 mg_status mg_graph_commit(mg_graph *g)
 {
     clear_error();
@@ -945,6 +986,8 @@ mg_status mg_graph_commit(mg_graph *g)
         // graph's current, possibly tuned, bin parameters)
         HostLayout L;
         build_layout(*h, L, g->heavy_deg, g->hchunk_size, g->tbin);
+        MG_CUDA(cudaStreamSynchronize(s));
+        drop_workspaces(g);
         MG_TRY(upload_arrays(g, h, L, true));
     } else {
         // the layout assumes the caller row offsets it was built from and
@@ -952,9 +995,10 @@ mg_status mg_graph_commit(mg_graph *g)
         // check the staged input with the pair checksum (formed during the
         // relabel pass), read both back in one copy and lay the graph out
         // again from the host when either fails
-        MG_TRY(dev_alloc(g->sym_sums, 24));
+        MG_TRY(dev_alloc(g->sym_sums, 32));
         unsigned long long *sums = g->sym_sums.as<unsigned long long>();
         MG_CUDA(cudaMemsetAsync(sums, 0, 24, s));
+        MG_CUDA(cudaMemsetAsync(sums + 3, 0xff, 8, s));
         const int32_t *ref_row = g->relabeled ? g->o_row.as<int32_t>() : g->row.as<int32_t>();
         k_rows_differ<<<g->num_sms * 4, 256, 0, s>>>((int32_t)n + 1, g->s_row.as<int32_t>(), ref_row, sums + 2);
         MG_CUDA(cudaGetLastError());
@@ -977,17 +1021,23 @@ mg_status mg_graph_commit(mg_graph *g)
                                                        g->wt.as<int32_t>(), sums);
             MG_CUDA(cudaGetLastError());
         }
-        MG_CUDA(cudaMemcpyAsync(g->sym_host, sums, 24, cudaMemcpyDeviceToHost, s));
+        MG_CUDA(cudaMemcpyAsync(g->sym_host, sums, 32, cudaMemcpyDeviceToHost, s));
         MG_CUDA(cudaStreamSynchronize(s));
         if (g->sym_host[2] != 0 || g->sym_host[0] != g->sym_host[1]) {
             HostLayout L;
             build_layout(*h, L, g->heavy_deg, g->hchunk_size, g->tbin);
+            drop_workspaces(g);
             MG_TRY(upload_arrays(g, h, L, true));
-        } else if (g->relabeled) {
-            // the staged arrays are now the current graph's caller-order CSR
-            std::swap(g->o_row, g->s_row);
-            std::swap(g->o_col, g->s_col);
-            std::swap(g->o_wt, g->s_wt);
+        } else {
+            // same layout, new weights: their least value bounds the SSSP
+            // pull's settled-row skip and gates SSSP on negative weights
+            g->min_weight = wmin_decode(g->sym_host[3]);
+            if (g->relabeled) {
+                // the staged arrays are now the current graph's caller-order CSR
+                std::swap(g->o_row, g->s_row);
+                std::swap(g->o_col, g->s_col);
+                std::swap(g->o_wt, g->s_wt);
+            }
         }
     }
     MG_CUDA(cudaEventRecord(g->ev_consumed, s));

@@ -1061,6 +1061,7 @@ static uint64_t key_of(const Args &a, int alg)
     uint64_t k = 1469598103934665603ull ^ (uint64_t)alg;
     const void *ptrs[] = {a.row, a.col, a.trow, a.tcol, a.label, a.sigma, a.bm, a.queue, a.heavy, a.ctl, a.wrows};
     for (const void *p : ptrs) k = (k ^ (uint64_t)(uintptr_t)p) * 1099511628211ull;
+    k = (k ^ (uint64_t)(uint32_t)a.wmin) * 1099511628211ull;  // the SSSP skip bound's least weight
     k ^= (uint64_t)a.bar_never << 63;  // captured kernel arguments include the injection flag
     k ^= (uint64_t)a.bc_ext << 62;     // and the path-count mode
     return k;

@@ -152,3 +152,96 @@ def test_staged_byte_weights(kind, wmax):
     d, _ = g.sssp(0)
     assert np.array_equal(d, O.sssp(O.csr_from_arrays(rp, col, wt), 0)[0])
     g.free()
+
+
+def _pairs(h):
+    rp, col, wt = h.arrays()
+    n = len(rp) - 1
+    src = np.repeat(np.arange(n, dtype=np.int64), np.diff(rp))
+    keep = src < col
+    return n, src[keep], col[keep].astype(np.int64), wt[keep].astype(np.int64)
+
+
+def _sym_csr(n, u, v, w):
+    """Symmetric CSR (both directions, one weight per pair)."""
+    s = np.concatenate([u, v])
+    d = np.concatenate([v, u])
+    ww = np.concatenate([w, w])
+    order = np.lexsort((d, s))
+    rp = np.zeros(n + 1, np.int64)
+    rp[1:] = np.cumsum(np.bincount(s, minlength=n))
+    return rp.astype(np.int32), d[order].astype(np.int32), ww[order].astype(np.int32)
+
+
+@pytest.mark.parametrize("direction", [mg.DIR_AUTO, mg.DIR_PULL])
+@pytest.mark.parametrize("pin", [False, True])   # int32 / byte-weight staging
+def test_commit_lowers_least_weight(direction, pin):
+    """New weights on the same structure with a smaller least weight: the
+    SSSP pull's settled-row bound must use the new least weight (also in
+    loops captured before the commit), and a negative weight must be
+    refused after the commit."""
+    n, u, v, _ = _pairs(mg.HostGraph.rmat(12, 16, seed=41))
+    rng = np.random.default_rng(3)
+    h0, og0 = _csr(*_sym_csr(n, u, v, rng.integers(40, 64, len(u))))
+    h1, og1 = _csr(*_sym_csr(n, u, v, rng.integers(1, 64, len(u))))
+    if pin:
+        h1.pin()
+    g = mg.Graph(h0)
+    for ex in (mg.EXEC_GRAPH, mg.EXEC_HOST):
+        d, _ = g.sssp(0, direction=direction, exec=ex)
+        assert np.array_equal(d, O.sssp(og0, 0)[0])
+    g.stage(h1)
+    g.commit()
+    for ex in (mg.EXEC_GRAPH, mg.EXEC_HOST):
+        for s in (0, 77, n - 1):
+            d, _ = g.sssp(s, direction=direction, exec=ex)
+            assert np.array_equal(d, O.sssp(og1, s)[0]), (ex, s)
+    w2 = rng.integers(1, 64, len(u))
+    w2[5] = -3
+    h2, _ = _csr(*_sym_csr(n, u, v, w2))
+    g.stage(h2)
+    g.commit()
+    with pytest.raises(mg.MGError) as e:
+        g.sssp(0)
+    assert e.value.status == mg.MG_ERR_INVALID
+    g.free()
+
+
+def test_commit_new_degrees_same_size_rebuilds_loops():
+    """Same n and m, hub edges rewired to low-degree vertices: the commit
+    lays the graph out again (the hub leaves the heavy-row chunks), and
+    loops captured before it must not replay the old bins."""
+    n, u, v, w = _pairs(mg.HostGraph.rmat(12, 16, seed=42))
+    deg = np.bincount(np.concatenate([u, v]), minlength=n)
+    hub = int(np.argmax(deg))
+    at_hub = np.nonzero((u == hub) | (v == hub))[0]
+    k = len(at_hub) - 8
+    assert deg[hub] > 600 and k > 500
+    keep = np.ones(len(u), bool)
+    keep[at_hub[:k]] = False
+    have = set(zip(u[keep].tolist(), v[keep].tolist()))
+    rng = np.random.default_rng(9)
+    low = np.nonzero(deg <= 4)[0]
+    nu, nv_ = [], []
+    while len(nu) < k:
+        a, b = sorted(rng.choice(low, 2, replace=False).tolist())
+        if (a, b) not in have:
+            have.add((a, b))
+            nu.append(a)
+            nv_.append(b)
+    u2 = np.concatenate([u[keep], nu])
+    v2 = np.concatenate([v[keep], nv_])
+    w2 = np.concatenate([w[keep], rng.integers(1, 64, k)])
+    h0, og0 = _csr(*_sym_csr(n, u, v, w))
+    h2, og2 = _csr(*_sym_csr(n, u2, v2, w2))
+    g = mg.Graph(h0)
+    _check_all(g, og0, 0)
+    g.stage(h2)
+    g.commit()
+    _check_all(g, og2, 0)
+    _check_all(g, og2, hub)
+    (_, sg, dl), _ = g.bc(3)
+    _, rsg, rdl = O.bc_f64(og2, 3)
+    assert np.array_equal(sg, rsg)
+    assert float(np.max(np.abs(dl - rdl) / np.maximum(np.abs(rdl), 1.0))) < 1e-5
+    g.free()
