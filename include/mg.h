@@ -146,7 +146,9 @@ mg_status mg_graph_reload(mg_graph *dg, const mg_host_graph *g);
  * the staged copy has buffers of its own.  mg_graph_commit makes later runs
  * wait for the copy and rebuilds the device CSR from it on the graph's
  * stream (row offsets compared on the device; a relabel pass when they
- * match the layout's).  No reference counterpart. */
+ * match the layout's, which also takes the new weights' least value for
+ * SSSP; otherwise the graph is laid out again and captured loops are
+ * rebuilt on their next run).  No reference counterpart. */
 mg_status mg_graph_stage(mg_graph *dg, const mg_host_graph *g);
 mg_status mg_graph_commit(mg_graph *dg);
 /* Replaces release_MultiGraph (release_structure.cu:4). */
