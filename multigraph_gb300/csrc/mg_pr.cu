@@ -987,8 +987,14 @@ mg_status mg_ppr_batch(mg_graph *g, const int32_t *seeds, int32_t nseeds, const 
             MG_CUDA(cudaGetLastError());
             return MG_OK;
         };
-        uint64_t key = 0x51ed270b27ull ^ (uint64_t)(uintptr_t)a.seeds ^ ((uint64_t)a.nseed << 48) ^
-                       ((uint64_t)(uintptr_t)a.X0 * 3) ^ ((uint64_t)(uintptr_t)a.hpart * 7) ^ ((uint64_t)(uintptr_t)a.ctl * 11);
+        // the captured kernels take the damping and the tolerance by value
+        uint32_t dbits, tbits;
+        std::memcpy(&dbits, &a.damping, 4);
+        std::memcpy(&tbits, &tol, 4);
+        uint64_t key = 0x51ed270b27ull ^ ((uint64_t)a.nseed << 48);
+        const void *ptrs[] = {a.seeds, a.X0, a.hpart, a.ctl, a.prow, a.pcol, a.hchunk};
+        for (const void *p : ptrs) key = (key ^ (uint64_t)(uintptr_t)p) * 0x100000001b3ull;
+        key = (key ^ ((uint64_t)dbits << 32 | tbits)) * 0x100000001b3ull;
         MG_TRY(run_loop(opt.profile ? MG_EXEC_HOST : opt.exec, opt.profile != 0, s, w->lg, key, body, &a.ctl->more,
                         g->pinned_flag, max_iter + 2));
         PPCtl hc;

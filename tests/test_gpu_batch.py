@@ -114,6 +114,25 @@ def test_ppr_batch_many_blocks():
     g.free()
 
 
+def test_ppr_batch_new_damping_and_tolerance():
+    """Calls with the same seed count reuse the captured loop only when the
+    damping and the tolerance (kernel arguments) are unchanged."""
+    h = mg.HostGraph.rmat(10, 16, seed=8)
+    g, og = _pair(h)
+    seeds = np.arange(0, 20) * 11 % og.nv
+    sweeps = {}
+    for d, tol in ((0.85, 1e-6), (0.5, 1e-6), (0.5, 1e-3), (0.85, 1e-6)):
+        x, info = g.ppr_batch(seeds, tol=tol, damping=d)
+        sweeps[(d, tol)] = info.iterations
+        for i in (0, 7, 19):
+            ref, _ = O.ppr_f64(og, int(seeds[i]), d, 1e-12)
+            err = float(np.max(np.abs(x[i].astype(np.float64) - ref)))
+            assert err < (1e-5 if tol < 1e-4 else 1e-2), (d, tol, i, err)
+    # a looser tolerance stops earlier (a replayed loop would keep 1e-6)
+    assert sweeps[(0.5, 1e-3)] < sweeps[(0.5, 1e-6)], sweeps
+    g.free()
+
+
 def _weighted(scale=10, seed=9):
     h = mg.HostGraph.rmat(scale, 16, seed=seed)
     g, og = _pair(h)
