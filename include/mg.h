@@ -308,18 +308,22 @@ mg_status mg_autotune(mg_graph *dg, int32_t algo, int32_t source, const char *ca
  * device allocator or pool callback, applications that reserve all device
  * memory at start-up, latency-bound loops where an allocation could
  * synchronise the device.  The caller passes device arrays it already owns:
- * a symmetric CSR (d_row [nv+1], d_col [ne], every edge stored both ways as
- * the loader's MG_LOAD_SYM produces it) and d_rank [nv] for the result.
+ * a symmetric CSR (d_row [nv+1] with d_row[0] == 0 and d_row[nv] == ne,
+ * checked; d_col [ne], every edge stored both ways as the loader's
+ * MG_LOAD_SYM produces it) and d_rank [nv] for the result.  damping 0
+ * selects 0.85, otherwise it must lie in (0, 1); tol 0 selects 1e-6,
+ * otherwise it must be positive (MG_ERR_INVALID).
  * Every intermediate lives in one fixed device array inside libmg sized for
  * MG_NOALLOC_MAX_VERTICES vertices (about 12 MB, held by each GPU that loads
  * the library until the process exits); larger graphs are rejected with
  * MG_ERR_RANGE.  Nothing is allocated: no cudaMalloc, cudaFree or allocating
  * library call.  Same result as mg_pagerank(MG_PR_TOPOLOGY): normalised
  * PageRank from x = 1/n until the L1 change <= tol.  Works on the current
- * device and enqueues on `stream` (a cudaStream_t, NULL = default stream).
- * The first call on a device looks up the array's device address; make it
- * before any stream capture.  All calls share the array: calls that overlap
- * on the GPU race. */
+ * device and enqueues on `stream` (a cudaStream_t, NULL = default stream);
+ * the call waits for that stream before it returns (it reads the
+ * convergence word back after every batch of 8 sweeps).  The first call on
+ * a device looks up the array's device address; make it before any stream
+ * capture.  All calls share the array: calls that overlap on the GPU race. */
 #define MG_NOALLOC_MAX_VERTICES (1 << 20)
 mg_status mg_pagerank_noalloc(const int32_t *d_row, const int32_t *d_col, int32_t nv, int32_t ne, float damping,
                               float tol, int32_t max_iter, float *d_rank, void *stream, int32_t *iterations_out,

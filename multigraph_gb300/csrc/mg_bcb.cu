@@ -331,11 +331,9 @@ mg_status bc_batched(mg_graph *g, const int32_t *src_engine, int32_t nsrc, const
         MG_CUDA(cudaGetLastError());
         return MG_OK;
     };
-    uint64_t key = 0x6263622d66776400ull;
-    const void *ptrs[] = {a.row, a.col, a.trow, a.tcol, a.vis, a.fm0, a.arch, a.sig, a.q, a.hpart, a.bc, a.ctl};
-    for (const void *p : ptrs) key = (key ^ (uint64_t)(uintptr_t)p) * 1099511628211ull;
-    key ^= (uint64_t)grid << 48 ^ (uint64_t)grid_f << 32 ^ (uint64_t)grid_b << 16 ^ (uint64_t)heavy ^
-           (uint64_t)a.ext << 1;
+    // every by-value argument of the captured kernels
+    const LoopKey key = LoopKey().add(a).add(grid).add(grid_f).add(grid_b).add(heavy).add(tp);
+    const LoopKey key_b = LoopKey(key).add(1);
     const int mode = opt.profile ? MG_EXEC_HOST : opt.exec;
     int32_t levels = 0, dense_levels = 0;
     for (int32_t g0 = 0; g0 < nsrc; g0 += W) {
@@ -348,7 +346,7 @@ mg_status bc_batched(mg_graph *g, const int32_t *src_engine, int32_t nsrc, const
         MG_TRY(run_loop(mode, opt.profile != 0, s, w->fwd, key, fwd, &a.ctl->more, g->pinned_flag, max_levels + 2));
         k_bbb_start<<<grid, THREADS, 0, s>>>(a);
         MG_CUDA(cudaGetLastError());
-        MG_TRY(run_loop(mode, opt.profile != 0, s, w->bwd, key ^ 0x5a5a, bwd, &a.ctl->more, g->pinned_flag,
+        MG_TRY(run_loop(mode, opt.profile != 0, s, w->bwd, key_b, bwd, &a.ctl->more, g->pinned_flag,
                         max_levels + 2));
         BbCtl hc;
         MG_CUDA(cudaMemcpyAsync(&hc, a.ctl, sizeof(hc), cudaMemcpyDeviceToHost, s));

@@ -133,14 +133,14 @@ void LoopGraph::destroy()
     if (graph) cudaGraphDestroy(graph);
     exec = nullptr;
     graph = nullptr;
-    key = 0;
+    key.clear();
 }
 
-mg_status run_loop(int exec_mode, bool profile, cudaStream_t stream, LoopGraph &lg, uint64_t key, const BodyFn &body,
+mg_status run_loop(int exec_mode, bool profile, cudaStream_t stream, LoopGraph &lg, const LoopKey &key, const BodyFn &body,
                    const int32_t *more_dev, int32_t *more_host, int max_host_iters)
 {
     if (exec_mode == MG_EXEC_GRAPH && !profile) {
-        if (!lg.exec || lg.key != key) {
+        if (!lg.exec || lg.key != key.bytes) {
             lg.destroy();
             cudaGraph_t g;
             MG_CUDA(cudaGraphCreate(&g, 0));
@@ -167,7 +167,7 @@ mg_status run_loop(int exec_mode, bool profile, cudaStream_t stream, LoopGraph &
             if (e != cudaSuccess) { cudaGraphDestroy(g); MG_CUDA(e); }
             lg.graph = g;
             lg.exec = ex;
-            lg.key = key;
+            lg.key = key.bytes;
         }
         MG_CUDA(cudaGraphLaunch(lg.exec, stream));
         return MG_OK;
@@ -968,6 +968,10 @@ static void drop_workspaces(mg_graph *g)
     free_bc_ws(g);
     free_ppr_ws(g);
     free_wpr_ws(g);
+    // the personalised-PageRank heavy-row table follows the pull offsets of
+    // the old layout: rebuild it on the next mg_ppr_batch
+    g->ppr_nhchunks = -1;
+    g->ppr_nhrows = 0;
 }
 
 mg_status mg_graph_commit(mg_graph *g)

@@ -72,14 +72,27 @@ private:
 // set, and always write the continue flag to *more_dev.
 using BodyFn = std::function<mg_status(cudaStream_t, cudaGraphConditionalHandle, int)>;
 
+// Key of a captured loop: the raw bytes of every by-value argument its
+// kernels take (whole argument structs, zero-filled before they are set so
+// that padding compares equal, plus launch shapes and scalars).  A cached
+// loop is replayed only when the key matches byte for byte.
+struct LoopKey {
+    std::string bytes;
+    template <class T> LoopKey &add(const T &v)
+    {
+        bytes.append(reinterpret_cast<const char *>(&v), sizeof(T));
+        return *this;
+    }
+};
+
 struct LoopGraph {
     cudaGraphExec_t exec = nullptr;
     cudaGraph_t graph = nullptr;
-    uint64_t key = 0;
+    std::string key;
     void destroy();
 };
 
-mg_status run_loop(int exec_mode, bool profile, cudaStream_t stream, LoopGraph &lg, uint64_t key,
+mg_status run_loop(int exec_mode, bool profile, cudaStream_t stream, LoopGraph &lg, const LoopKey &key,
                    const BodyFn &body, const int32_t *more_dev, int32_t *more_host, int max_host_iters);
 
 }  // namespace mgi

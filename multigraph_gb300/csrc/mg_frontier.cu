@@ -1056,15 +1056,12 @@ static Args make_args(mg_graph *g)
     return a;
 }
 
-static uint64_t key_of(const Args &a, int alg)
+// every by-value argument of the captured kernels: the whole Args (pointers,
+// sizes, the SSSP skip bound's least weight, the injection flag, the
+// path-count mode) and the launch grids
+static LoopKey key_of(const Args &a, int alg, int grid, int coop_grid)
 {
-    uint64_t k = 1469598103934665603ull ^ (uint64_t)alg;
-    const void *ptrs[] = {a.row, a.col, a.trow, a.tcol, a.label, a.sigma, a.bm, a.queue, a.heavy, a.ctl, a.wrows};
-    for (const void *p : ptrs) k = (k ^ (uint64_t)(uintptr_t)p) * 1099511628211ull;
-    k = (k ^ (uint64_t)(uint32_t)a.wmin) * 1099511628211ull;  // the SSSP skip bound's least weight
-    k ^= (uint64_t)a.bar_never << 63;  // captured kernel arguments include the injection flag
-    k ^= (uint64_t)a.bc_ext << 62;     // and the path-count mode
-    return k;
+    return LoopKey().add(alg).add(a).add(grid).add(coop_grid);
 }
 
 // Forward traversal of `alg` from src (or from the nsrc sources in srcs_host
@@ -1138,7 +1135,7 @@ static mg_status frontier_run_impl(mg_graph *g, int alg, int32_t src, const int3
         MG_CUDA(cudaGetLastError());
         return MG_OK;
     };
-    MG_TRY(run_loop(opt.profile ? MG_EXEC_HOST : opt.exec, opt.profile != 0, s, w->lg[alg], key_of(a, alg), body,
+    MG_TRY(run_loop(opt.profile ? MG_EXEC_HOST : opt.exec, opt.profile != 0, s, w->lg[alg], key_of(a, alg, grid, w->coop_grid[alg]), body,
                     &a.ctl->more, g->pinned_flag, max_iter + 2));
     // status readback
     FCtl hc;

@@ -17,10 +17,14 @@
 // Host code cannot use the array's name as a device address: it is a
 // host-side stand-in.  The first call on a device (that device current) asks
 // the runtime for the array's device address with cudaGetSymbolAddress and
-// caches it; make that first call before any stream capture.  All calls share
-// the array and it keeps the last call's contents; every call re-initialises
-// what it reads.  Calls that overlap on the GPU (two streams, or a call
-// enqueued before the previous one finished) race on the array.
+// caches it; make that first call before any stream capture.  Each call
+// waits for its stream: it enqueues sweeps in batches of NA_BATCH and reads
+// the control word back after each batch (sweeps after convergence are
+// no-ops, so the batching changes neither the result nor the sweep count).
+// All calls share the array and it keeps the last call's contents; every
+// call re-initialises what it reads.  Calls that overlap on the GPU (two
+// streams, or a call enqueued before the previous one finished) race on the
+// array.
 
 #include "mg_device.cuh"
 
@@ -31,6 +35,7 @@ namespace {
 
 constexpr int NA_THREADS = 256;
 constexpr int NA_MAX_BLOCKS = 1024;
+constexpr int NA_BATCH = 8;  // sweep + finish pairs enqueued per readback
 
 struct NaCtl {
     int32_t more, iter, cur, pad;
@@ -177,6 +182,23 @@ extern "C" mg_status mg_pagerank_noalloc(const int32_t *d_row, const int32_t *d_
     if (nv > MG_NOALLOC_MAX_VERTICES)
         return mgi::fail(MG_ERR_RANGE, "mg_pagerank_noalloc handles at most %d vertices (got %d)",
                          MG_NOALLOC_MAX_VERTICES, nv);
+    // 0 selects the default; anything else must be a damping in (0, 1) and a
+    // positive tolerance (NaN fails both tests)
+    if (damping != 0.0f && !(damping > 0.0f && damping < 1.0f))
+        return mgi::fail(MG_ERR_INVALID, "damping %g outside (0, 1)", (double)damping);
+    if (tol != 0.0f && !(tol > 0.0f))
+        return mgi::fail(MG_ERR_INVALID, "tolerance %g is not positive", (double)tol);
+    cudaStream_t s = (cudaStream_t)stream;
+    {
+        // the row offsets must span exactly the ne column ids
+        int32_t ends[2] = {-1, -1};
+        MG_CUDA(cudaMemcpyAsync(&ends[0], d_row, 4, cudaMemcpyDeviceToHost, s));
+        MG_CUDA(cudaMemcpyAsync(&ends[1], d_row + nv, 4, cudaMemcpyDeviceToHost, s));
+        MG_CUDA(cudaStreamSynchronize(s));
+        if (ends[0] != 0 || ends[1] != ne)
+            return mgi::fail(MG_ERR_INVALID, "row offsets run from %d to %d, expected 0 to ne = %d", ends[0], ends[1],
+                             ne);
+    }
     int dev = 0;
     MG_CUDA(cudaGetDevice(&dev));
     unsigned char *base = nullptr;
@@ -184,7 +206,6 @@ extern "C" mg_status mg_pagerank_noalloc(const int32_t *d_row, const int32_t *d_
     int nsm = 0;
     MG_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
     const int nblocks = std::max(1, std::min(NA_MAX_BLOCKS, nsm * 4));
-    cudaStream_t s = (cudaStream_t)stream;
     NaArgs a;
     a.n = nv;
     a.row = d_row;
@@ -195,16 +216,21 @@ extern "C" mg_status mg_pagerank_noalloc(const int32_t *d_row, const int32_t *d_
     a.c[1] = (float *)(base + 2 * NA_VEC);
     a.part = (double *)(base + 3 * NA_VEC);
     a.ctl = (NaCtl *)(base + 3 * NA_VEC + NA_PART);
-    a.damping = damping > 0.0f ? damping : 0.85f;
-    a.tol = tol > 0.0f ? tol : 1e-6f;
+    a.damping = damping != 0.0f ? damping : 0.85f;
+    a.tol = tol != 0.0f ? tol : 1e-6f;
     a.max_iter = max_iter > 0 ? max_iter : 10000;
     k_na_init<<<nblocks, NA_THREADS, 0, s>>>(a);
     k_na_init_ctl<<<1, 32, 0, s>>>(a, nblocks);
     MG_CUDA(cudaGetLastError());
     NaCtl h;
-    for (int it = 0; it < a.max_iter; it++) {
-        k_na_sweep<<<nblocks, NA_THREADS, 0, s>>>(a);
-        k_na_finish<<<1, 32, 0, s>>>(a, nblocks);
+    for (int it = 0; it < a.max_iter; it += NA_BATCH) {
+        // once the control word says stop, the remaining pairs of the batch
+        // return at once; k_na_finish stops at max_iter by itself
+        const int k = std::min(NA_BATCH, a.max_iter - it);
+        for (int j = 0; j < k; j++) {
+            k_na_sweep<<<nblocks, NA_THREADS, 0, s>>>(a);
+            k_na_finish<<<1, 32, 0, s>>>(a, nblocks);
+        }
         MG_CUDA(cudaGetLastError());
         MG_CUDA(cudaMemcpyAsync(&h, a.ctl, sizeof(NaCtl), cudaMemcpyDeviceToHost, s));
         MG_CUDA(cudaStreamSynchronize(s));

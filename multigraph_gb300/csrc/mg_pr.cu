@@ -631,13 +631,6 @@ void free_ppr_ws(mg_graph *g)
 
 void free_wpr_ws(mg_graph *g) { (void)g; }
 
-static uint64_t pkey(const PArgs &a, int v)
-{
-    uint64_t k = 0xcbf29ce484222325ull ^ (uint64_t)v;
-    const void *ptrs[] = {a.prow, a.pcol, a.pw, a.x[0], a.x[1], a.c[0], a.c[1], a.active, a.hpart, a.bpart, a.ctl, a.S, a.gvec};
-    for (const void *p : ptrs) k = (k ^ (uint64_t)(uintptr_t)p) * 0x100000001b3ull;
-    return k;
-}
 
 // Runs sweeps of variant V until convergence; the result is x[ctl.cur]
 // (c[ctl.cur] for the adjoint).
@@ -668,7 +661,9 @@ static mg_status pr_loop(mg_graph *g, PArgs &a, const mg_opts &opt, const char *
         return MG_OK;
     };
     int max_iter = opt.max_iter > 0 ? opt.max_iter : 10000;
-    MG_TRY(run_loop(opt.profile ? MG_EXEC_HOST : opt.exec, opt.profile != 0, s, g->pws->lg[V], pkey(a, V), body,
+    // the key holds every by-value argument of the captured kernels
+    const LoopKey key = LoopKey().add(V).add(a).add(grid).add(apply_grid);
+    MG_TRY(run_loop(opt.profile ? MG_EXEC_HOST : opt.exec, opt.profile != 0, s, g->pws->lg[V], key, body,
                     &a.ctl->more, g->pinned_flag, max_iter + 2));
     PCtl hc;
     MG_CUDA(cudaMemcpyAsync(&hc, a.ctl, sizeof(PCtl), cudaMemcpyDeviceToHost, s));
@@ -987,14 +982,9 @@ mg_status mg_ppr_batch(mg_graph *g, const int32_t *seeds, int32_t nseeds, const 
             MG_CUDA(cudaGetLastError());
             return MG_OK;
         };
-        // the captured kernels take the damping and the tolerance by value
-        uint32_t dbits, tbits;
-        std::memcpy(&dbits, &a.damping, 4);
-        std::memcpy(&tbits, &tol, 4);
-        uint64_t key = 0x51ed270b27ull ^ ((uint64_t)a.nseed << 48);
-        const void *ptrs[] = {a.seeds, a.X0, a.hpart, a.ctl, a.prow, a.pcol, a.hchunk};
-        for (const void *p : ptrs) key = (key ^ (uint64_t)(uintptr_t)p) * 0x100000001b3ull;
-        key = (key ^ ((uint64_t)dbits << 32 | tbits)) * 0x100000001b3ull;
+        // the captured kernels take the whole PPArgs (pointers, counts, the
+        // heavy-row table, damping), the tolerance and the grid by value
+        const LoopKey key = LoopKey().add(a).add(tol).add(grid);
         MG_TRY(run_loop(opt.profile ? MG_EXEC_HOST : opt.exec, opt.profile != 0, s, w->lg, key, body, &a.ctl->more,
                         g->pinned_flag, max_iter + 2));
         PPCtl hc;

@@ -36,6 +36,13 @@ def _check_all(g, og, src):
     x, info = g.pagerank(mg.PR_TOPOLOGY, tol=1e-6)
     ref, _ = O.pr_norm_f64(og, 0.85, 1e-6, info.iterations)
     assert float(np.max(np.abs(x.astype(np.float64) - ref))) < 1e-6
+    # personalised PageRank keeps its own heavy-row table (rows above 256
+    # in-edges in chunks): it must follow a re-layout
+    seeds = [src, og.nv - 1]
+    pp, pinfo = g.ppr_batch(seeds, tol=1e-7)
+    for i, s_ in enumerate(seeds):
+        pref, _ = O.ppr_f64(og, s_, 0.85, 0.0, pinfo.iterations)
+        assert float(np.max(np.abs(pp[i].astype(np.float64) - pref))) < 1e-6, s_
 
 
 @pytest.mark.parametrize("kind", ["rmat", "lattice"])   # relabeled / not relabeled
@@ -51,6 +58,8 @@ def test_reload_new_weights_and_new_structure(kind):
     _check_all(g, og1, 0)
     # same n and m, different degrees: laid out again
     h2, og2 = _csr(*_permuted(rp, col, wt2, 2))
+    if kind == "rmat":
+        assert int(np.max(np.diff(og2.csc_v))) > 256  # heavy personalised-PageRank rows
     g.reload(h2)
     _check_all(g, og2, 3)
     g.free()
