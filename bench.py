@@ -16,8 +16,13 @@ and batched_vs_plain: multi-source BC, personalised PageRank and the
 PageRank adjoint's forward / forward+backward times (skip with --no-batch).
 
 --impl reference times the reference's CPU implementation of the path (the
-oracle port of validate.cu: Bellman-Ford SSSP and the PageRank recurrence)
-on the host cores; rank 0 only.
+oracle port of validate.cu: Bellman-Ford SSSP and FP64 PageRank) on the host
+cores, whole steps, on the same R-MAT input built by the oracle's own
+generator (the product library is not loaded); rank 0 only.
+
+Every result of the GPU arm carries its error against the oracle: the timed
+step's SSSP distances (bit_exact) and PageRank vector (max_abs_err against
+FP64 run for the same sweeps), and each batched_vs_plain entry's result.
 
 Multi-GPU: the path does not shard (one traversal per graph), so N GPUs run
 N independent replicas (weak scaling); value = all ranks' edges / max time.
@@ -177,18 +182,18 @@ def build_graph(scale):
     return mg.HostGraph.rmat(scale, EDGE_FACTOR, seed=scale)
 
 
-def cpu_oracle_run(rp, col, wt, counts=None):
-    """The oracle's restatement of validate.cu on this host: Bellman-Ford SSSP
-    (validate.cu:131-148) and FP64 normalised PageRank.  Runs the full
-    workload (counts=None) or `counts = (sweeps, iterations)` of it."""
+def cpu_oracle_step(og):
+    """One step of the oracle's restatement of validate.cu on this host:
+    Bellman-Ford SSSP from 0 (validate.cu:131-148) and FP64 normalised
+    PageRank to the same L1 tolerance.  Returns (seconds SSSP, sweeps,
+    distances, seconds PageRank, sweeps, ranks)."""
     from oracle import oracle as O
-    g = O.csr_from_arrays(rp, col, wt)
     t0 = time.perf_counter()
-    _, sweeps = O.sssp(g, 0, counts[0] if counts else 0)
+    dist, sweeps = O.sssp(og, 0)
     t1 = time.perf_counter()
-    _, iters = O.pr_norm_f64(g, DAMPING, TOL, counts[1] if counts else 0)
+    x, iters = O.pr_norm_f64(og, DAMPING, TOL)
     t2 = time.perf_counter()
-    return t1 - t0, sweeps, t2 - t1, iters
+    return t1 - t0, sweeps, dist, t2 - t1, iters, x
 
 
 def batch_report(mg, device, exec_mode=None):
@@ -203,17 +208,27 @@ def batch_report(mg, device, exec_mode=None):
                  (0, 1], forward alone vs forward + backward
       lattice_bc_64: 64-source BC on the 4096 x 4096 lattice with 5 %
                  diagonal shortcuts; the plain figure is 64 x the mean of
-                 two timed single-source runs (a full plain sweep takes
-                 about 11 s); the batched and plain results of those two
+                 eight timed single-source runs (a full plain sweep takes
+                 about 9 s); the batched and plain results of those eight
                  sources are compared
-    Each entry carries the agreement of the two results."""
+    Each entry carries the agreement of the two results and the batched
+    result's error against the oracle (FP64 multi-source Brandes over all
+    256 sources; FP64 personalised PageRank for the same sweeps; BFS / CC
+    per graph; the FP64 adjoint's gradient; a long-double Brandes for two
+    lattice sources), computed on host threads while the GPU goes on."""
     import numpy as np
+    from concurrent.futures import ThreadPoolExecutor
+    from oracle import oracle as O
+    pool = ThreadPoolExecutor(max_workers=max(1, min(16, os.cpu_count() or 1)))
     out = {}
     ex = {} if exec_mode is None else {"exec": exec_mode}
     h = mg.HostGraph.rmat(20, EDGE_FACTOR, seed=20)
+    rp, col, wt = h.arrays()
+    og20 = O.csr_from_arrays(rp, col, wt)
     g = mg.Graph(h, device)
     rng = np.random.default_rng(20)
     src = rng.integers(0, g.nv, 256).astype(np.int32)
+    f_bc = [pool.submit(O.bc_multi_f64, og20, src[k:k + 32]) for k in range(0, 256, 32)]
     g.bc_multi(src[:32], out=False, **ex)
     bcb, ib = g.bc_multi(src, **ex)
     _, ib2 = g.bc_multi(src, out=False, **ex)
@@ -239,12 +254,29 @@ def batch_report(mg, device, exec_mode=None):
         x1, p1 = g.ppr_batch([int(s_)], tol=TOL)
         tp += p1.device_ms
         diff = max(diff, float(np.max(np.abs(x1[0] - xb[i]))))
+    # oracle: the first and last seed, FP64 for the sweeps of their 32-seed group
+    f_ppr = []
+    for k in (0, 224):
+        _, gi = g.ppr_batch(seeds[k:k + 32], out=False, tol=TOL)
+        for i in (k, k + 31):
+            f_ppr.append((i, pool.submit(O.ppr_f64, og20, int(seeds[i]), DAMPING, 0.0, gi.iterations)))
     out["ppr_256"] = {"graph": f"rmat20_ef16 n={g.nv} m={g.ne}", "batched_ms": tb, "plain_ms": tp,
                       "speedup": tp / tb, "sweeps": pb.iterations, "max_abs_diff": diff}
     g.free()
+    bc_ref = np.sum([f.result() for f in f_bc], axis=0)
+    out["bc_256"]["oracle_max_rel_err"] = float(np.max(np.abs(bcb - bc_ref)) / np.max(np.abs(bc_ref)))
+    out["bc_256"]["oracle"] = "FP64 Brandes over all 256 sources; bound 1e-5 (normwise relative)"
+    out["ppr_256"]["oracle_max_abs_err"] = max(float(np.max(np.abs(xb[i].astype(np.float64) - f.result()[0])))
+                                               for i, f in f_ppr)
+    out["ppr_256"]["oracle"] = "FP64 for seeds 0, 31, 224, 255 at their group's sweeps; bound 1e-6"
     rng = np.random.default_rng(64)
     hs = [mg.HostGraph.rmat(int(sc), int(ef), seed=int(i) + 1) for i, (sc, ef) in
           enumerate(zip(rng.integers(10, 19, 64), rng.integers(8, 33, 64)))]
+    ogs = []
+    for hh in hs:
+        a, b_, c_ = hh.arrays()
+        ogs.append(O.csr_from_arrays(a, b_, c_))
+    f_graphs = [pool.submit(lambda og: (O.bfs(og, 0), O.cc_minlabel(og)), og) for og in ogs]
     b = mg.Batch(hs, device)
     srcs = [0] * len(hs)
     b.bfs(srcs)
@@ -262,76 +294,107 @@ def batch_report(mg, device, exec_mode=None):
         same = same and bool(np.array_equal(lv, lb[k]) and np.array_equal(lab, cb[k]))
         gg.free()
     b.free()
+    oracle_exact = all(np.array_equal(lb[k], f.result()[0]) and np.array_equal(cb[k], f.result()[1])
+                       for k, f in enumerate(f_graphs))
     out["graphs_64"] = {"graphs": "64 R-MAT, scales U{10..18}, edge factor U{8..32}",
                         "edges": int(sum(hh.ne for hh in hs)), "batched_ms": tb, "plain_ms": tp,
-                        "speedup": tp / tb, "bit_exact": same}
+                        "speedup": tp / tb, "bit_exact": same, "oracle_bit_exact": bool(oracle_exact)}
     h = mg.HostGraph.rmat(21, EDGE_FACTOR, seed=21)
+    rp, col, wt = h.arrays()
+    og21 = O.csr_from_arrays(rp, col, wt)
     g = mg.Graph(h, device)
     rng = np.random.default_rng(21)
     w = rng.uniform(0.0, 1.0, g.ne)
     w = np.where(w == 0.0, 1.0, w).astype(np.float32)
     g.set_float_weights(w)
     gv = rng.standard_normal(g.nv).astype(np.float32)
+
+    def adjoint_ref():
+        w64, g64 = w.astype(np.float64), gv.astype(np.float64)
+        x64, _ = O.wpr_f64(og21, w64, DAMPING, 1e-14, 400)
+        _, gw64, _, _ = O.wpr_adjoint_f64(og21, w64, x64, g64, DAMPING, 1e-9 * float(np.sum(np.abs(g64))), 400)
+        return x64, gw64
+
+    f_adj = pool.submit(adjoint_ref)
     g.wpagerank(out=False, tol=TOL)
-    _, fi = g.wpagerank(out=False, tol=TOL)
-    _, bi = g.wpagerank_backward(gv, out=False, tol=TOL)
+    xw, fi = g.wpagerank(tol=TOL)
+    (grad, _), bi = g.wpagerank_backward(gv, tol=TOL)
     out["adjoint"] = {"graph": f"rmat21_ef16 n={g.nv} m={g.ne}", "forward_ms": fi.device_ms,
                       "backward_ms": bi.device_ms, "forward_backward_ms": fi.device_ms + bi.device_ms,
                       "forward_sweeps": fi.iterations, "backward_sweeps": bi.iterations}
     g.free()
     h = mg.HostGraph.lattice(4096, 4096, 0.05, seed=3)
+    rp, col, wt = h.arrays()
+    ogl = O.csr_from_arrays(rp, col, wt)
     g = mg.Graph(h, device)
     rng = np.random.default_rng(64)
     ls = rng.integers(0, g.nv, 64).astype(np.int32)
+    f_lat = pool.submit(O.bc_multi_ext, ogl, ls[:2])
     # the first run settles the path-count mode (this lattice's counts pass
     # the FP64 range, so its BC runs use extended counts) and captures loops
+    g.bc_multi(ls[:2], out=False)
+    b8, _ = g.bc_multi(ls[:8])
     b2, _ = g.bc_multi(ls[:2])
     _, lb = g.bc_multi(ls, out=False)
     t1 = []
     acc = np.zeros(g.nv, np.float64)
-    for s_ in ls[:2]:
+    for s_ in ls[:8]:
         (_, _, dl), i1 = g.bc(int(s_))
         t1.append(i1.device_ms)
         d = dl.astype(np.float64)
         d[int(s_)] = 0.0
         acc += d
     plain = 64 * float(np.mean(t1))
+    lat_ref = f_lat.result()
     out["lattice_bc_64"] = {"graph": f"lattice4096x4096 +5% shortcuts n={g.nv} m={g.ne}",
                             "batched_ms": lb.device_ms, "plain_ms_estimated": plain,
                             "speedup": plain / lb.device_ms, "levels_per_group": lb.iterations / 2,
-                            "two_source_max_rel_diff": float(np.max(np.abs(b2 - acc)) / np.max(np.abs(acc))),
-                            "all_finite": bool(np.all(np.isfinite(b2)) and np.all(np.isfinite(acc)))}
+                            "eight_source_max_rel_diff": float(np.max(np.abs(b8 - acc)) / np.max(np.abs(acc))),
+                            "all_finite": bool(np.all(np.isfinite(b8)) and np.all(np.isfinite(acc))),
+                            "oracle_max_rel_err": float(np.max(np.abs(b2 - lat_ref)) / np.max(np.abs(lat_ref))),
+                            "oracle": "long-double Brandes, sources 0 and 1 of the 64; bound 1e-5"}
     g.free()
+    x64, gw64 = f_adj.result()
+    out["adjoint"]["forward_oracle_max_abs_err"] = float(np.max(np.abs(xw.astype(np.float64) - x64)))
+    out["adjoint"]["grad_oracle_max_rel_err"] = float(np.max(np.abs(grad.astype(np.float64) - gw64))
+                                                      / np.max(np.abs(gw64)))
+    out["adjoint"]["oracle"] = "FP64 forward and adjoint; bounds 1e-6 (forward, max-abs), 1e-4 (gradient)"
+    pool.shutdown()
     return out
 
 
 def reference_arm(args):
+    """The reference's CPU path (the oracle port of validate.cu), whole steps
+    timed like the GPU arm's: --warmup untimed steps, then --steps timed
+    ones, each a complete Bellman-Ford SSSP plus FP64 PageRank to L1 change
+    1e-6.  The input comes from the oracle's R-MAT generator (byte-identical
+    to the GPU arm's graph), so the product library is never loaded."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return 0
-    h = build_graph(args.scale)
-    rp, col, wt = h.arrays()
-    m = int(len(col))
-    # one full run gives the sweep / iteration counts of the whole workload;
-    # timed steps are bounded samples (2 sweeps + 2 iterations) scaled to them
-    ts, S, tp, I = cpu_oracle_run(rp, col, wt)
+    from oracle import oracle as O
+    t0 = time.perf_counter()
+    og = O.gen_rmat(args.scale, EDGE_FACTOR, seed=args.scale)
+    gen_s = time.perf_counter() - t0
+    m = og.ne
     step_times = []
+    S = I = 0
     for i in range(args.warmup + args.steps):
-        a, s, b, it = cpu_oracle_run(rp, col, wt, (2, 2))
-        est = a / s * S + b / it * I
+        ts, S, _, tp, I, _ = cpu_oracle_step(og)
         if i >= args.warmup:
-            step_times.append(est)
-    t = statistics.median(step_times)
+            step_times.append(ts + tp)
+    t = statistics.mean(step_times)
     value = 2 * m / t / 1e9
     line = {
         "impl": "reference", "metric": "GTEPS", "value": value, "unit": "GTEPS", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "int32/fp64", "data": "synthetic",
         "config": {"workload": f"rmat{args.scale}_ef{EDGE_FACTOR}: SSSP(src 0) + PageRank(d=0.85, L1 tol 1e-6)",
-                   "nv": h.nv, "ne": m},
+                   "nv": og.nv, "ne": m},
         "cpu_baseline": {"value": value, "unit": "GTEPS", "cores": 1, "kind": "port",
-                         "sample": f"full run once ({S} Bellman-Ford sweeps, {I} PageRank sweeps, "
-                                   f"{ts + tp:.1f} s); steps time 2 sweeps + 2 iterations, scaled to the full counts"},
+                         "sample": f"whole steps: Bellman-Ford SSSP ({S} sweeps) + FP64 PageRank ({I} sweeps), "
+                                   f"single thread as validate.cu; mean of {args.steps} timed steps after "
+                                   f"{args.warmup} warm-up; input generated in {gen_s:.1f} s by the oracle"},
         "e2e": {"value": value, "unit": "GTEPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -406,18 +469,30 @@ def main():
     # in and both results out.  Double-buffered: the next step's copy
     # (mg_graph_stage, copy stream) overlaps this step's runs, and
     # mg_graph_commit rebuilds the device CSR from it before the next step.
-    h2d = h.stage_bytes()  # row offsets, column ids, weights (bytes: the pinned graph's weights fit)
+    h2d = h.stage_bytes()  # row offsets, column ids, weights: 4(n+1) + 8m bytes, all int32
     d2h = 8 * n
     torch.cuda.synchronize()
+    split = {"stage_ms": 0.0, "commit_ms": 0.0, "runs_ms": 0.0}
     t0 = time.perf_counter()
     g.stage(h)
     for i in range(args.steps):
+        ta = time.perf_counter()
         g.commit()
+        tb = time.perf_counter()
         if i + 1 < args.steps:
             g.stage(h)
-        step(out=True)
+        tc = time.perf_counter()
+        e_si, e_pi = step(out=True)
+        td = time.perf_counter()
+        split["commit_ms"] += (tb - ta) * 1e3
+        split["stage_ms"] += (tc - tb) * 1e3
+        split["runs_ms"] += (td - tc) * 1e3
     e2e_s = time.perf_counter() - t0
     e2e_val = 2 * m * args.steps / e2e_s / 1e9
+    split = {k: round(v / args.steps, 3) for k, v in split.items()}
+    # the last end-to-end step's results, checked against the oracle below
+    dist_gpu, _ = g.sssp(0, opts)
+    rank_gpu, rank_info = g.pagerank(mg.PR_TOPOLOGY, opts)
 
     # ---- per-kernel times (cudaEvents around every launch, host-driven loop)
     clocks.start(keep=clk_lines)
@@ -449,12 +524,22 @@ def main():
         pass
     total_ms = sum(v[1] for v in kt.values())
     cpu = None
+    errors = None
     if world == 1 and not args.no_cpu_baseline:
+        import numpy as np
+        from oracle import oracle as O
         rp, col, wt = h.arrays()
-        ts, S, tp, I = cpu_oracle_run(rp, col, wt)
+        og = O.csr_from_arrays(rp, col, wt)
+        ts, S, dist_ref, tp, I, rank_ref = cpu_oracle_step(og)
         cpu = {"value": 2 * m / (ts + tp) / 1e9, "unit": "GTEPS", "cores": 1, "kind": "port",
                "sample": f"one full step on the host: Bellman-Ford SSSP ({S} sweeps, {ts:.1f} s) + FP64 "
                          f"PageRank ({I} sweeps, {tp:.1f} s), single thread as validate.cu"}
+        if I != rank_info.iterations:   # compare iterates of the same sweep count
+            rank_ref, _ = O.pr_norm_f64(og, DAMPING, TOL, rank_info.iterations)
+        errors = {"sssp": {"bit_exact": bool(np.array_equal(dist_gpu, dist_ref)),
+                           "mismatches": int(np.sum(dist_gpu != dist_ref))},
+                  "pagerank": {"max_abs_err": float(np.max(np.abs(rank_gpu.astype(np.float64) - rank_ref))),
+                               "bound": 1e-6, "sweeps": rank_info.iterations, "oracle": "FP64, same sweeps"}}
     line = {
         "metric": "GTEPS", "value": value, "unit": "GTEPS", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
@@ -463,7 +548,9 @@ def main():
                    "nv": n, "ne": m, "sssp_iterations": si.iterations, "pr_sweeps": pi.iterations,
                    "parallelism": f"replicas x{world}", "l2": "inputs (column ids + weights, 1 GB) exceed L2",
                    "metric_family": "GTEPS and HBM GB/s against the measured peak"},
-        "e2e": {"value": e2e_val, "unit": "GTEPS", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "e2e": {"value": e2e_val, "unit": "GTEPS", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                "host_split_ms_per_step": split},
+        "errors": errors,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": (achieved / peak) if achieved else None, "traffic": traffic,
                      "kernel": "k_pr_light (PageRank pull sweep)", "algorithmic_bytes": alg_bytes,

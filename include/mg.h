@@ -86,13 +86,10 @@ mg_status mg_host_graph_from_csr(int32_t nv, int32_t ne, const int32_t *csc_v, c
                                  const int32_t *csc_ev, int32_t start_p, mg_host_graph **out);
 
 mg_status mg_host_graph_view(const mg_host_graph *g, mg_csr_view *view);
-/* Page-lock the host arrays so uploads run at full link speed (optional).
- * When every weight lies in [0, 255] a byte copy of the weights is kept
- * (page-locked too) and mg_graph_stage uploads it instead of the int32
- * weights. */
+/* Page-lock the host arrays so uploads run at full link speed (optional). */
 mg_status mg_host_graph_pin(mg_host_graph *g);
 /* Bytes mg_graph_stage copies to the device for this graph (row offsets,
- * column ids, weights as int32 or, after mg_host_graph_pin, as bytes). */
+ * column ids and weights, all int32). */
 int64_t mg_host_graph_stage_bytes(const mg_host_graph *g);
 void mg_host_graph_free(mg_host_graph *g);
 /* Write as MatrixMarket "coordinate integer general" (1-based, every CSR

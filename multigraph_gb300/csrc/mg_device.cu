@@ -489,8 +489,7 @@ static int32_t wmin_decode(unsigned long long enc)
 __global__ void k_relabel_edges(int32_t n, int32_t m, const int32_t *new2old, const int32_t *old2new,
                                 const int32_t *o_row, const int32_t *row_new, const int32_t *pos_row,
                                 const uint32_t *src0, uint32_t *dst0, const uint32_t *src1, uint32_t *dst1,
-                                int map_ids, unsigned long long *sums, const unsigned long long *skip,
-                                const uint8_t *src1_u8)
+                                int map_ids, unsigned long long *sums, const unsigned long long *skip)
 {
     if (skip && __ldcg(skip) != 0ull) return;
     const int lane = threadIdx.x & 31;
@@ -506,7 +505,7 @@ __global__ void k_relabel_edges(int32_t n, int32_t m, const int32_t *new2old, co
 #pragma unroll
         for (int j = 0; j < RELABEL_ILP; j++) {
             x[j] = q[j] >= 0 ? __ldg(&src0[q[j]]) : 0u;
-            y[j] = (q[j] >= 0 && dst1) ? (src1_u8 ? (uint32_t)__ldg(&src1_u8[q[j]]) : __ldg(&src1[q[j]])) : 0u;
+            y[j] = (q[j] >= 0 && dst1) ? __ldg(&src1[q[j]]) : 0u;
         }
         if (sums) {
 #pragma unroll
@@ -531,13 +530,6 @@ __global__ void k_relabel_edges(int32_t n, int32_t m, const int32_t *new2old, co
         sym_flush(sums, s_lo, s_hi);
         wmin_flush(&sums[3], wlo);
     }
-}
-
-// staged byte weights -> int32 (graphs that are not relabeled)
-__global__ void k_widen_u8(size_t m, const uint8_t *src, int32_t *dst)
-{
-    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < m; i += (size_t)gridDim.x * blockDim.x)
-        dst[i] = (int32_t)src[i];
 }
 
 // *differ = 1 when the staged caller row offsets a differ from b (the
@@ -633,7 +625,7 @@ __global__ void k_cc_label_old(int32_t n, const int32_t *parent, const int32_t *
 // positions; the optional pair checksum and skip word as k_relabel_edges
 static mg_status relabel_device(mg_graph *g, const mgi::DevBuf &src_row, const mgi::DevBuf &src_col,
                                 const mgi::DevBuf &src_wt, unsigned long long *sym_sums = nullptr,
-                                const unsigned long long *skip = nullptr, const uint8_t *src_wt8 = nullptr)
+                                const unsigned long long *skip = nullptr)
 {
     if (g->ne == 0) return MG_OK;
     const int grid = g->num_sms * 8;
@@ -646,7 +638,7 @@ static mg_status relabel_device(mg_graph *g, const mgi::DevBuf &src_row, const m
                                                  src_row.as<int32_t>(), g->row.as<int32_t>(),
                                                  g->pos_row.as<int32_t>(), src_col.as<uint32_t>(),
                                                  g->col.as<uint32_t>(), src_wt.as<uint32_t>(), g->wt.as<uint32_t>(),
-                                                 1, sym_sums, skip, src_wt8);
+                                                 1, sym_sums, skip);
     MG_CUDA(cudaGetLastError());
     return MG_OK;
 }
@@ -731,7 +723,7 @@ mg_status edges_to_engine(mg_graph *g, const void *src_caller, void *dst_engine)
                                                            g->o_row.as<int32_t>(), g->row.as<int32_t>(),
                                                            g->pos_row.as<int32_t>(), (const uint32_t *)src_caller,
                                                            (uint32_t *)dst_engine, nullptr, nullptr, 0, nullptr,
-                                                           nullptr, nullptr);
+                                                           nullptr);
     MG_CUDA(cudaGetLastError());
     return MG_OK;
 }
@@ -859,7 +851,7 @@ static void destroy_graph(mg_graph *g)
                       &g->hchunk, &g->hrows, &g->hrow_chunk, &g->fw, &g->o_fw, &g->ppr_hchunk, &g->ppr_hrows,
                       &g->ppr_hrow_chunk, &g->o_row, &g->o_col, &g->o_wt, &g->old2new, &g->new2old,
                       &g->wrows, &g->trows, &g->pos_row, &g->sym_sums, &g->s_row,
-                      &g->s_col, &g->s_wt, &g->s_wt8};
+                      &g->s_col, &g->s_wt};
     for (DevBuf *b : bufs) dev_free(*b);
     for (DevBuf &b : g->res_out) dev_free(b);
     if (g->pinned_flag) cudaFreeHost(g->pinned_flag);
@@ -935,22 +927,16 @@ mg_status mg_graph_stage(mg_graph *g, const mg_host_graph *h)
     const size_t n = (size_t)h->nv, m = (size_t)h->ne;
     // staging buffers, separate from the current graph's caller-order
     // arrays (o_*), which runs before the commit still read
-    // weights as bytes when the pinned host graph keeps a byte copy (a
-    // quarter of the weight traffic); widened to int32 at commit
-    const bool w8 = m > 0 && h->ev8.size() == m;
     MG_TRY(dev_alloc(g->s_row, (n + 1) * 4));
     MG_TRY(dev_alloc(g->s_col, std::max<size_t>(m, 4) * 4 + COL_PAD));
-    if (w8) MG_TRY(dev_alloc(g->s_wt8, std::max<size_t>(m, 16) + COL_PAD));
-    else MG_TRY(dev_alloc(g->s_wt, std::max<size_t>(m, 4) * 4 + COL_PAD));
+    MG_TRY(dev_alloc(g->s_wt, std::max<size_t>(m, 4) * 4 + COL_PAD));
     cudaStream_t cs = g->copy_stream;
     MG_CUDA(cudaStreamWaitEvent(cs, g->ev_consumed, 0));  // the last commit has read them
     MG_CUDA(cudaMemcpyAsync(g->s_row.p, h->v.data(), (n + 1) * 4, cudaMemcpyHostToDevice, cs));
     if (m) {
         MG_CUDA(cudaMemcpyAsync(g->s_col.p, h->e.data(), m * 4, cudaMemcpyHostToDevice, cs));
-        if (w8) MG_CUDA(cudaMemcpyAsync(g->s_wt8.p, h->ev8.data(), m, cudaMemcpyHostToDevice, cs));
-        else MG_CUDA(cudaMemcpyAsync(g->s_wt.p, h->ev.data(), m * 4, cudaMemcpyHostToDevice, cs));
+        MG_CUDA(cudaMemcpyAsync(g->s_wt.p, h->ev.data(), m * 4, cudaMemcpyHostToDevice, cs));
     }
-    g->staged_w8 = w8;
     MG_CUDA(cudaEventRecord(g->ev_staged, cs));
     g->staged_h = h;
     return MG_OK;
@@ -1008,18 +994,12 @@ mg_status mg_graph_commit(mg_graph *g)
         MG_CUDA(cudaGetLastError());
         if (g->relabeled) {
             // engine CSR from the staged caller-order arrays
-            MG_TRY(relabel_device(g, g->s_row, g->s_col, g->s_wt, sums, sums + 2,
-                                  g->staged_w8 ? g->s_wt8.as<uint8_t>() : nullptr));
+            MG_TRY(relabel_device(g, g->s_row, g->s_col, g->s_wt, sums, sums + 2));
         } else {
             MG_CUDA(cudaMemcpyAsync(g->row.p, g->s_row.p, (n + 1) * 4, cudaMemcpyDeviceToDevice, s));
             if (m) {
                 MG_CUDA(cudaMemcpyAsync(g->col.p, g->s_col.p, m * 4, cudaMemcpyDeviceToDevice, s));
-                if (g->staged_w8) {
-                    k_widen_u8<<<g->num_sms * 8, 256, 0, s>>>((size_t)m, g->s_wt8.as<uint8_t>(), g->wt.as<int32_t>());
-                    MG_CUDA(cudaGetLastError());
-                } else {
-                    MG_CUDA(cudaMemcpyAsync(g->wt.p, g->s_wt.p, m * 4, cudaMemcpyDeviceToDevice, s));
-                }
+                MG_CUDA(cudaMemcpyAsync(g->wt.p, g->s_wt.p, m * 4, cudaMemcpyDeviceToDevice, s));
             }
             k_sym_check<<<g->num_sms * 8, 256, 0, s>>>(g->nv, g->row.as<int32_t>(), g->col.as<int32_t>(),
                                                        g->wt.as<int32_t>(), sums);
@@ -1101,7 +1081,6 @@ void mg_host_graph_free(mg_host_graph *h)
         if (!h->v.empty()) cudaHostUnregister(h->v.data());
         if (!h->e.empty()) cudaHostUnregister(h->e.data());
         if (!h->ev.empty()) cudaHostUnregister(h->ev.data());
-        if (!h->ev8.empty()) cudaHostUnregister(h->ev8.data());
     }
     delete h;
 }
@@ -1115,15 +1094,6 @@ mg_status mg_host_graph_pin(mg_host_graph *h)
     if (!h->e.empty()) MG_CUDA(cudaHostRegister(h->e.data(), h->e.size() * 4, cudaHostRegisterDefault));
     if (!h->ev.empty()) MG_CUDA(cudaHostRegister(h->ev.data(), h->ev.size() * 4, cudaHostRegisterDefault));
     h->pinned = true;
-    // byte weights for the staged uploads, when they fit
-    const size_t m = h->ev.size();
-    bool fits = m > 0;
-    for (size_t i = 0; i < m && fits; i++) fits = (uint32_t)h->ev[i] <= 255u;
-    if (fits) {
-        h->ev8.resize(m);
-        for (size_t i = 0; i < m; i++) h->ev8[i] = (uint8_t)h->ev[i];
-        MG_CUDA(cudaHostRegister(h->ev8.data(), m, cudaHostRegisterDefault));
-    }
     return MG_OK;
 }
 
@@ -1131,7 +1101,7 @@ int64_t mg_host_graph_stage_bytes(const mg_host_graph *h)
 {
     if (!h) return 0;
     const int64_t n = h->nv, m = h->ne;
-    return 4 * (n + 1) + 4 * m + (h->ev8.empty() ? 4 : 1) * m;
+    return 4 * (n + 1) + 8 * m;
 }
 
 }  // extern "C"

@@ -117,8 +117,6 @@ struct mg_graph {
     cudaEvent_t ev_staged = nullptr, ev_consumed = nullptr;
     const mg_host_graph *staged_h = nullptr;
     mgi::DevBuf s_row, s_col, s_wt; // staged next input (caller order); swapped with o_* on commit
-    mgi::DevBuf s_wt8;             // staged weights as bytes (host graphs whose weights fit)
-    bool staged_w8 = false;
     mgi::DevBuf sym_sums;          // commit checks: pair checksum (2 x uint64), rows-differ word
     unsigned long long *sym_host = nullptr;  // pinned readback of sym_sums
     int32_t nv = 0, ne = 0;

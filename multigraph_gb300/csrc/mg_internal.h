@@ -11,9 +11,6 @@
 struct mg_host_graph {
     int32_t nv = 0, ne = 0, start_p = 0, tra = 0;
     std::vector<int32_t> v, e, ev;  // CSR row offsets, column ids, integer weights
-    // the weights as bytes when every one lies in [0, 255] (built by pin):
-    // mg_graph_stage then uploads 1 byte per edge instead of 4
-    std::vector<uint8_t> ev8;
     bool pinned = false;
 };
 

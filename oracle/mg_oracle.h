@@ -48,6 +48,19 @@ enum { ORC_OK = 0, ORC_ERR_IO = 1, ORC_ERR_PARSE = 2, ORC_ERR_RANGE = 3, ORC_ERR
  * seeded by time(), which is not reproducible). */
 int  orc_load_mtx(const char *path, int32_t source, uint32_t flags, uint64_t seed, orc_csr *out);
 void orc_csr_free(orc_csr *g);
+/* The same pipeline from an in-memory entry list (0-based ids in file order;
+ * val may be NULL for weight 1); ORC_LOAD_SYM adds each entry's mirror right
+ * after it, as the loader does for symmetric files (read_input.cu:88-96). */
+int  orc_from_entries(int32_t nv_decl, int64_t nentries, const int32_t *src, const int32_t *dst,
+                      const int32_t *val, int32_t source, uint32_t flags, orc_csr *out);
+/* R-MAT (Chakrabarti, Zhan, Faloutsos 2004): edge_factor * 2^scale draws of
+ * scale quadrant choices each (probabilities a, b, c, 1-a-b-c), draw i
+ * seeded with seed * 0xD1B54A32D192ED03 + i through splitmix64, self-loops
+ * dropped, integer weight wmin + (next draw % (wmax - wmin + 1)); then the
+ * symmetric loader pipeline above with source 0.  The synthetic input of
+ * the benchmarks, generated without the product library. */
+int  orc_gen_rmat(int32_t scale, int32_t edge_factor, double a, double b, double c, uint64_t seed,
+                  int32_t wmin, int32_t wmax, orc_csr *out);
 uint32_t orc_pattern_weight(uint64_t seed, uint64_t entry);
 
 /* validate.cu:106-130 -- FIFO BFS levels, ORC_IUNUSED for unreached. */
@@ -94,6 +107,15 @@ int    orc_wpr_adjoint_f64(const orc_csr *g, const double *w, const double *x, c
                            double *grad_w, double *grad_p);
 double orc_wpr_loss_f64(const orc_csr *g, const double *w, const double *gvec, double damping,
                         double tol, int32_t max_iter);
+/* Central finite differences (L(w + eps e_j) - L(w - eps e_j)) / (2 eps) of
+ * L = sum_i g_i x_i for the k CSR entries listed, each perturbed loss from a
+ * complete FP64 solve (written as the converged x plus the fixed point of
+ * the perturbation, all 2k solved together on nthreads host threads, until
+ * each one's L1 change <= rtol times its L1 norm).  x: orc_wpr_f64's result
+ * for w.  Returns the sweeps taken (-1: out of memory). */
+int    orc_wpr_fd_f64(const orc_csr *g, const double *w, const double *x, const double *gvec, double damping,
+                      const int32_t *entries, int32_t k, double eps, double rtol, int32_t max_iter,
+                      int32_t nthreads, double *fd_out);
 
 #ifdef __cplusplus
 }

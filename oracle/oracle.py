@@ -45,7 +45,7 @@ def build() -> str:
     src = os.path.join(HERE, "mg_oracle.c")
     if (not os.path.exists(LIB_PATH)) or os.path.getmtime(LIB_PATH) < max(
             os.path.getmtime(src), os.path.getmtime(os.path.join(HERE, "mg_oracle.h"))):
-        subprocess.check_call(["gcc", "-O2", "-fPIC", "-shared", "-ffp-contract=off",
+        subprocess.check_call(["gcc", "-O2", "-fPIC", "-shared", "-ffp-contract=off", "-pthread",
                                "-o", LIB_PATH, src, "-lm"])
     return LIB_PATH
 
@@ -86,6 +86,15 @@ def lib():
         L.orc_wpr_adjoint_f64.restype = C.c_int
         L.orc_wpr_loss_f64.argtypes = [C.c_void_p, _f64p, _f64p, C.c_double, C.c_double, C.c_int32]
         L.orc_wpr_loss_f64.restype = C.c_double
+        L.orc_from_entries.argtypes = [C.c_int32, C.c_int64, _i32p, _i32p, C.c_void_p, C.c_int32, C.c_uint32,
+                                       C.POINTER(_OrcCSR)]
+        L.orc_from_entries.restype = C.c_int
+        L.orc_gen_rmat.argtypes = [C.c_int32, C.c_int32, C.c_double, C.c_double, C.c_double, C.c_uint64,
+                                   C.c_int32, C.c_int32, C.POINTER(_OrcCSR)]
+        L.orc_gen_rmat.restype = C.c_int
+        L.orc_wpr_fd_f64.argtypes = [C.c_void_p, _f64p, _f64p, _f64p, C.c_double, _i32p, C.c_int32, C.c_double,
+                                     C.c_double, C.c_int32, C.c_int32, _f64p]
+        L.orc_wpr_fd_f64.restype = C.c_int
         _lib = L
     return _lib
 
@@ -123,11 +132,8 @@ def csr_from_arrays(row_ptr, col, wt=None, start_p=0) -> CSR:
     return CSR(nv, len(col), start_p, tra, row_ptr, col, wt)
 
 
-def load_mtx(path: str, source: int = 0, flags: int = LOAD_SYM, seed: int = 1) -> CSR:
-    s = _OrcCSR()
-    rc = lib().orc_load_mtx(path.encode(), source, flags, seed, C.byref(s))
-    if rc != 0:
-        raise OSError(rc, f"oracle loader failed with status {rc} on {path}")
+def _take(s) -> CSR:
+    """Copy a C-allocated orc_csr into numpy arrays and free it."""
     nv, ne = s.nv, s.ne
     v = np.ctypeslib.as_array(s.csc_v, shape=(nv + 1,)).copy()
     e = np.ctypeslib.as_array(s.csc_e, shape=(max(ne, 1),))[:ne].copy()
@@ -135,6 +141,39 @@ def load_mtx(path: str, source: int = 0, flags: int = LOAD_SYM, seed: int = 1) -
     out = CSR(nv, ne, s.start_p, s.tra, v, e, ev)
     lib().orc_csr_free(C.byref(s))
     return out
+
+
+def load_mtx(path: str, source: int = 0, flags: int = LOAD_SYM, seed: int = 1) -> CSR:
+    s = _OrcCSR()
+    rc = lib().orc_load_mtx(path.encode(), source, flags, seed, C.byref(s))
+    if rc != 0:
+        raise OSError(rc, f"oracle loader failed with status {rc} on {path}")
+    return _take(s)
+
+
+def from_entries(nv_decl: int, src, dst, val=None, source: int = 0, flags: int = LOAD_SYM) -> CSR:
+    """The loader pipeline on an in-memory entry list (0-based, file order)."""
+    src = np.ascontiguousarray(src, dtype=np.int32)
+    dst = np.ascontiguousarray(dst, dtype=np.int32)
+    vp = None
+    if val is not None:
+        val = np.ascontiguousarray(val, dtype=np.int32)
+        vp = val.ctypes.data_as(C.c_void_p)
+    s = _OrcCSR()
+    rc = lib().orc_from_entries(nv_decl, len(src), src, dst, vp, source, flags, C.byref(s))
+    if rc != 0:
+        raise ValueError(f"oracle loader failed with status {rc}")
+    return _take(s)
+
+
+def gen_rmat(scale: int, edge_factor: int = 16, a=0.57, b=0.19, c=0.19, seed: int = 1, wmin: int = 1,
+             wmax: int = 64) -> CSR:
+    """Symmetrised, deduplicated R-MAT graph (the benchmarks' synthetic input)."""
+    s = _OrcCSR()
+    rc = lib().orc_gen_rmat(scale, edge_factor, a, b, c, seed, wmin, wmax, C.byref(s))
+    if rc != 0:
+        raise ValueError(f"oracle R-MAT generator failed with status {rc}")
+    return _take(s)
 
 
 def pattern_weight(seed: int, entry: int) -> int:
@@ -244,6 +283,21 @@ def wpr_adjoint_f64(g: CSR, w, x, gvec, damping=0.85, tol=1e-12, max_iter=0):
     gp = np.empty(g.ne, dtype=np.float64)
     it = lib().orc_wpr_adjoint_f64(g._struct(), w, x, gvec, damping, tol, max_iter, lam, gw, gp)
     return lam, gw, gp, it
+
+
+def wpr_fd_f64(g: CSR, w, x, gvec, entries, damping=0.85, eps=1e-3, rtol=1e-10, max_iter=2000, nthreads=0):
+    """Central differences (L(w+eps) - L(w-eps)) / (2 eps) for the listed CSR
+    entries, every loss from a complete FP64 solve (x = wpr_f64's solution)."""
+    w = np.ascontiguousarray(w, dtype=np.float64)
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    gvec = np.ascontiguousarray(gvec, dtype=np.float64)
+    entries = np.ascontiguousarray(entries, dtype=np.int32)
+    out = np.empty(len(entries), dtype=np.float64)
+    nt = nthreads if nthreads > 0 else (os.cpu_count() or 1)
+    it = lib().orc_wpr_fd_f64(g._struct(), w, x, gvec, damping, entries, len(entries), eps, rtol, max_iter, nt, out)
+    if it < 0:
+        raise MemoryError("oracle finite differences: out of memory")
+    return out, it
 
 
 def wpr_loss_f64(g: CSR, w, gvec, damping=0.85, tol=1e-13, max_iter=0) -> float:

@@ -135,10 +135,10 @@ def test_weighted_runs_between_stage_and_commit():
 
 
 @pytest.mark.parametrize("kind", ["rmat", "lattice"])   # relabeled / not relabeled
-@pytest.mark.parametrize("wmax", [64, 255, 1000])
-def test_staged_byte_weights(kind, wmax):
-    """A pinned host graph whose weights fit in a byte is staged with byte
-    weights (a quarter of the weight traffic) and widened at commit."""
+@pytest.mark.parametrize("wmax", [64, 1000])
+def test_staged_pinned_weights(kind, wmax):
+    """A pinned host graph is staged with its int32 weights (row offsets,
+    column ids and weights: 4(n+1) + 8m bytes) and relabeled at commit."""
     h0 = mg.HostGraph.rmat(11, 16, seed=34) if kind == "rmat" else mg.HostGraph.lattice(40, 33, 0.05, seed=5)
     rp, col, wt = h0.arrays()
     n, m = len(rp) - 1, len(col)
@@ -146,16 +146,15 @@ def test_staged_byte_weights(kind, wmax):
     lo, hi = np.minimum(src, col), np.maximum(src, col)
     w = ((lo.astype(np.int64) * 7919 + hi * 104729) % wmax + 1).astype(np.int32)   # symmetric, in [1, wmax]
     h1, og1 = _csr(rp, col, w)
-    assert h1.stage_bytes() == 4 * (n + 1) + 8 * m
     h1.pin()
-    assert h1.stage_bytes() == 4 * (n + 1) + (5 if wmax <= 255 else 8) * m
+    assert h1.stage_bytes() == 4 * (n + 1) + 8 * m
     g = mg.Graph(h0)
     g.stage(h1)
     g.commit()
     for s in (0, 3):
         d, _ = g.sssp(s)
         assert np.array_equal(d, O.sssp(og1, s)[0]), (kind, wmax, s)
-    # and back to the first graph through the int32 path (not pinned)
+    # and back to the first graph (not pinned)
     g.stage(h0)
     g.commit()
     d, _ = g.sssp(0)
