@@ -42,6 +42,7 @@ SCALE = 22
 EDGE_FACTOR = 16
 DAMPING = 0.85
 TOL = 1e-6
+ADJ_FWD_TOL = 1e-9   # weighted PageRank forward ahead of the adjoint (gradient contract 1e-4)
 
 
 def parse():
@@ -316,12 +317,15 @@ def batch_report(mg, device, exec_mode=None):
         return x64, gw64
 
     f_adj = pool.submit(adjoint_ref)
-    g.wpagerank(out=False, tol=TOL)
-    xw, fi = g.wpagerank(tol=TOL)
+    # the forward to L1 change 1e-9: the gradient inherits its relative error
+    # (1e-6 leaves the gradient ~4e-3 off); the adjoint to 1e-6 of |g|_1
+    g.wpagerank(out=False, tol=ADJ_FWD_TOL)
+    xw, fi = g.wpagerank(tol=ADJ_FWD_TOL)
     (grad, _), bi = g.wpagerank_backward(gv, tol=TOL)
     out["adjoint"] = {"graph": f"rmat21_ef16 n={g.nv} m={g.ne}", "forward_ms": fi.device_ms,
                       "backward_ms": bi.device_ms, "forward_backward_ms": fi.device_ms + bi.device_ms,
-                      "forward_sweeps": fi.iterations, "backward_sweeps": bi.iterations}
+                      "forward_sweeps": fi.iterations, "backward_sweeps": bi.iterations,
+                      "tolerances": {"forward_l1": ADJ_FWD_TOL, "backward_l1_rel_g": TOL}}
     g.free()
     h = mg.HostGraph.lattice(4096, 4096, 0.05, seed=3)
     rp, col, wt = h.arrays()
@@ -490,6 +494,13 @@ def main():
     e2e_s = time.perf_counter() - t0
     e2e_val = 2 * m * args.steps / e2e_s / 1e9
     split = {k: round(v / args.steps, 3) for k, v in split.items()}
+    # the same upload + commit with no runs beside it (link speed alone)
+    torch.cuda.synchronize()
+    ta = time.perf_counter()
+    for _ in range(3):
+        g.stage(h)
+        g.commit()
+    split["upload_commit_alone_ms"] = round((time.perf_counter() - ta) / 3 * 1e3, 3)
     # the last end-to-end step's results, checked against the oracle below
     dist_gpu, _ = g.sssp(0, opts)
     rank_gpu, rank_info = g.pagerank(mg.PR_TOPOLOGY, opts)

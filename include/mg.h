@@ -86,7 +86,9 @@ mg_status mg_host_graph_from_csr(int32_t nv, int32_t ne, const int32_t *csc_v, c
                                  const int32_t *csc_ev, int32_t start_p, mg_host_graph **out);
 
 mg_status mg_host_graph_view(const mg_host_graph *g, mg_csr_view *view);
-/* Page-lock the host arrays so uploads run at full link speed (optional). */
+/* Make page-locked copies of the host arrays (driver allocations) from which
+ * mg_graph_stage uploads at full link speed (optional; doubles the graph's
+ * host memory until mg_host_graph_free). */
 mg_status mg_host_graph_pin(mg_host_graph *g);
 /* Bytes mg_graph_stage copies to the device for this graph (row offsets,
  * column ids and weights, all int32). */

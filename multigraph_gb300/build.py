@@ -25,7 +25,8 @@ LIB = os.path.join(PKG, "libmg.so")
 BIN = os.path.join(PKG, "bin")
 
 GENCODE = "-gencode=arch=compute_103a,code=sm_103a"
-CU_SOURCES = ["mg_device.cu", "mg_frontier.cu", "mg_pr.cu", "mg_cc.cu", "mg_tune.cu", "mg_noalloc.cu", "mg_bcb.cu"]
+CU_SOURCES = ["mg_device.cu", "mg_frontier.cu", "mg_pr.cu", "mg_hub.cu", "mg_cc.cu", "mg_tune.cu", "mg_noalloc.cu",
+              "mg_bcb.cu"]
 CU_FLAGS = {}  # per-file extra nvcc flags
 CPP_SOURCES = ["mg_host.cpp"]
 CLI_NAMES = ["BFS", "SSSP", "BC", "CC", "DATA_DRIVEN_PR", "TOPOLOGY_DRIVEN_PR"]

@@ -482,7 +482,8 @@ static int32_t wmin_decode(unsigned long long enc)
 // caller CSR -> engine CSR for up to two 4-byte edge arrays; the first is
 // mapped through old2new when map_ids (column ids).  With sums, the
 // symmetry checksum of (caller row, caller column, second array) is formed
-// on the way, and the least second-array value (the weights) in sums[3].
+// on the way, the least second-array value (the weights) in sums[3], and
+// sums[4] != 0 when some engine column id differs from the one it replaces.
 // A non-zero *skip (caller row offsets that differ from the
 // layout's, found by k_rows_differ earlier on the stream) returns at once:
 // the positions would not match the staged arrays.
@@ -498,6 +499,7 @@ __global__ void k_relabel_edges(int32_t n, int32_t m, const int32_t *new2old, co
     const int32_t nwarps = (gridDim.x * blockDim.x) >> 5;
     unsigned long long s_lo = 0, s_hi = 0;
     int32_t wlo = INT32_MAX;
+    int changed = 0;
     for (int32_t c0 = gwarp * RELABEL_ILP; c0 < nsteps; c0 += nwarps * RELABEL_ILP) {
         int32_t q[RELABEL_ILP], u[RELABEL_ILP];
         caller_positions(n, m, new2old, o_row, row_new, pos_row, c0, q, u);
@@ -522,6 +524,7 @@ __global__ void k_relabel_edges(int32_t n, int32_t m, const int32_t *new2old, co
         for (int j = 0; j < RELABEL_ILP; j++) {
             if (q[j] < 0) continue;
             const int32_t p = (c0 + j) * 32 + lane;
+            if (sums) changed |= __ldcs(&dst0[p]) != x[j];
             dst0[p] = x[j];
             if (dst1) dst1[p] = y[j];
         }
@@ -529,6 +532,7 @@ __global__ void k_relabel_edges(int32_t n, int32_t m, const int32_t *new2old, co
     if (sums) {
         sym_flush(sums, s_lo, s_hi);
         wmin_flush(&sums[3], wlo);
+        if (__any_sync(0xffffffffu, changed) && lane == 0) atomicOr(&sums[4], 1ull);
     }
 }
 
@@ -828,6 +832,7 @@ static mg_status upload_arrays(mg_graph *g, const mg_host_graph *h, const HostLa
         g->trow = g->row.as<int32_t>(); g->tcol = g->col.as<int32_t>(); g->twt = g->wt.as<int32_t>();
     }
     MG_TRY(upload_bins(g, L));
+    g->hub.valid = false;  // new pull columns
     g->h_prow = L.prow;
     g->symmetric = L.symmetric;
     g->weights_symmetric = L.wsym;
@@ -847,6 +852,7 @@ static void destroy_graph(mg_graph *g)
     free_bc_ws(g);
     free_ppr_ws(g);
     free_wpr_ws(g);
+    hub_free(g);
     DevBuf *bufs[] = {&g->row, &g->col, &g->wt, &g->trow_own, &g->tcol_own, &g->twt_own,
                       &g->hchunk, &g->hrows, &g->hrow_chunk, &g->fw, &g->o_fw, &g->ppr_hchunk, &g->ppr_hrows,
                       &g->ppr_hrow_chunk, &g->o_row, &g->o_col, &g->o_wt, &g->old2new, &g->new2old,
@@ -909,7 +915,7 @@ mg_status mg_graph_upload(const mg_host_graph *h, int32_t device, mg_graph **out
     MG_CUDA(cudaEventCreateWithFlags(&g->ev_staged, cudaEventDisableTiming));
     MG_CUDA(cudaEventCreateWithFlags(&g->ev_consumed, cudaEventDisableTiming));
     MG_CUDA(cudaMallocHost(&g->pinned_flag, 64));
-    MG_CUDA(cudaMallocHost(&g->sym_host, 32));
+    MG_CUDA(cudaMallocHost(&g->sym_host, 64));
     HostLayout L;
     build_layout(*h, L);
     MG_TRY(upload_arrays(g.get(), h, L, true));
@@ -932,10 +938,13 @@ mg_status mg_graph_stage(mg_graph *g, const mg_host_graph *h)
     MG_TRY(dev_alloc(g->s_wt, std::max<size_t>(m, 4) * 4 + COL_PAD));
     cudaStream_t cs = g->copy_stream;
     MG_CUDA(cudaStreamWaitEvent(cs, g->ev_consumed, 0));  // the last commit has read them
-    MG_CUDA(cudaMemcpyAsync(g->s_row.p, h->v.data(), (n + 1) * 4, cudaMemcpyHostToDevice, cs));
+    const int32_t *hv = h->pin_v ? h->pin_v : h->v.data();
+    const int32_t *he = h->pin_e ? h->pin_e : h->e.data();
+    const int32_t *hev = h->pin_ev ? h->pin_ev : h->ev.data();
+    MG_CUDA(cudaMemcpyAsync(g->s_row.p, hv, (n + 1) * 4, cudaMemcpyHostToDevice, cs));
     if (m) {
-        MG_CUDA(cudaMemcpyAsync(g->s_col.p, h->e.data(), m * 4, cudaMemcpyHostToDevice, cs));
-        MG_CUDA(cudaMemcpyAsync(g->s_wt.p, h->ev.data(), m * 4, cudaMemcpyHostToDevice, cs));
+        MG_CUDA(cudaMemcpyAsync(g->s_col.p, he, m * 4, cudaMemcpyHostToDevice, cs));
+        MG_CUDA(cudaMemcpyAsync(g->s_wt.p, hev, m * 4, cudaMemcpyHostToDevice, cs));
     }
     MG_CUDA(cudaEventRecord(g->ev_staged, cs));
     g->staged_h = h;
@@ -985,10 +994,13 @@ mg_status mg_graph_commit(mg_graph *g)
         // check the staged input with the pair checksum (formed during the
         // relabel pass), read both back in one copy and lay the graph out
         // again from the host when either fails
-        MG_TRY(dev_alloc(g->sym_sums, 32));
+        MG_TRY(dev_alloc(g->sym_sums, 64));
         unsigned long long *sums = g->sym_sums.as<unsigned long long>();
         MG_CUDA(cudaMemsetAsync(sums, 0, 24, s));
         MG_CUDA(cudaMemsetAsync(sums + 3, 0xff, 8, s));
+        // column change word: set by the relabel pass; the copy path below
+        // rewrites the columns without comparing, so it counts as changed
+        MG_CUDA(cudaMemsetAsync(sums + 4, g->relabeled ? 0 : 0xff, 8, s));
         const int32_t *ref_row = g->relabeled ? g->o_row.as<int32_t>() : g->row.as<int32_t>();
         k_rows_differ<<<g->num_sms * 4, 256, 0, s>>>((int32_t)n + 1, g->s_row.as<int32_t>(), ref_row, sums + 2);
         MG_CUDA(cudaGetLastError());
@@ -1005,7 +1017,7 @@ mg_status mg_graph_commit(mg_graph *g)
                                                        g->wt.as<int32_t>(), sums);
             MG_CUDA(cudaGetLastError());
         }
-        MG_CUDA(cudaMemcpyAsync(g->sym_host, sums, 32, cudaMemcpyDeviceToHost, s));
+        MG_CUDA(cudaMemcpyAsync(g->sym_host, sums, 40, cudaMemcpyDeviceToHost, s));
         MG_CUDA(cudaStreamSynchronize(s));
         if (g->sym_host[2] != 0 || g->sym_host[0] != g->sym_host[1]) {
             HostLayout L;
@@ -1016,6 +1028,9 @@ mg_status mg_graph_commit(mg_graph *g)
             // same layout, new weights: their least value bounds the SSSP
             // pull's settled-row skip and gates SSSP on negative weights
             g->min_weight = wmin_decode(g->sym_host[3]);
+            // PageRank's hub split follows the columns: rebuilt only when
+            // some column id changed
+            if (g->sym_host[4] != 0) g->hub.valid = false;
             if (g->relabeled) {
                 // the staged arrays are now the current graph's caller-order CSR
                 std::swap(g->o_row, g->s_row);
@@ -1078,9 +1093,9 @@ void mg_host_graph_free(mg_host_graph *h)
 {
     if (!h) return;
     if (h->pinned) {
-        if (!h->v.empty()) cudaHostUnregister(h->v.data());
-        if (!h->e.empty()) cudaHostUnregister(h->e.data());
-        if (!h->ev.empty()) cudaHostUnregister(h->ev.data());
+        if (h->pin_v) cudaFreeHost(h->pin_v);
+        if (h->pin_e) cudaFreeHost(h->pin_e);
+        if (h->pin_ev) cudaFreeHost(h->pin_ev);
     }
     delete h;
 }
@@ -1090,9 +1105,24 @@ mg_status mg_host_graph_pin(mg_host_graph *h)
     clear_error();
     if (!h) return fail(MG_ERR_INVALID, "null argument");
     if (h->pinned) return MG_OK;
-    if (!h->v.empty()) MG_CUDA(cudaHostRegister(h->v.data(), h->v.size() * 4, cudaHostRegisterDefault));
-    if (!h->e.empty()) MG_CUDA(cudaHostRegister(h->e.data(), h->e.size() * 4, cudaHostRegisterDefault));
-    if (!h->ev.empty()) MG_CUDA(cudaHostRegister(h->ev.data(), h->ev.size() * 4, cudaHostRegisterDefault));
+    // driver-allocated page-locked copies (registered malloc pages were
+    // measured slower for uploads that overlap running kernels)
+    auto copy = [](const std::vector<int32_t> &src, int32_t **dst) -> mg_status {
+        if (src.empty()) return MG_OK;
+        MG_CUDA(cudaHostAlloc((void **)dst, src.size() * 4, cudaHostAllocDefault));
+        std::memcpy(*dst, src.data(), src.size() * 4);
+        return MG_OK;
+    };
+    mg_status st = copy(h->v, &h->pin_v);
+    if (st == MG_OK) st = copy(h->e, &h->pin_e);
+    if (st == MG_OK) st = copy(h->ev, &h->pin_ev);
+    if (st != MG_OK) {
+        if (h->pin_v) cudaFreeHost(h->pin_v);
+        if (h->pin_e) cudaFreeHost(h->pin_e);
+        if (h->pin_ev) cudaFreeHost(h->pin_ev);
+        h->pin_v = h->pin_e = h->pin_ev = nullptr;
+        return st;
+    }
     h->pinned = true;
     return MG_OK;
 }

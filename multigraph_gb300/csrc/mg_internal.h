@@ -12,6 +12,9 @@ struct mg_host_graph {
     int32_t nv = 0, ne = 0, start_p = 0, tra = 0;
     std::vector<int32_t> v, e, ev;  // CSR row offsets, column ids, integer weights
     bool pinned = false;
+    // page-locked copies of v / e / ev made by mg_host_graph_pin (driver
+    // allocations: staged uploads read them at full link speed)
+    int32_t *pin_v = nullptr, *pin_e = nullptr, *pin_ev = nullptr;
 };
 
 namespace mgi {

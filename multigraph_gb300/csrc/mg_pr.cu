@@ -75,6 +75,12 @@ struct PArgs {
     const int32_t *hrow_chunk;
     int32_t nhrows;
     int32_t heavy_deg;
+    // hub split (unweighted forms on graphs with enough hub edges): prow /
+    // pcol hold the tail part, hsum the hub part's per-row sums of the
+    // sweep; heavy chunks keep their full-row numbering (prow_full, chunk)
+    const float *hsum;
+    const int32_t *prow_full;
+    int32_t chunk;
     float *x[2];             // iterate (ping-pong)
     float *c[2];             // gathered quantity: contribution x/deg (PR) or lambda (adjoint)
     const float *gvec;       // adjoint: g
@@ -205,6 +211,7 @@ struct PrRowOp {
     __device__ void finish(int32_t v, float s)
     {
         float dg = 0.0f;
+        if (a.hsum) s += __ldcg(&a.hsum[v]);
         resid += pr_apply<V>(a, c, v, s, any, dg);
         dangs += dg;
     }
@@ -230,6 +237,14 @@ __global__ void __launch_bounds__(THREADS) k_pr_light(PArgs a)
     __shared__ float s_part[THREADS / 32];
     for (int32_t ch = blockIdx.x; ch < a.nhchunks; ch += gridDim.x) {
         int32_t v = a.hchunk[3 * ch], b = a.hchunk[3 * ch + 1], e = a.hchunk[3 * ch + 2];
+        if (a.hsum) {
+            // the same piece of the row's tail part: piece k of the full
+            // row covers tail positions [k * chunk, (k + 1) * chunk)
+            const int32_t k = (b - a.prow_full[v]) / a.chunk;
+            const int32_t tb = a.prow[v], te = a.prow[v + 1];
+            b = min(te, tb + k * a.chunk);
+            e = min(te, b + a.chunk);
+        }
         float acc = 0.0f;
         if (!pr_row_skipped<V>(a, v)) {
             for (int32_t b0 = b; b0 < e; b0 += 8 * THREADS) {
@@ -283,6 +298,7 @@ __global__ void __launch_bounds__(THREADS) k_pr_apply(PArgs a, cudaGraphConditio
         for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
         if (lane == 0) {
             float dg = 0.0f;
+            if (a.hsum) s += __ldcg(&a.hsum[v]);
             resid += pr_apply<V>(a, c, v, s, any, dg);
             dangs += dg;
         }
@@ -650,7 +666,9 @@ static mg_status pr_loop(mg_graph *g, PArgs &a, const mg_opts &opt, const char *
     std::string hn = std::string(name) + "_apply";
     const int sh = P.slot(hn.c_str());
     const int apply_grid = std::max(1, std::min(std::min(grid, (a.nhrows + 7) / 8), g->num_sms * APPLY_PER_SM));
+    const int shs = a.hsum ? P.slot("pr_hub") : -1, shf = a.hsum ? P.slot("pr_hub_fix") : -1;
     BodyFn body = [&](cudaStream_t st, cudaGraphConditionalHandle h, int use_cond) -> mg_status {
+        if (a.hsum) MG_TRY(hub_launch(g, a.c[0], a.c[1], &a.ctl->cur, &a.ctl->more, st, shs, shf));
         P.begin(sl);
         k_pr_light<V><<<grid, THREADS, 0, st>>>(a);
         P.end();
@@ -662,12 +680,14 @@ static mg_status pr_loop(mg_graph *g, PArgs &a, const mg_opts &opt, const char *
     };
     int max_iter = opt.max_iter > 0 ? opt.max_iter : 10000;
     // the key holds every by-value argument of the captured kernels
-    const LoopKey key = LoopKey().add(V).add(a).add(grid).add(apply_grid);
+    // (and the hub split's build, whose sizes the hub kernels take by value)
+    const LoopKey key = LoopKey().add(V).add(a).add(grid).add(apply_grid).add(a.hsum ? g->hub.gen : 0ull);
     MG_TRY(run_loop(opt.profile ? MG_EXEC_HOST : opt.exec, opt.profile != 0, s, g->pws->lg[V], key, body,
                     &a.ctl->more, g->pinned_flag, max_iter + 2));
     PCtl hc;
     MG_CUDA(cudaMemcpyAsync(&hc, a.ctl, sizeof(PCtl), cudaMemcpyDeviceToHost, s));
     MG_CUDA(cudaStreamSynchronize(s));
+    if (a.hsum) MG_TRY(hub_check(g));
     if (info) {
         info->iterations = hc.iter;
         info->pull_iterations = hc.iter;
@@ -710,6 +730,16 @@ static mg_status pr_setup(mg_graph *g, PArgs &a, bool weighted_or_adj)
     a.bpart = w->bpart.as<double>();
     a.nblocks = grid;
     a.ctl = w->ctl.as<PCtl>();
+    if (!weighted_or_adj) {
+        MG_TRY(hub_prepare(g));
+        if (g->hub.use) {
+            a.prow = g->hub.toff.as<int32_t>();
+            a.pcol = g->hub.tcol.as<int32_t>();
+            a.hsum = g->hub.hsum.as<float>();
+            a.prow_full = g->trow;
+            a.chunk = g->hchunk_size;
+        }
+    }
     if (weighted_or_adj) {
         if (!g->has_fw) return fail(MG_ERR_UNSUPPORTED, "float edge weights not set (mg_graph_set_float_weights)");
         if (!g->symmetric) return fail(MG_ERR_UNSUPPORTED, "weighted PageRank needs a structurally symmetric graph");
