@@ -106,6 +106,7 @@ struct HubSplit {
     bool use = false;        // the split is in use (enough hub edges)
     uint64_t gen = 0;        // build number (process-wide): captured sweeps key on it
     int32_t H = 0, nrows = 0, nchunks = 0;
+    int32_t nlong = 0;       // chunks whose last row spans many chunks
     int64_t mh = 0;          // hub edges
     DevBuf hoff, toff;       // int32 [n+1]: hub / tail row offsets
     DevBuf hrows;            // int32 [nrows]: rows with hub edges, ascending
@@ -113,6 +114,7 @@ struct HubSplit {
     DevBuf rstart;           // uint32 bits: first hub edge of each row
     DevBuf crow;             // int32 [nchunks+1]: hub-row index of each chunk's first start
     DevBuf chead, ctail, cstart;  // per-chunk carries of the sweep
+    DevBuf cnext, clong;     // per chunk: next chunk with a row start; long-span chunks
     DevBuf hsum;             // float [n]: hub sums of the current sweep
     DevBuf tmp0, tmp1, tiles, err;
 };
@@ -231,10 +233,10 @@ mg_status bc_batched(mg_graph *g, const int32_t *src_engine, int32_t nsrc, const
                      const float **bc_dev);
 // PageRank hub split: build for the current pull columns (when stale),
 // enqueue one sweep's hub sums (contributions c0 / c1 picked by *cur; no-op
-// once *more is 0), report a bulk-copy wait that ran out, free
+// once *more is 0 or *off is not), report a bulk-copy wait that ran out, free
 mg_status hub_prepare(mg_graph *g);
 mg_status hub_launch(mg_graph *g, const float *c0, const float *c1, const int32_t *cur, const int32_t *more,
-                     cudaStream_t st, int slot_sweep, int slot_fix);
+                     const int32_t *off, cudaStream_t st, int slot_sweep, int slot_fix);
 mg_status hub_check(mg_graph *g);
 void hub_free(mg_graph *g);
 

@@ -40,6 +40,7 @@ constexpr int HUB_THREADS = 1024;   // one CTA per SM (shared memory bound)
 constexpr int HUB_ILP = 2;          // chunks in flight per warp
 constexpr int SCAN_T = 1024, SCAN_IPT = 4, SCAN_TILE = SCAN_T * SCAN_IPT;
 constexpr long long HUB_WAIT_LIMIT = 20000000ll;  // clock64 cycles (~10 ms) for the bulk copy
+constexpr int32_t FIX_SHORT = 8;    // carry spans up to this many chunks: a thread each
 
 // ---------------------------------------------------------------------------
 // exclusive scan of int32 (out[n] = total): tiles of 4096, tile totals
@@ -203,9 +204,13 @@ struct HubArgs {
     const float *c[2];        // contributions (ping-pong, ctl selects)
     const int32_t *cur;       // current iterate index (loop control block)
     const int32_t *more;      // loop continue flag
+    const int32_t *off;       // non-zero: sweeps run elsewhere (queue sweeps)
     float *hsum;              // per-row hub sums
     float *chead, *ctail;     // per chunk: sum before its first row start / of its open last row
     int32_t *cstart;          // per chunk: has a row start
+    const int32_t *cnext;     // per chunk with a start: the next chunk with one (nchunks: none)
+    const int32_t *clong;     // chunks whose last row spans more than FIX_SHORT chunks
+    int32_t nlong;
     int32_t *err;             // bulk copy wait ran out
     int32_t H, nchunks;
 };
@@ -282,7 +287,7 @@ __global__ void __launch_bounds__(HUB_THREADS, 1) k_hub_sweep(HubArgs a)
 {
     extern __shared__ __align__(128) float s_c[];   // [H + 4]
     __shared__ __align__(8) uint64_t mbar;
-    if (__ldg(a.more) == 0) return;
+    if (__ldg(a.more) == 0 || __ldg(a.off) != 0) return;
     const float *c = __ldg(a.cur) ? a.c[1] : a.c[0];
     if (!stage_hub(s_c, c, a.H, &mbar, a.err)) return;
     const int lane = threadIdx.x & 31;
@@ -365,19 +370,47 @@ __global__ void __launch_bounds__(HUB_THREADS, 1) k_hub_sweep(HubArgs a)
 }
 
 // rows that run past their chunk: the open tail plus the heads of the
-// following chunks, up to the first chunk with a row start (fixed order).
-// crow[ch + 1] - 1 is the hub-row index of chunk ch's last row start.
+// following chunks up to and including the next chunk with a row start
+// (cnext, fixed by the layout), summed in FP64 and rounded once: a hub row
+// can span hundreds of chunks, and an FP32 running sum of their heads would
+// carry rounding of a few 1e-6 that moves from sweep to sweep.  Spans of up
+// to FIX_SHORT chunks take a thread each; longer ones (clong) a warp each,
+// lane-strided then a fixed shuffle tree.  crow[ch + 1] - 1 is the hub-row
+// index of chunk ch's last row start.
 __global__ void k_hub_fix(HubArgs a)
 {
-    if (__ldg(a.more) == 0) return;
-    for (int32_t ch = blockIdx.x * blockDim.x + threadIdx.x; ch < a.nchunks; ch += gridDim.x * blockDim.x) {
-        if (!a.cstart[ch]) continue;
-        float total = a.ctail[ch];
-        for (int32_t k = ch + 1; k < a.nchunks; k++) {
-            total += a.chead[k];
-            if (a.cstart[k]) break;
-        }
-        a.hsum[__ldg(&a.hrows[__ldg(&a.crow[ch + 1]) - 1])] = total;
+    if (__ldg(a.more) == 0 || __ldg(a.off) != 0) return;
+    const int32_t tid = blockIdx.x * blockDim.x + threadIdx.x, nth = gridDim.x * blockDim.x;
+    for (int32_t ch = tid; ch < a.nchunks; ch += nth) {
+        if (!__ldg(&a.cstart[ch])) continue;
+        const int32_t last = min(__ldg(&a.cnext[ch]), a.nchunks - 1);
+        if (last - ch > FIX_SHORT) continue;
+        double total = a.ctail[ch];
+        for (int32_t k = ch + 1; k <= last; k++) total += a.chead[k];
+        a.hsum[__ldg(&a.hrows[__ldg(&a.crow[ch + 1]) - 1])] = (float)total;
+    }
+    const int lane = threadIdx.x & 31;
+    for (int32_t i = tid >> 5; i < a.nlong; i += nth >> 5) {
+        const int32_t ch = __ldg(&a.clong[i]);
+        const int32_t last = min(__ldg(&a.cnext[ch]), a.nchunks - 1);
+        double t = 0.0;
+        for (int32_t k = ch + 1 + lane; k <= last; k += 32) t += a.chead[k];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+        if (lane == 0) a.hsum[__ldg(&a.hrows[__ldg(&a.crow[ch + 1]) - 1])] = (float)(t + (double)a.ctail[ch]);
+    }
+}
+
+// layout: for every chunk with a row start, the next chunk with one (its
+// last row ends there), and the list of chunks whose span is long
+__global__ void k_hub_spans(const int32_t *cnt, int32_t nchunks, int32_t *cnext, int32_t *clong, int32_t *nlong)
+{
+    for (int32_t ch = blockIdx.x * blockDim.x + threadIdx.x; ch < nchunks; ch += gridDim.x * blockDim.x) {
+        if (!cnt[ch]) continue;
+        int32_t k = ch + 1;
+        while (k < nchunks && cnt[k] == 0) k++;
+        cnext[ch] = k;
+        if (min(k, nchunks - 1) - ch > FIX_SHORT) clong[atomicAdd(nlong, 1)] = ch;
     }
 }
 
@@ -403,7 +436,7 @@ void hub_free(mg_graph *g)
 {
     HubSplit &h = g->hub;
     DevBuf *bufs[] = {&h.hoff, &h.toff, &h.hrows, &h.hcol, &h.tcol, &h.rstart, &h.crow, &h.chead,
-                      &h.ctail, &h.cstart, &h.hsum, &h.tmp0, &h.tmp1, &h.tiles, &h.err};
+                      &h.ctail, &h.cstart, &h.cnext, &h.clong, &h.hsum, &h.tmp0, &h.tmp1, &h.tiles, &h.err};
     for (DevBuf *b : bufs) dev_free(*b);
     h = HubSplit();
 }
@@ -474,6 +507,13 @@ mg_status hub_prepare(mg_graph *g)
     k_chunk_starts<<<grid, 256, 0, s>>>(h.rstart.as<uint32_t>(), h.nchunks, h.tmp0.as<int32_t>());
     MG_CUDA(cudaGetLastError());
     MG_TRY(scan_excl(h.tmp0.as<int32_t>(), h.nchunks, h.crow.as<int32_t>(), h.tiles, s));
+    MG_TRY(dev_alloc(h.cnext, (size_t)h.nchunks * 4));
+    MG_TRY(dev_alloc(h.clong, (size_t)h.nchunks * 4 + 4));   // [0]: count, then the chunk ids
+    MG_CUDA(cudaMemsetAsync(h.clong.p, 0, 4, s));
+    k_hub_spans<<<grid, 256, 0, s>>>(h.tmp0.as<int32_t>(), h.nchunks, h.cnext.as<int32_t>(),
+                                     h.clong.as<int32_t>() + 1, h.clong.as<int32_t>());
+    MG_CUDA(cudaGetLastError());
+    MG_CUDA(cudaMemcpyAsync(&h.nlong, h.clong.p, 4, cudaMemcpyDeviceToHost, s));
     MG_CUDA(cudaStreamSynchronize(s));
     dev_free(h.tmp0);
     dev_free(h.tmp1);
@@ -485,7 +525,7 @@ mg_status hub_prepare(mg_graph *g)
 size_t hub_smem_bytes(const mg_graph *g) { return (size_t)(g->hub.H + 4) * 4; }
 
 mg_status hub_launch(mg_graph *g, const float *c0, const float *c1, const int32_t *cur, const int32_t *more,
-                     cudaStream_t st, int slot_sweep, int slot_fix)
+                     const int32_t *off, cudaStream_t st, int slot_sweep, int slot_fix)
 {
     HubSplit &h = g->hub;
     HubArgs a;
@@ -498,10 +538,14 @@ mg_status hub_launch(mg_graph *g, const float *c0, const float *c1, const int32_
     a.c[1] = c1;
     a.cur = cur;
     a.more = more;
+    a.off = off;
     a.hsum = h.hsum.as<float>();
     a.chead = h.chead.as<float>();
     a.ctail = h.ctail.as<float>();
     a.cstart = h.cstart.as<int32_t>();
+    a.cnext = h.cnext.as<int32_t>();
+    a.clong = h.clong.as<int32_t>() + 1;
+    a.nlong = h.nlong;
     a.err = h.err.as<int32_t>();
     a.H = h.H;
     a.nchunks = h.nchunks;

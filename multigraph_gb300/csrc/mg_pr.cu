@@ -50,6 +50,16 @@ struct PCtl {
     float base;           // (1-d)/n + d*dangling/n of the current sweep (set once per sweep)
     float tol_row;        // tol / n: per-vertex activity threshold of the data-driven form
     float lam_meanf;      // lam_mean as float
+    // data-driven form, frontier sweeps: once the active vertices' in-edges
+    // fall below m / SPARSE_ALPHA the sweeps run over a queue of them and
+    // update x[cur] / c[cur] in place (frozen vertices keep their values)
+    int32_t sparse;       // 1: queue sweeps
+    int32_t need_compact; // the queue is to be built from the active flags
+    int32_t qc;           // current queue (0 / 1)
+    int32_t dense_iters;  // sweeps that ran over every row
+    int32_t qn[2];        // queue sizes (qn[qc ^ 1]: appends of this sweep)
+    double dang_frozen;   // dangling mass of frozen vertices
+    long long act_edges;  // in-edges of the vertices still active
 };
 
 // per-sweep constants derived once (FP64 math stays out of the per-row path)
@@ -86,10 +96,19 @@ struct PArgs {
     const float *gvec;       // adjoint: g
     int32_t *active;         // data-driven masks
     float *hpart;            // heavy chunk partial sums
-    double *bpart;           // per-block partials: [3*grid] (resid, dangling, any)
+    double *bpart;           // per-block partials: [NPART*slots] (resid, dangling, any, active edges, frozen dangling)
     int32_t nblocks;
     PCtl *ctl;
+    // data-driven frontier sweeps: the full pull rows (the hub split keeps
+    // only the tail in prow / pcol), two queues, the queue sweep's new values
+    const int32_t *frow, *fcol;
+    int32_t *queue[2];
+    float *qval;
+    int64_t m;
 };
+
+constexpr int NPART = 5;       // partials per block slot
+constexpr int SPARSE_ALPHA = 16;  // queue sweeps once active in-edges < m / SPARSE_ALPHA
 
 // ---------------------------------------------------------------------------
 // per-row update.  s = gathered sum.  Returns |change|; sets *any when the
@@ -166,25 +185,38 @@ __device__ __forceinline__ bool pr_row_skipped(const PArgs &a, int32_t v)
     return V == V_D && a.active[v] == 0;
 }
 
-__device__ __forceinline__ void block_partials(const PArgs &a, int slot, double r, double dg, int any)
+__device__ __forceinline__ void block_partials(const PArgs &a, int slot, double r, double dg, int any,
+                                               double act = 0.0, double dfz = 0.0)
 {
-    __shared__ double sr[THREADS / 32], sd[THREADS / 32];
+    __shared__ double sp[NPART - 1][THREADS / 32];
     __shared__ int sa[THREADS / 32];
+    double v[NPART - 1] = {r, dg, act, dfz};
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
-        r += __shfl_xor_sync(0xffffffffu, r, o);
-        dg += __shfl_xor_sync(0xffffffffu, dg, o);
+#pragma unroll
+        for (int k = 0; k < NPART - 1; k++) v[k] += __shfl_xor_sync(0xffffffffu, v[k], o);
         any |= __shfl_xor_sync(0xffffffffu, any, o);
     }
-    if ((threadIdx.x & 31) == 0) { sr[threadIdx.x >> 5] = r; sd[threadIdx.x >> 5] = dg; sa[threadIdx.x >> 5] = any; }
+    if ((threadIdx.x & 31) == 0) {
+#pragma unroll
+        for (int k = 0; k < NPART - 1; k++) sp[k][threadIdx.x >> 5] = v[k];
+        sa[threadIdx.x >> 5] = any;
+    }
     __syncthreads();
     if (threadIdx.x == 0) {
-        double R = 0, D = 0;
+        double T[NPART - 1] = {0, 0, 0, 0};
         int A = 0;
-        for (int w = 0; w < THREADS / 32; w++) { R += sr[w]; D += sd[w]; A |= sa[w]; }
-        a.bpart[3 * slot] = R;
-        a.bpart[3 * slot + 1] = D;
-        a.bpart[3 * slot + 2] = (double)A;
+        for (int w = 0; w < THREADS / 32; w++) {
+#pragma unroll
+            for (int k = 0; k < NPART - 1; k++) T[k] += sp[k][w];
+            A |= sa[w];
+        }
+        double *o = a.bpart + (size_t)NPART * slot;
+        o[0] = T[0];
+        o[1] = T[1];
+        o[2] = (double)A;
+        o[3] = T[2];
+        o[4] = T[3];
     }
 }
 
@@ -197,6 +229,8 @@ struct PrRowOp {
     const PArgs &a;
     const PCtl &c;
     float resid = 0.0f, dangs = 0.0f;  // per-thread partials (blocks sum in FP64)
+    float dfz = 0.0f;                  // data-driven: dangling mass of frozen rows
+    double act = 0.0;                  // data-driven: in-edges of rows still active
     int any = 0;
     __device__ float identity() const { return 0.0f; }
     __device__ bool skip(int32_t v) const { return pr_row_skipped<V>(a, v); }
@@ -214,6 +248,10 @@ struct PrRowOp {
         if (a.hsum) s += __ldcg(&a.hsum[v]);
         resid += pr_apply<V>(a, c, v, s, any, dg);
         dangs += dg;
+        if (V == V_D) {
+            if (a.active[v]) act += (double)(a.frow[v + 1] - a.frow[v]);
+            else dfz += dg;
+        }
     }
 };
 
@@ -221,7 +259,7 @@ template <int V>
 __global__ void __launch_bounds__(THREADS) k_pr_light(PArgs a)
 {
     const PCtl c = *a.ctl;
-    if (c.more == 0) return;
+    if (c.more == 0 || c.sparse) return;
     const int lane = mgd::lane();
     const int gwarp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int nwarps = (gridDim.x * blockDim.x) >> 5;
@@ -270,12 +308,63 @@ __global__ void __launch_bounds__(THREADS) k_pr_light(PArgs a)
         }
         __syncthreads();
     }
-    block_partials(a, blockIdx.x, op.resid, op.dangs, op.any);
+    block_partials(a, blockIdx.x, op.resid, op.dangs, op.any, op.act, op.dfz);
+}
+
+// Sum of the partials of slots [s0, s1): lane-strided in slot order, then a
+// fixed shuffle tree and warp order (thread 0 gets T[0..3] and A).
+__device__ __forceinline__ void reduce_slots(const double *bpart, int s0, int s1, double T[NPART - 1], int &A)
+{
+    __shared__ double sp[NPART - 1][THREADS / 32];
+    __shared__ int sa[THREADS / 32];
+    double v[NPART - 1] = {0, 0, 0, 0};
+    int any = 0;
+    for (int b = s0 + (int)threadIdx.x; b < s1; b += blockDim.x) {
+        const double *o = bpart + (size_t)NPART * b;
+        v[0] += __ldcg(&o[0]);
+        v[1] += __ldcg(&o[1]);
+        any |= __ldcg(&o[2]) != 0.0;
+        v[2] += __ldcg(&o[3]);
+        v[3] += __ldcg(&o[4]);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+#pragma unroll
+        for (int k = 0; k < NPART - 1; k++) v[k] += __shfl_xor_sync(0xffffffffu, v[k], o);
+        any |= __shfl_xor_sync(0xffffffffu, any, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+#pragma unroll
+        for (int k = 0; k < NPART - 1; k++) sp[k][threadIdx.x >> 5] = v[k];
+        sa[threadIdx.x >> 5] = any;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int k = 0; k < NPART - 1; k++) T[k] = 0.0;
+        A = 0;
+        for (int w = 0; w < THREADS / 32; w++) {
+            for (int k = 0; k < NPART - 1; k++) T[k] += sp[k][w];
+            A |= sa[w];
+        }
+    }
+}
+
+// last block to arrive (per-launch counter ctl->done) returns true
+__device__ __forceinline__ bool last_block(PCtl *cp)
+{
+    __shared__ int s_last;
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) s_last = (atomicAdd(&cp->done, 1) == (int)gridDim.x - 1);
+    __syncthreads();
+    return s_last != 0;
 }
 
 // Heavy rows (warp per row, chunk partials summed lane-strided then by a
 // fixed shuffle tree), then the last block to arrive reduces every block's
 // partials in slot order and updates the loop state -- no block waits.
+// The data-driven form switches to queue sweeps here once the active
+// vertices' in-edges fall below m / SPARSE_ALPHA.
 template <int V>
 __global__ void __launch_bounds__(THREADS) k_pr_apply(PArgs a, cudaGraphConditionalHandle h, int use_cond)
 {
@@ -285,10 +374,11 @@ __global__ void __launch_bounds__(THREADS) k_pr_apply(PArgs a, cudaGraphConditio
         if (blockIdx.x == 0 && threadIdx.x == 0 && use_cond) cudaGraphSetConditional(h, 0u);
         return;
     }
+    if (c.sparse) return;   // queue sweeps (k_prd_*) drive the loop
     const int lane = mgd::lane();
     const int gwarp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int nwarps = (gridDim.x * blockDim.x) >> 5;
-    double resid = 0.0, dangs = 0.0;
+    double resid = 0.0, dangs = 0.0, act = 0.0, dfz = 0.0;
     int any = 0;
     for (int32_t i = gwarp; i < a.nhrows; i += nwarps) {
         int32_t v = a.hrows[i];
@@ -301,54 +391,166 @@ __global__ void __launch_bounds__(THREADS) k_pr_apply(PArgs a, cudaGraphConditio
             if (a.hsum) s += __ldcg(&a.hsum[v]);
             resid += pr_apply<V>(a, c, v, s, any, dg);
             dangs += dg;
+            if (V == V_D) {
+                if (a.active[v]) act += (double)(a.frow[v + 1] - a.frow[v]);
+                else dfz += dg;
+            }
         }
     }
-    block_partials(a, a.nblocks + blockIdx.x, resid, dangs, any);
-    __shared__ int s_last;
-    __threadfence();
-    __syncthreads();
-    if (threadIdx.x == 0) s_last = (atomicAdd(&cp->done, 1) == (int)gridDim.x - 1);
-    __syncthreads();
-    if (!s_last) return;
-    __shared__ double sr[THREADS / 32], sd[THREADS / 32];
-    __shared__ int sa[THREADS / 32];
-    resid = 0.0;
-    dangs = 0.0;
-    any = 0;
-    const int nslots = a.nblocks + gridDim.x;
-    for (int b = threadIdx.x; b < nslots; b += blockDim.x) {
-        resid += __ldcg(&a.bpart[3 * b]);
-        dangs += __ldcg(&a.bpart[3 * b + 1]);
-        any |= __ldcg(&a.bpart[3 * b + 2]) != 0.0;
-    }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-        resid += __shfl_xor_sync(0xffffffffu, resid, o);
-        dangs += __shfl_xor_sync(0xffffffffu, dangs, o);
-        any |= __shfl_xor_sync(0xffffffffu, any, o);
-    }
-    if (lane == 0) { sr[threadIdx.x >> 5] = resid; sd[threadIdx.x >> 5] = dangs; sa[threadIdx.x >> 5] = any; }
-    __syncthreads();
+    block_partials(a, a.nblocks + blockIdx.x, resid, dangs, any, act, dfz);
+    if (!last_block(cp)) return;
+    double T[NPART - 1];
+    int A;
+    reduce_slots(a.bpart, 0, a.nblocks + gridDim.x, T, A);
     if (threadIdx.x == 0) {
+        const double R = T[0], D = T[1];
         int more = 1;
-        {
-            double R = 0, D = 0;
-            int A = 0;
-            for (int w = 0; w < THREADS / 32; w++) { R += sr[w]; D += sd[w]; A |= sa[w]; }
-            cp->done = 0;
-            cp->iter = c.iter + 1;
-            cp->cur = c.cur ^ 1;
-            cp->resid = R;
-            cp->any = A;
-            if (V == V_ADJ) cp->lam_mean = D / c.n;
-            else cp->dangling = D;
-            pctl_derive(cp);
-            if (V == V_T_REF || V == V_D_REF) more = A;
-            else if (V == V_D) more = (A && R > (double)c.tol) ? 1 : 0;
-            else more = R > (double)c.tol ? 1 : 0;
-            if (more && cp->iter >= c.max_iter) { cp->status = 1; more = 0; }
-            cp->more = more;
+        cp->done = 0;
+        cp->iter = c.iter + 1;
+        cp->cur = c.cur ^ 1;
+        cp->resid = R;
+        cp->any = A;
+        if (V == V_ADJ) cp->lam_mean = D / c.n;
+        else cp->dangling = D;
+        pctl_derive(cp);
+        if (V == V_T_REF || V == V_D_REF) more = A;
+        else if (V == V_D) more = (A && R > (double)c.tol) ? 1 : 0;
+        else more = R > (double)c.tol ? 1 : 0;
+        if (more && cp->iter >= c.max_iter) { cp->status = 1; more = 0; }
+        cp->more = more;
+        if (V == V_D) {
+            cp->dense_iters = c.dense_iters + 1;
+            cp->act_edges = (long long)T[2];
+            cp->dang_frozen = T[3];
+            if (more && T[2] * SPARSE_ALPHA < (double)a.m) {
+                cp->sparse = 1;
+                cp->need_compact = 1;
+                cp->qc = 0;
+                cp->qn[0] = cp->qn[1] = 0;
+            }
         }
+        if (use_cond) cudaGraphSetConditional(h, more ? 1u : 0u);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// data-driven frontier sweeps (processi.cu:182-407: _process_f1 works from
+// the active vertices, process_f3 applies and requeues those still above
+// the per-vertex tolerance).  Pull form over the queue of active vertices;
+// the sweep's new values go to qval first and are applied in place by the
+// next kernel, so every gather of a sweep reads the previous iterate.
+// ---------------------------------------------------------------------------
+// queue = every still-active vertex (once, at the switch)
+__global__ void __launch_bounds__(THREADS) k_prd_compact(PArgs a)
+{
+    const PCtl c = *a.ctl;
+    if (!c.more || !c.sparse || !c.need_compact) return;
+    const int lane = mgd::lane();
+    for (int32_t b0 = (blockIdx.x * blockDim.x + threadIdx.x) & ~31; b0 < a.n; b0 += gridDim.x * blockDim.x) {
+        const int32_t v = b0 + lane;
+        const bool p = v < a.n && a.active[v] != 0;
+        const unsigned m = __ballot_sync(0xffffffffu, p);
+        int base = 0;
+        if (lane == 0 && m) base = atomicAdd(&a.ctl->qn[0], __popc(m));
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (p) a.queue[0][base + __popc(m & ((1u << lane) - 1u))] = v;
+    }
+}
+
+// one queue sweep: an 8-lane group per queued vertex (four per warp), its
+// full in-edge row summed lane-strided then by a fixed shuffle tree
+__global__ void __launch_bounds__(THREADS) k_prd_gather(PArgs a)
+{
+    const PCtl c = *a.ctl;
+    if (!c.more || !c.sparse) return;
+    const int lane = mgd::lane(), grp = lane >> 3, gl = lane & 7;
+    const int32_t gwarp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int32_t nwarps = (gridDim.x * blockDim.x) >> 5;
+    const int32_t nq = c.qn[c.qc];
+    const int32_t *q = a.queue[c.qc];
+    int32_t *nextq = a.queue[c.qc ^ 1];
+    const float *cc = a.c[c.cur];
+    const float *xc = a.x[c.cur];
+    const float d = c.damping;
+    double resid = 0.0, dangs = 0.0, act = 0.0, dfz = 0.0;
+    int any = 0;
+    for (int32_t base = gwarp * 4; base < nq; base += nwarps * 4) {
+        const int32_t i = base + grp;
+        int32_t v = -1, b = 0, e = 0;
+        if (i < nq) {
+            v = q[i];
+            b = a.frow[v];
+            e = a.frow[v + 1];
+        }
+        float sum = 0.0f;
+        for (int32_t p = b + gl; p < e; p += 8) sum += cc[__ldg(&a.fcol[p])];
+#pragma unroll
+        for (int o = 4; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
+        bool keep = false;
+        if (v >= 0 && gl == 0) {
+            const float xo = xc[v];
+            const float xn = c.base + d * sum;
+            const float diff = fabsf(xn - xo);
+            const int32_t od = a.outrow[v + 1] - a.outrow[v];
+            a.qval[i] = xn;
+            resid += diff;
+            if (od == 0) dangs += xn;
+            if (diff > c.tol_row) {
+                keep = true;
+                any = 1;
+                act += (double)(e - b);
+            } else {
+                a.active[v] = 0;   // frozen from now on, at xn
+                if (od == 0) dfz += xn;
+            }
+        }
+        // the group leaders that stay active requeue with one atomic per warp
+        const unsigned km = __ballot_sync(0xffffffffu, keep);
+        int qb = 0;
+        if (lane == 0 && km) qb = atomicAdd(&a.ctl->qn[c.qc ^ 1], __popc(km));
+        qb = __shfl_sync(0xffffffffu, qb, 0);
+        if (keep) nextq[qb + __popc(km & ((1u << lane) - 1u))] = v;
+    }
+    block_partials(a, blockIdx.x, resid, dangs, any, act, dfz);
+}
+
+// apply the queue sweep's values in place, then the last block updates the
+// loop state (the iterate stays in x[cur] / c[cur])
+__global__ void __launch_bounds__(THREADS) k_prd_apply(PArgs a, cudaGraphConditionalHandle h, int use_cond)
+{
+    PCtl *cp = a.ctl;
+    const PCtl c = *cp;
+    if (!c.more || !c.sparse) return;   // the dense apply set the loop condition
+    const int32_t nq = c.qn[c.qc];
+    const int32_t *q = a.queue[c.qc];
+    float *xc = a.x[c.cur];
+    float *cc = a.c[c.cur];
+    for (int32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < nq; i += gridDim.x * blockDim.x) {
+        const int32_t v = q[i];
+        const float xn = a.qval[i];
+        const int32_t od = a.outrow[v + 1] - a.outrow[v];
+        xc[v] = xn;
+        cc[v] = od > 0 ? xn / (float)od : 0.0f;
+    }
+    if (!last_block(cp)) return;
+    double T[NPART - 1];
+    int A;
+    reduce_slots(a.bpart, 0, a.nblocks, T, A);
+    if (threadIdx.x == 0) {
+        cp->done = 0;
+        cp->iter = c.iter + 1;
+        cp->resid = T[0];
+        cp->any = A;
+        cp->dangling = c.dang_frozen + T[1];
+        cp->dang_frozen = c.dang_frozen + T[3];
+        cp->act_edges = (long long)T[2];
+        cp->need_compact = 0;
+        cp->qn[c.qc] = 0;
+        cp->qc = c.qc ^ 1;
+        pctl_derive(cp);
+        int more = (A && T[0] > (double)c.tol) ? 1 : 0;
+        if (more && cp->iter >= c.max_iter) { cp->status = 1; more = 0; }
+        cp->more = more;
         if (use_cond) cudaGraphSetConditional(h, more ? 1u : 0u);
     }
 }
@@ -608,6 +810,7 @@ __global__ void k_ppr_store(int32_t n, const float *X, int32_t nseed, int32_t s0
 struct PrWS {
     mgi::DevBuf x0, x1, c0, c1, active, hpart, bpart, ctl, S, wT, gvec, grad, lam_keep, xkeep;
     mgi::DevBuf wT_caller, gvec_caller, grad_caller;  // caller-order staging of a relabeled graph
+    mgi::DevBuf q0, q1, qval;  // data-driven queue sweeps
     uint64_t wT_version = 0;  // fw_version that S and wT were derived from (0: none)
     mgi::LoopGraph lg[6];
 };
@@ -627,7 +830,7 @@ void free_pr_ws(mg_graph *g)
     PrWS *w = g->pws;
     DevBuf *bufs[] = {&w->x0, &w->x1, &w->c0, &w->c1, &w->active, &w->hpart, &w->bpart, &w->ctl, &w->S,
                       &w->wT, &w->gvec, &w->grad, &w->lam_keep, &w->xkeep, &w->wT_caller, &w->gvec_caller,
-                      &w->grad_caller};
+                      &w->grad_caller, &w->q0, &w->q1, &w->qval};
     for (DevBuf *b : bufs) dev_free(*b);
     for (auto &l : w->lg) l.destroy();
     delete w;
@@ -667,14 +870,28 @@ static mg_status pr_loop(mg_graph *g, PArgs &a, const mg_opts &opt, const char *
     const int sh = P.slot(hn.c_str());
     const int apply_grid = std::max(1, std::min(std::min(grid, (a.nhrows + 7) / 8), g->num_sms * APPLY_PER_SM));
     const int shs = a.hsum ? P.slot("pr_hub") : -1, shf = a.hsum ? P.slot("pr_hub_fix") : -1;
+    const int sqc = V == V_D ? P.slot("prd_compact") : -1, sqg = V == V_D ? P.slot("prd_gather") : -1,
+              sqa = V == V_D ? P.slot("prd_apply") : -1;
     BodyFn body = [&](cudaStream_t st, cudaGraphConditionalHandle h, int use_cond) -> mg_status {
-        if (a.hsum) MG_TRY(hub_launch(g, a.c[0], a.c[1], &a.ctl->cur, &a.ctl->more, st, shs, shf));
+        if (a.hsum) MG_TRY(hub_launch(g, a.c[0], a.c[1], &a.ctl->cur, &a.ctl->more, &a.ctl->sparse, st, shs, shf));
         P.begin(sl);
         k_pr_light<V><<<grid, THREADS, 0, st>>>(a);
         P.end();
         P.begin(sh);
         k_pr_apply<V><<<apply_grid, THREADS, 0, st>>>(a, h, use_cond);
         P.end();
+        if (V == V_D) {
+            // queue sweeps once the switch has happened (no-ops before)
+            P.begin(sqc);
+            k_prd_compact<<<grid, THREADS, 0, st>>>(a);
+            P.end();
+            P.begin(sqg);
+            k_prd_gather<<<grid, THREADS, 0, st>>>(a);
+            P.end();
+            P.begin(sqa);
+            k_prd_apply<<<grid, THREADS, 0, st>>>(a, h, use_cond);
+            P.end();
+        }
         MG_CUDA(cudaGetLastError());
         return MG_OK;
     };
@@ -690,7 +907,7 @@ static mg_status pr_loop(mg_graph *g, PArgs &a, const mg_opts &opt, const char *
     if (a.hsum) MG_TRY(hub_check(g));
     if (info) {
         info->iterations = hc.iter;
-        info->pull_iterations = hc.iter;
+        info->pull_iterations = V == V_D ? hc.dense_iters : hc.iter;   // sweeps over every row
         info->residual = hc.resid;
         info->edges_scanned = (int64_t)hc.iter * g->ne;
     }
@@ -711,7 +928,10 @@ static mg_status pr_setup(mg_graph *g, PArgs &a, bool weighted_or_adj)
     MG_TRY(dev_alloc(w->c1, n * 4));
     MG_TRY(dev_alloc(w->active, n * 4));
     MG_TRY(dev_alloc(w->hpart, (size_t)std::max(g->nhchunks, 1) * 4));
-    MG_TRY(dev_alloc(w->bpart, (size_t)grid * 2 * 3 * 8));  // sweep blocks + apply blocks
+    MG_TRY(dev_alloc(w->bpart, (size_t)grid * 2 * NPART * 8));  // sweep blocks + apply blocks
+    MG_TRY(dev_alloc(w->q0, n * 4));
+    MG_TRY(dev_alloc(w->q1, n * 4));
+    MG_TRY(dev_alloc(w->qval, n * 4));
     MG_TRY(dev_alloc(w->ctl, sizeof(PCtl)));
     std::memset(&a, 0, sizeof(a));
     a.n = g->nv;
@@ -730,6 +950,12 @@ static mg_status pr_setup(mg_graph *g, PArgs &a, bool weighted_or_adj)
     a.bpart = w->bpart.as<double>();
     a.nblocks = grid;
     a.ctl = w->ctl.as<PCtl>();
+    a.frow = g->trow;
+    a.fcol = g->tcol;
+    a.queue[0] = w->q0.as<int32_t>();
+    a.queue[1] = w->q1.as<int32_t>();
+    a.qval = w->qval.as<float>();
+    a.m = g->ne;
     if (!weighted_or_adj) {
         MG_TRY(hub_prepare(g));
         if (g->hub.use) {
