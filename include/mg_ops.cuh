@@ -9,15 +9,33 @@
 // but at template-instantiation time instead of by macro.  The hooks see
 // vertex values only, never the layout.
 //
-// The signatures are reduced to what each hook uses:
-//   initialize(v)                       value of an untouched vertex
-//   get_partial_result(src_val, w)      value a source offers along an edge
+// Hooks (int32 labels; the reference's V1T):
+//   initialize()                        label of an untouched vertex
+//   source_value()                      label of a traversal source
+//   get_partial_result(src, w)          offer a source makes along an edge
+//                                       (w: the edge's integer weight)
 //   accumulate(loc, data, iter)         fold an offer into *loc (atomic form)
 //   accumulate_nonAtomics(acc, data, iter)  same, into a private accumulator
 //   update_condition(old, acc, iter)    does a folded value improve the vertex?
-//   fused_update_condition(loc, data, iter)  fold + test in one step on the
-//                                       destination (push form); true =
-//                                       enqueue the destination
+//   fused_update_condition(loc, data, iter)  fold + test in one atomic step on
+//                                       the destination (push form); true =
+//                                       the destination improved (enqueue it)
+//
+// The frontier engine (mg_frontier_engine.cuh) reads these capability flags
+// of an operator:
+//   kLevelSync     labels are BFS levels: a vertex is final when first
+//                  reached (visited bitmap, archived level lists); otherwise
+//                  labels are relaxed until no offer improves them
+//   kFirstParent   level-synchronous pull stops at the first frontier
+//                  in-neighbour (BFS)
+//   kWeighted      offers read the edge weight
+//   kPathCounts    Brandes path counts travel with the levels (BC forward)
+//   kMinPlusBound  min-plus with non-negative weights: a pull level skips
+//                  rows at or below (least frontier label + least weight)
+// and kTag, the prefix of its profiler slot names.
+// A relaxed (non level-synchronous) operator must be monotone: an offer of
+// an unreached vertex (initialize()) or of a vertex relaxed earlier never
+// spoils a label, so dense pull levels may fold every in-neighbour's offer.
 #pragma once
 
 #include <cstdint>
@@ -28,7 +46,11 @@ constexpr int32_t UNSET = 0x64646464;
 
 // BFS levels: user_function.h:217-218, 241-242, 270-274, 338-345, 392-399
 struct Bfs {
+    static constexpr const char *kTag = "bfs";  // profiler slot prefix
+    static constexpr bool kLevelSync = true, kFirstParent = true, kWeighted = false, kPathCounts = false,
+                          kMinPlusBound = false;
     __device__ static __forceinline__ int32_t initialize() { return UNSET; }
+    __device__ static __forceinline__ int32_t source_value() { return 0; }
     __device__ static __forceinline__ int32_t get_partial_result(int32_t src_level, int32_t) { return src_level + 1; }
     __device__ static __forceinline__ void accumulate_nonAtomics(int32_t &acc, int32_t data, int32_t iter)
     {
@@ -45,7 +67,11 @@ struct Bfs {
 
 // SSSP distances: user_function.h:220-221, 244-246, 276-278, 305-309, 346-360, 400-408
 struct Sssp {
+    static constexpr const char *kTag = "sssp";  // profiler slot prefix
+    static constexpr bool kLevelSync = false, kFirstParent = false, kWeighted = true, kPathCounts = false,
+                          kMinPlusBound = true;
     __device__ static __forceinline__ int32_t initialize() { return UNSET; }
+    __device__ static __forceinline__ int32_t source_value() { return 0; }
     __device__ static __forceinline__ int32_t get_partial_result(int32_t src_dist, int32_t w) { return src_dist + w; }
     __device__ static __forceinline__ void accumulate(int32_t *loc, int32_t data, int32_t) { atomicMin(loc, data); }
     __device__ static __forceinline__ void accumulate_nonAtomics(int32_t &acc, int32_t data, int32_t)
@@ -53,20 +79,13 @@ struct Sssp {
         if (data < acc) acc = data;
     }
     __device__ static __forceinline__ bool update_condition(int32_t old, int32_t acc, int32_t) { return acc < old; }
-    // atomicMin on the distance, then the destination's bit in the next
-    // frontier bitmap so it is enqueued once per iteration (the reference
-    // stamps vfc with atomicMax for the same purpose)
-    __device__ static __forceinline__ bool fused_update_condition(int32_t *loc, int32_t data, uint32_t *next_bm,
-                                                                  int32_t v)
+    // atomicMin on the distance; true when it lowered it (the engine then
+    // sets the destination's bit in the next frontier bitmap, so it is
+    // enqueued once per iteration -- the reference stamps vfc with atomicMax
+    // for the same purpose)
+    __device__ static __forceinline__ bool fused_update_condition(int32_t *loc, int32_t data, int32_t)
     {
-        if (data < *loc) {
-            int32_t old = atomicMin(loc, data);
-            if (data < old) {
-                uint32_t bit = 1u << (v & 31);
-                return (atomicOr(&next_bm[v >> 5], bit) & bit) == 0;
-            }
-        }
-        return false;
+        return data < *loc && data < atomicMin(loc, data);
     }
 };
 
@@ -187,7 +206,11 @@ __device__ __forceinline__ void pc_atomic_add(PathCount *loc, PathCount x, bool 
 // BC forward (levels + path counts): user_function.h:223-226, 247-251, 279-287, 310-317, 362-373, 409-417
 // Path counts are PathCounts here (the reference uses int32).
 struct BcForward {
+    static constexpr const char *kTag = "bc";  // profiler slot prefix
+    static constexpr bool kLevelSync = true, kFirstParent = false, kWeighted = false, kPathCounts = true,
+                          kMinPlusBound = false;
     __device__ static __forceinline__ int32_t initialize() { return UNSET; }
+    __device__ static __forceinline__ int32_t source_value() { return 0; }
     __device__ static __forceinline__ int32_t get_partial_result(int32_t src_level, int32_t) { return src_level + 1; }
     __device__ static __forceinline__ void accumulate(PathCount *sigma_loc, PathCount sigma_src, bool ext, int32_t *ovf)
     {

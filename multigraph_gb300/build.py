@@ -40,8 +40,7 @@ def _nvcc() -> str:
 
 
 def _headers():
-    return [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".h", ".cuh"))] + [
-        os.path.join(INCLUDE, "mg.h")]
+    return [os.path.join(d, f) for d in (CSRC, INCLUDE) for f in os.listdir(d) if f.endswith((".h", ".cuh"))]
 
 
 def _stale(target: str, deps) -> bool:

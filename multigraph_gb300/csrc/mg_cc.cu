@@ -269,7 +269,7 @@ mg_status cc_run(mg_graph *g, mg_run_info *info, const std::vector<int32_t> *vof
     return MG_OK;
 }
 
-mg_status frontier_run_multi(mg_graph *g, int alg, const int32_t *srcs_host, int32_t nsrc, const mg_opts &opt,
+mg_status frontier_bfs_multi(mg_graph *g, const int32_t *srcs_host, int32_t nsrc, const mg_opts &opt,
                              mg_run_info *info);
 const void *frontier_label(mg_graph *g);
 
@@ -354,7 +354,7 @@ mg_status mg_batch_bfs(mg_batch *b, const int32_t *sources, const mg_opts *o, in
     mg_graph *g = b->dg;
     mg_opts opt;
     MG_TRY(begin_run(g, o, opt, info));
-    MG_TRY(frontier_run_multi(g, 0, srcs.data(), (int32_t)srcs.size(), opt, info));
+    MG_TRY(frontier_bfs_multi(g, srcs.data(), (int32_t)srcs.size(), opt, info));
     MG_TRY(to_caller(g, MG_RES_LEVEL, frontier_label(g), 4, 1, &g->res[MG_RES_LEVEL]));
     MG_TRY(end_run(g, opt, info));
     return copy_out(g, levels_out, g->res[MG_RES_LEVEL], (size_t)g->nv * 4);

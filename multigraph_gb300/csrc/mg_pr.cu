@@ -31,7 +31,6 @@ namespace {
 
 constexpr int THREADS = 256;
 
-enum { V_T_REF = MG_PR_TOPOLOGY_REF, V_D_REF = MG_PR_DATA_REF, V_T = MG_PR_TOPOLOGY, V_D = MG_PR_DATA, V_WEIGHTED = 4, V_ADJ = 5 };
 
 struct PCtl {
     int32_t more;
@@ -111,78 +110,174 @@ constexpr int NPART = 5;       // partials per block slot
 constexpr int SPARSE_ALPHA = 16;  // queue sweeps once active in-edges < m / SPARSE_ALPHA
 
 // ---------------------------------------------------------------------------
-// per-row update.  s = gathered sum.  Returns |change|; sets *any when the
-// row counts as changed / active; *dang = x_new when the row's out-degree is 0.
+// PageRank operators: the engine (k_pr_light / k_pr_apply / k_prd_*) is a
+// template over one of these.  Hooks:
+//   apply(a, c, v, s, any, dang)  row v's update from its gathered sum s:
+//                                 writes the next iterate and contribution,
+//                                 returns |change|, sets any when the row
+//                                 counts as changed / active, dang = the new
+//                                 value when the row is dangling
+//   init(a, v, x0)                start value and contribution of row v
+//   more(any, R, tol)             continue after a sweep with any / L1 change R
+// Flags: kDataDriven (inactive rows frozen and skipped; queue sweeps),
+// kWeights (gathers scaled by the staged per-edge weight; the others take
+// the shared-memory hub split), kAdjoint (the iterate lives in c; its mean
+// replaces the dangling mass); kSlot: the workspace's captured-loop slot.
 // ---------------------------------------------------------------------------
-template <int V>
-__device__ __forceinline__ float pr_apply(const PArgs &a, const PCtl &c, int32_t v, float s, int &any, float &dang)
-{
-    const int cur = c.cur, nxt = cur ^ 1;
-    float xo = a.x[cur][v];
-    float xn;
-    int32_t od = a.outrow[v + 1] - a.outrow[v];
-    if (V == V_T_REF) {
-        // processi.cu:631-638 / validate.cu:59-70
-        float f1 = mgops::PrRef::apply(s);
+// PR_T: the reference recurrence (processi.cu:631-638 / validate.cu:59-70)
+struct PrTopologyRef {
+    static constexpr bool kDataDriven = false, kWeights = false, kAdjoint = false;
+    static constexpr int kSlot = 0;
+    __device__ static __forceinline__ float apply(const PArgs &a, const PCtl &c, int32_t v, float s, int &any, float &)
+    {
+        const int cur = c.cur, nxt = cur ^ 1;
+        const float xo = a.x[cur][v];
+        const int32_t od = a.outrow[v + 1] - a.outrow[v];
+        const float f1 = mgops::PrRef::apply(s);
+        float xn = xo;
         if (fabsf(f1 - xo) > mgops::PrRef::TOL) { xn = f1; any = 1; }
-        else xn = xo;
         a.x[nxt][v] = xn;
         a.c[nxt][v] = mgops::PrRef::get_partial_result(xn, od);
-    } else if (V == V_D_REF) {
-        // processi.cu:640-655 / validate.cu:71-84 (values always move; the
-        // sticky mask only decides termination)
-        float f1 = mgops::PrRef::apply(s);
+        return fabsf(xn - xo);
+    }
+    __device__ static __forceinline__ int more(int any, double, float) { return any; }
+};
+
+// PR_D: the reference recurrence with the sticky per-vertex mask
+// (processi.cu:640-655 / validate.cu:71-84): values always move, the mask
+// only decides termination
+struct PrDataRef {
+    static constexpr bool kDataDriven = false, kWeights = false, kAdjoint = false;
+    static constexpr int kSlot = 1;
+    __device__ static __forceinline__ float apply(const PArgs &a, const PCtl &c, int32_t v, float s, int &any, float &)
+    {
+        const int cur = c.cur, nxt = cur ^ 1;
+        const float xo = a.x[cur][v];
+        const int32_t od = a.outrow[v + 1] - a.outrow[v];
+        const float f1 = mgops::PrRef::apply(s);
         if (a.active[v] == 1 && fabsf(f1 - xo) > mgops::PrRef::TOL * xo) any = 1;
         else a.active[v] = 0;
-        xn = f1;
+        a.x[nxt][v] = f1;
+        a.c[nxt][v] = mgops::PrRef::get_partial_result(f1, od);
+        return fabsf(f1 - xo);
+    }
+    __device__ static __forceinline__ int more(int any, double, float) { return any; }
+};
+
+// normalised topology-driven: (1-d)/n + d (sum + dangling/n) for every row
+struct PrTopology {
+    static constexpr bool kDataDriven = false, kWeights = false, kAdjoint = false;
+    static constexpr int kSlot = 2;
+    __device__ static __forceinline__ float apply(const PArgs &a, const PCtl &c, int32_t v, float s, int &,
+                                                  float &dang)
+    {
+        const int cur = c.cur, nxt = cur ^ 1;
+        const float xo = a.x[cur][v];
+        const int32_t od = a.outrow[v + 1] - a.outrow[v];
+        const float xn = c.base + c.damping * s;
         a.x[nxt][v] = xn;
-        a.c[nxt][v] = mgops::PrRef::get_partial_result(xn, od);
-    } else if (V == V_T || V == V_D) {
-        const float d = c.damping;
-        if (V == V_D && a.active[v] == 0) {
-            xn = xo;  // frozen
-        } else {
-            xn = c.base + d * s;
-            if (V == V_D) {
-                if (fabsf(xn - xo) <= c.tol_row) a.active[v] = 0;
-                else any = 1;
-            }
+        a.c[nxt][v] = od > 0 ? xn / (float)od : 0.0f;
+        if (od == 0) dang = xn;
+        return fabsf(xn - xo);
+    }
+    __device__ static __forceinline__ int more(int, double R, float tol) { return R > (double)tol; }
+};
+
+// normalised data-driven: a row freezes (for good) once its change is at
+// most tol / n; frozen rows keep their value and are skipped
+struct PrData {
+    static constexpr bool kDataDriven = true, kWeights = false, kAdjoint = false;
+    static constexpr int kSlot = 3;
+    __device__ static __forceinline__ float apply(const PArgs &a, const PCtl &c, int32_t v, float s, int &any,
+                                                  float &dang)
+    {
+        const int cur = c.cur, nxt = cur ^ 1;
+        const float xo = a.x[cur][v];
+        const int32_t od = a.outrow[v + 1] - a.outrow[v];
+        float xn = xo;   // frozen
+        if (a.active[v] != 0) {
+            xn = c.base + c.damping * s;
+            if (fabsf(xn - xo) <= c.tol_row) a.active[v] = 0;
+            else any = 1;
         }
         a.x[nxt][v] = xn;
         a.c[nxt][v] = od > 0 ? xn / (float)od : 0.0f;
         if (od == 0) dang = xn;
-    } else if (V == V_WEIGHTED) {
-        const float d = c.damping;
-        xn = c.base + d * s;
+        return fabsf(xn - xo);
+    }
+    __device__ static __forceinline__ int more(int any, double R, float tol) { return any && R > (double)tol; }
+};
+
+// weighted: P_uv = w_uv / S_u
+struct PrWeighted {
+    static constexpr bool kDataDriven = false, kWeights = true, kAdjoint = false;
+    static constexpr int kSlot = 4;
+    __device__ static __forceinline__ float apply(const PArgs &a, const PCtl &c, int32_t v, float s, int &,
+                                                  float &dang)
+    {
+        const int cur = c.cur, nxt = cur ^ 1;
+        const float xo = a.x[cur][v];
+        const float xn = c.base + c.damping * s;
         a.x[nxt][v] = xn;
-        float Su = a.S[v];
+        const float Su = a.S[v];
         a.c[nxt][v] = Su > 0.0f ? xn / Su : 0.0f;
         if (!(Su > 0.0f)) dang = xn;
-    } else {  // V_ADJ: lambda_new = g + d * (t + [S_u == 0] * mean(lambda))
-        const float d = c.damping;
-        float Su = a.S[v];
-        float t = Su > 0.0f ? s / Su : c.lam_meanf;
-        xn = a.gvec[v] + d * t;
-        xo = a.c[cur][v];
+        return fabsf(xn - xo);
+    }
+    __device__ static __forceinline__ int more(int, double R, float tol) { return R > (double)tol; }
+};
+
+// adjoint: lambda_new = g + d * (t + [S_u == 0] * mean(lambda))
+struct PrAdjoint {
+    static constexpr bool kDataDriven = false, kWeights = true, kAdjoint = true;
+    static constexpr int kSlot = 5;
+    __device__ static __forceinline__ float apply(const PArgs &a, const PCtl &c, int32_t v, float s, int &,
+                                                  float &dang)
+    {
+        const int cur = c.cur, nxt = cur ^ 1;
+        const float Su = a.S[v];
+        const float t = Su > 0.0f ? s / Su : c.lam_meanf;
+        const float xn = a.gvec[v] + c.damping * t;
+        const float xo = a.c[cur][v];
         a.c[nxt][v] = xn;
         dang = xn;  // sum of lambda for the mean
+        return fabsf(xn - xo);
     }
-    return fabsf(xn - xo);
+    __device__ static __forceinline__ int more(int, double R, float tol) { return R > (double)tol; }
+};
+
+// start values: x = x0, contributions (lambda = g for the adjoint), masks
+template <class Op>
+__device__ __forceinline__ void pr_init_row(const PArgs &a, int32_t v, float x0)
+{
+    if constexpr (Op::kAdjoint) {
+        a.c[0][v] = a.gvec[v];
+        return;
+    }
+    a.x[0][v] = x0;
+    if constexpr (Op::kWeights) {
+        const float Su = a.S[v];
+        a.c[0][v] = Su > 0.0f ? x0 / Su : 0.0f;
+    } else {
+        const int32_t od = a.outrow[v + 1] - a.outrow[v];
+        a.c[0][v] = od > 0 ? x0 / (float)od : 0.0f;
+    }
+    if (a.active) a.active[v] = 1;
 }
 
 // gathered value for edge e from source u
-template <int V>
+template <class Op>
 __device__ __forceinline__ float pr_gather(const PArgs &a, int cur, int32_t e, int32_t u)
 {
     float cv = a.c[cur][u];
-    if (V == V_WEIGHTED || V == V_ADJ) cv *= a.pw[e];
+    if (Op::kWeights) cv *= a.pw[e];
     return cv;
 }
 
-template <int V>
+template <class Op>
 __device__ __forceinline__ bool pr_row_skipped(const PArgs &a, int32_t v)
 {
-    return V == V_D && a.active[v] == 0;
+    return Op::kDataDriven && a.active[v] == 0;
 }
 
 __device__ __forceinline__ void block_partials(const PArgs &a, int slot, double r, double dg, int any,
@@ -221,11 +316,11 @@ __device__ __forceinline__ void block_partials(const PArgs &a, int slot, double 
 }
 
 // row reduction for one PageRank sweep (bins_reduce interface)
-template <int V>
+template <class Op>
 struct PrRowOp {
     using T = float;
-    static constexpr bool kRowAware = (V == V_D);                      // inactive rows are skipped
-    static constexpr bool kWeights = (V == V_WEIGHTED || V == V_ADJ);  // staged float weight bits
+    static constexpr bool kRowAware = Op::kDataDriven;  // inactive rows are skipped
+    static constexpr bool kWeights = Op::kWeights;      // staged float weight bits
     const PArgs &a;
     const PCtl &c;
     float resid = 0.0f, dangs = 0.0f;  // per-thread partials (blocks sum in FP64)
@@ -233,7 +328,7 @@ struct PrRowOp {
     double act = 0.0;                  // data-driven: in-edges of rows still active
     int any = 0;
     __device__ float identity() const { return 0.0f; }
-    __device__ bool skip(int32_t v) const { return pr_row_skipped<V>(a, v); }
+    __device__ bool skip(int32_t v) const { return pr_row_skipped<Op>(a, v); }
     __device__ float edge(int32_t, int32_t, int32_t u, int32_t w) const
     {
         float cv = a.c[c.cur][u];
@@ -246,16 +341,16 @@ struct PrRowOp {
     {
         float dg = 0.0f;
         if (a.hsum) s += __ldcg(&a.hsum[v]);
-        resid += pr_apply<V>(a, c, v, s, any, dg);
+        resid += Op::apply(a, c, v, s, any, dg);
         dangs += dg;
-        if (V == V_D) {
+        if (Op::kDataDriven) {
             if (a.active[v]) act += (double)(a.frow[v + 1] - a.frow[v]);
             else dfz += dg;
         }
     }
 };
 
-template <int V>
+template <class Op>
 __global__ void __launch_bounds__(THREADS) k_pr_light(PArgs a)
 {
     const PCtl c = *a.ctl;
@@ -263,7 +358,7 @@ __global__ void __launch_bounds__(THREADS) k_pr_light(PArgs a)
     const int lane = mgd::lane();
     const int gwarp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int nwarps = (gridDim.x * blockDim.x) >> 5;
-    PrRowOp<V> op{a, c};
+    PrRowOp<Op> op{a, c};
     (void)lane;
     (void)gwarp;
     (void)nwarps;
@@ -284,7 +379,7 @@ __global__ void __launch_bounds__(THREADS) k_pr_light(PArgs a)
             e = min(te, b + a.chunk);
         }
         float acc = 0.0f;
-        if (!pr_row_skipped<V>(a, v)) {
+        if (!pr_row_skipped<Op>(a, v)) {
             for (int32_t b0 = b; b0 < e; b0 += 8 * THREADS) {
                 int32_t u[8];
 #pragma unroll
@@ -294,7 +389,7 @@ __global__ void __launch_bounds__(THREADS) k_pr_light(PArgs a)
                 }
 #pragma unroll
                 for (int j = 0; j < 8; j++)
-                    if (u[j] >= 0) acc += pr_gather<V>(a, c.cur, b0 + threadIdx.x + j * THREADS, u[j]);
+                    if (u[j] >= 0) acc += pr_gather<Op>(a, c.cur, b0 + threadIdx.x + j * THREADS, u[j]);
             }
         }
 #pragma unroll
@@ -365,7 +460,7 @@ __device__ __forceinline__ bool last_block(PCtl *cp)
 // partials in slot order and updates the loop state -- no block waits.
 // The data-driven form switches to queue sweeps here once the active
 // vertices' in-edges fall below m / SPARSE_ALPHA.
-template <int V>
+template <class Op>
 __global__ void __launch_bounds__(THREADS) k_pr_apply(PArgs a, cudaGraphConditionalHandle h, int use_cond)
 {
     PCtl *cp = a.ctl;
@@ -389,9 +484,9 @@ __global__ void __launch_bounds__(THREADS) k_pr_apply(PArgs a, cudaGraphConditio
         if (lane == 0) {
             float dg = 0.0f;
             if (a.hsum) s += __ldcg(&a.hsum[v]);
-            resid += pr_apply<V>(a, c, v, s, any, dg);
+            resid += Op::apply(a, c, v, s, any, dg);
             dangs += dg;
-            if (V == V_D) {
+            if (Op::kDataDriven) {
                 if (a.active[v]) act += (double)(a.frow[v + 1] - a.frow[v]);
                 else dfz += dg;
             }
@@ -410,15 +505,13 @@ __global__ void __launch_bounds__(THREADS) k_pr_apply(PArgs a, cudaGraphConditio
         cp->cur = c.cur ^ 1;
         cp->resid = R;
         cp->any = A;
-        if (V == V_ADJ) cp->lam_mean = D / c.n;
+        if (Op::kAdjoint) cp->lam_mean = D / c.n;
         else cp->dangling = D;
         pctl_derive(cp);
-        if (V == V_T_REF || V == V_D_REF) more = A;
-        else if (V == V_D) more = (A && R > (double)c.tol) ? 1 : 0;
-        else more = R > (double)c.tol ? 1 : 0;
+        more = Op::more(A, R, c.tol) ? 1 : 0;
         if (more && cp->iter >= c.max_iter) { cp->status = 1; more = 0; }
         cp->more = more;
-        if (V == V_D) {
+        if (Op::kDataDriven) {
             cp->dense_iters = c.dense_iters + 1;
             cp->act_edges = (long long)T[2];
             cp->dang_frozen = T[3];
@@ -556,24 +649,11 @@ __global__ void __launch_bounds__(THREADS) k_prd_apply(PArgs a, cudaGraphConditi
 }
 
 // init: x = x0, contributions, masks
-template <int V>
+template <class Op>
 __global__ void k_pr_init(PArgs a, float x0)
 {
-    for (int32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < a.n; v += gridDim.x * blockDim.x) {
-        if (V == V_ADJ) {
-            a.c[0][v] = a.gvec[v];
-            continue;
-        }
-        a.x[0][v] = x0;
-        if (V == V_WEIGHTED) {
-            float Su = a.S[v];
-            a.c[0][v] = Su > 0.0f ? x0 / Su : 0.0f;
-        } else {
-            int32_t od = a.outrow[v + 1] - a.outrow[v];
-            a.c[0][v] = od > 0 ? x0 / (float)od : 0.0f;
-        }
-        if (a.active) a.active[v] = 1;
-    }
+    for (int32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < a.n; v += gridDim.x * blockDim.x)
+        pr_init_row<Op>(a, v, x0);
 }
 
 __global__ void k_pr_ctl_init(PCtl *c, int32_t n, int32_t max_iter, float damping, float tol, double dangling0,
@@ -858,7 +938,7 @@ void free_wpr_ws(mg_graph *g) { (void)g; }
 // counter (R-MAT 22: 27 us per apply at 8, 20 us at 4)
 constexpr int APPLY_PER_SM = 4;
 
-template <int V>
+template <class Op>
 static mg_status pr_loop(mg_graph *g, PArgs &a, const mg_opts &opt, const char *name, mg_run_info *info,
                          int *final_cur)
 {
@@ -870,17 +950,17 @@ static mg_status pr_loop(mg_graph *g, PArgs &a, const mg_opts &opt, const char *
     const int sh = P.slot(hn.c_str());
     const int apply_grid = std::max(1, std::min(std::min(grid, (a.nhrows + 7) / 8), g->num_sms * APPLY_PER_SM));
     const int shs = a.hsum ? P.slot("pr_hub") : -1, shf = a.hsum ? P.slot("pr_hub_fix") : -1;
-    const int sqc = V == V_D ? P.slot("prd_compact") : -1, sqg = V == V_D ? P.slot("prd_gather") : -1,
-              sqa = V == V_D ? P.slot("prd_apply") : -1;
+    const int sqc = Op::kDataDriven ? P.slot("prd_compact") : -1, sqg = Op::kDataDriven ? P.slot("prd_gather") : -1,
+              sqa = Op::kDataDriven ? P.slot("prd_apply") : -1;
     BodyFn body = [&](cudaStream_t st, cudaGraphConditionalHandle h, int use_cond) -> mg_status {
         if (a.hsum) MG_TRY(hub_launch(g, a.c[0], a.c[1], &a.ctl->cur, &a.ctl->more, &a.ctl->sparse, st, shs, shf));
         P.begin(sl);
-        k_pr_light<V><<<grid, THREADS, 0, st>>>(a);
+        k_pr_light<Op><<<grid, THREADS, 0, st>>>(a);
         P.end();
         P.begin(sh);
-        k_pr_apply<V><<<apply_grid, THREADS, 0, st>>>(a, h, use_cond);
+        k_pr_apply<Op><<<apply_grid, THREADS, 0, st>>>(a, h, use_cond);
         P.end();
-        if (V == V_D) {
+        if (Op::kDataDriven) {
             // queue sweeps once the switch has happened (no-ops before)
             P.begin(sqc);
             k_prd_compact<<<grid, THREADS, 0, st>>>(a);
@@ -898,8 +978,8 @@ static mg_status pr_loop(mg_graph *g, PArgs &a, const mg_opts &opt, const char *
     int max_iter = opt.max_iter > 0 ? opt.max_iter : 10000;
     // the key holds every by-value argument of the captured kernels
     // (and the hub split's build, whose sizes the hub kernels take by value)
-    const LoopKey key = LoopKey().add(V).add(a).add(grid).add(apply_grid).add(a.hsum ? g->hub.gen : 0ull);
-    MG_TRY(run_loop(opt.profile ? MG_EXEC_HOST : opt.exec, opt.profile != 0, s, g->pws->lg[V], key, body,
+    const LoopKey key = LoopKey().add(Op::kSlot).add(a).add(grid).add(apply_grid).add(a.hsum ? g->hub.gen : 0ull);
+    MG_TRY(run_loop(opt.profile ? MG_EXEC_HOST : opt.exec, opt.profile != 0, s, g->pws->lg[Op::kSlot], key, body,
                     &a.ctl->more, g->pinned_flag, max_iter + 2));
     PCtl hc;
     MG_CUDA(cudaMemcpyAsync(&hc, a.ctl, sizeof(PCtl), cudaMemcpyDeviceToHost, s));
@@ -907,7 +987,7 @@ static mg_status pr_loop(mg_graph *g, PArgs &a, const mg_opts &opt, const char *
     if (a.hsum) MG_TRY(hub_check(g));
     if (info) {
         info->iterations = hc.iter;
-        info->pull_iterations = V == V_D ? hc.dense_iters : hc.iter;   // sweeps over every row
+        info->pull_iterations = Op::kDataDriven ? hc.dense_iters : hc.iter;   // sweeps over every row
         info->residual = hc.resid;
         info->edges_scanned = (int64_t)hc.iter * g->ne;
     }
@@ -1025,20 +1105,20 @@ mg_status mg_pagerank(mg_graph *g, int32_t variant, const mg_opts *o, float *ran
     int cur = 0;
     switch (variant) {
     case MG_PR_TOPOLOGY_REF:
-        k_pr_init<V_T_REF><<<grid, THREADS, 0, s>>>(a, x0);
-        MG_TRY(pr_loop<V_T_REF>(g, a, opt, "pr_pull", info, &cur));
+        k_pr_init<PrTopologyRef><<<grid, THREADS, 0, s>>>(a, x0);
+        MG_TRY(pr_loop<PrTopologyRef>(g, a, opt, "pr_pull", info, &cur));
         break;
     case MG_PR_DATA_REF:
-        k_pr_init<V_D_REF><<<grid, THREADS, 0, s>>>(a, x0);
-        MG_TRY(pr_loop<V_D_REF>(g, a, opt, "pr_pull", info, &cur));
+        k_pr_init<PrDataRef><<<grid, THREADS, 0, s>>>(a, x0);
+        MG_TRY(pr_loop<PrDataRef>(g, a, opt, "pr_pull", info, &cur));
         break;
     case MG_PR_TOPOLOGY:
-        k_pr_init<V_T><<<grid, THREADS, 0, s>>>(a, x0);
-        MG_TRY(pr_loop<V_T>(g, a, opt, "pr_pull", info, &cur));
+        k_pr_init<PrTopology><<<grid, THREADS, 0, s>>>(a, x0);
+        MG_TRY(pr_loop<PrTopology>(g, a, opt, "pr_pull", info, &cur));
         break;
     default:
-        k_pr_init<V_D><<<grid, THREADS, 0, s>>>(a, x0);
-        MG_TRY(pr_loop<V_D>(g, a, opt, "pr_pull", info, &cur));
+        k_pr_init<PrData><<<grid, THREADS, 0, s>>>(a, x0);
+        MG_TRY(pr_loop<PrData>(g, a, opt, "pr_pull", info, &cur));
         break;
     }
     MG_TRY(to_caller(g, MG_RES_RANK, a.x[cur], 4, 1, &g->res[MG_RES_RANK]));
@@ -1084,9 +1164,9 @@ mg_status mg_wpagerank(mg_graph *g, const mg_opts *o, float *x_out, mg_run_info 
     // rows without out-edges are dangling (their mass is spread uniformly)
     float x0 = g->nv > 0 ? 1.0f / g->nv : 0.0f;
     k_pr_ctl_init<<<1, 32, 0, s>>>(a.ctl, g->nv, max_iter, d, tol, g->nv ? (double)g->n_dangling / g->nv : 0.0, 0.0);
-    k_pr_init<V_WEIGHTED><<<grid, THREADS, 0, s>>>(a, x0);
+    k_pr_init<PrWeighted><<<grid, THREADS, 0, s>>>(a, x0);
     int cur = 0;
-    MG_TRY(pr_loop<V_WEIGHTED>(g, a, opt, "wpr_pull", info, &cur));
+    MG_TRY(pr_loop<PrWeighted>(g, a, opt, "wpr_pull", info, &cur));
     MG_CUDA(cudaMemcpyAsync(w->xkeep.p, a.x[cur], (size_t)g->nv * 4, cudaMemcpyDeviceToDevice, s));
     MG_TRY(to_caller(g, MG_RES_RANK, w->xkeep.p, 4, 1, &g->res[MG_RES_RANK]));
     MG_TRY(end_run(g, opt, info));
@@ -1134,9 +1214,9 @@ mg_status mg_wpagerank_backward(mg_graph *g, const float *g_host, const mg_opts 
     gm = g->nv ? gm / g->nv : 0.0;
     const float tol_abs = (float)(tol * std::max(g1, 1e-30));
     k_pr_ctl_init<<<1, 32, 0, s>>>(a.ctl, g->nv, max_iter, d, tol_abs, 0.0, gm);
-    k_pr_init<V_ADJ><<<grid, THREADS, 0, s>>>(a, 0.0f);
+    k_pr_init<PrAdjoint><<<grid, THREADS, 0, s>>>(a, 0.0f);
     int cur = 0;
-    MG_TRY(pr_loop<V_ADJ>(g, a, opt, "wpr_adjoint", info, &cur));
+    MG_TRY(pr_loop<PrAdjoint>(g, a, opt, "wpr_adjoint", info, &cur));
     float *lam = a.c[cur];
     MG_CUDA(cudaMemcpyAsync(w->lam_keep.p, lam, (size_t)g->nv * 4, cudaMemcpyDeviceToDevice, s));
     int sg = g->prof.slot("wpr_grad");
