@@ -324,21 +324,33 @@ __global__ void __launch_bounds__(HUB_THREADS, 1) k_hub_sweep(HubArgs a)
                 if (lane >= o) before += t;
             }
             before -= nst;
-            int32_t ridx = crow[j] + before - 1;   // row of the open segment (-1: none yet in this lane)
+            // per-lane segmented sums, branch-free: outv[i] is the total of
+            // the row that ends just before edge i (outf[i]: it started in
+            // this lane too); the row indices are loaded together afterwards
+            const int32_t rbase = crow[j] + before;   // hub-row index of this lane's first start
             float head = 0.0f, run = 0.0f;
             bool started = false;
+            float outv[8];
+            bool outf[8];
 #pragma unroll
             for (int i = 0; i < 8; i++) {
-                if ((fl >> i) & 1u) {
-                    if (!started) head = run;
-                    else a.hsum[__ldg(&a.hrows[ridx])] = run;   // a row that starts and ends in this lane
-                    started = true;
-                    run = 0.0f;
-                    ridx++;
-                }
+                const bool st = (fl >> i) & 1u;
+                outf[i] = st && started;
+                outv[i] = run;
+                head = (st && !started) ? run : head;
+                run = st ? 0.0f : run;
+                started = started || st;
                 run += v[i];
             }
             if (!started) head = run;
+            int32_t rrow[8];
+#pragma unroll
+            for (int i = 0; i < 8; i++)
+                if (outf[i]) rrow[i] = __ldg(&a.hrows[rbase + __popc(fl & ((1u << i) - 1u)) - 1]);
+#pragma unroll
+            for (int i = 0; i < 8; i++)
+                if (outf[i]) a.hsum[rrow[i]] = outv[i];
+            const int32_t ridx = rbase + nst - 1;   // the lane's last start (when started)
             // T = sum of heads from this lane up to and including the first
             // lane (>= this one) that has a row start
             float T = head;

@@ -39,7 +39,7 @@ def _check_all(g, og, src):
     # personalised PageRank keeps its own heavy-row table (rows above 256
     # in-edges in chunks): it must follow a re-layout
     seeds = [src, og.nv - 1]
-    pp, pinfo = g.ppr_batch(seeds, tol=1e-7)
+    pp, pinfo = g.ppr_batch(seeds, tol=1e-6)
     for i, s_ in enumerate(seeds):
         pref, _ = O.ppr_f64(og, s_, 0.85, 0.0, pinfo.iterations)
         assert float(np.max(np.abs(pp[i].astype(np.float64) - pref))) < 1e-6, s_
