@@ -97,26 +97,29 @@ mg_status run_loop(int exec_mode, bool profile, cudaStream_t stream, LoopGraph &
 
 }  // namespace mgi
 
-// shared-memory hub split of the pull rows for PageRank sweeps (mg_hub.cu):
-// in-edges from the first H vertices as 16-bit ids, gathered from shared
-// memory; the others as int32 ids with offsets toff
+// shared-memory segmented pull for PageRank sweeps (mg_hub.cu): in-edges
+// grouped by 224 KB source segments as 16-bit ids, gathered from shared
+// memory; partial sums per (row, segment) pair; ids past the last segment
+// stay in an int32 tail (offsets toff) gathered through L2
 namespace mgi {
 struct HubSplit {
     bool valid = false;      // built for the current pull columns
-    bool use = false;        // the split is in use (enough hub edges)
+    bool use = false;        // the split is in use (enough covered edges)
     uint64_t gen = 0;        // build number (process-wide): captured sweeps key on it
-    int32_t H = 0, nrows = 0, nchunks = 0;
-    int32_t nlong = 0;       // chunks whose last row spans many chunks
-    int64_t mh = 0;          // hub edges
-    DevBuf hoff, toff;       // int32 [n+1]: hub / tail row offsets
-    DevBuf hrows;            // int32 [nrows]: rows with hub edges, ascending
-    DevBuf hcol, tcol;       // uint16 hub stream (whole chunks), int32 tail stream
-    DevBuf rstart;           // uint32 bits: first hub edge of each row
-    DevBuf crow;             // int32 [nchunks+1]: hub-row index of each chunk's first start
+    int32_t H = 0, nseg = 0, nchunks = 0;
+    int32_t nlong = 0;       // chunks whose last pair spans many chunks
+    int64_t npairs = 0, covered = 0;  // (row, segment) pairs; edges in the segments
+    DevBuf hcol;             // uint16 segment streams (whole chunks), segment-major
+    DevBuf rstart;           // uint32 bits: first edge of each pair
+    DevBuf crow;             // int32 [nchunks+1]: pair index of each chunk's first start
+    DevBuf slot;             // int32 [npairs]: each pair's place in P
+    DevBuf segchunk;         // int32 [nseg+1]: first chunk of each segment
+    DevBuf pair_off;         // int32 [n+1]: row v's pairs in P
+    DevBuf P;                // float [npairs]: pair sums of the current sweep
+    DevBuf toff, tcol;       // tail rows: offsets [n+1], int32 ids
     DevBuf chead, ctail, cstart;  // per-chunk carries of the sweep
-    DevBuf cnext, clong;     // per chunk: next chunk with a row start; long-span chunks
-    DevBuf hsum;             // float [n]: hub sums of the current sweep
-    DevBuf tmp0, tmp1, tiles, err;
+    DevBuf cnext, clong;     // per chunk: next chunk with a start; long-span chunks
+    DevBuf err;
 };
 }  // namespace mgi
 
@@ -185,7 +188,7 @@ struct mg_graph {
     bool pos_valid = false;                // pos_row follows the current row offsets
     std::vector<int32_t> h_old2new;        // host copy for mapping sources
     mgi::DevBuf res_out[8];                // results in the caller's ids
-    // PageRank's shared-memory hub split (rebuilt when the columns change)
+    // PageRank's shared-memory segmented pull (rebuilt when the columns change)
     mgi::HubSplit hub;
     // per-algorithm workspaces
     FrontierWS *fws = nullptr;
@@ -231,8 +234,8 @@ mg_status rebin(mg_graph *g, int32_t heavy, int32_t chunk, int32_t tbin);
 // float scores in engine order stay in the graph's BC workspace
 mg_status bc_batched(mg_graph *g, const int32_t *src_engine, int32_t nsrc, const mg_opts &opt, mg_run_info *info,
                      const float **bc_dev);
-// PageRank hub split: build for the current pull columns (when stale),
-// enqueue one sweep's hub sums (contributions c0 / c1 picked by *cur; no-op
+// PageRank segmented pull: build for the current pull columns (when stale),
+// enqueue one sweep's pair sums (contributions c0 / c1 picked by *cur; no-op
 // once *more is 0 or *off is not), report a bulk-copy wait that ran out, free
 mg_status hub_prepare(mg_graph *g);
 mg_status hub_launch(mg_graph *g, const float *c0, const float *c1, const int32_t *cur, const int32_t *more,

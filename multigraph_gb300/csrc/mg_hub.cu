@@ -1,218 +1,74 @@
-// mg_hub.cu -- shared-memory hub split of the pull rows for PageRank sweeps.
+// mg_hub.cu -- shared-memory segmented pull for PageRank sweeps.
 //
 // The reference turns the random gathers of its dense PageRank phases into
 // partition-local work: edges are regrouped into 16-bit tile streams by
 // source partition (gen_structure.cu:1534-1947, sp1/sp2/mapper) and each
 // partition's values are summed in shared memory (processi.cu:682-894,
-// _phase1/_phase2).  Re-derived for GB300 and the hub-first vertex order:
-// with hubs at the lowest ids, the first HUB_MAX vertices (the most a CTA's
-// 227 KB of shared memory holds as FP32) are the sources of most edges
-// (R-MAT 22: 59.6 % of 128 M), so each pull row is split once per layout
-// into
-//   hub part  : in-edges from ids < H, as 16-bit ids in one stream
-//               (hub_col16, row offsets hub_off), gathered from a shared-
-//               memory copy of the contributions c[0, H) that every CTA
-//               stages with one bulk copy (cp.async.bulk) per sweep;
-//   tail part : the other in-edges, int32 ids (hub_tcol, offsets
-//               hub_toff), gathered through L2 by the degree-binned sweep.
-// The hub stream is cut into 256-edge chunks, a warp each: every lane takes
-// 8 consecutive edges with one 128-bit load, a bitmap marks the first hub
-// edge of every row, and a segmented sum (per lane, then a shuffle tree
-// across lanes) gives every row that ends inside the chunk its total; a row
-// that runs past the chunk is finished by k_hub_fix, which adds the chunk
-// heads that follow in order.  Sums are formed in a fixed order, so sweeps
-// are reproducible.  Rows with no hub edge keep hub_sum = 0.
+// _phase1/_phase2).  Re-derived for GB300: the source ids are cut into
+// segments of H = SEG_H vertices (the most a CTA's 227 KB of shared memory
+// holds as FP32 contributions, 224 KB), and each pull row's in-edges are
+// grouped by segment once per layout:
+//   segment streams : for segment s, the rows that have in-edges from it
+//                     (ascending), each row's edges from s as 16-bit local
+//                     ids (id - s*H), padded to whole 256-edge chunks; a
+//                     bitmap marks the first edge of every (row, segment)
+//                     pair; slot[] gives each pair its place in P;
+//   P, pair_off     : the pairs' partial sums in row-major order (row v's
+//                     pairs at P[pair_off[v] .. pair_off[v+1]), segments
+//                     ascending), summed by the row's finish;
+//   tail            : in-edges from ids beyond the last segment (graphs
+//                     with more than SEG_MAX segments' worth of vertices),
+//                     int32 ids gathered through L2 by the degree-binned
+//                     sweep.
+// One sweep: k_hub_sweep streams the chunks -- each CTA a contiguous,
+// edge-balanced range, staging the contributions c[s*H, (s+1)*H) of every
+// segment its range enters with bulk copies (cp.async.bulk on an mbarrier),
+// each warp a chunk at a time: every lane takes 8 consecutive edges with one
+// 128-bit load and gathers from shared memory, a segmented sum (per lane,
+// then a shuffle tree across lanes) gives every pair that ends inside the
+// chunk its total; k_hub_fix finishes the pairs that run past their chunk
+// (FP64, fixed order).  Sums are formed in a fixed order, so sweeps are
+// reproducible.
 //
-// Per sweep the hub part moves 2 B per hub edge (plus 1 bit of row starts)
-// instead of 4 B of ids and a 32-byte L2 sector per gather.
+// Per sweep the streams move 2 B per edge plus 1 bit per edge and 4 B per
+// pair, instead of 4 B of ids and a 32-byte L2 sector per gather.
 
 #include "mg_device.cuh"
 
 #include <algorithm>
 #include <atomic>
 #include <cstring>
+#include <functional>
+#include <thread>
 
 namespace {
 
-constexpr int32_t HUB_MAX = 57344;  // hub vertices staged per CTA: 224 KB of FP32 contributions
+constexpr int32_t SEG_H = 57344;    // vertices per segment: 224 KB of FP32 contributions
+constexpr int32_t SEG_MAX = 64;     // segments at most; ids beyond stay in the L2 tail
 constexpr int HUB_CHUNK = 256;      // edges per warp chunk: 8 per lane
 constexpr int HUB_THREADS = 1024;   // one CTA per SM (shared memory bound)
 constexpr int HUB_ILP = 2;          // chunks in flight per warp
-constexpr int SCAN_T = 1024, SCAN_IPT = 4, SCAN_TILE = SCAN_T * SCAN_IPT;
-constexpr long long HUB_WAIT_LIMIT = 20000000ll;  // clock64 cycles (~10 ms) for the bulk copy
+constexpr long long HUB_WAIT_LIMIT = 20000000ll;  // clock64 cycles (~10 ms) for a bulk copy
 constexpr int32_t FIX_SHORT = 8;    // carry spans up to this many chunks: a thread each
 
-// ---------------------------------------------------------------------------
-// exclusive scan of int32 (out[n] = total): tiles of 4096, tile totals
-// scanned by one block, offsets added back
-// ---------------------------------------------------------------------------
-__device__ __forceinline__ int32_t block_excl_scan(int32_t v, int32_t *s_warp, int32_t *total)
-{
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    int32_t x = v;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        int32_t t = __shfl_up_sync(0xffffffffu, x, o);
-        if (lane >= o) x += t;
-    }
-    if (lane == 31) s_warp[w] = x;
-    __syncthreads();
-    if (w == 0) {
-        int32_t y = lane < (int)(blockDim.x >> 5) ? s_warp[lane] : 0;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            int32_t t = __shfl_up_sync(0xffffffffu, y, o);
-            if (lane >= o) y += t;
-        }
-        s_warp[lane] = y;  // inclusive warp totals
-    }
-    __syncthreads();
-    const int32_t before = w ? s_warp[w - 1] : 0;
-    *total = s_warp[(blockDim.x >> 5) - 1];
-    __syncthreads();
-    return before + x - v;
-}
-
-__global__ void __launch_bounds__(SCAN_T) k_scan_tiles(const int32_t *in, int32_t n, int32_t *out, int32_t *tile_sum)
-{
-    __shared__ int32_t s_warp[32];
-    const int64_t base = (int64_t)blockIdx.x * SCAN_TILE + (int64_t)threadIdx.x * SCAN_IPT;
-    int32_t v[SCAN_IPT], s = 0;
-#pragma unroll
-    for (int i = 0; i < SCAN_IPT; i++) {
-        v[i] = base + i < n ? in[base + i] : 0;
-        s += v[i];
-    }
-    int32_t tot;
-    int32_t e = block_excl_scan(s, s_warp, &tot);
-#pragma unroll
-    for (int i = 0; i < SCAN_IPT; i++) {
-        if (base + i < n) out[base + i] = e;
-        e += v[i];
-    }
-    if (threadIdx.x == 0) tile_sum[blockIdx.x] = tot;
-}
-
-// one block: exclusive scan of the tile totals in place; total -> *grand
-__global__ void __launch_bounds__(SCAN_T) k_scan_part(int32_t *tile_sum, int32_t ntiles, int32_t *grand)
-{
-    __shared__ int32_t s_warp[32];
-    int32_t carry = 0;
-    for (int32_t b0 = 0; b0 < ntiles; b0 += SCAN_T) {
-        const int32_t i = b0 + threadIdx.x;
-        const int32_t v = i < ntiles ? tile_sum[i] : 0;
-        int32_t tot;
-        const int32_t e = block_excl_scan(v, s_warp, &tot);
-        if (i < ntiles) tile_sum[i] = carry + e;
-        carry += tot;
-    }
-    if (threadIdx.x == 0) *grand = carry;
-}
-
-__global__ void k_scan_add(int32_t *out, int32_t n, const int32_t *tile_sum)
-{
-    const int64_t base = (int64_t)blockIdx.x * SCAN_TILE;
-    const int32_t add = tile_sum[blockIdx.x];
-    for (int i = threadIdx.x; i < SCAN_TILE; i += blockDim.x)
-        if (base + i < n) out[base + i] += add;
-}
-
-// ---------------------------------------------------------------------------
-// layout build
-// ---------------------------------------------------------------------------
-// hub edges per row (warp per row) and the has-hub-edges flag
-__global__ void k_hub_count(int32_t n, const int32_t *prow, const int32_t *pcol, int32_t H, int32_t *hcnt,
-                            int32_t *hflag)
-{
-    const int lane = threadIdx.x & 31;
-    const int32_t gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int32_t nw = (gridDim.x * blockDim.x) >> 5;
-    for (int32_t v = gw; v < n; v += nw) {
-        const int32_t b = prow[v], e = prow[v + 1];
-        int32_t c = 0;
-        for (int32_t p = b + lane; p < e; p += 32) c += __ldg(&pcol[p]) < H;
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
-        if (lane == 0) {
-            hcnt[v] = c;
-            hflag[v] = c > 0;
-        }
-    }
-}
-
-// stable split of every row (warp per row, ballot-ordered writes), tail
-// offsets, the hub-row list and the row-start bits of the hub stream
-__global__ void k_hub_scatter(int32_t n, const int32_t *prow, const int32_t *pcol, int32_t H, const int32_t *hoff,
-                              const int32_t *hidx, uint16_t *hcol, int32_t *tcol, int32_t *toff, int32_t *hrows,
-                              uint32_t *rstart)
-{
-    const int lane = threadIdx.x & 31;
-    const unsigned lt = (1u << lane) - 1u;
-    const int32_t gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int32_t nw = (gridDim.x * blockDim.x) >> 5;
-    for (int32_t v = gw; v < n; v += nw) {
-        const int32_t b = prow[v], e = prow[v + 1];
-        const int32_t hb = hoff[v], tb = b - hb;
-        int32_t nh = 0, nt = 0;
-        for (int32_t p0 = b; p0 < e; p0 += 32) {
-            const int32_t p = p0 + lane;
-            const int32_t c = p < e ? __ldg(&pcol[p]) : -1;
-            const bool hub = p < e && c < H, tl = p < e && c >= H;
-            const unsigned mh = __ballot_sync(0xffffffffu, hub), mt = __ballot_sync(0xffffffffu, tl);
-            if (hub) hcol[hb + nh + __popc(mh & lt)] = (uint16_t)c;
-            if (tl) tcol[tb + nt + __popc(mt & lt)] = c;
-            nh += __popc(mh);
-            nt += __popc(mt);
-        }
-        if (lane == 0) {
-            toff[v] = tb;
-            if (v == n - 1) toff[n] = prow[n] - hoff[n];
-            if (nh > 0) {
-                hrows[hidx[v]] = v;
-                atomicOr(&rstart[hb >> 5], 1u << (hb & 31));
-            }
-        }
-    }
-}
-
-// padding of the hub stream up to whole chunks: id H (a zero in shared memory)
-__global__ void k_hub_pad(uint16_t *hcol, int64_t from, int64_t to, int32_t H)
-{
-    for (int64_t i = from + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < to; i += (int64_t)gridDim.x * blockDim.x)
-        hcol[i] = (uint16_t)H;
-}
-
-// row starts per chunk (8 bitmap words each)
-__global__ void k_chunk_starts(const uint32_t *rstart, int32_t nchunks, int32_t *cnt)
-{
-    for (int32_t c = blockIdx.x * blockDim.x + threadIdx.x; c < nchunks; c += gridDim.x * blockDim.x) {
-        int32_t s = 0;
-#pragma unroll
-        for (int k = 0; k < 8; k++) s += __popc(rstart[8 * c + k]);
-        cnt[c] = s;
-    }
-}
-
-// ---------------------------------------------------------------------------
-// sweep
-// ---------------------------------------------------------------------------
 struct HubArgs {
-    const uint16_t *hcol;     // hub stream (padded to whole chunks)
-    const uint32_t *rstart;   // row-start bits of the hub stream
-    const int32_t *crow;      // hub-row index of each chunk's first row start
-    const int32_t *hrows;     // rows that have hub edges, ascending
+    const uint16_t *hcol;     // segment streams (each padded to whole chunks), segment-major
+    const uint32_t *rstart;   // bits: first edge of each (row, segment) pair
+    const int32_t *crow;      // [nchunks+1] pair index (segment-major) of each chunk's first start
+    const int32_t *slot;      // per pair (segment-major): its place in P
+    const int32_t *segchunk;  // [nseg+1] first chunk of each segment
     const float *c[2];        // contributions (ping-pong, ctl selects)
     const int32_t *cur;       // current iterate index (loop control block)
     const int32_t *more;      // loop continue flag
     const int32_t *off;       // non-zero: sweeps run elsewhere (queue sweeps)
-    float *hsum;              // per-row hub sums
-    float *chead, *ctail;     // per chunk: sum before its first row start / of its open last row
-    int32_t *cstart;          // per chunk: has a row start
+    float *P;                 // pair partial sums, row-major
+    float *chead, *ctail;     // per chunk: sum before its first start / of its open last pair
+    int32_t *cstart;          // per chunk: has a start
     const int32_t *cnext;     // per chunk with a start: the next chunk with one (nchunks: none)
-    const int32_t *clong;     // chunks whose last row spans more than FIX_SHORT chunks
+    const int32_t *clong;     // chunks whose last pair spans more than FIX_SHORT chunks
     int32_t nlong;
-    int32_t *err;             // bulk copy wait ran out
-    int32_t H, nchunks;
+    int32_t *err;             // a bulk copy wait ran out
+    int32_t n, H, nseg, nchunks;
 };
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p)
@@ -220,16 +76,29 @@ __device__ __forceinline__ uint32_t smem_u32(const void *p)
     return (uint32_t)__cvta_generic_to_shared(p);
 }
 
-// Stage c[0, H) into shared memory with bulk copies on an mbarrier; the
-// wait is bounded (HUB_WAIT_LIMIT cycles), after which *err is set and the
-// CTA returns false (it still waits, bounded, for its copies to land).
-__device__ __forceinline__ bool stage_hub(float *s_c, const float *c, int32_t H, uint64_t *mbar, int32_t *err)
+__device__ __forceinline__ bool mbar_try(uint32_t bar, uint32_t parity)
 {
-    const uint32_t bar = smem_u32(mbar);
-    const uint32_t bytes = (uint32_t)H * 4u;
+    uint32_t done;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(done)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    return done != 0;
+}
+
+// Stage `bytes` (a multiple of 16) from src into s_c with bulk copies
+// completing on the mbarrier (phase `parity`).  Thread 0 waits, bounded by
+// HUB_WAIT_LIMIT cycles; on timeout it sets *err, waits again (bounded)
+// for the copies to land, and the CTA returns false.
+__device__ __forceinline__ bool stage_segment(float *s_c, const float *src, uint32_t bytes, uint32_t bar,
+                                              uint32_t parity, int32_t *err)
+{
+    __shared__ int s_ok;
+    __syncthreads();   // every warp is done with the previous segment
     if (threadIdx.x == 0) {
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar));
-        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
         constexpr uint32_t PIECE = 32768;
@@ -238,43 +107,21 @@ __device__ __forceinline__ bool stage_hub(float *s_c, const float *c, int32_t H,
             asm volatile(
                 "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
                     smem_u32(reinterpret_cast<char *>(s_c) + off)),
-                "l"(reinterpret_cast<const char *>(c) + off), "r"(sz), "r"(bar)
+                "l"(reinterpret_cast<const char *>(src) + off), "r"(sz), "r"(bar)
                 : "memory");
         }
-    }
-    if (threadIdx.x < 4) s_c[H + threadIdx.x] = 0.0f;  // the padding id's slot
-    __syncthreads();
-    __shared__ int s_ok;
-    if (threadIdx.x == 0) {
-        uint32_t done = 0;
-        const long long t0 = clock64();
         bool ok = true;
-        while (!done) {
-            asm volatile(
-                "{\n\t.reg .pred p;\n\t"
-                "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0;\n\t"
-                "selp.u32 %0, 1, 0, p;\n\t}"
-                : "=r"(done)
-                : "r"(bar)
-                : "memory");
-            if (!done && clock64() - t0 > HUB_WAIT_LIMIT) {
+        const long long t0 = clock64();
+        while (!mbar_try(bar, parity)) {
+            if (clock64() - t0 > HUB_WAIT_LIMIT) {
                 ok = false;
                 break;
             }
         }
         if (!ok) {
             atomicExch(err, 1);
-            // the copies may still land: wait for them (bounded again)
-            // before the CTA's shared memory is released
             const long long t1 = clock64();
-            while (!done && clock64() - t1 < HUB_WAIT_LIMIT) {
-                asm volatile(
-                    "{\n\t.reg .pred p;\n\t"
-                    "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0;\n\t"
-                    "selp.u32 %0, 1, 0, p;\n\t}"
-                    : "=r"(done)
-                    : "r"(bar)
-                    : "memory");
+            while (!mbar_try(bar, parity) && clock64() - t1 < HUB_WAIT_LIMIT) {
             }
         }
         s_ok = ok;
@@ -283,112 +130,139 @@ __device__ __forceinline__ bool stage_hub(float *s_c, const float *c, int32_t H,
     return s_ok != 0;
 }
 
+// one 256-edge chunk: 8 edges per lane, segmented sums, pair totals to P
+__device__ __forceinline__ void sweep_chunk(const HubArgs &a, const float *s_c, int32_t ch, uint4 cols,
+                                            uint32_t word, int32_t crow)
+{
+    const int lane = threadIdx.x & 31;
+    const uint32_t fl = (word >> ((lane & 3) * 8)) & 0xffu;
+    const uint32_t w32[4] = {cols.x, cols.y, cols.z, cols.w};
+    float v[8];
+#pragma unroll
+    for (int i = 0; i < 8; i++) v[i] = s_c[(w32[i >> 1] >> ((i & 1) * 16)) & 0xffffu];
+    // pair index of this lane's first start
+    const int nst = __popc(fl);
+    int32_t before = nst;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int32_t t = __shfl_up_sync(0xffffffffu, before, o);
+        if (lane >= o) before += t;
+    }
+    before -= nst;
+    // per-lane segmented sums, branch-free: outv[i] is the total of the pair
+    // that ends just before edge i (outf[i]: it started in this lane too);
+    // the slots are loaded together afterwards
+    const int32_t rbase = crow + before;
+    float head = 0.0f, run = 0.0f;
+    bool started = false;
+    float outv[8];
+    bool outf[8];
+#pragma unroll
+    for (int i = 0; i < 8; i++) {
+        const bool st = (fl >> i) & 1u;
+        outf[i] = st && started;
+        outv[i] = run;
+        head = (st && !started) ? run : head;
+        run = st ? 0.0f : run;
+        started = started || st;
+        run += v[i];
+    }
+    if (!started) head = run;
+    int32_t sl[8];
+#pragma unroll
+    for (int i = 0; i < 8; i++)
+        if (outf[i]) sl[i] = __ldg(&a.slot[rbase + __popc(fl & ((1u << i) - 1u)) - 1]);
+#pragma unroll
+    for (int i = 0; i < 8; i++)
+        if (outf[i]) a.P[sl[i]] = outv[i];
+    const int32_t ridx = rbase + nst - 1;   // the lane's last start (when started)
+    // T = sum of heads from this lane up to and including the first lane
+    // (>= this one) that has a start
+    float T = head;
+    int F = started;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const float T2 = __shfl_down_sync(0xffffffffu, T, o);
+        const int F2 = __shfl_down_sync(0xffffffffu, F, o);
+        if (lane + o < 32 && !F) {
+            T += T2;
+            F |= F2;
+        }
+    }
+    const float Tn = __shfl_down_sync(0xffffffffu, T, 1);
+    const int Fn = __shfl_down_sync(0xffffffffu, F, 1);
+    const unsigned any = __ballot_sync(0xffffffffu, started);
+    if (started) {
+        const bool closed = lane < 31 && Fn;
+        const float total = run + (lane < 31 ? Tn : 0.0f);
+        if (closed) a.P[__ldg(&a.slot[ridx])] = total;
+        else a.ctail[ch] = total;   // the chunk's last pair runs on
+    }
+    if (lane == 0) {
+        a.chead[ch] = T;
+        a.cstart[ch] = any != 0u;
+    }
+}
+
 __global__ void __launch_bounds__(HUB_THREADS, 1) k_hub_sweep(HubArgs a)
 {
     extern __shared__ __align__(128) float s_c[];   // [H + 4]
     __shared__ __align__(8) uint64_t mbar;
     if (__ldg(a.more) == 0 || __ldg(a.off) != 0) return;
     const float *c = __ldg(a.cur) ? a.c[1] : a.c[0];
-    if (!stage_hub(s_c, c, a.H, &mbar, a.err)) return;
-    const int lane = threadIdx.x & 31;
-    const int32_t gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int32_t nw = (gridDim.x * blockDim.x) >> 5;
-    for (int32_t c0 = gw * HUB_ILP; c0 < a.nchunks; c0 += nw * HUB_ILP) {
-        uint4 cols[HUB_ILP];
-        uint32_t word[HUB_ILP];
-        int32_t crow[HUB_ILP];
+    const uint32_t bar = smem_u32(&mbar);
+    if (threadIdx.x == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar));
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (threadIdx.x < 4) s_c[a.H + threadIdx.x] = 0.0f;   // the padding id's slot
+    // this CTA's edge-balanced chunk range, cut at segment boundaries
+    const int32_t c_lo = (int32_t)((int64_t)a.nchunks * blockIdx.x / gridDim.x);
+    const int32_t c_hi = (int32_t)((int64_t)a.nchunks * (blockIdx.x + 1) / gridDim.x);
+    const int32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    constexpr int32_t NW = HUB_THREADS / 32;
+    uint32_t phase = 0;
+    int32_t s = 0;
+    while (s < a.nseg && __ldg(&a.segchunk[s + 1]) <= c_lo) s++;
+    for (int32_t lo = c_lo; lo < c_hi && s < a.nseg; s++) {
+        const int32_t hi = min(c_hi, __ldg(&a.segchunk[s + 1]));
+        if (hi <= lo) continue;
+        const int32_t base = s * a.H;
+        const int32_t len = min(a.H, a.n - base);
+        if (!stage_segment(s_c, c + base, (uint32_t)((len + 3) & ~3) * 4u, bar, phase, a.err)) return;
+        phase ^= 1u;
+        for (int32_t c0 = lo + warp * HUB_ILP; c0 < hi; c0 += NW * HUB_ILP) {
+            uint4 cols[HUB_ILP];
+            uint32_t word[HUB_ILP];
+            int32_t crow[HUB_ILP];
 #pragma unroll
-        for (int j = 0; j < HUB_ILP; j++) {
-            const int32_t ch = c0 + j;
-            if (ch < a.nchunks) {
-                cols[j] = __ldcs(reinterpret_cast<const uint4 *>(a.hcol + (int64_t)ch * HUB_CHUNK) + lane);
-                word[j] = __ldcs(&a.rstart[(int64_t)ch * 8 + (lane >> 2)]);
-                crow[j] = __ldg(&a.crow[ch]);
-            }
-        }
-#pragma unroll
-        for (int j = 0; j < HUB_ILP; j++) {
-            const int32_t ch = c0 + j;
-            if (ch >= a.nchunks) break;   // warp-uniform
-            const uint32_t fl = (word[j] >> ((lane & 3) * 8)) & 0xffu;
-            const uint32_t w32[4] = {cols[j].x, cols[j].y, cols[j].z, cols[j].w};
-            float v[8];
-#pragma unroll
-            for (int i = 0; i < 8; i++) v[i] = s_c[(w32[i >> 1] >> ((i & 1) * 16)) & 0xffffu];
-            // hub-row index of this lane's first row start
-            const int nst = __popc(fl);
-            int32_t before = nst;
-#pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-                const int32_t t = __shfl_up_sync(0xffffffffu, before, o);
-                if (lane >= o) before += t;
-            }
-            before -= nst;
-            // per-lane segmented sums, branch-free: outv[i] is the total of
-            // the row that ends just before edge i (outf[i]: it started in
-            // this lane too); the row indices are loaded together afterwards
-            const int32_t rbase = crow[j] + before;   // hub-row index of this lane's first start
-            float head = 0.0f, run = 0.0f;
-            bool started = false;
-            float outv[8];
-            bool outf[8];
-#pragma unroll
-            for (int i = 0; i < 8; i++) {
-                const bool st = (fl >> i) & 1u;
-                outf[i] = st && started;
-                outv[i] = run;
-                head = (st && !started) ? run : head;
-                run = st ? 0.0f : run;
-                started = started || st;
-                run += v[i];
-            }
-            if (!started) head = run;
-            int32_t rrow[8];
-#pragma unroll
-            for (int i = 0; i < 8; i++)
-                if (outf[i]) rrow[i] = __ldg(&a.hrows[rbase + __popc(fl & ((1u << i) - 1u)) - 1]);
-#pragma unroll
-            for (int i = 0; i < 8; i++)
-                if (outf[i]) a.hsum[rrow[i]] = outv[i];
-            const int32_t ridx = rbase + nst - 1;   // the lane's last start (when started)
-            // T = sum of heads from this lane up to and including the first
-            // lane (>= this one) that has a row start
-            float T = head;
-            int F = started;
-#pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-                const float T2 = __shfl_down_sync(0xffffffffu, T, o);
-                const int F2 = __shfl_down_sync(0xffffffffu, F, o);
-                if (lane + o < 32 && !F) {
-                    T += T2;
-                    F |= F2;
+            for (int j = 0; j < HUB_ILP; j++) {
+                const int32_t ch = c0 + j;
+                if (ch < hi) {
+                    cols[j] = __ldcs(reinterpret_cast<const uint4 *>(a.hcol + (int64_t)ch * HUB_CHUNK) + lane);
+                    word[j] = __ldcs(&a.rstart[(int64_t)ch * 8 + (lane >> 2)]);
+                    crow[j] = __ldg(&a.crow[ch]);
                 }
             }
-            const float Tn = __shfl_down_sync(0xffffffffu, T, 1);
-            const int Fn = __shfl_down_sync(0xffffffffu, F, 1);
-            const unsigned any = __ballot_sync(0xffffffffu, started);
-            if (started) {
-                const bool closed = lane < 31 && Fn;
-                const float total = run + (lane < 31 ? Tn : 0.0f);
-                if (closed) a.hsum[__ldg(&a.hrows[ridx])] = total;
-                else a.ctail[ch] = total;   // the chunk's last row runs on
-            }
-            if (lane == 0) {
-                a.chead[ch] = T;
-                a.cstart[ch] = any != 0u;
+#pragma unroll
+            for (int j = 0; j < HUB_ILP; j++) {
+                const int32_t ch = c0 + j;
+                if (ch >= hi) break;   // warp-uniform
+                sweep_chunk(a, s_c, ch, cols[j], word[j], crow[j]);
             }
         }
+        lo = hi;
     }
 }
 
-// rows that run past their chunk: the open tail plus the heads of the
-// following chunks up to and including the next chunk with a row start
+// pairs that run past their chunk: the open tail plus the heads of the
+// following chunks up to and including the next chunk with a start
 // (cnext, fixed by the layout), summed in FP64 and rounded once: a hub row
 // can span hundreds of chunks, and an FP32 running sum of their heads would
 // carry rounding of a few 1e-6 that moves from sweep to sweep.  Spans of up
 // to FIX_SHORT chunks take a thread each; longer ones (clong) a warp each,
-// lane-strided then a fixed shuffle tree.  crow[ch + 1] - 1 is the hub-row
-// index of chunk ch's last row start.
+// lane-strided then a fixed shuffle tree.  crow[ch + 1] - 1 is the pair
+// index of chunk ch's last start.
 __global__ void k_hub_fix(HubArgs a)
 {
     if (__ldg(a.more) == 0 || __ldg(a.off) != 0) return;
@@ -399,7 +273,7 @@ __global__ void k_hub_fix(HubArgs a)
         if (last - ch > FIX_SHORT) continue;
         double total = a.ctail[ch];
         for (int32_t k = ch + 1; k <= last; k++) total += a.chead[k];
-        a.hsum[__ldg(&a.hrows[__ldg(&a.crow[ch + 1]) - 1])] = (float)total;
+        a.P[__ldg(&a.slot[__ldg(&a.crow[ch + 1]) - 1])] = (float)total;
     }
     const int lane = threadIdx.x & 31;
     for (int32_t i = tid >> 5; i < a.nlong; i += nth >> 5) {
@@ -409,20 +283,7 @@ __global__ void k_hub_fix(HubArgs a)
         for (int32_t k = ch + 1 + lane; k <= last; k += 32) t += a.chead[k];
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
-        if (lane == 0) a.hsum[__ldg(&a.hrows[__ldg(&a.crow[ch + 1]) - 1])] = (float)(t + (double)a.ctail[ch]);
-    }
-}
-
-// layout: for every chunk with a row start, the next chunk with one (its
-// last row ends there), and the list of chunks whose span is long
-__global__ void k_hub_spans(const int32_t *cnt, int32_t nchunks, int32_t *cnext, int32_t *clong, int32_t *nlong)
-{
-    for (int32_t ch = blockIdx.x * blockDim.x + threadIdx.x; ch < nchunks; ch += gridDim.x * blockDim.x) {
-        if (!cnt[ch]) continue;
-        int32_t k = ch + 1;
-        while (k < nchunks && cnt[k] == 0) k++;
-        cnext[ch] = k;
-        if (min(k, nchunks - 1) - ch > FIX_SHORT) clong[atomicAdd(nlong, 1)] = ch;
+        if (lane == 0) a.P[__ldg(&a.slot[__ldg(&a.crow[ch + 1]) - 1])] = (float)(t + (double)a.ctail[ch]);
     }
 }
 
@@ -430,105 +291,200 @@ __global__ void k_hub_spans(const int32_t *cnt, int32_t nchunks, int32_t *cnext,
 
 namespace mgi {
 
-// exclusive scan of in[0, n) into out[0, n], out[n] = total (on the stream)
-static mg_status scan_excl(const int32_t *in, int32_t n, int32_t *out, DevBuf &tiles, cudaStream_t s)
-{
-    const int32_t ntiles = std::max(1, (n + SCAN_TILE - 1) / SCAN_TILE);
-    MG_TRY(dev_alloc(tiles, (size_t)(ntiles + 1) * 4));
-    int32_t *t = tiles.as<int32_t>();
-    if (n > 0) k_scan_tiles<<<ntiles, SCAN_T, 0, s>>>(in, n, out, t);
-    else MG_CUDA(cudaMemsetAsync(t, 0, 4, s));
-    k_scan_part<<<1, SCAN_T, 0, s>>>(t, n > 0 ? ntiles : 1, out + n);
-    if (n > 0) k_scan_add<<<ntiles, 256, 0, s>>>(out, n, t);
-    MG_CUDA(cudaGetLastError());
-    return MG_OK;
-}
-
 void hub_free(mg_graph *g)
 {
     HubSplit &h = g->hub;
-    DevBuf *bufs[] = {&h.hoff, &h.toff, &h.hrows, &h.hcol, &h.tcol, &h.rstart, &h.crow, &h.chead,
-                      &h.ctail, &h.cstart, &h.cnext, &h.clong, &h.hsum, &h.tmp0, &h.tmp1, &h.tiles, &h.err};
+    DevBuf *bufs[] = {&h.hcol, &h.rstart, &h.crow, &h.slot, &h.segchunk, &h.pair_off, &h.P, &h.toff,
+                      &h.tcol, &h.chead, &h.ctail, &h.cstart, &h.cnext, &h.clong, &h.err};
     for (DevBuf *b : bufs) dev_free(*b);
     h = HubSplit();
 }
 
 static std::atomic<uint64_t> g_hub_builds{0};
 
+// Build the segmented layout from the pull CSR (copied back from the
+// device): row-parallel host passes over the edges (count, then write),
+// each thread a contiguous row range whose share of every segment's stream
+// is contiguous too, so the streams come out segment-major with rows
+// ascending.
 mg_status hub_prepare(mg_graph *g)
 {
     HubSplit &h = g->hub;
     if (h.valid) return MG_OK;
     h.gen = ++g_hub_builds;
+    h.use = false;
     cudaStream_t s = g->stream;
     const int32_t n = g->nv;
     const int64_t m = g->ne;
-    h.use = false;
-    h.H = std::min<int32_t>(HUB_MAX, n & ~3);
-    if (n == 0 || m == 0 || h.H < 4) {
+    if (n < 4 || m == 0) {
         h.valid = true;
         return MG_OK;
     }
-    const int32_t *prow = g->trow, *pcol = g->tcol;
-    MG_TRY(dev_alloc(h.tmp0, (size_t)(n + 1) * 4));   // hub edges per row, later starts per chunk
-    MG_TRY(dev_alloc(h.tmp1, (size_t)(n + 1) * 4));   // has-hub-edges flags
-    MG_TRY(dev_alloc(h.hoff, (size_t)(n + 1) * 4));
-    MG_TRY(dev_alloc(h.toff, (size_t)(n + 1) * 4));
-    const int grid = g->num_sms * 8;
-    k_hub_count<<<grid, 256, 0, s>>>(n, prow, pcol, h.H, h.tmp0.as<int32_t>(), h.tmp1.as<int32_t>());
-    MG_CUDA(cudaGetLastError());
-    MG_TRY(scan_excl(h.tmp0.as<int32_t>(), n, h.hoff.as<int32_t>(), h.tiles, s));
-    // hub-row indices go into toff for now (rewritten by the scatter)
-    MG_TRY(scan_excl(h.tmp1.as<int32_t>(), n, h.toff.as<int32_t>(), h.tiles, s));
-    int32_t tot[2] = {0, 0};
-    MG_CUDA(cudaMemcpyAsync(&tot[0], h.hoff.as<int32_t>() + n, 4, cudaMemcpyDeviceToHost, s));
-    MG_CUDA(cudaMemcpyAsync(&tot[1], h.toff.as<int32_t>() + n, 4, cudaMemcpyDeviceToHost, s));
+    const int32_t H = SEG_H;
+    const int32_t nseg = std::min<int32_t>(SEG_MAX, (n + H - 1) / H);
+    const int64_t cover = std::min<int64_t>(n, (int64_t)nseg * H);
+    std::vector<int32_t> prow((size_t)n + 1), pcol((size_t)m);
+    MG_CUDA(cudaMemcpyAsync(prow.data(), g->trow, ((size_t)n + 1) * 4, cudaMemcpyDeviceToHost, s));
+    MG_CUDA(cudaMemcpyAsync(pcol.data(), g->tcol, (size_t)m * 4, cudaMemcpyDeviceToHost, s));
     MG_CUDA(cudaStreamSynchronize(s));
-    h.mh = tot[0];
-    h.nrows = tot[1];
-    // the split pays when a quarter of the edges or more come from the hubs
-    if (h.mh * 4 < m) {
-        dev_free(h.tmp0);
-        dev_free(h.tmp1);
+    const int nt = std::max(1, std::min(host_threads(0), 32));
+    // row ranges of equal edge counts
+    std::vector<int32_t> rlo((size_t)nt + 1, n);
+    rlo[0] = 0;
+    for (int t = 1; t < nt; t++) {
+        const int64_t goal = m * t / nt;
+        rlo[t] = (int32_t)(std::lower_bound(prow.begin(), prow.end(), (int32_t)goal) - prow.begin());
+        rlo[t] = std::min(std::max(rlo[t], rlo[t - 1]), n);
+    }
+    auto run = [&](const std::function<void(int)> &fn) {
+        std::vector<std::thread> th;
+        for (int t = 1; t < nt; t++) th.emplace_back(fn, t);
+        fn(0);
+        for (auto &x : th) x.join();
+    };
+    // pass 1: per thread and segment the edges and pairs; per row its pairs
+    // and tail edges
+    std::vector<int64_t> tedge((size_t)nt * nseg, 0), tpair((size_t)nt * nseg, 0);
+    std::vector<int32_t> npair((size_t)n + 1, 0), ntail((size_t)n + 1, 0);
+    run([&](int t) {
+        int64_t *te = &tedge[(size_t)t * nseg], *tp = &tpair[(size_t)t * nseg];
+        for (int32_t v = rlo[t]; v < rlo[t + 1]; v++) {
+            uint64_t mask = 0;
+            int32_t nt_ = 0;
+            for (int32_t p = prow[v]; p < prow[v + 1]; p++) {
+                const int32_t c = pcol[p];
+                if (c < cover) {
+                    const int sg = c / H;
+                    te[sg]++;
+                    mask |= 1ull << sg;
+                } else {
+                    nt_++;
+                }
+            }
+            npair[v] = __builtin_popcountll(mask);
+            ntail[v] = nt_;
+            for (uint64_t mm = mask; mm; mm &= mm - 1) tp[__builtin_ctzll(mm)]++;
+        }
+    });
+    int64_t covered = 0;
+    for (int64_t x : tedge) covered += x;
+    // the segmented pull pays when a quarter of the edges or more are covered
+    if (covered * 4 < m) {
         h.valid = true;
         return MG_OK;
     }
-    h.nchunks = (int32_t)((h.mh + HUB_CHUNK - 1) / HUB_CHUNK);
-    const int64_t padded = (int64_t)h.nchunks * HUB_CHUNK;
-    MG_TRY(dev_alloc(h.hcol, (size_t)padded * 2 + 16));
-    MG_TRY(dev_alloc(h.tcol, (size_t)std::max<int64_t>(m - h.mh, 1) * 4 + 16));
-    MG_TRY(dev_alloc(h.hrows, (size_t)std::max(h.nrows, 1) * 4));
-    MG_TRY(dev_alloc(h.rstart, (size_t)h.nchunks * 32 + 16));
-    MG_TRY(dev_alloc(h.crow, (size_t)(h.nchunks + 1) * 4));
-    MG_TRY(dev_alloc(h.chead, (size_t)h.nchunks * 4));
-    MG_TRY(dev_alloc(h.ctail, (size_t)h.nchunks * 4));
-    MG_TRY(dev_alloc(h.cstart, (size_t)h.nchunks * 4));
-    MG_TRY(dev_alloc(h.hsum, (size_t)n * 4));
+    // offsets: segments' chunks, per-thread shares, row-major pair slots, tail rows
+    std::vector<int32_t> segchunk((size_t)nseg + 1, 0);
+    std::vector<int64_t> segpair((size_t)nseg + 1, 0);
+    std::vector<int64_t> toffE((size_t)nt * nseg), toffP((size_t)nt * nseg);
+    for (int sg = 0; sg < nseg; sg++) {
+        int64_t e = 0, pp = 0;
+        for (int t = 0; t < nt; t++) {
+            toffE[(size_t)t * nseg + sg] = e;
+            toffP[(size_t)t * nseg + sg] = segpair[sg] + pp;
+            e += tedge[(size_t)t * nseg + sg];
+            pp += tpair[(size_t)t * nseg + sg];
+        }
+        segchunk[sg + 1] = segchunk[sg] + (int32_t)((e + HUB_CHUNK - 1) / HUB_CHUNK);
+        segpair[sg + 1] = segpair[sg] + pp;
+    }
+    const int32_t nchunks = segchunk[nseg];
+    const int64_t npairs = segpair[nseg];
+    if (npairs > INT32_MAX || (int64_t)nchunks * HUB_CHUNK > INT32_MAX)
+        return fail(MG_ERR_RANGE, "segmented PageRank layout too large");
+    std::vector<int32_t> pair_off((size_t)n + 1, 0), toff((size_t)n + 1, 0);
+    for (int32_t v = 0; v < n; v++) {
+        pair_off[v + 1] = pair_off[v] + npair[v];
+        toff[v + 1] = toff[v] + ntail[v];
+    }
+    std::vector<uint16_t> hcol((size_t)nchunks * HUB_CHUNK, (uint16_t)H);
+    std::vector<uint32_t> rstart((size_t)nchunks * 8, 0u);
+    std::vector<int32_t> slot((size_t)std::max<int64_t>(npairs, 1)), tcol((size_t)std::max<int32_t>(toff[n], 1));
+    // pass 2: every row's edges into its segments' streams.  A thread's
+    // share of a segment's stream starts on a chunk of its own only by
+    // chance, so the row-start bits are set with atomic ORs.
+    std::vector<std::atomic<uint32_t>> rbits((size_t)nchunks * 8);
+    for (auto &b : rbits) b.store(0u, std::memory_order_relaxed);
+    run([&](int t) {
+        std::vector<int64_t> ep((size_t)nseg), pp((size_t)nseg);
+        for (int sg = 0; sg < nseg; sg++) {
+            ep[sg] = (int64_t)segchunk[sg] * HUB_CHUNK + toffE[(size_t)t * nseg + sg];
+            pp[sg] = toffP[(size_t)t * nseg + sg];
+        }
+        int32_t cnt[SEG_MAX];
+        int64_t start[SEG_MAX];
+        for (int32_t v = rlo[t]; v < rlo[t + 1]; v++) {
+            std::memset(cnt, 0, sizeof(int32_t) * nseg);
+            int32_t tp = toff[v];
+            for (int32_t p = prow[v]; p < prow[v + 1]; p++) {
+                const int32_t c = pcol[p];
+                if (c < cover) cnt[c / H]++;
+                else tcol[tp++] = c;
+            }
+            int32_t rank = 0;
+            for (int sg = 0; sg < nseg; sg++) {
+                if (!cnt[sg]) continue;
+                const int64_t e0 = ep[sg];
+                start[sg] = e0;
+                rbits[(size_t)(e0 >> 5)].fetch_or(1u << (e0 & 31), std::memory_order_relaxed);
+                slot[pp[sg]++] = pair_off[v] + rank++;
+                ep[sg] += cnt[sg];
+            }
+            for (int32_t p = prow[v]; p < prow[v + 1]; p++) {
+                const int32_t c = pcol[p];
+                if (c < cover) {
+                    const int sg = c / H;
+                    hcol[start[sg]++] = (uint16_t)(c - sg * H);
+                }
+            }
+        }
+    });
+    for (size_t i = 0; i < rstart.size(); i++) rstart[i] = rbits[i].load(std::memory_order_relaxed);
+    // pair index of every chunk's first start; span of every chunk's last pair
+    std::vector<int32_t> crow((size_t)nchunks + 1, 0), cnext((size_t)std::max(nchunks, 1), 0), clong;
+    for (int32_t ch = 0; ch < nchunks; ch++) {
+        int32_t k = 0;
+        for (int w = 0; w < 8; w++) k += __builtin_popcount(rstart[(size_t)ch * 8 + w]);
+        crow[ch + 1] = crow[ch] + k;
+    }
+    {
+        int32_t next = nchunks;
+        for (int32_t ch = nchunks - 1; ch >= 0; ch--) {
+            cnext[ch] = next;
+            if (crow[ch + 1] > crow[ch]) {
+                if (std::min(next, nchunks - 1) - ch > FIX_SHORT) clong.push_back(ch);
+                next = ch;
+            }
+        }
+    }
+    auto up = [&](DevBuf &b, const void *src, size_t bytes) -> mg_status {
+        MG_TRY(dev_alloc(b, std::max<size_t>(bytes, 16) + 16));
+        if (bytes) MG_CUDA(cudaMemcpyAsync(b.p, src, bytes, cudaMemcpyHostToDevice, s));
+        return MG_OK;
+    };
+    MG_TRY(up(h.hcol, hcol.data(), hcol.size() * 2));
+    MG_TRY(up(h.rstart, rstart.data(), rstart.size() * 4));
+    MG_TRY(up(h.crow, crow.data(), crow.size() * 4));
+    MG_TRY(up(h.slot, slot.data(), (size_t)npairs * 4));
+    MG_TRY(up(h.segchunk, segchunk.data(), segchunk.size() * 4));
+    MG_TRY(up(h.pair_off, pair_off.data(), pair_off.size() * 4));
+    MG_TRY(up(h.toff, toff.data(), toff.size() * 4));
+    MG_TRY(up(h.tcol, tcol.data(), (size_t)toff[n] * 4));
+    MG_TRY(up(h.cnext, cnext.data(), (size_t)nchunks * 4));
+    MG_TRY(up(h.clong, clong.data(), clong.size() * 4));
+    MG_TRY(dev_alloc(h.P, (size_t)std::max<int64_t>(npairs, 1) * 4));
+    MG_TRY(dev_alloc(h.chead, (size_t)std::max(nchunks, 1) * 4));
+    MG_TRY(dev_alloc(h.ctail, (size_t)std::max(nchunks, 1) * 4));
+    MG_TRY(dev_alloc(h.cstart, (size_t)std::max(nchunks, 1) * 4));
     MG_TRY(dev_alloc(h.err, 16));
-    MG_TRY(dev_alloc(h.tmp0, (size_t)(std::max(n, h.nchunks) + 1) * 4));   // starts per chunk
-    // hub-row indices: copy out of toff before the scatter rewrites it
-    MG_TRY(dev_alloc(h.tmp1, (size_t)(n + 1) * 4));
-    MG_CUDA(cudaMemcpyAsync(h.tmp1.p, h.toff.p, (size_t)(n + 1) * 4, cudaMemcpyDeviceToDevice, s));
-    MG_CUDA(cudaMemsetAsync(h.rstart.p, 0, (size_t)h.nchunks * 32, s));
-    MG_CUDA(cudaMemsetAsync(h.hsum.p, 0, (size_t)n * 4, s));
     MG_CUDA(cudaMemsetAsync(h.err.p, 0, 16, s));
-    k_hub_scatter<<<grid, 256, 0, s>>>(n, prow, pcol, h.H, h.hoff.as<int32_t>(), h.tmp1.as<int32_t>(),
-                                       h.hcol.as<uint16_t>(), h.tcol.as<int32_t>(), h.toff.as<int32_t>(),
-                                       h.hrows.as<int32_t>(), h.rstart.as<uint32_t>());
-    if (padded > h.mh) k_hub_pad<<<1, 256, 0, s>>>(h.hcol.as<uint16_t>(), h.mh, padded, h.H);
-    k_chunk_starts<<<grid, 256, 0, s>>>(h.rstart.as<uint32_t>(), h.nchunks, h.tmp0.as<int32_t>());
-    MG_CUDA(cudaGetLastError());
-    MG_TRY(scan_excl(h.tmp0.as<int32_t>(), h.nchunks, h.crow.as<int32_t>(), h.tiles, s));
-    MG_TRY(dev_alloc(h.cnext, (size_t)h.nchunks * 4));
-    MG_TRY(dev_alloc(h.clong, (size_t)h.nchunks * 4 + 4));   // [0]: count, then the chunk ids
-    MG_CUDA(cudaMemsetAsync(h.clong.p, 0, 4, s));
-    k_hub_spans<<<grid, 256, 0, s>>>(h.tmp0.as<int32_t>(), h.nchunks, h.cnext.as<int32_t>(),
-                                     h.clong.as<int32_t>() + 1, h.clong.as<int32_t>());
-    MG_CUDA(cudaGetLastError());
-    MG_CUDA(cudaMemcpyAsync(&h.nlong, h.clong.p, 4, cudaMemcpyDeviceToHost, s));
     MG_CUDA(cudaStreamSynchronize(s));
-    dev_free(h.tmp0);
-    dev_free(h.tmp1);
+    h.H = H;
+    h.nseg = nseg;
+    h.nchunks = nchunks;
+    h.npairs = npairs;
+    h.nlong = (int32_t)clong.size();
+    h.covered = covered;
     h.use = true;
     h.valid = true;
     return MG_OK;
@@ -545,21 +501,24 @@ mg_status hub_launch(mg_graph *g, const float *c0, const float *c1, const int32_
     a.hcol = h.hcol.as<uint16_t>();
     a.rstart = h.rstart.as<uint32_t>();
     a.crow = h.crow.as<int32_t>();
-    a.hrows = h.hrows.as<int32_t>();
+    a.slot = h.slot.as<int32_t>();
+    a.segchunk = h.segchunk.as<int32_t>();
     a.c[0] = c0;
     a.c[1] = c1;
     a.cur = cur;
     a.more = more;
     a.off = off;
-    a.hsum = h.hsum.as<float>();
+    a.P = h.P.as<float>();
     a.chead = h.chead.as<float>();
     a.ctail = h.ctail.as<float>();
     a.cstart = h.cstart.as<int32_t>();
     a.cnext = h.cnext.as<int32_t>();
-    a.clong = h.clong.as<int32_t>() + 1;
+    a.clong = h.clong.as<int32_t>();
     a.nlong = h.nlong;
     a.err = h.err.as<int32_t>();
+    a.n = g->nv;
     a.H = h.H;
+    a.nseg = h.nseg;
     a.nchunks = h.nchunks;
     const size_t smem = hub_smem_bytes(g);
     MG_CUDA(cudaFuncSetAttribute(k_hub_sweep, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
@@ -574,7 +533,7 @@ mg_status hub_launch(mg_graph *g, const float *c0, const float *c1, const int32_
     return MG_OK;
 }
 
-// the bulk-copy wait of some sweep ran out (read after the run)
+// a bulk-copy wait of some sweep ran out (read after the run)
 mg_status hub_check(mg_graph *g)
 {
     if (!g->hub.use) return MG_OK;
@@ -583,7 +542,7 @@ mg_status hub_check(mg_graph *g)
     MG_CUDA(cudaStreamSynchronize(g->stream));
     if (e) {
         MG_CUDA(cudaMemsetAsync(g->hub.err.p, 0, 4, g->stream));
-        return fail(MG_ERR_CUDA, "PageRank hub sweep: shared-memory staging did not complete");
+        return fail(MG_ERR_CUDA, "PageRank segmented sweep: shared-memory staging did not complete");
     }
     return MG_OK;
 }

@@ -84,10 +84,12 @@ struct PArgs {
     const int32_t *hrow_chunk;
     int32_t nhrows;
     int32_t heavy_deg;
-    // hub split (unweighted forms on graphs with enough hub edges): prow /
-    // pcol hold the tail part, hsum the hub part's per-row sums of the
-    // sweep; heavy chunks keep their full-row numbering (prow_full, chunk)
-    const float *hsum;
+    // segmented pull (unweighted forms on graphs where it covers enough
+    // edges): prow / pcol hold the tail part, P the sweep's per-(row,
+    // segment) sums, row v's at P[pair_off[v] .. pair_off[v+1]); heavy
+    // chunks keep their full-row numbering (prow_full, chunk)
+    const float *P;
+    const int32_t *pair_off;
     const int32_t *prow_full;
     int32_t chunk;
     float *x[2];             // iterate (ping-pong)
@@ -315,6 +317,15 @@ __device__ __forceinline__ void block_partials(const PArgs &a, int slot, double 
     }
 }
 
+// the row's segment partial sums (segments ascending; 0 without the split)
+__device__ __forceinline__ float seg_sum(const PArgs &a, int32_t v)
+{
+    float s = 0.0f;
+    if (a.P)
+        for (int32_t p = __ldg(&a.pair_off[v]), e = __ldg(&a.pair_off[v + 1]); p < e; p++) s += __ldcg(&a.P[p]);
+    return s;
+}
+
 // row reduction for one PageRank sweep (bins_reduce interface)
 template <class Op>
 struct PrRowOp {
@@ -340,7 +351,7 @@ struct PrRowOp {
     __device__ void finish(int32_t v, float s)
     {
         float dg = 0.0f;
-        if (a.hsum) s += __ldcg(&a.hsum[v]);
+        s += seg_sum(a, v);
         resid += Op::apply(a, c, v, s, any, dg);
         dangs += dg;
         if (Op::kDataDriven) {
@@ -370,7 +381,7 @@ __global__ void __launch_bounds__(THREADS) k_pr_light(PArgs a)
     __shared__ float s_part[THREADS / 32];
     for (int32_t ch = blockIdx.x; ch < a.nhchunks; ch += gridDim.x) {
         int32_t v = a.hchunk[3 * ch], b = a.hchunk[3 * ch + 1], e = a.hchunk[3 * ch + 2];
-        if (a.hsum) {
+        if (a.P) {
             // the same piece of the row's tail part: piece k of the full
             // row covers tail positions [k * chunk, (k + 1) * chunk)
             const int32_t k = (b - a.prow_full[v]) / a.chunk;
@@ -483,7 +494,7 @@ __global__ void __launch_bounds__(THREADS) k_pr_apply(PArgs a, cudaGraphConditio
         for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
         if (lane == 0) {
             float dg = 0.0f;
-            if (a.hsum) s += __ldcg(&a.hsum[v]);
+            s += seg_sum(a, v);
             resid += Op::apply(a, c, v, s, any, dg);
             dangs += dg;
             if (Op::kDataDriven) {
@@ -949,11 +960,11 @@ static mg_status pr_loop(mg_graph *g, PArgs &a, const mg_opts &opt, const char *
     std::string hn = std::string(name) + "_apply";
     const int sh = P.slot(hn.c_str());
     const int apply_grid = std::max(1, std::min(std::min(grid, (a.nhrows + 7) / 8), g->num_sms * APPLY_PER_SM));
-    const int shs = a.hsum ? P.slot("pr_hub") : -1, shf = a.hsum ? P.slot("pr_hub_fix") : -1;
+    const int shs = a.P ? P.slot("pr_hub") : -1, shf = a.P ? P.slot("pr_hub_fix") : -1;
     const int sqc = Op::kDataDriven ? P.slot("prd_compact") : -1, sqg = Op::kDataDriven ? P.slot("prd_gather") : -1,
               sqa = Op::kDataDriven ? P.slot("prd_apply") : -1;
     BodyFn body = [&](cudaStream_t st, cudaGraphConditionalHandle h, int use_cond) -> mg_status {
-        if (a.hsum) MG_TRY(hub_launch(g, a.c[0], a.c[1], &a.ctl->cur, &a.ctl->more, &a.ctl->sparse, st, shs, shf));
+        if (a.P) MG_TRY(hub_launch(g, a.c[0], a.c[1], &a.ctl->cur, &a.ctl->more, &a.ctl->sparse, st, shs, shf));
         P.begin(sl);
         k_pr_light<Op><<<grid, THREADS, 0, st>>>(a);
         P.end();
@@ -978,13 +989,13 @@ static mg_status pr_loop(mg_graph *g, PArgs &a, const mg_opts &opt, const char *
     int max_iter = opt.max_iter > 0 ? opt.max_iter : 10000;
     // the key holds every by-value argument of the captured kernels
     // (and the hub split's build, whose sizes the hub kernels take by value)
-    const LoopKey key = LoopKey().add(Op::kSlot).add(a).add(grid).add(apply_grid).add(a.hsum ? g->hub.gen : 0ull);
+    const LoopKey key = LoopKey().add(Op::kSlot).add(a).add(grid).add(apply_grid).add(a.P ? g->hub.gen : 0ull);
     MG_TRY(run_loop(opt.profile ? MG_EXEC_HOST : opt.exec, opt.profile != 0, s, g->pws->lg[Op::kSlot], key, body,
                     &a.ctl->more, g->pinned_flag, max_iter + 2));
     PCtl hc;
     MG_CUDA(cudaMemcpyAsync(&hc, a.ctl, sizeof(PCtl), cudaMemcpyDeviceToHost, s));
     MG_CUDA(cudaStreamSynchronize(s));
-    if (a.hsum) MG_TRY(hub_check(g));
+    if (a.P) MG_TRY(hub_check(g));
     if (info) {
         info->iterations = hc.iter;
         info->pull_iterations = Op::kDataDriven ? hc.dense_iters : hc.iter;   // sweeps over every row
@@ -1004,8 +1015,10 @@ static mg_status pr_setup(mg_graph *g, PArgs &a, bool weighted_or_adj)
     const int grid = launch_grid(g, THREADS, 8);
     MG_TRY(dev_alloc(w->x0, n * 4));
     MG_TRY(dev_alloc(w->x1, n * 4));
-    MG_TRY(dev_alloc(w->c0, n * 4));
-    MG_TRY(dev_alloc(w->c1, n * 4));
+    // 16 bytes of slack: the segmented sweep stages contributions in
+    // 16-byte units, up to 12 bytes past the last vertex
+    MG_TRY(dev_alloc(w->c0, n * 4 + 16));
+    MG_TRY(dev_alloc(w->c1, n * 4 + 16));
     MG_TRY(dev_alloc(w->active, n * 4));
     MG_TRY(dev_alloc(w->hpart, (size_t)std::max(g->nhchunks, 1) * 4));
     MG_TRY(dev_alloc(w->bpart, (size_t)grid * 2 * NPART * 8));  // sweep blocks + apply blocks
@@ -1041,7 +1054,8 @@ static mg_status pr_setup(mg_graph *g, PArgs &a, bool weighted_or_adj)
         if (g->hub.use) {
             a.prow = g->hub.toff.as<int32_t>();
             a.pcol = g->hub.tcol.as<int32_t>();
-            a.hsum = g->hub.hsum.as<float>();
+            a.P = g->hub.P.as<float>();
+            a.pair_off = g->hub.pair_off.as<int32_t>();
             a.prow_full = g->trow;
             a.chunk = g->hchunk_size;
         }
