@@ -10,7 +10,7 @@
 // grouped by segment once per layout:
 //   segment streams : for segment s, the rows that have in-edges from it
 //                     (ascending), each row's edges from s as 16-bit local
-//                     ids (id - s*H), padded to whole 256-edge chunks; a
+//                     ids (id - s*H), padded to whole 1024-edge chunks; a
 //                     bitmap marks the first edge of every (row, segment)
 //                     pair; slot[] gives each pair its place in P;
 //   P, pair_off     : the pairs' partial sums in row-major order (row v's
@@ -23,12 +23,14 @@
 // One sweep: k_hub_sweep streams the chunks -- each CTA a contiguous,
 // edge-balanced range, staging the contributions c[s*H, (s+1)*H) of every
 // segment its range enters with bulk copies (cp.async.bulk on an mbarrier),
-// each warp a chunk at a time: every lane takes 8 consecutive edges with one
-// 128-bit load and gathers from shared memory, a segmented sum (per lane,
-// then a shuffle tree across lanes) gives every pair that ends inside the
-// chunk its total; k_hub_fix finishes the pairs that run past their chunk
-// (FP64, fixed order).  Sums are formed in a fixed order, so sweeps are
-// reproducible.
+// each warp a 1024-edge chunk at a time: every lane takes 32 consecutive
+// edges with four 128-bit loads and gathers from shared memory, a segmented
+// sum (per lane, then a shuffle tree across lanes) gives every pair that
+// ends inside the chunk its total; k_hub_fix finishes the pairs that run
+// past their chunk (FP64, fixed order).  (With 8 edges per lane the chunk's
+// fixed work -- the cross-lane scans and carries -- made the kernel
+// issue-bound: ~350 warp instructions per 256 edges.)  Sums are formed in
+// a fixed order, so sweeps are reproducible.
 //
 // Per sweep the streams move 2 B per edge plus 1 bit per edge and 4 B per
 // pair, instead of 4 B of ids and a 32-byte L2 sector per gather.
@@ -45,9 +47,8 @@ namespace {
 
 constexpr int32_t SEG_H = 57344;    // vertices per segment: 224 KB of FP32 contributions
 constexpr int32_t SEG_MAX = 64;     // segments at most; ids beyond stay in the L2 tail
-constexpr int HUB_CHUNK = 256;      // edges per warp chunk: 8 per lane
+constexpr int HUB_CHUNK = 1024;     // edges per warp chunk: 32 per lane
 constexpr int HUB_THREADS = 1024;   // one CTA per SM (shared memory bound)
-constexpr int HUB_ILP = 2;          // chunks in flight per warp
 constexpr long long HUB_WAIT_LIMIT = 20000000ll;  // clock64 cycles (~10 ms) for a bulk copy
 constexpr int32_t FIX_SHORT = 8;    // carry spans up to this many chunks: a thread each
 
@@ -130,18 +131,18 @@ __device__ __forceinline__ bool stage_segment(float *s_c, const float *src, uint
     return s_ok != 0;
 }
 
-// one 256-edge chunk: 8 edges per lane, segmented sums, pair totals to P
-__device__ __forceinline__ void sweep_chunk(const HubArgs &a, const float *s_c, int32_t ch, uint4 cols,
-                                            uint32_t word, int32_t crow)
+// One chunk of HUB_CHUNK = 1024 edges: every lane takes 32 consecutive
+// edges (four 128-bit loads of 16-bit ids) and their 32 start bits (one
+// word), gathers from shared memory and forms segmented sums; the pair
+// totals that end inside the lane go straight to P, the open ends are joined
+// across lanes by a shuffle tree, and the chunk's carries go to
+// chead / ctail / cstart.
+__device__ __forceinline__ void sweep_chunk(const HubArgs &a, const float *s_c, int32_t ch, const uint4 (&cols)[4],
+                                            uint32_t bits, int32_t crow)
 {
     const int lane = threadIdx.x & 31;
-    const uint32_t fl = (word >> ((lane & 3) * 8)) & 0xffu;
-    const uint32_t w32[4] = {cols.x, cols.y, cols.z, cols.w};
-    float v[8];
-#pragma unroll
-    for (int i = 0; i < 8; i++) v[i] = s_c[(w32[i >> 1] >> ((i & 1) * 16)) & 0xffffu];
     // pair index of this lane's first start
-    const int nst = __popc(fl);
+    const int nst = __popc(bits);
     int32_t before = nst;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
@@ -149,33 +150,42 @@ __device__ __forceinline__ void sweep_chunk(const HubArgs &a, const float *s_c, 
         if (lane >= o) before += t;
     }
     before -= nst;
-    // per-lane segmented sums, branch-free: outv[i] is the total of the pair
-    // that ends just before edge i (outf[i]: it started in this lane too);
-    // the slots are loaded together afterwards
-    const int32_t rbase = crow + before;
+    int32_t k = crow + before - 1;   // pair index of the open pair (after its start)
     float head = 0.0f, run = 0.0f;
     bool started = false;
-    float outv[8];
-    bool outf[8];
 #pragma unroll
-    for (int i = 0; i < 8; i++) {
-        const bool st = (fl >> i) & 1u;
-        outf[i] = st && started;
-        outv[i] = run;
-        head = (st && !started) ? run : head;
-        run = st ? 0.0f : run;
-        started = started || st;
-        run += v[i];
+    for (int g = 0; g < 4; g++) {
+        const uint32_t w32[4] = {cols[g].x, cols[g].y, cols[g].z, cols[g].w};
+        float v[8];
+#pragma unroll
+        for (int i = 0; i < 8; i++) v[i] = s_c[(w32[i >> 1] >> ((i & 1) * 16)) & 0xffffu];
+        // branch-free segmented sums: outv[i] is the total of the pair that
+        // ends just before edge 8g+i (outf[i]: it started in this lane);
+        // the slots of the group are loaded together, then stored to
+        float outv[8];
+        bool outf[8];
+        int32_t oidx[8];
+#pragma unroll
+        for (int i = 0; i < 8; i++) {
+            const bool st = (bits >> (8 * g + i)) & 1u;
+            outf[i] = st && started;
+            outv[i] = run;
+            oidx[i] = k;
+            head = (st && !started) ? run : head;
+            run = st ? 0.0f : run;
+            started = started || st;
+            k += st ? 1 : 0;
+            run += v[i];
+        }
+        int32_t sl[8];
+#pragma unroll
+        for (int i = 0; i < 8; i++)
+            if (outf[i]) sl[i] = __ldg(&a.slot[oidx[i]]);
+#pragma unroll
+        for (int i = 0; i < 8; i++)
+            if (outf[i]) a.P[sl[i]] = outv[i];
     }
     if (!started) head = run;
-    int32_t sl[8];
-#pragma unroll
-    for (int i = 0; i < 8; i++)
-        if (outf[i]) sl[i] = __ldg(&a.slot[rbase + __popc(fl & ((1u << i) - 1u)) - 1]);
-#pragma unroll
-    for (int i = 0; i < 8; i++)
-        if (outf[i]) a.P[sl[i]] = outv[i];
-    const int32_t ridx = rbase + nst - 1;   // the lane's last start (when started)
     // T = sum of heads from this lane up to and including the first lane
     // (>= this one) that has a start
     float T = head;
@@ -195,7 +205,7 @@ __device__ __forceinline__ void sweep_chunk(const HubArgs &a, const float *s_c, 
     if (started) {
         const bool closed = lane < 31 && Fn;
         const float total = run + (lane < 31 ? Tn : 0.0f);
-        if (closed) a.P[__ldg(&a.slot[ridx])] = total;
+        if (closed) a.P[__ldg(&a.slot[k])] = total;
         else a.ctail[ch] = total;   // the chunk's last pair runs on
     }
     if (lane == 0) {
@@ -231,25 +241,13 @@ __global__ void __launch_bounds__(HUB_THREADS, 1) k_hub_sweep(HubArgs a)
         const int32_t len = min(a.H, a.n - base);
         if (!stage_segment(s_c, c + base, (uint32_t)((len + 3) & ~3) * 4u, bar, phase, a.err)) return;
         phase ^= 1u;
-        for (int32_t c0 = lo + warp * HUB_ILP; c0 < hi; c0 += NW * HUB_ILP) {
-            uint4 cols[HUB_ILP];
-            uint32_t word[HUB_ILP];
-            int32_t crow[HUB_ILP];
+        for (int32_t ch = lo + warp; ch < hi; ch += NW) {
+            const uint4 *src = reinterpret_cast<const uint4 *>(a.hcol + (int64_t)ch * HUB_CHUNK) + lane * 4;
+            uint4 cols[4];
 #pragma unroll
-            for (int j = 0; j < HUB_ILP; j++) {
-                const int32_t ch = c0 + j;
-                if (ch < hi) {
-                    cols[j] = __ldcs(reinterpret_cast<const uint4 *>(a.hcol + (int64_t)ch * HUB_CHUNK) + lane);
-                    word[j] = __ldcs(&a.rstart[(int64_t)ch * 8 + (lane >> 2)]);
-                    crow[j] = __ldg(&a.crow[ch]);
-                }
-            }
-#pragma unroll
-            for (int j = 0; j < HUB_ILP; j++) {
-                const int32_t ch = c0 + j;
-                if (ch >= hi) break;   // warp-uniform
-                sweep_chunk(a, s_c, ch, cols[j], word[j], crow[j]);
-            }
+            for (int g = 0; g < 4; g++) cols[g] = __ldcs(src + g);
+            const uint32_t bits = __ldcs(&a.rstart[(int64_t)ch * 32 + lane]);
+            sweep_chunk(a, s_c, ch, cols, bits, __ldg(&a.crow[ch]));
         }
         lo = hi;
     }
@@ -398,12 +396,12 @@ mg_status hub_prepare(mg_graph *g)
         toff[v + 1] = toff[v] + ntail[v];
     }
     std::vector<uint16_t> hcol((size_t)nchunks * HUB_CHUNK, (uint16_t)H);
-    std::vector<uint32_t> rstart((size_t)nchunks * 8, 0u);
+    std::vector<uint32_t> rstart((size_t)nchunks * (HUB_CHUNK / 32), 0u);
     std::vector<int32_t> slot((size_t)std::max<int64_t>(npairs, 1)), tcol((size_t)std::max<int32_t>(toff[n], 1));
     // pass 2: every row's edges into its segments' streams.  A thread's
     // share of a segment's stream starts on a chunk of its own only by
     // chance, so the row-start bits are set with atomic ORs.
-    std::vector<std::atomic<uint32_t>> rbits((size_t)nchunks * 8);
+    std::vector<std::atomic<uint32_t>> rbits((size_t)nchunks * (HUB_CHUNK / 32));
     for (auto &b : rbits) b.store(0u, std::memory_order_relaxed);
     run([&](int t) {
         std::vector<int64_t> ep((size_t)nseg), pp((size_t)nseg);
@@ -444,7 +442,7 @@ mg_status hub_prepare(mg_graph *g)
     std::vector<int32_t> crow((size_t)nchunks + 1, 0), cnext((size_t)std::max(nchunks, 1), 0), clong;
     for (int32_t ch = 0; ch < nchunks; ch++) {
         int32_t k = 0;
-        for (int w = 0; w < 8; w++) k += __builtin_popcount(rstart[(size_t)ch * 8 + w]);
+        for (int w = 0; w < HUB_CHUNK / 32; w++) k += __builtin_popcount(rstart[(size_t)ch * (HUB_CHUNK / 32) + w]);
         crow[ch + 1] = crow[ch] + k;
     }
     {
