@@ -109,11 +109,14 @@ struct HubSplit {
     int32_t H = 0, nseg = 0, nchunks = 0;
     int32_t nlong = 0;       // chunks whose last pair spans many chunks
     int64_t npairs = 0, covered = 0;  // (row, segment) pairs; edges in the segments
+    int64_t ntail = 0;       // edges past the last segment
+    int32_t grid = 0;        // CTAs of the sweep (one per SM)
     DevBuf hcol;             // uint16 segment streams (whole chunks), segment-major
     DevBuf rstart;           // uint32 bits: first edge of each pair
     DevBuf crow;             // int32 [nchunks+1]: pair index of each chunk's first start
     DevBuf slot;             // int32 [npairs]: each pair's place in P
     DevBuf segchunk;         // int32 [nseg+1]: first chunk of each segment
+    DevBuf cta_lo;           // int32 [grid+1]: each CTA's chunk range
     DevBuf pair_off;         // int32 [n+1]: row v's pairs in P
     DevBuf P;                // float [npairs]: pair sums of the current sweep
     DevBuf toff, tcol;       // tail rows: offsets [n+1], int32 ids

@@ -51,6 +51,7 @@ constexpr int HUB_CHUNK = 1024;     // edges per warp chunk: 32 per lane
 constexpr int HUB_THREADS = 1024;   // one CTA per SM (shared memory bound)
 constexpr long long HUB_WAIT_LIMIT = 20000000ll;  // clock64 cycles (~10 ms) for a bulk copy
 constexpr int32_t FIX_SHORT = 8;    // carry spans up to this many chunks: a thread each
+constexpr int64_t START_COST = 32;  // a pair start's cost in edges, for balancing CTA ranges
 
 struct HubArgs {
     const uint16_t *hcol;     // segment streams (each padded to whole chunks), segment-major
@@ -58,6 +59,7 @@ struct HubArgs {
     const int32_t *crow;      // [nchunks+1] pair index (segment-major) of each chunk's first start
     const int32_t *slot;      // per pair (segment-major): its place in P
     const int32_t *segchunk;  // [nseg+1] first chunk of each segment
+    const int32_t *cta_lo;    // [grid+1] each CTA's chunk range, balanced by edges + starts
     const float *c[2];        // contributions (ping-pong, ctl selects)
     const int32_t *cur;       // current iterate index (loop control block)
     const int32_t *more;      // loop continue flag
@@ -153,37 +155,57 @@ __device__ __forceinline__ void sweep_chunk(const HubArgs &a, const float *s_c, 
     int32_t k = crow + before - 1;   // pair index of the open pair (after its start)
     float head = 0.0f, run = 0.0f;
     bool started = false;
+    if (bits == 0) {
+        // no pair starts in this lane: its 32 edges all continue the open
+        // pair; summed as a pairwise tree (the same adds, a rounding error of
+        // five steps instead of 32: long hub sums stay steady from sweep to
+        // sweep, which the FP32 fixed-point iteration needs to settle)
+        float t[16];
 #pragma unroll
-    for (int g = 0; g < 4; g++) {
-        const uint32_t w32[4] = {cols[g].x, cols[g].y, cols[g].z, cols[g].w};
-        float v[8];
+        for (int g = 0; g < 4; g++) {
+            const uint32_t w32[4] = {cols[g].x, cols[g].y, cols[g].z, cols[g].w};
 #pragma unroll
-        for (int i = 0; i < 8; i++) v[i] = s_c[(w32[i >> 1] >> ((i & 1) * 16)) & 0xffffu];
-        // branch-free segmented sums: outv[i] is the total of the pair that
-        // ends just before edge 8g+i (outf[i]: it started in this lane);
-        // the slots of the group are loaded together, then stored to
-        float outv[8];
-        bool outf[8];
-        int32_t oidx[8];
-#pragma unroll
-        for (int i = 0; i < 8; i++) {
-            const bool st = (bits >> (8 * g + i)) & 1u;
-            outf[i] = st && started;
-            outv[i] = run;
-            oidx[i] = k;
-            head = (st && !started) ? run : head;
-            run = st ? 0.0f : run;
-            started = started || st;
-            k += st ? 1 : 0;
-            run += v[i];
+            for (int i = 0; i < 4; i++)
+                t[4 * g + i] = s_c[w32[i] & 0xffffu] + s_c[w32[i] >> 16];
         }
-        int32_t sl[8];
 #pragma unroll
-        for (int i = 0; i < 8; i++)
-            if (outf[i]) sl[i] = __ldg(&a.slot[oidx[i]]);
+        for (int w = 8; w > 0; w >>= 1)
 #pragma unroll
-        for (int i = 0; i < 8; i++)
-            if (outf[i]) a.P[sl[i]] = outv[i];
+            for (int i = 0; i < w; i++) t[i] = t[i] + t[i + w];
+        head = t[0];
+    } else {
+#pragma unroll
+        for (int g = 0; g < 4; g++) {
+            const uint32_t w32[4] = {cols[g].x, cols[g].y, cols[g].z, cols[g].w};
+            float v[8];
+#pragma unroll
+            for (int i = 0; i < 8; i++) v[i] = s_c[(w32[i >> 1] >> ((i & 1) * 16)) & 0xffffu];
+            // branch-free segmented sums: outv[i] is the total of the pair
+            // that ends just before edge 8g+i (outf[i]: it started in this
+            // lane); the slots of the group are loaded together, then stored to
+            float outv[8];
+            bool outf[8];
+            int32_t oidx[8];
+#pragma unroll
+            for (int i = 0; i < 8; i++) {
+                const bool st = (bits >> (8 * g + i)) & 1u;
+                outf[i] = st && started;
+                outv[i] = run;
+                oidx[i] = k;
+                head = (st && !started) ? run : head;
+                run = st ? 0.0f : run;
+                started = started || st;
+                k += st ? 1 : 0;
+                run += v[i];
+            }
+            int32_t sl[8];
+#pragma unroll
+            for (int i = 0; i < 8; i++)
+                if (outf[i]) sl[i] = __ldg(&a.slot[oidx[i]]);
+#pragma unroll
+            for (int i = 0; i < 8; i++)
+                if (outf[i]) a.P[sl[i]] = outv[i];
+        }
     }
     if (!started) head = run;
     // T = sum of heads from this lane up to and including the first lane
@@ -226,9 +248,9 @@ __global__ void __launch_bounds__(HUB_THREADS, 1) k_hub_sweep(HubArgs a)
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     if (threadIdx.x < 4) s_c[a.H + threadIdx.x] = 0.0f;   // the padding id's slot
-    // this CTA's edge-balanced chunk range, cut at segment boundaries
-    const int32_t c_lo = (int32_t)((int64_t)a.nchunks * blockIdx.x / gridDim.x);
-    const int32_t c_hi = (int32_t)((int64_t)a.nchunks * (blockIdx.x + 1) / gridDim.x);
+    // this CTA's chunk range (balanced by edges and pair starts), cut at
+    // segment boundaries
+    const int32_t c_lo = __ldg(&a.cta_lo[blockIdx.x]), c_hi = __ldg(&a.cta_lo[blockIdx.x + 1]);
     const int32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     constexpr int32_t NW = HUB_THREADS / 32;
     uint32_t phase = 0;
@@ -292,7 +314,7 @@ namespace mgi {
 void hub_free(mg_graph *g)
 {
     HubSplit &h = g->hub;
-    DevBuf *bufs[] = {&h.hcol, &h.rstart, &h.crow, &h.slot, &h.segchunk, &h.pair_off, &h.P, &h.toff,
+    DevBuf *bufs[] = {&h.hcol, &h.rstart, &h.crow, &h.slot, &h.segchunk, &h.cta_lo, &h.pair_off, &h.P, &h.toff,
                       &h.tcol, &h.chead, &h.ctail, &h.cstart, &h.cnext, &h.clong, &h.err};
     for (DevBuf *b : bufs) dev_free(*b);
     h = HubSplit();
@@ -455,6 +477,22 @@ mg_status hub_prepare(mg_graph *g)
             }
         }
     }
+    // CTA ranges: a chunk costs its 1024 edges plus START_COST per pair start
+    // (the slot load and scattered store of a short pair's total); chunk
+    // counts alone left one SM four times as busy as the average
+    const int G = g->num_sms;
+    std::vector<int32_t> cta_lo((size_t)G + 1, nchunks);
+    {
+        const int64_t total = (int64_t)nchunks * HUB_CHUNK + START_COST * (int64_t)crow[nchunks];
+        int64_t acc = 0;
+        int b = 0;
+        cta_lo[0] = 0;
+        for (int32_t ch = 0; ch < nchunks && b + 1 < G; ch++) {
+            acc += HUB_CHUNK + START_COST * (int64_t)(crow[ch + 1] - crow[ch]);
+            while (b + 1 < G && acc * G >= total * (b + 1)) cta_lo[++b] = ch + 1;
+        }
+        while (b + 1 <= G) cta_lo[++b] = nchunks;
+    }
     auto up = [&](DevBuf &b, const void *src, size_t bytes) -> mg_status {
         MG_TRY(dev_alloc(b, std::max<size_t>(bytes, 16) + 16));
         if (bytes) MG_CUDA(cudaMemcpyAsync(b.p, src, bytes, cudaMemcpyHostToDevice, s));
@@ -465,6 +503,7 @@ mg_status hub_prepare(mg_graph *g)
     MG_TRY(up(h.crow, crow.data(), crow.size() * 4));
     MG_TRY(up(h.slot, slot.data(), (size_t)npairs * 4));
     MG_TRY(up(h.segchunk, segchunk.data(), segchunk.size() * 4));
+    MG_TRY(up(h.cta_lo, cta_lo.data(), cta_lo.size() * 4));
     MG_TRY(up(h.pair_off, pair_off.data(), pair_off.size() * 4));
     MG_TRY(up(h.toff, toff.data(), toff.size() * 4));
     MG_TRY(up(h.tcol, tcol.data(), (size_t)toff[n] * 4));
@@ -483,6 +522,8 @@ mg_status hub_prepare(mg_graph *g)
     h.npairs = npairs;
     h.nlong = (int32_t)clong.size();
     h.covered = covered;
+    h.ntail = toff[n];
+    h.grid = G;
     h.use = true;
     h.valid = true;
     return MG_OK;
@@ -501,6 +542,7 @@ mg_status hub_launch(mg_graph *g, const float *c0, const float *c1, const int32_
     a.crow = h.crow.as<int32_t>();
     a.slot = h.slot.as<int32_t>();
     a.segchunk = h.segchunk.as<int32_t>();
+    a.cta_lo = h.cta_lo.as<int32_t>();
     a.c[0] = c0;
     a.c[1] = c1;
     a.cur = cur;
@@ -522,7 +564,7 @@ mg_status hub_launch(mg_graph *g, const float *c0, const float *c1, const int32_
     MG_CUDA(cudaFuncSetAttribute(k_hub_sweep, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     Profiler &P = g->prof;
     P.begin(slot_sweep);
-    k_hub_sweep<<<g->num_sms, HUB_THREADS, smem, st>>>(a);
+    k_hub_sweep<<<h.grid, HUB_THREADS, smem, st>>>(a);
     P.end();
     P.begin(slot_fix);
     k_hub_fix<<<std::max(1, std::min(g->num_sms * 4, (h.nchunks + 255) / 256)), 256, 0, st>>>(a);

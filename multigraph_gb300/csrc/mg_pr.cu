@@ -92,6 +92,7 @@ struct PArgs {
     const int32_t *pair_off;
     const int32_t *prow_full;
     int32_t chunk;
+    int32_t seg_only;        // every in-edge sits in a segment: rows finish in k_pr_seg
     float *x[2];             // iterate (ping-pong)
     float *c[2];             // gathered quantity: contribution x/deg (PR) or lambda (adjoint)
     const float *gvec;       // adjoint: g
@@ -464,6 +465,20 @@ __device__ __forceinline__ bool last_block(PCtl *cp)
     if (threadIdx.x == 0) s_last = (atomicAdd(&cp->done, 1) == (int)gridDim.x - 1);
     __syncthreads();
     return s_last != 0;
+}
+
+// Row finish when every in-edge sits in a segment (no tail, no heavy-row
+// chunks): a thread per row sums its pairs' partials (segments ascending;
+// consecutive rows read consecutive pair ranges) and applies the update.
+template <class Op>
+__global__ void __launch_bounds__(THREADS) k_pr_seg(PArgs a)
+{
+    const PCtl c = *a.ctl;
+    if (c.more == 0 || c.sparse) return;
+    PrRowOp<Op> op{a, c};
+    for (int32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < a.n; v += gridDim.x * blockDim.x)
+        op.finish(v, 0.0f);
+    block_partials(a, blockIdx.x, op.resid, op.dangs, op.any, op.act, op.dfz);
 }
 
 // Heavy rows (warp per row, chunk partials summed lane-strided then by a
@@ -966,7 +981,8 @@ static mg_status pr_loop(mg_graph *g, PArgs &a, const mg_opts &opt, const char *
     BodyFn body = [&](cudaStream_t st, cudaGraphConditionalHandle h, int use_cond) -> mg_status {
         if (a.P) MG_TRY(hub_launch(g, a.c[0], a.c[1], &a.ctl->cur, &a.ctl->more, &a.ctl->sparse, st, shs, shf));
         P.begin(sl);
-        k_pr_light<Op><<<grid, THREADS, 0, st>>>(a);
+        if (a.seg_only) k_pr_seg<Op><<<grid, THREADS, 0, st>>>(a);
+        else k_pr_light<Op><<<grid, THREADS, 0, st>>>(a);
         P.end();
         P.begin(sh);
         k_pr_apply<Op><<<apply_grid, THREADS, 0, st>>>(a, h, use_cond);
@@ -1056,6 +1072,12 @@ static mg_status pr_setup(mg_graph *g, PArgs &a, bool weighted_or_adj)
             a.pcol = g->hub.tcol.as<int32_t>();
             a.P = g->hub.P.as<float>();
             a.pair_off = g->hub.pair_off.as<int32_t>();
+            if (g->hub.ntail == 0) {
+                // rows finish in k_pr_seg; k_pr_apply only reduces
+                a.seg_only = 1;
+                a.nhchunks = 0;
+                a.nhrows = 0;
+            }
             a.prow_full = g->trow;
             a.chunk = g->hchunk_size;
         }
