@@ -494,13 +494,26 @@ def main():
     e2e_s = time.perf_counter() - t0
     e2e_val = 2 * m * args.steps / e2e_s / 1e9
     split = {k: round(v / args.steps, 3) for k, v in split.items()}
-    # the same upload + commit with no runs beside it (link speed alone)
+    # the same upload + commit with no runs beside it (link speed alone),
+    # and the two parts on their own
     torch.cuda.synchronize()
     ta = time.perf_counter()
     for _ in range(3):
         g.stage(h)
         g.commit()
     split["upload_commit_alone_ms"] = round((time.perf_counter() - ta) / 3 * 1e3, 3)
+    up, co = 0.0, 0.0
+    for _ in range(3):
+        t1 = time.perf_counter()
+        g.stage(h)
+        torch.cuda.synchronize()
+        t2 = time.perf_counter()
+        g.commit()
+        t3 = time.perf_counter()
+        up += t2 - t1
+        co += t3 - t2
+    split["upload_alone_ms"] = round(up / 3 * 1e3, 3)
+    split["commit_alone_ms"] = round(co / 3 * 1e3, 3)
     # the last end-to-end step's results, checked against the oracle below
     dist_gpu, _ = g.sssp(0, opts)
     rank_gpu, rank_info = g.pagerank(mg.PR_TOPOLOGY, opts)

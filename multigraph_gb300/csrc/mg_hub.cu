@@ -172,7 +172,7 @@ __device__ __forceinline__ void sweep_chunk(const HubArgs &a, const float *s_c, 
         for (int w = 8; w > 0; w >>= 1)
 #pragma unroll
             for (int i = 0; i < w; i++) t[i] = t[i] + t[i + w];
-        head = t[0];
+        run = t[0];   // head = run below: the lane's whole sum continues the open pair
     } else {
 #pragma unroll
         for (int g = 0; g < 4; g++) {
