@@ -444,35 +444,11 @@ def main():
 
     for _ in range(args.warmup):
         si, pi = step()
-    clocks = ClockSampler(local)
-    clocks.start()
-    time.sleep(0.3)
-    # ---- device-resident timed region
-    if dist:
-        dist.barrier()
-    torch.cuda.synchronize()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    launches = 0
-    for _ in range(args.steps):
-        si, pi = step()
-        # SSSP: init + (push, frontier min, pull, compact, decide) per iteration + id mapping;
-        # PageRank: 2 inits + (sweep, apply) per sweep + id mapping
-        launches += 2 + 5 * si.iterations + 3 + 2 * pi.iterations
-    e1.record(stream)
-    torch.cuda.synchronize()
-    if dist:
-        dist.barrier()
-    ms, value = aggregate(e0.elapsed_time(e1), 2 * m, args.steps, world, dist, torch.device("cuda", local))
-    ms_per_step = ms / args.steps
-    # the clock sampler runs around the device-timed region and the
-    # per-kernel timing pass, not around the host-synchronised end-to-end loop
-    clk_lines = clocks.pause()
-
     # ---- end to end through the C ABI: every step copies the pinned host CSR
     # in and both results out.  Double-buffered: the next step's copy
     # (mg_graph_stage, copy stream) overlaps this step's runs, and
     # mg_graph_commit rebuilds the device CSR from it before the next step.
+    # Measured before the clock sampler (a thread polling NVML) first starts.
     h2d = h.stage_bytes()  # row offsets, column ids, weights: 4(n+1) + 8m bytes, all int32
     d2h = 8 * n
     torch.cuda.synchronize()
@@ -514,7 +490,32 @@ def main():
         co += t3 - t2
     split["upload_alone_ms"] = round(up / 3 * 1e3, 3)
     split["commit_alone_ms"] = round(co / 3 * 1e3, 3)
-    # the last end-to-end step's results, checked against the oracle below
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.3)
+    # ---- device-resident timed region
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    launches = 0
+    for _ in range(args.steps):
+        si, pi = step()
+        # SSSP: init + (push, frontier min, pull, compact, decide) per iteration + id mapping;
+        # PageRank: 2 inits + (sweep, apply) per sweep + id mapping
+        launches += 2 + 5 * si.iterations + 3 + 2 * pi.iterations
+    e1.record(stream)
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    ms, value = aggregate(e0.elapsed_time(e1), 2 * m, args.steps, world, dist, torch.device("cuda", local))
+    ms_per_step = ms / args.steps
+    # the clock sampler runs around the device-timed region and the
+    # per-kernel timing pass, not around the host-synchronised end-to-end loop
+    clk_lines = clocks.pause()
+
+    # results on the last committed input, checked against the oracle below
     dist_gpu, _ = g.sssp(0, opts)
     rank_gpu, rank_info = g.pagerank(mg.PR_TOPOLOGY, opts)
 
@@ -548,6 +549,19 @@ def main():
                 "dense_ms_per_sweep": dense_ms / max(di.pull_iterations, 1),
                 "queue_ms_per_sweep": (queue_ms / nq) if nq else None}
 
+    # the two pull layouts of the sweep, one profiled PageRank each
+    def layout_sweep_ms(layout):
+        o = mg.default_opts(tol=TOL, damping=DAMPING, profile=1, pr_layout=layout)
+        _, li = g.pagerank(mg.PR_TOPOLOGY, o, out=False)
+        lkt = li.kernel_times()
+        return round(sum(lkt.get(k, (0, 0.0))[1] for k in ("pr_hub", "pr_hub_fix", "pr_pull"))
+                     / max(li.iterations, 1), 4)
+
+    layouts = None
+    if world == 1:
+        layouts = {"gather_ms_per_sweep": layout_sweep_ms(mg.PR_LAYOUT_GATHER),
+                   "segmented_ms_per_sweep": layout_sweep_ms(mg.PR_LAYOUT_SEGMENTED),
+                   "default": "gather"}
     dd = None
     if world == 1:
         dd = data_driven(TOL)
@@ -555,8 +569,8 @@ def main():
         dd["xd"], _ = g.pagerank(mg.PR_DATA, opts)
     batched = None if (args.no_batch or world > 1) else batch_report(mg, local)
     peak, peak_kind = peaks()
-    # one PageRank sweep = the hub kernel (shared-memory gathers), its
-    # carry fix-up and the tail sweep (L2 gathers), launched back to back
+    # one PageRank sweep of the default (gather) layout = k_pr_light; the
+    # segmented layout's kernels (k_hub_sweep, k_hub_fix) would be summed in
     sweep = kt.get("pr_pull", [1, 0.0])
     nsw = max(sweep[0], 1)
     parts = {k: kt[k][1] / nsw for k in ("pr_hub", "pr_hub_fix", "pr_pull") if k in kt}
@@ -607,10 +621,11 @@ def main():
         "errors": errors,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": (achieved / peak) if achieved else None, "traffic": traffic,
-                     "kernel": "PageRank sweep: k_hub_sweep + k_hub_fix + k_pr_light", "algorithmic_bytes": alg_bytes,
+                     "kernel": "PageRank pull sweep k_pr_light (gather layout)", "algorithmic_bytes": alg_bytes,
                      "avg_launch_ms": avg_ms, "parts_ms": parts, "peak_kind": peak_kind,
                      "kernel_share": (avg_ms * nsw / total_ms) if total_ms else None},
         "pagerank_data_driven": dd,
+        "pagerank_layouts": layouts,
         "cpu_baseline": cpu,
         "clocks": clk,
         "gpu_launches": launches,

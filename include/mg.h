@@ -175,8 +175,13 @@ typedef struct mg_opts {
     float damping;         /* PageRank d (0.85)                                */
     float tol;             /* PageRank tolerance                               */
     int32_t profile;       /* 1: host loop with cudaEvents around each kernel  */
-    int32_t reserved[8];
+    int32_t pr_layout;     /* PageRank pull sweep over unweighted graphs:      */
+                           /* MG_PR_LAYOUT_GATHER (L2 gathers, default) or     */
+                           /* MG_PR_LAYOUT_SEGMENTED (shared-memory segments)  */
+    int32_t reserved[7];
 } mg_opts;
+
+enum { MG_PR_LAYOUT_GATHER = 0, MG_PR_LAYOUT_SEGMENTED = 1 };
 
 /* Fill *o with the defaults (exec graph, auto direction, tuned thresholds). */
 void mg_opts_default(mg_opts *o);

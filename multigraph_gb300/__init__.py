@@ -33,6 +33,7 @@ LOAD_SYM, LOAD_NSYM, LOAD_CC = 1, 2, 4
 EXEC_GRAPH, EXEC_HOST = 0, 1
 DIR_AUTO, DIR_PUSH, DIR_PULL = 0, 1, 2
 PR_TOPOLOGY_REF, PR_DATA_REF, PR_TOPOLOGY, PR_DATA = 0, 1, 2, 3
+PR_LAYOUT_GATHER, PR_LAYOUT_SEGMENTED = 0, 1
 ALGO_BFS, ALGO_SSSP, ALGO_BC, ALGO_CC, ALGO_PR = range(5)
 IUNUSED = 0x64646464
 
@@ -46,7 +47,10 @@ class MGError(RuntimeError):
 class Opts(C.Structure):
     _fields_ = [("exec", C.c_int32), ("direction", C.c_int32), ("max_iter", C.c_int32), ("alpha", C.c_int32),
                 ("beta", C.c_int32), ("damping", C.c_float), ("tol", C.c_float), ("profile", C.c_int32),
-                ("reserved", C.c_int32 * 8)]
+                ("pr_layout", C.c_int32), ("reserved", C.c_int32 * 7)]
+
+
+_OPT_FIELDS = frozenset(name for name, _ in Opts._fields_ if name != "reserved")
 
 
 class KernelTime(C.Structure):
@@ -187,6 +191,8 @@ def default_opts(**kw) -> Opts:
     o = Opts()
     lib.mg_opts_default(C.byref(o))
     for k, v in kw.items():
+        if k not in _OPT_FIELDS:
+            raise TypeError(f"unknown mg_opts field {k!r}")
         setattr(o, k, v)
     return o
 
@@ -337,6 +343,8 @@ class Graph:
     def _opts(opts, kw):
         o = opts if opts is not None else default_opts()
         for k, v in kw.items():
+            if k not in _OPT_FIELDS:
+                raise TypeError(f"unknown mg_opts field {k!r}")
             setattr(o, k, v)
         return o
 

@@ -1023,7 +1023,7 @@ static mg_status pr_loop(mg_graph *g, PArgs &a, const mg_opts &opt, const char *
     return MG_OK;
 }
 
-static mg_status pr_setup(mg_graph *g, PArgs &a, bool weighted_or_adj)
+static mg_status pr_setup(mg_graph *g, PArgs &a, bool weighted_or_adj, int32_t layout = MG_PR_LAYOUT_GATHER)
 {
     if (!g->pws) g->pws = new PrWS();
     PrWS *w = g->pws;
@@ -1065,7 +1065,7 @@ static mg_status pr_setup(mg_graph *g, PArgs &a, bool weighted_or_adj)
     a.queue[1] = w->q1.as<int32_t>();
     a.qval = w->qval.as<float>();
     a.m = g->ne;
-    if (!weighted_or_adj) {
+    if (!weighted_or_adj && layout == MG_PR_LAYOUT_SEGMENTED) {
         MG_TRY(hub_prepare(g));
         if (g->hub.use) {
             a.prow = g->hub.toff.as<int32_t>();
@@ -1126,8 +1126,10 @@ mg_status mg_pagerank(mg_graph *g, int32_t variant, const mg_opts *o, float *ran
     mg_opts opt;
     MG_TRY(begin_run(g, o, opt, info));
     if (variant < 0 || variant > 3) return fail(MG_ERR_INVALID, "unknown PageRank variant %d", variant);
+    if (opt.pr_layout != MG_PR_LAYOUT_GATHER && opt.pr_layout != MG_PR_LAYOUT_SEGMENTED)
+        return fail(MG_ERR_INVALID, "unknown PageRank layout %d", opt.pr_layout);
     PArgs a;
-    MG_TRY(pr_setup(g, a, false));
+    MG_TRY(pr_setup(g, a, false, opt.pr_layout));
     cudaStream_t s = g->stream;
     const int grid = a.nblocks;
     const bool ref = variant == MG_PR_TOPOLOGY_REF || variant == MG_PR_DATA_REF;

@@ -26,9 +26,10 @@ def _all(g, og, src):
     rlv, rsg, rdl = O.bc_f64(og, src)
     assert np.array_equal(blv, rlv) and np.array_equal(sg, rsg)
     assert np.allclose(dl, rdl, rtol=1e-5, atol=1e-6)
-    x, info = g.pagerank(mg.PR_TOPOLOGY, tol=1e-6)
-    ref, _ = O.pr_norm_f64(og, 0.85, 1e-6, info.iterations)
-    assert float(np.max(np.abs(x.astype(np.float64) - ref))) < 1e-6
+    for layout in (mg.PR_LAYOUT_GATHER, mg.PR_LAYOUT_SEGMENTED):
+        x, info = g.pagerank(mg.PR_TOPOLOGY, tol=1e-6, pr_layout=layout)
+        ref, _ = O.pr_norm_f64(og, 0.85, 1e-6, info.iterations)
+        assert float(np.max(np.abs(x.astype(np.float64) - ref))) < 1e-6, layout
     bc, _ = g.bc_multi([src, src])
     assert np.allclose(bc, O.bc_multi_f64(og, [src, src]), rtol=1e-5, atol=1e-5)
 

@@ -162,30 +162,33 @@ def test_sssp_small_and_zero_weights(direction, wmax):
     g.free()
 
 
+@pytest.mark.parametrize("layout", ["gather", "segmented"])
 @pytest.mark.parametrize("scale", [17, 18])
-def test_pagerank_hub_split(scale):
-    """Graphs with more vertices than the shared-memory hub segment holds:
-    each sweep sums the hub part of every row from shared memory and the
-    tail part through L2 (heavy rows in chunks of both).  Every form against
-    the oracle; the sums are formed in a fixed order, so two runs agree
-    bit for bit, in graph and host loops alike."""
+def test_pagerank_hub_split(scale, layout):
+    """Graphs with more vertices than one shared-memory segment holds, in
+    both pull layouts: L2 gathers over degree bins, and segments (each
+    sweep sums every row's per-segment parts from shared memory, heavy rows
+    in chunks).  Every form against the oracle; the sums are formed in a
+    fixed order, so two runs agree bit for bit, in graph and host loops
+    alike."""
     h = mg.HostGraph.rmat(scale, 16, seed=scale)
     rp, col, wt = h.arrays()
     og = O.csr_from_arrays(rp, col, wt)
     g = mg.Graph(h)
+    lay = mg.PR_LAYOUT_SEGMENTED if layout == "segmented" else mg.PR_LAYOUT_GATHER
     try:
         assert og.nv > 60000
-        x, info = g.pagerank(mg.PR_TOPOLOGY, tol=1e-6)
+        x, info = g.pagerank(mg.PR_TOPOLOGY, tol=1e-6, pr_layout=lay)
         ref, _ = O.pr_norm_f64(og, 0.85, 1e-6, info.iterations)
         assert float(np.max(np.abs(x.astype(np.float64) - ref))) < 1e-6
-        x2, _ = g.pagerank(mg.PR_TOPOLOGY, tol=1e-6)
-        x3, _ = g.pagerank(mg.PR_TOPOLOGY, tol=1e-6, exec=mg.EXEC_HOST)
+        x2, _ = g.pagerank(mg.PR_TOPOLOGY, tol=1e-6, pr_layout=lay)
+        x3, _ = g.pagerank(mg.PR_TOPOLOGY, tol=1e-6, exec=mg.EXEC_HOST, pr_layout=lay)
         assert np.array_equal(x, x2) and np.array_equal(x, x3)
-        xd, _ = g.pagerank(mg.PR_DATA, tol=1e-6)
+        xd, _ = g.pagerank(mg.PR_DATA, tol=1e-6, pr_layout=lay)
         exact, _ = O.pr_norm_f64(og, 0.85, 1e-11, 500)
         assert float(np.max(np.abs(xd.astype(np.float64) - exact))) < 1e-6
         for variant, mode in [(mg.PR_TOPOLOGY_REF, 0), (mg.PR_DATA_REF, 1)]:
-            xr, _ = g.pagerank(variant)
+            xr, _ = g.pagerank(variant, pr_layout=lay)
             rr, _ = O.pr_ref_f64(og, mode)
             assert float(np.max(np.abs(xr - rr) / np.maximum(np.abs(rr), 1e-12))) < 0.05, variant
     finally:
