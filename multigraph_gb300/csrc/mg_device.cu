@@ -392,13 +392,13 @@ __global__ void k_pos_rows(int32_t n, int32_t m, const int32_t *row_new, int32_t
 
 constexpr int RELABEL_ILP = 4;
 
-// caller position of this lane's position 32c + lane (-1 past the end)
-__device__ __forceinline__ void caller_positions(int32_t n, int32_t m, const int32_t *new2old, const int32_t *o_row,
-                                                 const int32_t *row_new, const int32_t *pos_row, int32_t c0,
-                                                 int32_t (&q)[RELABEL_ILP], int32_t (&crow)[RELABEL_ILP])
+// engine row rr and its start st of this lane's position 32c + lane, for
+// RELABEL_ILP consecutive 32-position steps from c0
+__device__ __forceinline__ void engine_rows(int32_t m, const int32_t *row_new, const int32_t *pos_row, int32_t c0,
+                                            int32_t (&rr)[RELABEL_ILP], int32_t (&st)[RELABEL_ILP])
 {
     const int lane = threadIdx.x & 31;
-    int32_t ra[RELABEL_ILP], rb[RELABEL_ILP], w[RELABEL_ILP], rr[RELABEL_ILP], st[RELABEL_ILP];
+    int32_t ra[RELABEL_ILP], rb[RELABEL_ILP], w[RELABEL_ILP];
     const int32_t nsteps = (m + 31) / 32;
 #pragma unroll
     for (int j = 0; j < RELABEL_ILP; j++) {
@@ -421,14 +421,28 @@ __device__ __forceinline__ void caller_positions(int32_t n, int32_t m, const int
             st[j] = __ldg(&row_new[rr[j]]);
         }
     }
+}
+
+// Caller position of every engine position (once per layout): engine row
+// r holds caller row new2old[r]'s edges in caller order, so position p of
+// row r comes from o_row[new2old[r]] + (p - row_new[r]).
+__global__ void k_caller_pos(int32_t m, const int32_t *new2old, const int32_t *o_row, const int32_t *row_new,
+                             const int32_t *pos_row, int32_t *cpos)
+{
+    const int lane = threadIdx.x & 31;
+    const int32_t nsteps = (m + 31) / 32;
+    const int32_t gwarp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int32_t nwarps = (gridDim.x * blockDim.x) >> 5;
+    for (int32_t c0 = gwarp * RELABEL_ILP; c0 < nsteps; c0 += nwarps * RELABEL_ILP) {
+        int32_t rr[RELABEL_ILP], st[RELABEL_ILP];
+        engine_rows(m, row_new, pos_row, c0, rr, st);
 #pragma unroll
-    for (int j = 0; j < RELABEL_ILP; j++) rr[j] = __ldg(&new2old[rr[j]]);
+        for (int j = 0; j < RELABEL_ILP; j++) rr[j] = __ldg(&new2old[rr[j]]);
 #pragma unroll
-    for (int j = 0; j < RELABEL_ILP; j++) crow[j] = rr[j];
-#pragma unroll
-    for (int j = 0; j < RELABEL_ILP; j++) {
-        const int32_t p = (c0 + j) * 32 + lane;
-        q[j] = (c0 + j < nsteps && p < m) ? __ldg(&o_row[rr[j]]) + (p - st[j]) : -1;
+        for (int j = 0; j < RELABEL_ILP; j++) {
+            const int32_t p = (c0 + j) * 32 + lane;
+            if (c0 + j < nsteps && p < m) cpos[p] = __ldg(&o_row[rr[j]]) + (p - st[j]);
+        }
     }
 }
 
@@ -479,20 +493,28 @@ static int32_t wmin_decode(unsigned long long enc)
     return enc == ~0ull ? 0 : (int32_t)((long long)enc + INT32_MIN);
 }
 
-// caller CSR -> engine CSR for up to two 4-byte edge arrays; the first is
-// mapped through old2new when map_ids (column ids).  With sums, the
-// symmetry checksum of (caller row, caller column, second array) is formed
-// on the way, the least second-array value (the weights) in sums[3], and
-// sums[4] != 0 when some engine column id differs from the one it replaces.
-// A non-zero *skip (caller row offsets that differ from the
-// layout's, found by k_rows_differ earlier on the stream) returns at once:
-// the positions would not match the staged arrays.
-__global__ void k_relabel_edges(int32_t n, int32_t m, const int32_t *new2old, const int32_t *old2new,
-                                const int32_t *o_row, const int32_t *row_new, const int32_t *pos_row,
-                                const uint32_t *src0, uint32_t *dst0, const uint32_t *src1, uint32_t *dst1,
-                                int map_ids, unsigned long long *sums, const unsigned long long *skip)
+// caller CSR -> engine CSR for up to two 4-byte edge arrays through the
+// caller-position table; the first is mapped through old2new when map_ids
+// (column ids).  kSums: the symmetry checksum of (engine row, engine column,
+// second array) is formed on the way (the relabel is a bijection, so the
+// engine graph is symmetric exactly when the caller's is), the least
+// second-array value (the weights) in sums[3], and sums[4] != 0 when some
+// engine column id differs from the one it replaces.  A non-zero *skip
+// (caller row offsets that differ from the layout's, found by
+// k_rows_differ earlier on the stream) returns at once: the positions would
+// not match the staged arrays.  Every load of a step is issued before its
+// stores; the only dependent load is the old2new gather.
+template <bool kSums>
+__global__ void __launch_bounds__(256) k_relabel_edges(int32_t m, const int32_t *__restrict__ old2new,
+                                                       const int32_t *__restrict__ row_new,
+                                                       const int32_t *__restrict__ pos_row,
+                                                       const int32_t *__restrict__ cpos,
+                                                       const uint32_t *__restrict__ src0, uint32_t *__restrict__ dst0,
+                                                       const uint32_t *__restrict__ src1, uint32_t *__restrict__ dst1,
+                                                       int map_ids, unsigned long long *sums,
+                                                       const unsigned long long *skip)
 {
-    if (skip && __ldcg(skip) != 0ull) return;
+    if (kSums && skip && __ldcg(skip) != 0ull) return;
     const int lane = threadIdx.x & 31;
     const int32_t nsteps = (m + 31) / 32;
     const int32_t gwarp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -501,35 +523,42 @@ __global__ void k_relabel_edges(int32_t n, int32_t m, const int32_t *new2old, co
     int32_t wlo = INT32_MAX;
     int changed = 0;
     for (int32_t c0 = gwarp * RELABEL_ILP; c0 < nsteps; c0 += nwarps * RELABEL_ILP) {
-        int32_t q[RELABEL_ILP], u[RELABEL_ILP];
-        caller_positions(n, m, new2old, o_row, row_new, pos_row, c0, q, u);
-        uint32_t x[RELABEL_ILP], y[RELABEL_ILP];
+        int32_t q[RELABEL_ILP], rr[RELABEL_ILP], st[RELABEL_ILP];
+        uint32_t x[RELABEL_ILP], y[RELABEL_ILP], old[RELABEL_ILP];
 #pragma unroll
         for (int j = 0; j < RELABEL_ILP; j++) {
-            x[j] = q[j] >= 0 ? __ldg(&src0[q[j]]) : 0u;
-            y[j] = (q[j] >= 0 && dst1) ? __ldg(&src1[q[j]]) : 0u;
+            const int32_t p = (c0 + j) * 32 + lane;
+            q[j] = (c0 + j < nsteps && p < m) ? __ldcs(&cpos[p]) : -1;
         }
-        if (sums) {
+        if (kSums) engine_rows(m, row_new, pos_row, c0, rr, st);
 #pragma unroll
-            for (int j = 0; j < RELABEL_ILP; j++)
-                if (q[j] >= 0) {
-                    sym_add(s_lo, s_hi, u[j], (int32_t)x[j], y[j]);
-                    if (dst1) wlo = min(wlo, (int32_t)y[j]);
-                }
+        for (int j = 0; j < RELABEL_ILP; j++) {
+            const int32_t p = (c0 + j) * 32 + lane;
+            x[j] = q[j] >= 0 ? __ldcs(&src0[q[j]]) : 0u;
+            y[j] = (q[j] >= 0 && dst1) ? __ldcs(&src1[q[j]]) : 0u;
+            old[j] = (kSums && q[j] >= 0) ? __ldcs(&dst0[p]) : 0u;
         }
 #pragma unroll
         for (int j = 0; j < RELABEL_ILP; j++)
             if (q[j] >= 0 && map_ids) x[j] = (uint32_t)__ldg(&old2new[x[j]]);
+        if (kSums) {
+#pragma unroll
+            for (int j = 0; j < RELABEL_ILP; j++)
+                if (q[j] >= 0) {
+                    sym_add(s_lo, s_hi, rr[j], (int32_t)x[j], y[j]);
+                    if (dst1) wlo = min(wlo, (int32_t)y[j]);
+                    changed |= old[j] != x[j];
+                }
+        }
 #pragma unroll
         for (int j = 0; j < RELABEL_ILP; j++) {
             if (q[j] < 0) continue;
             const int32_t p = (c0 + j) * 32 + lane;
-            if (sums) changed |= __ldcs(&dst0[p]) != x[j];
-            dst0[p] = x[j];
-            if (dst1) dst1[p] = y[j];
+            __stcs(&dst0[p], x[j]);
+            if (dst1) __stcs(&dst1[p], y[j]);
         }
     }
-    if (sums) {
+    if (kSums) {
         sym_flush(sums, s_lo, s_hi);
         wmin_flush(&sums[3], wlo);
         if (__any_sync(0xffffffffu, changed) && lane == 0) atomicOr(&sums[4], 1ull);
@@ -567,20 +596,11 @@ __global__ void k_sym_check(int32_t n, const int32_t *row, const int32_t *col, c
 }
 
 // inverse of k_relabel_edges for per-edge payloads (engine order -> caller order)
-__global__ void k_unrelabel_edges(int32_t n, int32_t m, const int32_t *new2old, const int32_t *o_row,
-                                  const int32_t *row_new, const int32_t *pos_row, const uint32_t *src, uint32_t *dst)
+__global__ void k_unrelabel_edges(int32_t m, const int32_t *__restrict__ cpos, const uint32_t *__restrict__ src,
+                                  uint32_t *__restrict__ dst)
 {
-    const int lane = threadIdx.x & 31;
-    const int32_t nsteps = (m + 31) / 32;
-    const int32_t gwarp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int32_t nwarps = (gridDim.x * blockDim.x) >> 5;
-    for (int32_t c0 = gwarp * RELABEL_ILP; c0 < nsteps; c0 += nwarps * RELABEL_ILP) {
-        int32_t q[RELABEL_ILP], crow[RELABEL_ILP];
-        caller_positions(n, m, new2old, o_row, row_new, pos_row, c0, q, crow);
-#pragma unroll
-        for (int j = 0; j < RELABEL_ILP; j++)
-            if (q[j] >= 0) dst[q[j]] = __ldg(&src[(c0 + j) * 32 + lane]);
-    }
+    for (int32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < m; p += gridDim.x * blockDim.x)
+        dst[__ldcs(&cpos[p])] = __ldcs(&src[p]);
 }
 
 // caller-order result: dst[r*n + v] = src[r*n + old2new[v]]
@@ -626,7 +646,9 @@ __global__ void k_cc_label_old(int32_t n, const int32_t *parent, const int32_t *
 }
 
 // engine CSR (col, wt) from caller-order arrays with the current layout's
-// positions; the optional pair checksum and skip word as k_relabel_edges
+// positions; the optional pair checksum and skip word as k_relabel_edges.
+// The first call of a layout builds the position tables from src_row (the
+// layout's caller row offsets).
 static mg_status relabel_device(mg_graph *g, const mgi::DevBuf &src_row, const mgi::DevBuf &src_col,
                                 const mgi::DevBuf &src_wt, unsigned long long *sym_sums = nullptr,
                                 const unsigned long long *skip = nullptr)
@@ -635,14 +657,24 @@ static mg_status relabel_device(mg_graph *g, const mgi::DevBuf &src_row, const m
     const int grid = g->num_sms * 8;
     if (!g->pos_valid) {  // once per layout
         MG_TRY(dev_alloc(g->pos_row, ((size_t)g->ne / 32 + 2) * 4));
+        MG_TRY(dev_alloc(g->cpos, (size_t)g->ne * 4));
         k_pos_rows<<<grid, 256, 0, g->stream>>>(g->nv, g->ne, g->row.as<int32_t>(), g->pos_row.as<int32_t>());
+        k_caller_pos<<<grid, 256, 0, g->stream>>>(g->ne, g->new2old.as<int32_t>(), src_row.as<int32_t>(),
+                                                  g->row.as<int32_t>(), g->pos_row.as<int32_t>(),
+                                                  g->cpos.as<int32_t>());
+        MG_CUDA(cudaGetLastError());
         g->pos_valid = true;
     }
-    k_relabel_edges<<<grid, 256, 0, g->stream>>>(g->nv, g->ne, g->new2old.as<int32_t>(), g->old2new.as<int32_t>(),
-                                                 src_row.as<int32_t>(), g->row.as<int32_t>(),
-                                                 g->pos_row.as<int32_t>(), src_col.as<uint32_t>(),
-                                                 g->col.as<uint32_t>(), src_wt.as<uint32_t>(), g->wt.as<uint32_t>(),
-                                                 1, sym_sums, skip);
+    if (sym_sums)
+        k_relabel_edges<true><<<grid, 256, 0, g->stream>>>(
+            g->ne, g->old2new.as<int32_t>(), g->row.as<int32_t>(), g->pos_row.as<int32_t>(), g->cpos.as<int32_t>(),
+            src_col.as<uint32_t>(), g->col.as<uint32_t>(), src_wt.as<uint32_t>(), g->wt.as<uint32_t>(), 1, sym_sums,
+            skip);
+    else
+        k_relabel_edges<false><<<grid, 256, 0, g->stream>>>(
+            g->ne, g->old2new.as<int32_t>(), g->row.as<int32_t>(), g->pos_row.as<int32_t>(), g->cpos.as<int32_t>(),
+            src_col.as<uint32_t>(), g->col.as<uint32_t>(), src_wt.as<uint32_t>(), g->wt.as<uint32_t>(), 1, nullptr,
+            nullptr);
     MG_CUDA(cudaGetLastError());
     return MG_OK;
 }
@@ -723,11 +755,9 @@ mg_status edges_to_engine(mg_graph *g, const void *src_caller, void *dst_engine)
         return MG_OK;
     }
     if (g->ne == 0) return MG_OK;
-    k_relabel_edges<<<g->num_sms * 8, 256, 0, g->stream>>>(g->nv, g->ne, g->new2old.as<int32_t>(), nullptr,
-                                                           g->o_row.as<int32_t>(), g->row.as<int32_t>(),
-                                                           g->pos_row.as<int32_t>(), (const uint32_t *)src_caller,
-                                                           (uint32_t *)dst_engine, nullptr, nullptr, 0, nullptr,
-                                                           nullptr);
+    k_relabel_edges<false><<<g->num_sms * 8, 256, 0, g->stream>>>(
+        g->ne, g->old2new.as<int32_t>(), g->row.as<int32_t>(), g->pos_row.as<int32_t>(), g->cpos.as<int32_t>(),
+        (const uint32_t *)src_caller, (uint32_t *)dst_engine, nullptr, nullptr, 0, nullptr, nullptr);
     MG_CUDA(cudaGetLastError());
     return MG_OK;
 }
@@ -739,10 +769,8 @@ mg_status edges_to_caller(mg_graph *g, const void *src_engine, void *dst_caller)
         return MG_OK;
     }
     if (g->ne == 0) return MG_OK;
-    k_unrelabel_edges<<<g->num_sms * 8, 256, 0, g->stream>>>(g->nv, g->ne, g->new2old.as<int32_t>(),
-                                                             g->o_row.as<int32_t>(), g->row.as<int32_t>(),
-                                                             g->pos_row.as<int32_t>(), (const uint32_t *)src_engine,
-                                                             (uint32_t *)dst_caller);
+    k_unrelabel_edges<<<g->num_sms * 8, 256, 0, g->stream>>>(g->ne, g->cpos.as<int32_t>(),
+                                                             (const uint32_t *)src_engine, (uint32_t *)dst_caller);
     MG_CUDA(cudaGetLastError());
     return MG_OK;
 }
@@ -856,7 +884,7 @@ static void destroy_graph(mg_graph *g)
     DevBuf *bufs[] = {&g->row, &g->col, &g->wt, &g->trow_own, &g->tcol_own, &g->twt_own,
                       &g->hchunk, &g->hrows, &g->hrow_chunk, &g->fw, &g->o_fw, &g->ppr_hchunk, &g->ppr_hrows,
                       &g->ppr_hrow_chunk, &g->o_row, &g->o_col, &g->o_wt, &g->old2new, &g->new2old,
-                      &g->wrows, &g->trows, &g->pos_row, &g->sym_sums, &g->s_row,
+                      &g->wrows, &g->trows, &g->pos_row, &g->cpos, &g->sym_sums, &g->s_row,
                       &g->s_col, &g->s_wt};
     for (DevBuf *b : bufs) dev_free(*b);
     for (DevBuf &b : g->res_out) dev_free(b);

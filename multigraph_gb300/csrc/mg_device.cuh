@@ -188,6 +188,7 @@ struct mg_graph {
     mgi::DevBuf o_fw;                      // float weights in caller CSR order
     mgi::DevBuf old2new, new2old;          // int32 [nv]
     mgi::DevBuf pos_row;                   // int32 [ne/32 + 2]: engine row of position 32k
+    mgi::DevBuf cpos;                      // int32 [ne]: caller position of each engine position
     bool pos_valid = false;                // pos_row follows the current row offsets
     std::vector<int32_t> h_old2new;        // host copy for mapping sources
     mgi::DevBuf res_out[8];                // results in the caller's ids
