@@ -183,6 +183,31 @@ def build_graph(scale):
     return mg.HostGraph.rmat(scale, EDGE_FACTOR, seed=scale)
 
 
+def torus_plus_rmat(side, scale, seed):
+    """A side x side torus (4-regular: the uniform start is its fixed point)
+    plus a disjoint R-MAT component without isolated vertices, as one host
+    graph: the workload on which data-driven PageRank's queue sweeps run."""
+    import numpy as np
+    import multigraph_gb300 as mg
+    n_t = side * side
+    v = np.arange(n_t, dtype=np.int64)
+    r, c = v // side, v % side
+    src = [v, v]
+    dst = [r * side + (c + 1) % side, ((r + 1) % side) * side + c]
+    hr = mg.HostGraph.rmat(scale, 16, seed=seed)
+    rp, col, _ = hr.arrays()
+    hr.free()
+    rows = np.repeat(np.arange(len(rp) - 1), np.diff(rp))
+    keep = np.flatnonzero(np.diff(rp) > 0)
+    newid = np.full(len(rp) - 1, -1, np.int64)
+    newid[keep] = np.arange(len(keep))
+    up = rows < col
+    src.append(n_t + newid[rows[up]])
+    dst.append(n_t + newid[col[up]])
+    return mg.HostGraph.from_entries(n_t + len(keep), np.concatenate(src).astype(np.int32),
+                                     np.concatenate(dst).astype(np.int32))
+
+
 def cpu_oracle_step(og):
     """One step of the oracle's restatement of validate.cu on this host:
     Bellman-Ford SSSP from 0 (validate.cu:131-148) and FP64 normalised
@@ -562,9 +587,45 @@ def main():
         layouts = {"gather_ms_per_sweep": layout_sweep_ms(mg.PR_LAYOUT_GATHER),
                    "segmented_ms_per_sweep": layout_sweep_ms(mg.PR_LAYOUT_SEGMENTED),
                    "default": "gather"}
+    # data-driven PageRank where the queue sweeps engage: 2048 x 2048 torus
+    # + R-MAT 14 (active in-edges ~1 % of m after the first sweeps)
+    def mixed_data_driven(tol=1e-8):
+        hm = torus_plus_rmat(2048, 14, 14)
+        gm = mg.Graph(hm, local)
+        try:
+            o = mg.default_opts(tol=tol, damping=DAMPING)
+            gm.pagerank(mg.PR_DATA, o, out=False)   # warm-up (captures the loop)
+            gm.pagerank(mg.PR_TOPOLOGY, o, out=False)
+            # whole runs in the captured loop (cudaEvents around each run)
+            _, dgi = gm.pagerank(mg.PR_DATA, o, out=False)
+            _, tgi = gm.pagerank(mg.PR_TOPOLOGY, o, out=False)
+            o.profile = 1
+            _, mi = gm.pagerank(mg.PR_DATA, o, out=False)
+            mkt = mi.kernel_times()
+            dense = sum(mkt.get(k, (0, 0.0))[1] for k in ("pr_pull", "pr_pull_apply"))
+            queue = sum(mkt.get(k, (0, 0.0))[1] for k in ("prd_compact", "prd_gather", "prd_apply"))
+            nq = mi.iterations - mi.pull_iterations
+            o.profile = 0
+            o2 = mg.default_opts(tol=tol, damping=DAMPING, profile=1)
+            _, ti = gm.pagerank(mg.PR_TOPOLOGY, o2, out=False)
+            tkt = ti.kernel_times()
+            topo = sum(tkt.get(k, (0, 0.0))[1] for k in ("pr_pull", "pr_pull_apply"))
+            return {"workload": f"torus 2048x2048 + rmat14 (nv {gm.nv}, ne {gm.ne}), L1 tol {tol}",
+                    "sweeps": mi.iterations, "dense_sweeps": mi.pull_iterations, "queue_sweeps": nq,
+                    "dense_ms_per_sweep": round(dense / max(mi.pull_iterations, 1), 4),
+                    "queue_ms_per_sweep": round(queue / nq, 4) if nq else None,
+                    "per_kernel_timing": "cudaEvents around every launch of a host-driven loop",
+                    "data_driven_run_ms": round(dgi.device_ms, 3),
+                    "topology_driven": {"sweeps": ti.iterations, "run_ms": round(tgi.device_ms, 3),
+                                        "ms_per_sweep": round(topo / max(ti.iterations, 1), 4)}}
+        finally:
+            gm.free()
+            hm.free()
+
     dd = None
     if world == 1:
         dd = data_driven(TOL)
+        dd["queue_workload"] = mixed_data_driven()
         dd["loose_tolerance"] = data_driven(1e-3)
         dd["xd"], _ = g.pagerank(mg.PR_DATA, opts)
     batched = None if (args.no_batch or world > 1) else batch_report(mg, local)
@@ -578,10 +639,18 @@ def main():
     alg_bytes = 4 * m + 4 * (n + 1) + 12 * n
     achieved = alg_bytes / (avg_ms / 1e3) / 1e9 if avg_ms > 0 else None
     traffic = None
+    l2 = None
     try:
         with open(os.path.join(ROOT, "profiles", "pr_sweep_traffic.json")) as f:
             tr = json.load(f)
         traffic = tr["dram_bytes_per_edge"] * m + tr["dram_bytes_per_vertex"] * n
+        # the sweep's other bound: the L2-resident contribution gathers
+        l2 = {"lts_throughput_frac": tr["lts_throughput_pct_of_peak"] / 100.0,
+              "l2_sector_hit_rate": tr["lts_t_sector_hit_rate_pct"] / 100.0,
+              "l1_sector_hit_rate": tr["l1tex_t_sector_hit_rate_pct"] / 100.0,
+              "source": "ncu, one sweep launch at R-MAT 21 (profiles/pr_sweep_rmat21.md)"}
+        if avg_ms > 0 and args.scale == 22:   # the floor was measured on this graph
+            l2["gather_floor_frac"] = tr["gather_floor_us_rmat22"] / 1e3 / avg_ms
     except Exception:
         pass
     total_ms = sum(v[1] for v in kt.values())
@@ -623,7 +692,7 @@ def main():
                      "frac": (achieved / peak) if achieved else None, "traffic": traffic,
                      "kernel": "PageRank pull sweep k_pr_light (gather layout)", "algorithmic_bytes": alg_bytes,
                      "avg_launch_ms": avg_ms, "parts_ms": parts, "peak_kind": peak_kind,
-                     "kernel_share": (avg_ms * nsw / total_ms) if total_ms else None},
+                     "kernel_share": (avg_ms * nsw / total_ms) if total_ms else None, "l2": l2},
         "pagerank_data_driven": dd,
         "pagerank_layouts": layouts,
         "cpu_baseline": cpu,

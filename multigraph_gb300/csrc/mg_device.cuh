@@ -334,55 +334,47 @@ struct WarpStage {
 };
 
 // Grid-wide barrier for persistent kernels launched cooperatively (every
-// block resident).  Two levels so that no counter sees more than a few
-// dozen arrivals: block b arrives on counter 2 + (b % GRID_SYNC_GROUPS); the
-// last arrival of a group arrives on bar[0]; the last of those resets
-// bar[0] and bumps the generation bar[1], on which every other block waits.
-// bar holds 2 + GRID_SYNC_GROUPS words, zero before the launch.  The fences
-// on both sides order every block's writes before the barrier against every
-// block's reads after it.  The wait is bounded: after GRID_SYNC_LIMIT cycles
-// (about 2 s) the block sets *err and the barrier returns false, so a broken
-// launch ends with an error status instead of a hang; callers return at
-// once on false.
+// block resident).  bar[0] counts arrivals and only grows: a block's
+// arrival returns the count before it, so its barrier is the one that
+// completes when the count reaches the next multiple of gridDim.x, and the
+// block waits for that (a block that has already left and arrives at the
+// next barrier only raises the count further).  One atomic per block and a
+// polled load, with no reset on the critical path (a two-level counter with
+// resets and a generation word took about twice as long per barrier).  bar
+// is zero before the launch, and every launch on it uses the same grid.
+// The fences on both sides order every block's writes before the barrier
+// against every block's reads after it.  The wait is bounded: after
+// GRID_SYNC_LIMIT cycles (about 2 s) the block sets *err and the barrier
+// returns false, so a broken launch ends with an error status instead of a
+// hang; callers return at once on false.
 constexpr long long GRID_SYNC_LIMIT = 4000000000ll;
 constexpr long long GRID_SYNC_TEST_LIMIT = 20000000ll;  // ~10 ms: the injected-failure wait
-constexpr unsigned GRID_SYNC_GROUPS = 32;
+constexpr unsigned GRID_SYNC_GROUPS = 32;               // words reserved after the counter
 
-// `never` (failure injection, MG_FAIL_BARRIER): no block counts as the last
-// arrival, so every block waits out GRID_SYNC_TEST_LIMIT and the barrier
-// fails the way a lost block would make it fail.
+// `never` (failure injection, MG_FAIL_BARRIER): every block waits for one
+// more grid's worth of arrivals than will come, so every block waits out
+// GRID_SYNC_TEST_LIMIT and the barrier fails the way a lost block would
+// make it fail.
 __device__ __forceinline__ bool grid_sync(unsigned *bar, int *err, int never = 0)
 {
     __shared__ int s_ok;
     __syncthreads();
     if (threadIdx.x == 0) {
-        volatile unsigned *gen = bar + 1;
-        const unsigned g0 = *gen;
-        const unsigned grp = blockIdx.x % GRID_SYNC_GROUPS;
-        const unsigned ngroups = min(gridDim.x, GRID_SYNC_GROUPS);
-        const unsigned in_grp = (gridDim.x - grp + GRID_SYNC_GROUPS - 1) / GRID_SYNC_GROUPS;
+        const unsigned G = gridDim.x;
         __threadfence();
-        int ok = 1;
-        bool last = false;
-        if (atomicAdd(&bar[2 + grp], 1u) == in_grp - 1 && !never) {
-            atomicExch(&bar[2 + grp], 0u);
-            last = atomicAdd(&bar[0], 1u) == ngroups - 1;
-        }
+        const unsigned before = atomicAdd(&bar[0], 1u);
+        const unsigned target = (before / G + 1u + (never ? 1u : 0u)) * G;
+        const volatile unsigned *count = bar;
         const long long limit = never ? GRID_SYNC_TEST_LIMIT : GRID_SYNC_LIMIT;
-        if (last) {
-            atomicExch(&bar[0], 0u);
-            __threadfence();
-            atomicAdd(&bar[1], 1u);
-        } else {
-            const long long t0 = clock64();
-            while (*gen == g0) {
-                if (clock64() - t0 > limit) {
-                    ok = 0;
-                    atomicExch(err, 1);
-                    break;
-                }
-                __nanosleep(32);
+        int ok = 1;
+        const long long t0 = clock64();
+        while ((int)(*count - target) < 0) {
+            if (clock64() - t0 > limit) {
+                ok = 0;
+                atomicExch(err, 1);
+                break;
             }
+            __nanosleep(16);
         }
         __threadfence();
         s_ok = ok && *(volatile int *)err == 0;

@@ -100,6 +100,7 @@ struct PArgs {
     float *hpart;            // heavy chunk partial sums
     double *bpart;           // per-block partials: [NPART*slots] (resid, dangling, any, active edges, frozen dangling)
     int32_t nblocks;
+    int32_t qblocks;          // grid of the queue sweeps (k_prd_gather / k_prd_apply)
     PCtl *ctl;
     // data-driven frontier sweeps: the full pull rows (the hub split keeps
     // only the tail in prow / pcol), two queues, the queue sweep's new values
@@ -654,7 +655,7 @@ __global__ void __launch_bounds__(THREADS) k_prd_apply(PArgs a, cudaGraphConditi
     if (!last_block(cp)) return;
     double T[NPART - 1];
     int A;
-    reduce_slots(a.bpart, 0, a.nblocks, T, A);
+    reduce_slots(a.bpart, 0, gridDim.x, T, A);
     if (threadIdx.x == 0) {
         cp->done = 0;
         cp->iter = c.iter + 1;
@@ -993,10 +994,10 @@ static mg_status pr_loop(mg_graph *g, PArgs &a, const mg_opts &opt, const char *
             k_prd_compact<<<grid, THREADS, 0, st>>>(a);
             P.end();
             P.begin(sqg);
-            k_prd_gather<<<grid, THREADS, 0, st>>>(a);
+            k_prd_gather<<<a.qblocks, THREADS, 0, st>>>(a);
             P.end();
             P.begin(sqa);
-            k_prd_apply<<<grid, THREADS, 0, st>>>(a, h, use_cond);
+            k_prd_apply<<<a.qblocks, THREADS, 0, st>>>(a, h, use_cond);
             P.end();
         }
         MG_CUDA(cudaGetLastError());
@@ -1058,6 +1059,10 @@ static mg_status pr_setup(mg_graph *g, PArgs &a, bool weighted_or_adj, int32_t l
     a.hpart = w->hpart.as<float>();
     a.bpart = w->bpart.as<double>();
     a.nblocks = grid;
+    // queue sweeps run while the active in-edges are below m / SPARSE_ALPHA:
+    // two blocks per SM keep their block partials and the last block's
+    // reduction small
+    a.qblocks = std::min(grid, 2 * g->num_sms);
     a.ctl = w->ctl.as<PCtl>();
     a.frow = g->trow;
     a.fcol = g->tcol;
