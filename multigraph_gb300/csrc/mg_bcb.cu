@@ -168,6 +168,127 @@ __global__ void __launch_bounds__(THREADS) k_bbb_next(BbArgs a, cudaGraphConditi
     if (use_cond) cudaGraphSetConditional(h, more ? 1u : 0u);
 }
 
+// ---------------------------------------------------------------------------
+// Persistent sweeps for low-degree graphs (lattices, road networks): their
+// thousands of levels hold a few thousand entries each, so a level's
+// launches cost more than its work.  One cooperative launch (every block
+// resident) runs consecutive sparse forward levels -- mark | barrier | pull
+// | barrier | heavy | barrier | compact | barrier, then every block decides
+// the next level on its own copy of the loop state from the level's
+// counters (the same inputs give the same decision everywhere) -- until
+// the sweep ends or the direction test picks a dense level, which the
+// per-level kernels above then run.  Another launch runs every backward
+// level: pull | barrier | heavy | barrier | next | barrier.  The phase
+// bodies are the per-level kernels' own.  A barrier timeout sets status 3.
+
+__device__ __forceinline__ LvlCnt load_cnt_l2(const LvlCnt *k)
+{
+    LvlCnt r;
+    r.ncand = __ldcg(&k->ncand);
+    r.nnew = __ldcg(&k->nnew);
+    r.nfh_build = __ldcg(&k->nfh_build);
+    r.status = __ldcg(&k->status);
+    r.nfe = __ldcg(&k->nfe);
+    return r;
+}
+
+template <bool TP, bool EXT>
+__global__ void __launch_bounds__(THREADS) k_bb_levels(BbArgs a, int heavy)
+{
+    __shared__ BbCtl s_c;
+    __shared__ int32_t s_off[2];
+    if (threadIdx.x == 0) {
+        s_c = load_ctl_l2(a.ctl);
+        s_off[0] = __ldcg(&a.off[s_c.d]);
+        s_off[1] = __ldcg(&a.off[s_c.d + 1]);
+    }
+    __syncthreads();
+    bool ran = false, ok = true;
+    for (int32_t lv = 0;; lv++) {
+        const BbCtl c = s_c;
+        if (c.more == 0 || c.dense) break;
+        ran = true;
+        LvlCnt *k = a.pcnt + (lv & 3);
+        if (blockIdx.x == 0 && threadIdx.x == 0) a.pcnt[(lv + 2) & 3] = LvlCnt{0, 0, 0, 0, 0ull};
+        const int32_t b0 = s_off[0], b1 = s_off[1];
+        bb_mark_phase(a, c, b0, b1, &k->ncand);
+        if (!(ok = mgd::grid_sync(a.bar, a.bar_err))) break;
+        const int32_t ncand = __ldcg(&k->ncand);
+        bb_pull_phase<TP, EXT>(a, c, ncand);
+        if (!(ok = mgd::grid_sync(a.bar, a.bar_err))) break;
+        if (heavy) {
+            bb_heavy_phase(a, c);
+            if (!(ok = mgd::grid_sync(a.bar, a.bar_err))) break;
+        }
+        bb_compact_phase(a, c, b0, b1, ncand, k);
+        if (!(ok = mgd::grid_sync(a.bar, a.bar_err))) break;
+        if (threadIdx.x == 0) {
+            BbCtl n = c;
+            int32_t off_d2;
+            bb_decide(n, load_cnt_l2(k), __ldcg(&a.ctl->ovf), b1, off_d2, a.m);
+            if (blockIdx.x == 0) a.off[c.d + 2] = off_d2;
+            s_c = n;
+            s_off[0] = b1;
+            s_off[1] = off_d2;
+        }
+        __syncthreads();
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0 && (ran || !ok)) {
+        BbCtl n = s_c;
+        if (!ok || *(volatile int *)a.bar_err) {
+            n.status = 3;
+            n.more = 0;
+        }
+        n.ovf |= __ldcg(&a.ctl->ovf);
+        n.k = LvlCnt{0, 0, 0, 0, 0ull};
+        n.done = 0;
+        *a.ctl = n;
+    }
+}
+
+template <bool TP, bool EXT>
+__global__ void __launch_bounds__(THREADS) k_bbb_levels(BbArgs a, int heavy)
+{
+    __shared__ BbCtl s_c;
+    if (threadIdx.x == 0) s_c = load_ctl_l2(a.ctl);
+    __syncthreads();
+    if (s_c.more == 0) return;
+    bool ok = true;
+    int32_t L = s_c.L;
+    for (; L >= 1; L--) {
+        bbb_pull_phase<TP, EXT>(a, L);
+        if (!(ok = mgd::grid_sync(a.bar, a.bar_err))) break;
+        if (heavy) {
+            bbb_heavy_phase<EXT>(a, L);
+            if (!(ok = mgd::grid_sync(a.bar, a.bar_err))) break;
+        }
+        bbb_next_phase(a, L);
+        if (!(ok = mgd::grid_sync(a.bar, a.bar_err))) break;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        a.ctl->L = ok ? 0 : L;
+        a.ctl->more = 0;
+        a.ctl->done = 0;
+        if (!ok || *(volatile int *)a.bar_err) a.ctl->status = 3;
+    }
+}
+
+template <class K>
+mg_status launch_coop(K kernel, int grid, cudaStream_t st, const BbArgs &a, int heavy)
+{
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)grid);
+    cfg.blockDim = dim3(THREADS);
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    MG_CUDA(cudaLaunchKernelEx(&cfg, kernel, a, heavy));
+    return MG_OK;
+}
+
 __global__ void k_bb_to_float(int32_t n, const double *bc, float *out)
 {
     for (int32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x) out[v] = (float)bc[v];
@@ -177,8 +298,9 @@ __global__ void k_bb_to_float(int32_t n, const double *bc, float *out)
 
 
 struct BcWS {
-    mgi::DevBuf vis, fm, cbm, cand, arch, amask, off, sig, q, hpart, hmask, bc, bcf, fheavy, src, ctl;
+    mgi::DevBuf vis, fm, cbm, cand, arch, amask, off, sig, q, hpart, hmask, bc, bcf, fheavy, src, ctl, bar, pcnt;
     mgi::LoopGraph fwd, bwd;
+    int coop_f = 0, coop_b = 0;   // resident grids of the persistent sweeps (0: not sized yet)
 };
 
 namespace mgi {
@@ -191,7 +313,8 @@ void free_bc_ws(mg_graph *g)
     if (!g->bws) return;
     BcWS *w = g->bws;
     DevBuf *bufs[] = {&w->vis, &w->fm, &w->cbm, &w->cand, &w->arch, &w->amask, &w->off, &w->sig,
-                      &w->q, &w->hpart, &w->hmask, &w->bc, &w->bcf, &w->fheavy, &w->src, &w->ctl};
+                      &w->q, &w->hpart, &w->hmask, &w->bc, &w->bcf, &w->fheavy, &w->src, &w->ctl,
+                      &w->bar, &w->pcnt};
     for (DevBuf *b : bufs) dev_free(*b);
     w->fwd.destroy();
     w->bwd.destroy();
@@ -230,6 +353,8 @@ mg_status bc_batched(mg_graph *g, const int32_t *src_engine, int32_t nsrc, const
     MG_TRY(dev_alloc(w->fheavy, n * 4));
     MG_TRY(dev_alloc(w->src, W * 4));
     MG_TRY(dev_alloc(w->ctl, sizeof(BbCtl)));
+    MG_TRY(dev_alloc(w->bar, 64));
+    MG_TRY(dev_alloc(w->pcnt, 4 * sizeof(LvlCnt)));
 
     BbArgs a;
     std::memset(&a, 0, sizeof(a));
@@ -257,6 +382,9 @@ mg_status bc_batched(mg_graph *g, const int32_t *src_engine, int32_t nsrc, const
     a.fheavy = w->fheavy.as<int32_t>();
     a.src = w->src.as<int32_t>();
     a.ctl = w->ctl.as<BbCtl>();
+    a.bar = w->bar.as<unsigned>();
+    a.bar_err = reinterpret_cast<int *>(a.bar + 1);
+    a.pcnt = w->pcnt.as<LvlCnt>();
 
     cudaStream_t s = g->stream;
     MG_CUDA(cudaMemsetAsync(a.bc, 0, n * 8, s));
@@ -277,6 +405,21 @@ mg_status bc_batched(mg_graph *g, const int32_t *src_engine, int32_t nsrc, const
     }
     const int grid_f = launch_grid(g, THREADS, std::max(1, std::min(8, occ_f)));
     const int grid_b = launch_grid(g, THREADS, std::max(1, std::min(8, occ_b)));
+    // low-degree graphs run their sparse levels in persistent sweeps, whose
+    // grids are what stays resident
+    if (tp && w->coop_f == 0) {
+        int of = 0, ob = 0, ofx = 0, obx = 0;
+        MG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&of, k_bb_levels<true, false>, THREADS, 0));
+        MG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&ofx, k_bb_levels<true, true>, THREADS, 0));
+        MG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&ob, k_bbb_levels<true, false>, THREADS, 0));
+        MG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&obx, k_bbb_levels<true, true>, THREADS, 0));
+        const int pf = std::min({of, ofx, 8}), pb = std::min({ob, obx, 8});
+        if (pf < 1 || pb < 1) return fail(MG_ERR_CUDA, "persistent batched BC kernels do not fit on an SM");
+        w->coop_f = pf * g->num_sms;
+        w->coop_b = pb * g->num_sms;
+    }
+    const bool persist = tp;
+    const int coop_f = w->coop_f, coop_b = w->coop_b;
     const int alpha = opt.alpha > 0 ? opt.alpha : 15;
     const int max_levels = g->nv + 2;
     // heavy-row folds only on graphs that have heavy rows
@@ -285,7 +428,15 @@ mg_status bc_batched(mg_graph *g, const int32_t *src_engine, int32_t nsrc, const
     const int s_mark = P.slot("bcb_mark"), s_pull = P.slot("bcb_pull"), s_heavy = P.slot("bcb_heavy");
     const int s_comp = P.slot("bcb_compact_decide");
     const int s_bp = P.slot("bcb_back"), s_bh = P.slot("bcb_back_heavy"), s_bn = P.slot("bcb_back_next");
+    const int s_lv = persist ? P.slot("bcb_levels") : -1, s_blv = persist ? P.slot("bcb_back_levels") : -1;
     BodyFn fwd = [&](cudaStream_t st, cudaGraphConditionalHandle h, int use_cond) -> mg_status {
+        if (persist) {
+            MG_CUDA(cudaMemsetAsync(a.pcnt, 0, 4 * sizeof(LvlCnt), st));
+            P.begin(s_lv);
+            if (a.ext) MG_TRY(launch_coop(k_bb_levels<true, true>, coop_f, st, a, (int)heavy));
+            else MG_TRY(launch_coop(k_bb_levels<true, false>, coop_f, st, a, (int)heavy));
+            P.end();
+        }
         P.begin(s_mark);
         k_bb_mark<<<grid, THREADS, 0, st>>>(a);
         P.end();
@@ -332,7 +483,7 @@ mg_status bc_batched(mg_graph *g, const int32_t *src_engine, int32_t nsrc, const
         return MG_OK;
     };
     // every by-value argument of the captured kernels
-    const LoopKey key = LoopKey().add(a).add(grid).add(grid_f).add(grid_b).add(heavy).add(tp);
+    const LoopKey key = LoopKey().add(a).add(grid).add(grid_f).add(grid_b).add(heavy).add(tp).add(coop_f);
     const LoopKey key_b = LoopKey(key).add(1);
     const int mode = opt.profile ? MG_EXEC_HOST : opt.exec;
     int32_t levels = 0, dense_levels = 0;
@@ -341,17 +492,29 @@ mg_status bc_batched(mg_graph *g, const int32_t *src_engine, int32_t nsrc, const
         MG_CUDA(cudaMemcpyAsync(w->src.p, src_engine + g0, (size_t)cnt * 4, cudaMemcpyHostToDevice, s));
         MG_CUDA(cudaMemsetAsync(a.vis, 0, n * 4, s));
         MG_CUDA(cudaMemsetAsync(a.fm0, 0, 3 * n * 4, s));
+        MG_CUDA(cudaMemsetAsync(a.bar, 0, 64, s));
         k_bb_init<<<1, 32, 0, s>>>(a, cnt, opt.direction, alpha, max_levels);
         MG_CUDA(cudaGetLastError());
         MG_TRY(run_loop(mode, opt.profile != 0, s, w->fwd, key, fwd, &a.ctl->more, g->pinned_flag, max_levels + 2));
         k_bbb_start<<<grid, THREADS, 0, s>>>(a);
         MG_CUDA(cudaGetLastError());
-        MG_TRY(run_loop(mode, opt.profile != 0, s, w->bwd, key_b, bwd, &a.ctl->more, g->pinned_flag,
-                        max_levels + 2));
+        if (persist) {
+            // every backward level in one launch (the barrier words again
+            // from zero: this grid differs from the forward one)
+            MG_CUDA(cudaMemsetAsync(a.bar, 0, 64, s));
+            P.begin(s_blv);
+            if (a.ext) MG_TRY(launch_coop(k_bbb_levels<true, true>, coop_b, s, a, (int)heavy));
+            else MG_TRY(launch_coop(k_bbb_levels<true, false>, coop_b, s, a, (int)heavy));
+            P.end();
+        } else {
+            MG_TRY(run_loop(mode, opt.profile != 0, s, w->bwd, key_b, bwd, &a.ctl->more, g->pinned_flag,
+                            max_levels + 2));
+        }
         BbCtl hc;
         MG_CUDA(cudaMemcpyAsync(&hc, a.ctl, sizeof(hc), cudaMemcpyDeviceToHost, s));
         MG_CUDA(cudaStreamSynchronize(s));
         if (hc.status == 1) return fail(MG_ERR_ITER_LIMIT, "batched BC: level cap %d reached", max_levels);
+        if (hc.status == 3) return fail(MG_ERR_CUDA, "batched BC: grid barrier of a persistent sweep timed out");
         if (hc.status != 0) return fail(MG_ERR_CUDA, "batched BC: level archive overflow");
         if (hc.ovf && !g->bc_ext) {
             // a path count passed FP64's comfortable range: this graph's BC

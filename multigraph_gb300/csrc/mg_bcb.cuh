@@ -96,7 +96,7 @@ struct BbCtl {
     int32_t nfh;        // heavy frontier entries at level d
     int32_t nlevels;    // levels 0..nlevels-1 archived (set when the forward sweep ends)
     int32_t L;          // backward level
-    int32_t status;     // 1: level cap reached, 2: archive overflow
+    int32_t status;     // 1: level cap reached, 2: archive overflow, 3: grid barrier timeout
     int32_t dirmode;    // MG_DIR_*
     int32_t alpha;
     int32_t max_levels;
@@ -162,6 +162,11 @@ struct BbArgs {
     int32_t *fheavy;
     const int32_t *src;          // the group's sources (engine ids), W entries
     BbCtl *ctl;
+    // persistent sweeps (low-degree graphs): grid barrier words (zero before
+    // each sweep), the barrier's error word, four rotating level counters
+    unsigned *bar;
+    int *bar_err;
+    LvlCnt *pcnt;
 };
 
 __device__ __forceinline__ uint32_t *fm_of(const BbArgs &a, int i) { return i ? a.fm1 : a.fm0; }
