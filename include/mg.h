@@ -325,9 +325,9 @@ mg_status mg_autotune(mg_graph *dg, int32_t algo, int32_t source, const char *ca
  * PageRank from x = 1/n until the L1 change <= tol.  Works on the current
  * device and enqueues on `stream` (a cudaStream_t, NULL = default stream);
  * the call waits for that stream before it returns (it reads the
- * convergence word back after every batch of 8 sweeps).  The first call on
- * a device looks up the array's device address; make it before any stream
- * capture.  All calls share the array: calls that overlap on the GPU race. */
+ * convergence word back after every batch of 8 sweeps), so it must not be
+ * called on a stream that is being captured.  All calls share the array:
+ * calls that overlap on the GPU race. */
 #define MG_NOALLOC_MAX_VERTICES (1 << 20)
 mg_status mg_pagerank_noalloc(const int32_t *d_row, const int32_t *d_col, int32_t nv, int32_t ne, float damping,
                               float tol, int32_t max_iter, float *d_rank, void *stream, int32_t *iterations_out,

@@ -179,6 +179,19 @@ def _check(status: int, where: str):
         raise MGError(status, where, lib.mg_last_error().decode())
 
 
+def _result(out, shape, dtype) -> Optional[np.ndarray]:
+    """Host buffer for a run's result: `out` itself when it is an array of
+    that shape and type (C-contiguous, writable: a caller reusing buffers,
+    or page-locked ones, across runs), a new array when `out` is true,
+    nothing (result left on the device) when it is false."""
+    if isinstance(out, np.ndarray):
+        if out.shape != tuple(shape) or out.dtype != np.dtype(dtype) or not out.flags.c_contiguous \
+                or not out.flags.writeable:
+            raise ValueError(f"out must be a writable C-contiguous {np.dtype(dtype)} array of shape {tuple(shape)}")
+        return out
+    return np.empty(shape, dtype) if out else None
+
+
 def _ptr(a: Optional[np.ndarray]):
     return None if a is None else a.ctypes.data_as(C.c_void_p)
 
@@ -351,21 +364,21 @@ class Graph:
     def bfs(self, source: int, opts: Opts = None, out: bool = True, **kw):
         o = self._opts(opts, kw)
         info = RunInfo()
-        res = np.empty(self.nv, np.int32) if out else None
+        res = _result(out, (self.nv,), np.int32)
         _check(lib.mg_bfs(self._h, source, C.byref(o), _ptr(res), C.byref(info)), "mg_bfs")
         return res, info
 
     def sssp(self, source: int, opts: Opts = None, out: bool = True, **kw):
         o = self._opts(opts, kw)
         info = RunInfo()
-        res = np.empty(self.nv, np.int32) if out else None
+        res = _result(out, (self.nv,), np.int32)
         _check(lib.mg_sssp(self._h, source, C.byref(o), _ptr(res), C.byref(info)), "mg_sssp")
         return res, info
 
     def cc(self, opts: Opts = None, out: bool = True, **kw):
         o = self._opts(opts, kw)
         info = RunInfo()
-        res = np.empty(self.nv, np.int32) if out else None
+        res = _result(out, (self.nv,), np.int32)
         _check(lib.mg_cc(self._h, C.byref(o), _ptr(res), C.byref(info)), "mg_cc")
         return res, info
 
@@ -382,14 +395,14 @@ class Graph:
         o = self._opts(opts, kw)
         info = RunInfo()
         s = np.ascontiguousarray(sources, dtype=np.int32)
-        res = np.empty(self.nv, np.float32) if out else None
+        res = _result(out, (self.nv,), np.float32)
         _check(lib.mg_bc_multi(self._h, _ptr(s), len(s), C.byref(o), _ptr(res), C.byref(info)), "mg_bc_multi")
         return res, info
 
     def pagerank(self, variant: int = PR_TOPOLOGY, opts: Opts = None, out: bool = True, **kw):
         o = self._opts(opts, kw)
         info = RunInfo()
-        res = np.empty(self.nv, np.float32) if out else None
+        res = _result(out, (self.nv,), np.float32)
         _check(lib.mg_pagerank(self._h, variant, C.byref(o), _ptr(res), C.byref(info)), "mg_pagerank")
         return res, info
 
@@ -397,14 +410,14 @@ class Graph:
         o = self._opts(opts, kw)
         info = RunInfo()
         s = np.ascontiguousarray(seeds, dtype=np.int32)
-        res = np.empty((len(s), self.nv), np.float32) if out else None
+        res = _result(out, (len(s), self.nv), np.float32)
         _check(lib.mg_ppr_batch(self._h, _ptr(s), len(s), C.byref(o), _ptr(res), C.byref(info)), "mg_ppr_batch")
         return res, info
 
     def wpagerank(self, opts: Opts = None, out: bool = True, **kw):
         o = self._opts(opts, kw)
         info = RunInfo()
-        res = np.empty(self.nv, np.float32) if out else None
+        res = _result(out, (self.nv,), np.float32)
         _check(lib.mg_wpagerank(self._h, C.byref(o), _ptr(res), C.byref(info)), "mg_wpagerank")
         return res, info
 

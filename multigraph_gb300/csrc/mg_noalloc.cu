@@ -17,8 +17,8 @@
 // Host code cannot use the array's name as a device address: it is a
 // host-side stand-in.  The first call on a device (that device current) asks
 // the runtime for the array's device address with cudaGetSymbolAddress and
-// caches it; make that first call before any stream capture.  Each call
-// waits for its stream: it enqueues sweeps in batches of NA_BATCH and reads
+// caches it.  No call may be made on a stream that is being captured: each
+// call waits for its stream: it enqueues sweeps in batches of NA_BATCH and reads
 // the control word back after each batch (sweeps after convergence are
 // no-ops, so the batching changes neither the result nor the sweep count).
 // All calls share the array and it keeps the last call's contents; every

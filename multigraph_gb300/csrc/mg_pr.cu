@@ -366,6 +366,9 @@ struct PrRowOp {
 template <class Op>
 __global__ void __launch_bounds__(THREADS) k_pr_light(PArgs a)
 {
+    // lets k_pr_apply (launched with programmatic dependent launch) be
+    // scheduled while this sweep runs; it waits for the sweep's completion
+    mgd::pdl_enter();
     const PCtl c = *a.ctl;
     if (c.more == 0 || c.sparse) return;
     const int lane = mgd::lane();
@@ -490,6 +493,7 @@ __global__ void __launch_bounds__(THREADS) k_pr_seg(PArgs a)
 template <class Op>
 __global__ void __launch_bounds__(THREADS) k_pr_apply(PArgs a, cudaGraphConditionalHandle h, int use_cond)
 {
+    mgd::pdl_enter();
     PCtl *cp = a.ctl;
     const PCtl c = *cp;
     if (c.more == 0) {
@@ -986,7 +990,7 @@ static mg_status pr_loop(mg_graph *g, PArgs &a, const mg_opts &opt, const char *
         else k_pr_light<Op><<<grid, THREADS, 0, st>>>(a);
         P.end();
         P.begin(sh);
-        k_pr_apply<Op><<<apply_grid, THREADS, 0, st>>>(a, h, use_cond);
+        MG_TRY(launch_pdl(k_pr_apply<Op>, apply_grid, THREADS, st, a, h, use_cond));
         P.end();
         if (Op::kDataDriven) {
             // queue sweeps once the switch has happened (no-ops before)
