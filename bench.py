@@ -546,8 +546,17 @@ def main():
     clk_lines = clocks.pause()
 
     # results on the last committed input, checked against the oracle below
-    dist_gpu, _ = g.sssp(0, opts)
+    dist_gpu, sssp_info = g.sssp(0, opts)
     rank_gpu, rank_info = g.pagerank(mg.PR_TOPOLOGY, opts)
+    # each run alone (captured loops, cudaEvents around the run; result copies excluded)
+    _, s1 = g.sssp(0, opts, out=False)
+    _, p1 = g.pagerank(mg.PR_TOPOLOGY, opts, out=False)
+    per_run = {"sssp_ms": round(s1.device_ms, 4), "sssp_iterations": s1.iterations,
+               "sssp_gteps": round(m / (s1.device_ms / 1e3) / 1e9, 2),
+               "pagerank_ms": round(p1.device_ms, 4), "pagerank_sweeps": p1.iterations,
+               "pagerank_iterations_per_s": round(p1.iterations / (p1.device_ms / 1e3), 1),
+               "pagerank_gteps": round(m / (p1.device_ms / 1e3) / 1e9, 2),
+               "pagerank_edge_sweeps_per_s": round(m * p1.iterations / (p1.device_ms / 1e3) / 1e9, 2)}
 
     # ---- per-kernel times (cudaEvents around every launch, host-driven loop)
     clocks.start(keep=clk_lines)
@@ -693,8 +702,10 @@ def main():
         "e2e": {"value": e2e_val, "unit": "GTEPS", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "host_split_ms_per_step": split},
         "errors": errors,
+        "per_run": per_run,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": (achieved / peak) if achieved else None, "traffic": traffic,
+                     "frac_of_nominal_7900": (achieved / 7900.0) if achieved else None,
                      "kernel": "PageRank pull sweep k_pr_light (gather layout)", "algorithmic_bytes": alg_bytes,
                      "avg_launch_ms": avg_ms, "parts_ms": parts, "peak_kind": peak_kind,
                      "kernel_share": (avg_ms * nsw / total_ms) if total_ms else None, "l2": l2},
