@@ -12,7 +12,7 @@
 //               in-edges; then rows above heavy in-edges in chunks, one CTA
 //               each, partial sums written per chunk (tbin / heavy / chunk
 //               default to 32 / 512 / 2048, mg_autotune re-picks them);
-//   k_pr_apply  heavy rows summed chunk by chunk in order (warp per row),
+//   k_pr_apply  heavy rows summed chunk by chunk in order (thread per row),
 //               then the last block to finish sums every block's residual
 //               partials in slot order: convergence test, loop condition.
 // Sums are therefore deterministic (fixed order) run to run.
@@ -430,7 +430,27 @@ __device__ __forceinline__ void reduce_slots(const double *bpart, int s0, int s1
     __shared__ int sa[THREADS / 32];
     double v[NPART - 1] = {0, 0, 0, 0};
     int any = 0;
-    for (int b = s0 + (int)threadIdx.x; b < s1; b += blockDim.x) {
+    int b = s0 + (int)threadIdx.x;
+    // four slots' loads in flight, then added in slot order (the same sums
+    // as one slot at a time)
+    for (; b + 3 * (int)blockDim.x < s1; b += 4 * blockDim.x) {
+        double r[4][NPART];
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+            const double *o = bpart + (size_t)NPART * (b + j * blockDim.x);
+#pragma unroll
+            for (int k = 0; k < NPART; k++) r[j][k] = __ldcg(&o[k]);
+        }
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+            v[0] += r[j][0];
+            v[1] += r[j][1];
+            any |= r[j][2] != 0.0;
+            v[2] += r[j][3];
+            v[3] += r[j][4];
+        }
+    }
+    for (; b < s1; b += blockDim.x) {
         const double *o = bpart + (size_t)NPART * b;
         v[0] += __ldcg(&o[0]);
         v[1] += __ldcg(&o[1]);
@@ -501,26 +521,31 @@ __global__ void __launch_bounds__(THREADS) k_pr_apply(PArgs a, cudaGraphConditio
         return;
     }
     if (c.sparse) return;   // queue sweeps (k_prd_*) drive the loop
-    const int lane = mgd::lane();
-    const int gwarp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int nwarps = (gridDim.x * blockDim.x) >> 5;
     double resid = 0.0, dangs = 0.0, act = 0.0, dfz = 0.0;
     int any = 0;
-    for (int32_t i = gwarp; i < a.nhrows; i += nwarps) {
-        int32_t v = a.hrows[i];
+    // a thread per heavy row: its chunk partials summed in chunk order, four
+    // loads in flight (a row has a few chunks; every row's chain of loads
+    // runs side by side instead of one warp walking two rows in turn)
+    for (int32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < a.nhrows; i += gridDim.x * blockDim.x) {
+        const int32_t v = a.hrows[i];
+        const int32_t k1 = a.hrow_chunk[i + 1];
+        int32_t k = a.hrow_chunk[i];
         float s = 0.0f;
-        for (int32_t k = a.hrow_chunk[i] + lane; k < a.hrow_chunk[i + 1]; k += 32) s += a.hpart[k];
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-        if (lane == 0) {
-            float dg = 0.0f;
-            s += seg_sum(a, v);
-            resid += Op::apply(a, c, v, s, any, dg);
-            dangs += dg;
-            if (Op::kDataDriven) {
-                if (a.active[v]) act += (double)(a.frow[v + 1] - a.frow[v]);
-                else dfz += dg;
-            }
+        for (; k + 4 <= k1; k += 4) {
+            const float p0 = a.hpart[k], p1 = a.hpart[k + 1], p2 = a.hpart[k + 2], p3 = a.hpart[k + 3];
+            s += p0;
+            s += p1;
+            s += p2;
+            s += p3;
+        }
+        for (; k < k1; k++) s += a.hpart[k];
+        float dg = 0.0f;
+        s += seg_sum(a, v);
+        resid += Op::apply(a, c, v, s, any, dg);
+        dangs += dg;
+        if (Op::kDataDriven) {
+            if (a.active[v]) act += (double)(a.frow[v + 1] - a.frow[v]);
+            else dfz += dg;
         }
     }
     block_partials(a, a.nblocks + blockIdx.x, resid, dangs, any, act, dfz);
@@ -979,7 +1004,8 @@ static mg_status pr_loop(mg_graph *g, PArgs &a, const mg_opts &opt, const char *
     const int sl = P.slot(name);
     std::string hn = std::string(name) + "_apply";
     const int sh = P.slot(hn.c_str());
-    const int apply_grid = std::max(1, std::min(std::min(grid, (a.nhrows + 7) / 8), g->num_sms * APPLY_PER_SM));
+    const int apply_grid = std::max(1, std::min(std::min(grid, (a.nhrows + THREADS - 1) / THREADS),
+                                                g->num_sms * APPLY_PER_SM));
     const int shs = a.P ? P.slot("pr_hub") : -1, shf = a.P ? P.slot("pr_hub_fix") : -1;
     const int sqc = Op::kDataDriven ? P.slot("prd_compact") : -1, sqg = Op::kDataDriven ? P.slot("prd_gather") : -1,
               sqa = Op::kDataDriven ? P.slot("prd_apply") : -1;
