@@ -504,6 +504,15 @@ def main():
     # a fresh array is first touched inside the timed loop
     res_t = (torch.empty(n, dtype=torch.int32, pin_memory=True), torch.empty(n, dtype=torch.float32, pin_memory=True))
     res_bufs = (res_t[0].numpy(), res_t[1].numpy())
+    # untimed warm-up of the end-to-end loop itself: the first staged
+    # uploads of a process overlap the runs poorly (on boxes that have just
+    # run other GPU work, about ten steps' worth), later ones fully
+    g.stage(h)
+    for i in range(max(args.warmup, 10)):
+        g.commit()
+        g.stage(h)
+        step(bufs=res_bufs)
+    g.commit()
     torch.cuda.synchronize()
     split = {"stage_ms": 0.0, "commit_ms": 0.0, "runs_ms": 0.0}
     t0 = time.perf_counter()
@@ -604,7 +613,7 @@ def main():
         o = mg.default_opts(tol=tol, damping=DAMPING, profile=1)
         _, di = g.pagerank(mg.PR_DATA, o, out=False)
         dkt = di.kernel_times()
-        dense_ms = sum(dkt.get(k, (0, 0.0))[1] for k in ("pr_hub", "pr_hub_fix", "pr_pull", "pr_pull_apply"))
+        dense_ms = sum(dkt.get(k, (0, 0.0))[1] for k in ("pr_hub", "pr_pull", "pr_pull_apply"))
         queue_ms = sum(dkt.get(k, (0, 0.0))[1] for k in ("prd_compact", "prd_gather", "prd_apply"))
         nq = di.iterations - di.pull_iterations
         return {"tol": tol, "sweeps": di.iterations, "dense_sweeps": di.pull_iterations, "queue_sweeps": nq,
@@ -616,14 +625,14 @@ def main():
         o = mg.default_opts(tol=TOL, damping=DAMPING, profile=1, pr_layout=layout)
         _, li = g.pagerank(mg.PR_TOPOLOGY, o, out=False)
         lkt = li.kernel_times()
-        return round(sum(lkt.get(k, (0, 0.0))[1] for k in ("pr_hub", "pr_hub_fix", "pr_pull"))
+        return round(sum(lkt.get(k, (0, 0.0))[1] for k in ("pr_hub", "pr_pull"))
                      / max(li.iterations, 1), 4)
 
     layouts = None
     if world == 1:
         layouts = {"gather_ms_per_sweep": layout_sweep_ms(mg.PR_LAYOUT_GATHER),
                    "segmented_ms_per_sweep": layout_sweep_ms(mg.PR_LAYOUT_SEGMENTED),
-                   "default": "gather"}
+                   "default": "segmented" if "pr_hub" in kt else "gather"}
     # data-driven PageRank where the queue sweeps engage: 2048 x 2048 torus
     # + R-MAT 14 (active in-edges ~1 % of m after the first sweeps)
     def mixed_data_driven(tol=1e-8):
@@ -667,26 +676,29 @@ def main():
         dd["xd"], _ = g.pagerank(mg.PR_DATA, opts)
     batched = None if (args.no_batch or world > 1) else batch_report(mg, local)
     peak, peak_kind = peaks()
-    # one PageRank sweep of the default (gather) layout = k_pr_light; the
-    # segmented layout's kernels (k_hub_sweep, k_hub_fix) would be summed in
+    # one PageRank sweep of the layout the default options chose: segmented
+    # = k_hub_sweep (pr_hub) + the row finish k_pr_seg (pr_pull); gather =
+    # k_pr_light (pr_pull)
+    segmented = "pr_hub" in kt
     sweep = kt.get("pr_pull", [1, 0.0])
     nsw = max(sweep[0], 1)
-    parts = {k: kt[k][1] / nsw for k in ("pr_hub", "pr_hub_fix", "pr_pull") if k in kt}
+    parts = {k: kt[k][1] / nsw for k in ("pr_hub", "pr_pull") if k in kt}
     avg_ms = sum(parts.values())
     alg_bytes = 4 * m + 4 * (n + 1) + 12 * n
     achieved = alg_bytes / (avg_ms / 1e3) / 1e9 if avg_ms > 0 else None
     traffic = None
     l2 = None
     try:
-        with open(os.path.join(ROOT, "profiles", "pr_sweep_traffic.json")) as f:
+        tname = "pr_segmented_traffic.json" if segmented else "pr_sweep_traffic.json"
+        with open(os.path.join(ROOT, "profiles", tname)) as f:
             tr = json.load(f)
         traffic = tr["dram_bytes_per_edge"] * m + tr["dram_bytes_per_vertex"] * n
         # the sweep's other bound: the L2-resident contribution gathers
         l2 = {"lts_throughput_frac": tr["lts_throughput_pct_of_peak"] / 100.0,
               "l2_sector_hit_rate": tr["lts_t_sector_hit_rate_pct"] / 100.0,
               "l1_sector_hit_rate": tr["l1tex_t_sector_hit_rate_pct"] / 100.0,
-              "source": "ncu, one sweep launch at R-MAT 21 (profiles/pr_sweep_rmat21.md)"}
-        if avg_ms > 0 and args.scale == 22:   # the floor was measured on this graph
+              "source": "ncu at R-MAT 21 (profiles/" + tr["summary"].split("/")[-1] + ")"}
+        if avg_ms > 0 and args.scale == 22 and "gather_floor_us_rmat22" in tr:   # measured on this graph
             l2["gather_floor_frac"] = tr["gather_floor_us_rmat22"] / 1e3 / avg_ms
     except Exception:
         pass
@@ -729,7 +741,9 @@ def main():
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": (achieved / peak) if achieved else None, "traffic": traffic,
                      "frac_of_nominal_7900": (achieved / 7900.0) if achieved else None,
-                     "kernel": "PageRank pull sweep k_pr_light (gather layout)", "algorithmic_bytes": alg_bytes,
+                     "kernel": ("PageRank sweep, segmented layout: k_hub_sweep + row finish k_pr_seg" if segmented
+                                else "PageRank pull sweep k_pr_light (gather layout)"),
+                     "algorithmic_bytes": alg_bytes,
                      "avg_launch_ms": avg_ms, "parts_ms": parts, "peak_kind": peak_kind,
                      "kernel_share": (avg_ms * nsw / total_ms) if total_ms else None, "l2": l2},
         "pagerank_data_driven": dd,

@@ -176,12 +176,17 @@ typedef struct mg_opts {
     float tol;             /* PageRank tolerance                               */
     int32_t profile;       /* 1: host loop with cudaEvents around each kernel  */
     int32_t pr_layout;     /* PageRank pull sweep over unweighted graphs:      */
-                           /* MG_PR_LAYOUT_GATHER (L2 gathers, default) or     */
-                           /* MG_PR_LAYOUT_SEGMENTED (shared-memory segments)  */
+                           /* MG_PR_LAYOUT_AUTO (default: segmented where it   */
+                           /* applies, unless mg_autotune measured the gather  */
+                           /* layout faster on this graph),                    */
+                           /* MG_PR_LAYOUT_GATHER (L2 gathers over degree      */
+                           /* bins) or MG_PR_LAYOUT_SEGMENTED (shared-memory   */
+                           /* segments; gather where a quarter of the edges    */
+                           /* or fewer fall in segments)                       */
     int32_t reserved[7];
 } mg_opts;
 
-enum { MG_PR_LAYOUT_GATHER = 0, MG_PR_LAYOUT_SEGMENTED = 1 };
+enum { MG_PR_LAYOUT_GATHER = 0, MG_PR_LAYOUT_SEGMENTED = 1, MG_PR_LAYOUT_AUTO = 2 };
 
 /* Fill *o with the defaults (exec graph, auto direction, tuned thresholds). */
 void mg_opts_default(mg_opts *o);

@@ -33,7 +33,7 @@ LOAD_SYM, LOAD_NSYM, LOAD_CC = 1, 2, 4
 EXEC_GRAPH, EXEC_HOST = 0, 1
 DIR_AUTO, DIR_PUSH, DIR_PULL = 0, 1, 2
 PR_TOPOLOGY_REF, PR_DATA_REF, PR_TOPOLOGY, PR_DATA = 0, 1, 2, 3
-PR_LAYOUT_GATHER, PR_LAYOUT_SEGMENTED = 0, 1
+PR_LAYOUT_GATHER, PR_LAYOUT_SEGMENTED, PR_LAYOUT_AUTO = 0, 1, 2
 ALGO_BFS, ALGO_SSSP, ALGO_BC, ALGO_CC, ALGO_PR = range(5)
 IUNUSED = 0x64646464
 

@@ -916,6 +916,7 @@ void mg_opts_default(mg_opts *o)
     o->damping = 0.85f;
     o->tol = 1e-6f;
     o->profile = 0;
+    o->pr_layout = MG_PR_LAYOUT_AUTO;
 }
 
 mg_status mg_graph_upload(const mg_host_graph *h, int32_t device, mg_graph **out)
@@ -995,6 +996,8 @@ static void drop_workspaces(mg_graph *g)
     // the old layout: rebuild it on the next mg_ppr_batch
     g->ppr_nhchunks = -1;
     g->ppr_nhrows = 0;
+    // a new layout has not been timed by mg_autotune
+    g->pr_prefer_gather = false;
 }
 
 mg_status mg_graph_commit(mg_graph *g)

@@ -106,23 +106,23 @@ struct HubSplit {
     bool valid = false;      // built for the current pull columns
     bool use = false;        // the split is in use (enough covered edges)
     uint64_t gen = 0;        // build number (process-wide): captured sweeps key on it
-    int32_t H = 0, nseg = 0, nchunks = 0;
-    int32_t nlong = 0;       // chunks whose last pair spans many chunks
-    int64_t npairs = 0, covered = 0;  // (row, segment) pairs; edges in the segments
+    int32_t H = 0, nseg = 0; // vertices per segment; segments
+    int32_t ngroups = 0;     // warp groups of equal-length pieces
+    int64_t npieces = 0, covered = 0;  // pieces (P entries); edges in the segments
     int64_t ntail = 0;       // edges past the last segment
     int32_t grid = 0;        // CTAs of the sweep (one per SM)
-    DevBuf hcol;             // uint16 segment streams (whole chunks), segment-major
-    DevBuf rstart;           // uint32 bits: first edge of each pair
-    DevBuf crow;             // int32 [nchunks+1]: pair index of each chunk's first start
-    DevBuf slot;             // int32 [npairs]: each pair's place in P
-    DevBuf segchunk;         // int32 [nseg+1]: first chunk of each segment
-    DevBuf cta_lo;           // int32 [grid+1]: each CTA's chunk range
-    DevBuf pair_off;         // int32 [n+1]: row v's pairs in P
-    DevBuf P;                // float [npairs]: pair sums of the current sweep
+    int32_t nfw = 0, nfg = 0, nft = 0;  // finish bins: warp / 8-lane / thread rows
+    DevBuf hdat;             // uint16 local ids: per group [lambda][GROUP], groups segment-major
+    DevBuf goff;             // int32 [ngroups+1]: each group's first step (GROUP ids per step)
+    DevBuf pslot;            // int32 [ngroups*GROUP]: each piece's place in P (padding: npieces)
+    DevBuf segg;             // int32 [nseg+1]: first group of each segment
+    DevBuf cpart;            // int32 [grid+1]: each CTA's parts (a part: one segment's groups)
+    DevBuf pseg;             // int32 [nparts]: each part's segment
+    DevBuf wb;               // int32 [nparts*33]: each part's group range per warp
+    DevBuf pair_off;         // int32 [n+1]: row v's pieces in P
+    DevBuf P;                // float [npieces+1]: piece sums of the current sweep (+ padding slot)
     DevBuf toff, tcol;       // tail rows: offsets [n+1], int32 ids
-    DevBuf chead, ctail, cstart;  // per-chunk carries of the sweep
-    DevBuf cnext, clong;     // per chunk: next chunk with a start; long-span chunks
-    DevBuf err;
+    DevBuf fin;              // int32 [n]: rows of the finish bins (warp | 8-lane | thread)
 };
 }  // namespace mgi
 
@@ -184,6 +184,7 @@ struct mg_graph {
     // hub-first relabeling: the engines run on ids ordered by descending
     // log2 degree; results are mapped back before they leave the library
     bool relabeled = false;
+    bool pr_prefer_gather = false; // mg_autotune measured the gather PageRank layout faster (MG_PR_LAYOUT_AUTO)
     mgi::DevBuf o_row, o_col, o_wt;        // the CSR in the caller's ids (as uploaded)
     mgi::DevBuf o_fw;                      // float weights in caller CSR order
     mgi::DevBuf old2new, new2old;          // int32 [nv]
@@ -243,8 +244,9 @@ mg_status bc_batched(mg_graph *g, const int32_t *src_engine, int32_t nsrc, const
 // once *more is 0 or *off is not), report a bulk-copy wait that ran out, free
 mg_status hub_prepare(mg_graph *g);
 mg_status hub_launch(mg_graph *g, const float *c0, const float *c1, const int32_t *cur, const int32_t *more,
-                     const int32_t *off, cudaStream_t st, int slot_sweep, int slot_fix);
+                     const int32_t *off, cudaStream_t st, int slot_sweep);
 mg_status hub_check(mg_graph *g);
+bool hub_covers_all(const mg_graph *g);   // the segments hold every vertex id
 void hub_free(mg_graph *g);
 
 // Launch with programmatic dependent launch on the stream's previous kernel:
@@ -271,6 +273,37 @@ inline mg_status launch_pdl(K kernel, int grid, int block, cudaStream_t st, Args
 // device helpers
 // ---------------------------------------------------------------------------
 namespace mgd {
+
+// Compensated (Kahan) add: t += x, r carrying the low part lost so far
+// (the exact sum is t - r).  A long sum of similar terms then rounds about
+// once instead of once per term.
+__device__ __forceinline__ void kahan_add(float &t, float &r, float x)
+{
+    const float y = x - r;
+    const float u = t + y;
+    r = (u - t) - y;
+    t = u;
+}
+
+// Warp-wide sum of the lanes' compensated sums (t - r), every lane gets the
+// total: an xor tree whose adds carry their exact rounding errors (TwoSum),
+// so the total rounds about once.  TwoSum is exact in either operand order,
+// so every lane forms the same value.
+__device__ __forceinline__ float warp_sum_comp(float t, float r)
+{
+    float v = t - r, c = 0.0f;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const float vo = __shfl_xor_sync(0xffffffffu, v, o);
+        const float co = __shfl_xor_sync(0xffffffffu, c, o);
+        const float u = v + vo;
+        const float bp = u - v;
+        const float e = (v - (u - bp)) + (vo - bp);
+        c = (c + co) + e;
+        v = u;
+    }
+    return v + c;
+}
 
 // warp-bin rows below this many edges are summed by an 8-lane group (four
 // rows per warp in flight, mg_bins.cuh), longer ones by a whole warp

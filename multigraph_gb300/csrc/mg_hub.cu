@@ -8,32 +8,32 @@
 // segments of H = SEG_H vertices (the most a CTA's 227 KB of shared memory
 // holds as FP32 contributions, 224 KB), and each pull row's in-edges are
 // grouped by segment once per layout:
-//   segment streams : for segment s, the rows that have in-edges from it
-//                     (ascending), each row's edges from s as 16-bit local
-//                     ids (id - s*H), padded to whole 1024-edge chunks; a
-//                     bitmap marks the first edge of every (row, segment)
-//                     pair; slot[] gives each pair its place in P;
-//   P, pair_off     : the pairs' partial sums in row-major order (row v's
-//                     pairs at P[pair_off[v] .. pair_off[v+1]), segments
-//                     ascending), summed by the row's finish;
+//   pairs, pieces   : a (row, segment) pair is the row's in-edges from the
+//                     segment; it is cut into pieces of at most PIECE_MAX
+//                     edges (the row's order kept);
+//   warp groups     : per segment, pieces of equal length lambda are bucketed
+//                     (rows ascending) and packed GROUP at a time, padded;
+//                     a group stores its ids as 16-bit local ids (id - s*H)
+//                     step-major, [lambda][GROUP], so each step is one
+//                     coalesced 256-byte warp load (four pieces per lane);
+//   P, pair_off     : the pieces' sums in row-major order (row v's pieces at
+//                     P[pair_off[v] .. pair_off[v+1]), segments ascending),
+//                     summed by the row's finish; pslot gives each packed
+//                     piece its place in P;
 //   tail            : in-edges from ids beyond the last segment (graphs
 //                     with more than SEG_MAX segments' worth of vertices),
 //                     int32 ids gathered through L2 by the degree-binned
 //                     sweep.
-// One sweep: k_hub_sweep streams the chunks -- each CTA a contiguous,
-// edge-balanced range, staging the contributions c[s*H, (s+1)*H) of every
-// segment its range enters with bulk copies (cp.async.bulk on an mbarrier),
-// each warp a 1024-edge chunk at a time: every lane takes 32 consecutive
-// edges with four 128-bit loads and gathers from shared memory, a segmented
-// sum (per lane, then a shuffle tree across lanes) gives every pair that
-// ends inside the chunk its total; k_hub_fix finishes the pairs that run
-// past their chunk (FP64, fixed order).  (With 8 edges per lane the chunk's
-// fixed work -- the cross-lane scans and carries -- made the kernel
-// issue-bound: ~350 warp instructions per 256 edges.)  Sums are formed in
-// a fixed order, so sweeps are reproducible.
+// One sweep: k_hub_sweep gives each CTA a contiguous range of groups
+// (balanced by the groups' steps plus a fixed cost per group), stages the
+// contributions c[s*H, (s+1)*H) of every segment its range enters, and each
+// warp sums one group at a time: a lane adds its four pieces' edges in order
+// from shared memory and stores the four totals to P.  Pieces never cross a
+// group, so there are no carries between lanes, warps or CTAs; every sum is
+// formed in a fixed order, so sweeps are reproducible.
 //
-// Per sweep the streams move 2 B per edge plus 1 bit per edge and 4 B per
-// pair, instead of 4 B of ids and a 32-byte L2 sector per gather.
+// Per sweep the streams move 2 B per edge (plus padding, ~5 % on R-MAT) and
+// 8 B per piece, instead of 4 B of ids and a 32-byte L2 sector per gather.
 
 #include "mg_device.cuh"
 
@@ -47,263 +47,127 @@ namespace {
 
 constexpr int32_t SEG_H = 57344;    // vertices per segment: 224 KB of FP32 contributions
 constexpr int32_t SEG_MAX = 64;     // segments at most; ids beyond stay in the L2 tail
-constexpr int HUB_CHUNK = 1024;     // edges per warp chunk: 32 per lane
+constexpr int32_t PIECE_MAX = 64;   // edges per piece at most
+constexpr int32_t GROUP = 128;      // pieces per warp group: four per lane
 constexpr int HUB_THREADS = 1024;   // one CTA per SM (shared memory bound)
-constexpr long long HUB_WAIT_LIMIT = 20000000ll;  // clock64 cycles (~10 ms) for a bulk copy
-constexpr int32_t FIX_SHORT = 8;    // carry spans up to this many chunks: a thread each
-constexpr int64_t START_COST = 32;  // a pair start's cost in edges, for balancing CTA ranges
+constexpr int HUB_UNROLL = 4;       // steps (256-byte warp loads) in flight per warp
+constexpr int STAGE_BATCH = 4;      // 16-byte loads in flight per thread while staging a segment
+constexpr int64_t GROUP_COST = 16;  // a group's fixed cost in steps, for balancing CTA ranges
+// finish bins by pieces per row: rows with more than FIN_WARP pieces a warp
+// each, the rest a thread each (8-lane groups, FIN_THREAD < pieces <=
+// FIN_WARP, walked rows one after another and were slower)
+constexpr int32_t FIN_WARP = 32;
+constexpr int32_t FIN_THREAD = 32;
 
 struct HubArgs {
-    const uint16_t *hcol;     // segment streams (each padded to whole chunks), segment-major
-    const uint32_t *rstart;   // bits: first edge of each (row, segment) pair
-    const int32_t *crow;      // [nchunks+1] pair index (segment-major) of each chunk's first start
-    const int32_t *slot;      // per pair (segment-major): its place in P
-    const int32_t *segchunk;  // [nseg+1] first chunk of each segment
-    const int32_t *cta_lo;    // [grid+1] each CTA's chunk range, balanced by edges + starts
+    const uint2 *hdat;        // groups' ids, four 16-bit ids per lane per step
+    const int32_t *goff;      // [ngroups+1] each group's first step
+    const int4 *pslot;        // [ngroups*GROUP/4] the four P slots of each lane's pieces
+    const int32_t *cpart;     // [grid+1] each CTA's parts
+    const int32_t *pseg;      // [nparts] each part's segment
+    const int32_t *wb;        // [nparts*33] each part's group range per warp
     const float *c[2];        // contributions (ping-pong, ctl selects)
     const int32_t *cur;       // current iterate index (loop control block)
     const int32_t *more;      // loop continue flag
     const int32_t *off;       // non-zero: sweeps run elsewhere (queue sweeps)
-    float *P;                 // pair partial sums, row-major
-    float *chead, *ctail;     // per chunk: sum before its first start / of its open last pair
-    int32_t *cstart;          // per chunk: has a start
-    const int32_t *cnext;     // per chunk with a start: the next chunk with one (nchunks: none)
-    const int32_t *clong;     // chunks whose last pair spans more than FIX_SHORT chunks
-    int32_t nlong;
-    int32_t *err;             // a bulk copy wait ran out
-    int32_t n, H, nseg, nchunks;
+    float *P;                 // piece sums, row-major
+    int32_t n, H, nseg;
 };
 
-__device__ __forceinline__ uint32_t smem_u32(const void *p)
+// One warp streams groups [ga, gb) (contiguous in hdat): the next
+// HUB_UNROLL steps are loaded while the current ones are summed, across
+// group ends, so the loads run back to back instead of one latency chain per
+// group.  The groups' first steps come from goff 32 at a time (one load,
+// then shuffles); each group's slots are loaded when it starts.
+__device__ __forceinline__ void stream_groups(const HubArgs &a, const float *s_c, int32_t ga, int32_t gb, int lane)
 {
-    return (uint32_t)__cvta_generic_to_shared(p);
-}
-
-__device__ __forceinline__ bool mbar_try(uint32_t bar, uint32_t parity)
-{
-    uint32_t done;
-    asm volatile(
-        "{\n\t.reg .pred p;\n\t"
-        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-        "selp.u32 %0, 1, 0, p;\n\t}"
-        : "=r"(done)
-        : "r"(bar), "r"(parity)
-        : "memory");
-    return done != 0;
-}
-
-// Stage `bytes` (a multiple of 16) from src into s_c with bulk copies
-// completing on the mbarrier (phase `parity`).  Thread 0 waits, bounded by
-// HUB_WAIT_LIMIT cycles; on timeout it sets *err, waits again (bounded)
-// for the copies to land, and the CTA returns false.
-__device__ __forceinline__ bool stage_segment(float *s_c, const float *src, uint32_t bytes, uint32_t bar,
-                                              uint32_t parity, int32_t *err)
-{
-    __shared__ int s_ok;
-    __syncthreads();   // every warp is done with the previous segment
-    if (threadIdx.x == 0) {
-        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
-        constexpr uint32_t PIECE = 32768;
-        for (uint32_t off = 0; off < bytes; off += PIECE) {
-            const uint32_t sz = min(PIECE, bytes - off);
-            asm volatile(
-                "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-                    smem_u32(reinterpret_cast<char *>(s_c) + off)),
-                "l"(reinterpret_cast<const char *>(src) + off), "r"(sz), "r"(bar)
-                : "memory");
+    constexpr unsigned FULL = 0xffffffffu;
+    const uint2 *D = a.hdat + lane;
+    int32_t cbase = ga;
+    int32_t cg = __ldg(&a.goff[min(cbase + lane, gb)]);
+    int32_t t = __shfl_sync(FULL, cg, 0);
+    const int32_t tend = __ldg(&a.goff[gb]);
+    int32_t g = ga;
+    int32_t gend = __shfl_sync(FULL, cg, 1);
+    int4 sl = __ldg(&a.pslot[(int64_t)g * 32 + lane]);
+    // compensated sums (Kahan): a piece of up to PIECE_MAX edges is exact to
+    // about one rounding, so a hub row's total does not drift by a few 1e-6
+    // from sweep to sweep as its inputs settle
+    float s0 = 0.0f, s1 = 0.0f, s2 = 0.0f, s3 = 0.0f, r0 = 0.0f, r1 = 0.0f, r2 = 0.0f, r3 = 0.0f;
+    uint2 wc[HUB_UNROLL], wn[HUB_UNROLL];
+#pragma unroll
+    for (int j = 0; j < HUB_UNROLL; j++) wc[j] = t + j < tend ? __ldcs(D + (int64_t)(t + j) * 32) : make_uint2(0u, 0u);
+    while (t < tend) {
+#pragma unroll
+        for (int j = 0; j < HUB_UNROLL; j++) {
+            const int32_t q = t + HUB_UNROLL + j;
+            wn[j] = q < tend ? __ldcs(D + (int64_t)q * 32) : make_uint2(0u, 0u);
         }
-        bool ok = true;
-        const long long t0 = clock64();
-        while (!mbar_try(bar, parity)) {
-            if (clock64() - t0 > HUB_WAIT_LIMIT) {
-                ok = false;
-                break;
+#pragma unroll
+        for (int j = 0; j < HUB_UNROLL; j++) {
+            if (t < tend) {
+                mgd::kahan_add(s0, r0, s_c[wc[j].x & 0xffffu]);
+                mgd::kahan_add(s1, r1, s_c[wc[j].x >> 16]);
+                mgd::kahan_add(s2, r2, s_c[wc[j].y & 0xffffu]);
+                mgd::kahan_add(s3, r3, s_c[wc[j].y >> 16]);
+                t++;
+                if (t == gend) {   // group g is complete (warp-uniform)
+                    a.P[sl.x] = s0 - r0;
+                    a.P[sl.y] = s1 - r1;
+                    a.P[sl.z] = s2 - r2;
+                    a.P[sl.w] = s3 - r3;
+                    s0 = s1 = s2 = s3 = r0 = r1 = r2 = r3 = 0.0f;
+                    g++;
+                    if (g < gb) {
+                        if (g + 1 - cbase >= 32) {
+                            cbase = g + 1;
+                            cg = __ldg(&a.goff[min(cbase + lane, gb)]);
+                        }
+                        gend = __shfl_sync(FULL, cg, g + 1 - cbase);
+                        sl = __ldg(&a.pslot[(int64_t)g * 32 + lane]);
+                    }
+                }
             }
         }
-        if (!ok) {
-            atomicExch(err, 1);
-            const long long t1 = clock64();
-            while (!mbar_try(bar, parity) && clock64() - t1 < HUB_WAIT_LIMIT) {
-            }
-        }
-        s_ok = ok;
-    }
-    __syncthreads();
-    return s_ok != 0;
-}
-
-// One chunk of HUB_CHUNK = 1024 edges: every lane takes 32 consecutive
-// edges (four 128-bit loads of 16-bit ids) and their 32 start bits (one
-// word), gathers from shared memory and forms segmented sums; the pair
-// totals that end inside the lane go straight to P, the open ends are joined
-// across lanes by a shuffle tree, and the chunk's carries go to
-// chead / ctail / cstart.
-__device__ __forceinline__ void sweep_chunk(const HubArgs &a, const float *s_c, int32_t ch, const uint4 (&cols)[4],
-                                            uint32_t bits, int32_t crow)
-{
-    const int lane = threadIdx.x & 31;
-    // pair index of this lane's first start
-    const int nst = __popc(bits);
-    int32_t before = nst;
 #pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        const int32_t t = __shfl_up_sync(0xffffffffu, before, o);
-        if (lane >= o) before += t;
-    }
-    before -= nst;
-    int32_t k = crow + before - 1;   // pair index of the open pair (after its start)
-    float head = 0.0f, run = 0.0f;
-    bool started = false;
-    if (bits == 0) {
-        // no pair starts in this lane: its 32 edges all continue the open
-        // pair; summed as a pairwise tree (the same adds, a rounding error of
-        // five steps instead of 32: long hub sums stay steady from sweep to
-        // sweep, which the FP32 fixed-point iteration needs to settle)
-        float t[16];
-#pragma unroll
-        for (int g = 0; g < 4; g++) {
-            const uint32_t w32[4] = {cols[g].x, cols[g].y, cols[g].z, cols[g].w};
-#pragma unroll
-            for (int i = 0; i < 4; i++)
-                t[4 * g + i] = s_c[w32[i] & 0xffffu] + s_c[w32[i] >> 16];
-        }
-#pragma unroll
-        for (int w = 8; w > 0; w >>= 1)
-#pragma unroll
-            for (int i = 0; i < w; i++) t[i] = t[i] + t[i + w];
-        run = t[0];   // head = run below: the lane's whole sum continues the open pair
-    } else {
-#pragma unroll
-        for (int g = 0; g < 4; g++) {
-            const uint32_t w32[4] = {cols[g].x, cols[g].y, cols[g].z, cols[g].w};
-            float v[8];
-#pragma unroll
-            for (int i = 0; i < 8; i++) v[i] = s_c[(w32[i >> 1] >> ((i & 1) * 16)) & 0xffffu];
-            // branch-free segmented sums: outv[i] is the total of the pair
-            // that ends just before edge 8g+i (outf[i]: it started in this
-            // lane); the slots of the group are loaded together, then stored to
-            float outv[8];
-            bool outf[8];
-            int32_t oidx[8];
-#pragma unroll
-            for (int i = 0; i < 8; i++) {
-                const bool st = (bits >> (8 * g + i)) & 1u;
-                outf[i] = st && started;
-                outv[i] = run;
-                oidx[i] = k;
-                head = (st && !started) ? run : head;
-                run = st ? 0.0f : run;
-                started = started || st;
-                k += st ? 1 : 0;
-                run += v[i];
-            }
-            int32_t sl[8];
-#pragma unroll
-            for (int i = 0; i < 8; i++)
-                if (outf[i]) sl[i] = __ldg(&a.slot[oidx[i]]);
-#pragma unroll
-            for (int i = 0; i < 8; i++)
-                if (outf[i]) a.P[sl[i]] = outv[i];
-        }
-    }
-    if (!started) head = run;
-    // T = sum of heads from this lane up to and including the first lane
-    // (>= this one) that has a start
-    float T = head;
-    int F = started;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        const float T2 = __shfl_down_sync(0xffffffffu, T, o);
-        const int F2 = __shfl_down_sync(0xffffffffu, F, o);
-        if (lane + o < 32 && !F) {
-            T += T2;
-            F |= F2;
-        }
-    }
-    const float Tn = __shfl_down_sync(0xffffffffu, T, 1);
-    const int Fn = __shfl_down_sync(0xffffffffu, F, 1);
-    const unsigned any = __ballot_sync(0xffffffffu, started);
-    if (started) {
-        const bool closed = lane < 31 && Fn;
-        const float total = run + (lane < 31 ? Tn : 0.0f);
-        if (closed) a.P[__ldg(&a.slot[k])] = total;
-        else a.ctail[ch] = total;   // the chunk's last pair runs on
-    }
-    if (lane == 0) {
-        a.chead[ch] = T;
-        a.cstart[ch] = any != 0u;
+        for (int j = 0; j < HUB_UNROLL; j++) wc[j] = wn[j];
     }
 }
 
 __global__ void __launch_bounds__(HUB_THREADS, 1) k_hub_sweep(HubArgs a)
 {
-    extern __shared__ __align__(128) float s_c[];   // [H + 4]
-    __shared__ __align__(8) uint64_t mbar;
+    extern __shared__ __align__(16) float s_c[];   // [H + 4]
     if (__ldg(a.more) == 0 || __ldg(a.off) != 0) return;
     const float *c = __ldg(a.cur) ? a.c[1] : a.c[0];
-    const uint32_t bar = smem_u32(&mbar);
-    if (threadIdx.x == 0) {
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar));
-        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-    }
     if (threadIdx.x < 4) s_c[a.H + threadIdx.x] = 0.0f;   // the padding id's slot
-    // this CTA's chunk range (balanced by edges and pair starts), cut at
-    // segment boundaries
-    const int32_t c_lo = __ldg(&a.cta_lo[blockIdx.x]), c_hi = __ldg(&a.cta_lo[blockIdx.x + 1]);
     const int32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    constexpr int32_t NW = HUB_THREADS / 32;
-    uint32_t phase = 0;
-    int32_t s = 0;
-    while (s < a.nseg && __ldg(&a.segchunk[s + 1]) <= c_lo) s++;
-    for (int32_t lo = c_lo; lo < c_hi && s < a.nseg; s++) {
-        const int32_t hi = min(c_hi, __ldg(&a.segchunk[s + 1]));
-        if (hi <= lo) continue;
+    const int32_t p0 = __ldg(&a.cpart[blockIdx.x]), p1 = __ldg(&a.cpart[blockIdx.x + 1]);
+    for (int32_t pi = p0; pi < p1; pi++) {
+        const int32_t s = __ldg(&a.pseg[pi]);
+        // stage c[s*H, s*H + len) (16-byte units; the arrays carry 16 bytes
+        // of slack past the last vertex)
         const int32_t base = s * a.H;
-        const int32_t len = min(a.H, a.n - base);
-        if (!stage_segment(s_c, c + base, (uint32_t)((len + 3) & ~3) * 4u, bar, phase, a.err)) return;
-        phase ^= 1u;
-        for (int32_t ch = lo + warp; ch < hi; ch += NW) {
-            const uint4 *src = reinterpret_cast<const uint4 *>(a.hcol + (int64_t)ch * HUB_CHUNK) + lane * 4;
-            uint4 cols[4];
+        const int32_t n4 = (min(a.H, a.n - base) + 3) >> 2;
+        __syncthreads();   // every warp is done with the previous segment
+        const float4 *src = reinterpret_cast<const float4 *>(c + base);
+        float4 *dst = reinterpret_cast<float4 *>(s_c);
+        // all of a thread's loads in flight at once, in batches of STAGE_BATCH
+        for (int32_t i0 = threadIdx.x; i0 < n4; i0 += STAGE_BATCH * HUB_THREADS) {
+            float4 v[STAGE_BATCH];
 #pragma unroll
-            for (int g = 0; g < 4; g++) cols[g] = __ldcs(src + g);
-            const uint32_t bits = __ldcs(&a.rstart[(int64_t)ch * 32 + lane]);
-            sweep_chunk(a, s_c, ch, cols, bits, __ldg(&a.crow[ch]));
+            for (int k = 0; k < STAGE_BATCH; k++) {
+                const int32_t i = i0 + k * HUB_THREADS;
+                if (i < n4) v[k] = __ldcg(&src[i]);
+            }
+#pragma unroll
+            for (int k = 0; k < STAGE_BATCH; k++) {
+                const int32_t i = i0 + k * HUB_THREADS;
+                if (i < n4) dst[i] = v[k];
+            }
         }
-        lo = hi;
-    }
-}
-
-// pairs that run past their chunk: the open tail plus the heads of the
-// following chunks up to and including the next chunk with a start
-// (cnext, fixed by the layout), summed in FP64 and rounded once: a hub row
-// can span hundreds of chunks, and an FP32 running sum of their heads would
-// carry rounding of a few 1e-6 that moves from sweep to sweep.  Spans of up
-// to FIX_SHORT chunks take a thread each; longer ones (clong) a warp each,
-// lane-strided then a fixed shuffle tree.  crow[ch + 1] - 1 is the pair
-// index of chunk ch's last start.
-__global__ void k_hub_fix(HubArgs a)
-{
-    if (__ldg(a.more) == 0 || __ldg(a.off) != 0) return;
-    const int32_t tid = blockIdx.x * blockDim.x + threadIdx.x, nth = gridDim.x * blockDim.x;
-    for (int32_t ch = tid; ch < a.nchunks; ch += nth) {
-        if (!__ldg(&a.cstart[ch])) continue;
-        const int32_t last = min(__ldg(&a.cnext[ch]), a.nchunks - 1);
-        if (last - ch > FIX_SHORT) continue;
-        double total = a.ctail[ch];
-        for (int32_t k = ch + 1; k <= last; k++) total += a.chead[k];
-        a.P[__ldg(&a.slot[__ldg(&a.crow[ch + 1]) - 1])] = (float)total;
-    }
-    const int lane = threadIdx.x & 31;
-    for (int32_t i = tid >> 5; i < a.nlong; i += nth >> 5) {
-        const int32_t ch = __ldg(&a.clong[i]);
-        const int32_t last = min(__ldg(&a.cnext[ch]), a.nchunks - 1);
-        double t = 0.0;
-        for (int32_t k = ch + 1 + lane; k <= last; k += 32) t += a.chead[k];
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
-        if (lane == 0) a.P[__ldg(&a.slot[__ldg(&a.crow[ch + 1]) - 1])] = (float)(t + (double)a.ctail[ch]);
+        __syncthreads();
+        const int32_t ga = __ldg(&a.wb[pi * 33 + warp]), gb = __ldg(&a.wb[pi * 33 + warp + 1]);
+        if (ga < gb) stream_groups(a, s_c, ga, gb, lane);
     }
 }
 
@@ -314,8 +178,8 @@ namespace mgi {
 void hub_free(mg_graph *g)
 {
     HubSplit &h = g->hub;
-    DevBuf *bufs[] = {&h.hcol, &h.rstart, &h.crow, &h.slot, &h.segchunk, &h.cta_lo, &h.pair_off, &h.P, &h.toff,
-                      &h.tcol, &h.chead, &h.ctail, &h.cstart, &h.cnext, &h.clong, &h.err};
+    DevBuf *bufs[] = {&h.hdat, &h.goff, &h.pslot, &h.segg, &h.cpart, &h.pseg, &h.wb, &h.pair_off, &h.P, &h.toff,
+                      &h.tcol, &h.fin};
     for (DevBuf *b : bufs) dev_free(*b);
     h = HubSplit();
 }
@@ -324,9 +188,8 @@ static std::atomic<uint64_t> g_hub_builds{0};
 
 // Build the segmented layout from the pull CSR (copied back from the
 // device): row-parallel host passes over the edges (count, then write),
-// each thread a contiguous row range whose share of every segment's stream
-// is contiguous too, so the streams come out segment-major with rows
-// ascending.
+// each thread a contiguous row range whose pieces take consecutive places
+// in every (segment, length) bucket, so buckets come out rows ascending.
 mg_status hub_prepare(mg_graph *g)
 {
     HubSplit &h = g->hub;
@@ -343,6 +206,7 @@ mg_status hub_prepare(mg_graph *g)
     const int32_t H = SEG_H;
     const int32_t nseg = std::min<int32_t>(SEG_MAX, (n + H - 1) / H);
     const int64_t cover = std::min<int64_t>(n, (int64_t)nseg * H);
+    constexpr int32_t L = PIECE_MAX;
     std::vector<int32_t> prow((size_t)n + 1), pcol((size_t)m);
     MG_CUDA(cudaMemcpyAsync(prow.data(), g->trow, ((size_t)n + 1) * 4, cudaMemcpyDeviceToHost, s));
     MG_CUDA(cudaMemcpyAsync(pcol.data(), g->tcol, (size_t)m * 4, cudaMemcpyDeviceToHost, s));
@@ -362,77 +226,86 @@ mg_status hub_prepare(mg_graph *g)
         fn(0);
         for (auto &x : th) x.join();
     };
-    // pass 1: per thread and segment the edges and pairs; per row its pairs
-    // and tail edges
-    std::vector<int64_t> tedge((size_t)nt * nseg, 0), tpair((size_t)nt * nseg, 0);
-    std::vector<int32_t> npair((size_t)n + 1, 0), ntail((size_t)n + 1, 0);
+    // bucket (segment sg, piece length lam) of thread t: bc[(t * nseg + sg) * (L + 1) + lam]
+    const size_t NB = (size_t)nseg * (L + 1);
+    std::vector<int64_t> bc((size_t)nt * NB, 0), tcov((size_t)nt, 0);
+    std::vector<int32_t> npc((size_t)n, 0), ntl((size_t)n, 0);
+    // pass 1: per row its pieces and tail edges; per thread its bucket counts
     run([&](int t) {
-        int64_t *te = &tedge[(size_t)t * nseg], *tp = &tpair[(size_t)t * nseg];
+        int64_t *b = &bc[(size_t)t * NB];
+        int32_t cnt[SEG_MAX];
+        int64_t cov = 0;
         for (int32_t v = rlo[t]; v < rlo[t + 1]; v++) {
-            uint64_t mask = 0;
-            int32_t nt_ = 0;
+            std::memset(cnt, 0, sizeof(int32_t) * nseg);
+            int32_t tl = 0;
             for (int32_t p = prow[v]; p < prow[v + 1]; p++) {
                 const int32_t c = pcol[p];
-                if (c < cover) {
-                    const int sg = c / H;
-                    te[sg]++;
-                    mask |= 1ull << sg;
-                } else {
-                    nt_++;
-                }
+                if (c < cover) cnt[c / H]++;
+                else tl++;
             }
-            npair[v] = __builtin_popcountll(mask);
-            ntail[v] = nt_;
-            for (uint64_t mm = mask; mm; mm &= mm - 1) tp[__builtin_ctzll(mm)]++;
+            int32_t pieces = 0;
+            for (int sg = 0; sg < nseg; sg++) {
+                if (!cnt[sg]) continue;
+                cov += cnt[sg];
+                const int32_t full = cnt[sg] / L, rem = cnt[sg] % L;
+                b[(size_t)sg * (L + 1) + L] += full;
+                if (rem) b[(size_t)sg * (L + 1) + rem]++;
+                pieces += full + (rem ? 1 : 0);
+            }
+            npc[v] = pieces;
+            ntl[v] = tl;
         }
+        tcov[t] = cov;
     });
     int64_t covered = 0;
-    for (int64_t x : tedge) covered += x;
+    for (int64_t x : tcov) covered += x;
     // the segmented pull pays when a quarter of the edges or more are covered
     if (covered * 4 < m) {
         h.valid = true;
         return MG_OK;
     }
-    // offsets: segments' chunks, per-thread shares, row-major pair slots, tail rows
-    std::vector<int32_t> segchunk((size_t)nseg + 1, 0);
-    std::vector<int64_t> segpair((size_t)nseg + 1, 0);
-    std::vector<int64_t> toffE((size_t)nt * nseg), toffP((size_t)nt * nseg);
+    // buckets in order: segments ascending, lengths descending; each padded
+    // to whole groups.  tb: thread t's first place in its bucket.
+    std::vector<int64_t> tb((size_t)nt * NB, 0);
+    std::vector<int32_t> segg((size_t)nseg + 1, 0);
+    std::vector<int32_t> glam;      // steps of every group
+    int64_t place = 0;              // padded place of the next bucket's first piece
     for (int sg = 0; sg < nseg; sg++) {
-        int64_t e = 0, pp = 0;
-        for (int t = 0; t < nt; t++) {
-            toffE[(size_t)t * nseg + sg] = e;
-            toffP[(size_t)t * nseg + sg] = segpair[sg] + pp;
-            e += tedge[(size_t)t * nseg + sg];
-            pp += tpair[(size_t)t * nseg + sg];
+        segg[sg] = (int32_t)glam.size();
+        for (int32_t lam = L; lam >= 1; lam--) {
+            const size_t k = (size_t)sg * (L + 1) + lam;
+            int64_t size = 0;
+            for (int t = 0; t < nt; t++) {
+                tb[(size_t)t * NB + k] = place + size;
+                size += bc[(size_t)t * NB + k];
+            }
+            const int64_t groups = (size + GROUP - 1) / GROUP;
+            for (int64_t q = 0; q < groups; q++) glam.push_back(lam);
+            place += groups * GROUP;
         }
-        segchunk[sg + 1] = segchunk[sg] + (int32_t)((e + HUB_CHUNK - 1) / HUB_CHUNK);
-        segpair[sg + 1] = segpair[sg] + pp;
     }
-    const int32_t nchunks = segchunk[nseg];
-    const int64_t npairs = segpair[nseg];
-    if (npairs > INT32_MAX || (int64_t)nchunks * HUB_CHUNK > INT32_MAX)
-        return fail(MG_ERR_RANGE, "segmented PageRank layout too large");
+    const int32_t ngroups = (int32_t)glam.size();
+    segg[nseg] = ngroups;
+    std::vector<int64_t> goff64((size_t)ngroups + 1, 0);
+    for (int32_t q = 0; q < ngroups; q++) goff64[q + 1] = goff64[q] + glam[q];
     std::vector<int32_t> pair_off((size_t)n + 1, 0), toff((size_t)n + 1, 0);
     for (int32_t v = 0; v < n; v++) {
-        pair_off[v + 1] = pair_off[v] + npair[v];
-        toff[v + 1] = toff[v] + ntail[v];
+        pair_off[v + 1] = pair_off[v] + npc[v];
+        toff[v + 1] = toff[v] + ntl[v];
     }
-    std::vector<uint16_t> hcol((size_t)nchunks * HUB_CHUNK, (uint16_t)H);
-    std::vector<uint32_t> rstart((size_t)nchunks * (HUB_CHUNK / 32), 0u);
-    std::vector<int32_t> slot((size_t)std::max<int64_t>(npairs, 1)), tcol((size_t)std::max<int32_t>(toff[n], 1));
-    // pass 2: every row's edges into its segments' streams.  A thread's
-    // share of a segment's stream starts on a chunk of its own only by
-    // chance, so the row-start bits are set with atomic ORs.
-    std::vector<std::atomic<uint32_t>> rbits((size_t)nchunks * (HUB_CHUNK / 32));
-    for (auto &b : rbits) b.store(0u, std::memory_order_relaxed);
+    const int64_t npieces = pair_off[n];
+    if (npieces >= INT32_MAX || goff64[ngroups] >= INT32_MAX)
+        return fail(MG_ERR_RANGE, "segmented PageRank layout too large");
+    std::vector<int32_t> goff(goff64.begin(), goff64.end());
+    std::vector<uint16_t> hdat((size_t)goff64[ngroups] * GROUP, (uint16_t)H);
+    std::vector<int32_t> pslot((size_t)ngroups * GROUP, (int32_t)npieces);
+    std::vector<int32_t> tcol((size_t)std::max<int32_t>(toff[n], 1));
+    // pass 2: every row's pieces into their buckets, every edge into its
+    // piece's step and lane
     run([&](int t) {
-        std::vector<int64_t> ep((size_t)nseg), pp((size_t)nseg);
-        for (int sg = 0; sg < nseg; sg++) {
-            ep[sg] = (int64_t)segchunk[sg] * HUB_CHUNK + toffE[(size_t)t * nseg + sg];
-            pp[sg] = toffP[(size_t)t * nseg + sg];
-        }
-        int32_t cnt[SEG_MAX];
-        int64_t start[SEG_MAX];
+        std::vector<int64_t> next(tb.begin() + (size_t)t * NB, tb.begin() + (size_t)(t + 1) * NB);
+        int32_t cnt[SEG_MAX], full[SEG_MAX], e[SEG_MAX];
+        int64_t qfull[SEG_MAX], qrem[SEG_MAX];
         for (int32_t v = rlo[t]; v < rlo[t + 1]; v++) {
             std::memset(cnt, 0, sizeof(int32_t) * nseg);
             int32_t tp = toff[v];
@@ -441,150 +314,153 @@ mg_status hub_prepare(mg_graph *g)
                 if (c < cover) cnt[c / H]++;
                 else tcol[tp++] = c;
             }
-            int32_t rank = 0;
+            int32_t slot = pair_off[v];   // the row's pieces: segments ascending, pieces in order
             for (int sg = 0; sg < nseg; sg++) {
+                e[sg] = 0;
                 if (!cnt[sg]) continue;
-                const int64_t e0 = ep[sg];
-                start[sg] = e0;
-                rbits[(size_t)(e0 >> 5)].fetch_or(1u << (e0 & 31), std::memory_order_relaxed);
-                slot[pp[sg]++] = pair_off[v] + rank++;
-                ep[sg] += cnt[sg];
+                full[sg] = cnt[sg] / L;
+                const int32_t rem = cnt[sg] % L;
+                int64_t &nf = next[(size_t)sg * (L + 1) + L];
+                qfull[sg] = nf;
+                for (int32_t i = 0; i < full[sg]; i++) pslot[(size_t)(nf++)] = slot++;
+                if (rem) {
+                    int64_t &nr = next[(size_t)sg * (L + 1) + rem];
+                    qrem[sg] = nr;
+                    pslot[(size_t)(nr++)] = slot++;
+                }
             }
             for (int32_t p = prow[v]; p < prow[v + 1]; p++) {
                 const int32_t c = pcol[p];
-                if (c < cover) {
-                    const int sg = c / H;
-                    hcol[start[sg]++] = (uint16_t)(c - sg * H);
-                }
+                if (c >= cover) continue;
+                const int sg = c / H;
+                const int32_t i = e[sg] / L, k = e[sg] % L;
+                e[sg]++;
+                const int64_t q = i < full[sg] ? qfull[sg] + i : qrem[sg];
+                const int64_t grp = q / GROUP;
+                hdat[(size_t)(goff64[grp] * GROUP + (int64_t)k * GROUP + q % GROUP)] = (uint16_t)(c - sg * H);
             }
         }
     });
-    for (size_t i = 0; i < rstart.size(); i++) rstart[i] = rbits[i].load(std::memory_order_relaxed);
-    // pair index of every chunk's first start; span of every chunk's last pair
-    std::vector<int32_t> crow((size_t)nchunks + 1, 0), cnext((size_t)std::max(nchunks, 1), 0), clong;
-    for (int32_t ch = 0; ch < nchunks; ch++) {
-        int32_t k = 0;
-        for (int w = 0; w < HUB_CHUNK / 32; w++) k += __builtin_popcount(rstart[(size_t)ch * (HUB_CHUNK / 32) + w]);
-        crow[ch + 1] = crow[ch] + k;
-    }
-    {
-        int32_t next = nchunks;
-        for (int32_t ch = nchunks - 1; ch >= 0; ch--) {
-            cnext[ch] = next;
-            if (crow[ch + 1] > crow[ch]) {
-                if (std::min(next, nchunks - 1) - ch > FIX_SHORT) clong.push_back(ch);
-                next = ch;
-            }
-        }
-    }
-    // CTA ranges: a chunk costs its 1024 edges plus START_COST per pair start
-    // (the slot load and scattered store of a short pair's total); chunk
-    // counts alone left one SM four times as busy as the average
+    // CTA ranges, balanced by cost: a group costs its steps plus
+    // GROUP_COST (its slot loads and scattered stores); each range cut at
+    // segment boundaries into parts, each part split over the CTA's warps
+    // by the same cost
     const int G = g->num_sms;
-    std::vector<int32_t> cta_lo((size_t)G + 1, nchunks);
-    {
-        const int64_t total = (int64_t)nchunks * HUB_CHUNK + START_COST * (int64_t)crow[nchunks];
-        int64_t acc = 0;
-        int b = 0;
-        cta_lo[0] = 0;
-        for (int32_t ch = 0; ch < nchunks && b + 1 < G; ch++) {
-            acc += HUB_CHUNK + START_COST * (int64_t)(crow[ch + 1] - crow[ch]);
-            while (b + 1 < G && acc * G >= total * (b + 1)) cta_lo[++b] = ch + 1;
+    constexpr int NW = HUB_THREADS / 32;
+    std::vector<int64_t> gcum((size_t)ngroups + 1, 0);
+    for (int32_t q = 0; q < ngroups; q++) gcum[q + 1] = gcum[q] + glam[q] + GROUP_COST;
+    auto cut = [&](int32_t lo, int32_t hi, int parts, int32_t *out) {
+        // out[0..parts]: boundaries in [lo, hi] of equal cost
+        out[0] = lo;
+        for (int k = 1; k < parts; k++) {
+            const int64_t goal = gcum[lo] + (gcum[hi] - gcum[lo]) * k / parts;
+            int32_t b = (int32_t)(std::lower_bound(gcum.begin() + lo, gcum.begin() + hi, goal) - gcum.begin());
+            out[k] = std::min(std::max(b, out[k - 1]), hi);
         }
-        while (b + 1 <= G) cta_lo[++b] = nchunks;
+        out[parts] = hi;
+    };
+    std::vector<int32_t> cta_lo((size_t)G + 1);
+    cut(0, ngroups, G, cta_lo.data());
+    std::vector<int32_t> cpart((size_t)G + 1, 0), pseg, wb;
+    for (int b = 0; b < G; b++) {
+        cpart[b] = (int32_t)pseg.size();
+        int32_t lo = cta_lo[b];
+        const int32_t hi = cta_lo[b + 1];
+        while (lo < hi) {
+            const int32_t sg = (int32_t)(std::upper_bound(segg.begin(), segg.end(), lo) - segg.begin()) - 1;
+            const int32_t e = std::min(hi, segg[sg + 1]);
+            pseg.push_back(sg);
+            const size_t k = wb.size();
+            wb.resize(k + NW + 1);
+            cut(lo, e, NW, &wb[k]);
+            lo = e;
+        }
+    }
+    cpart[G] = (int32_t)pseg.size();
+    // finish bins (rows of graphs without a tail finish in k_pr_seg)
+    std::vector<int32_t> fin((size_t)n);
+    int32_t nfw = 0, nfg = 0, nft = 0;
+    for (int32_t v = 0; v < n; v++) nfw += npc[v] > FIN_WARP;
+    for (int32_t v = 0; v < n; v++) nfg += npc[v] > FIN_THREAD && npc[v] <= FIN_WARP;
+    nft = n - nfw - nfg;
+    {
+        int32_t iw = 0, ig = nfw, it = nfw + nfg;
+        for (int32_t v = 0; v < n; v++) {
+            if (npc[v] > FIN_WARP) fin[(size_t)iw++] = v;
+            else if (npc[v] > FIN_THREAD) fin[(size_t)ig++] = v;
+            else fin[(size_t)it++] = v;
+        }
     }
     auto up = [&](DevBuf &b, const void *src, size_t bytes) -> mg_status {
         MG_TRY(dev_alloc(b, std::max<size_t>(bytes, 16) + 16));
         if (bytes) MG_CUDA(cudaMemcpyAsync(b.p, src, bytes, cudaMemcpyHostToDevice, s));
         return MG_OK;
     };
-    MG_TRY(up(h.hcol, hcol.data(), hcol.size() * 2));
-    MG_TRY(up(h.rstart, rstart.data(), rstart.size() * 4));
-    MG_TRY(up(h.crow, crow.data(), crow.size() * 4));
-    MG_TRY(up(h.slot, slot.data(), (size_t)npairs * 4));
-    MG_TRY(up(h.segchunk, segchunk.data(), segchunk.size() * 4));
-    MG_TRY(up(h.cta_lo, cta_lo.data(), cta_lo.size() * 4));
+    MG_TRY(up(h.hdat, hdat.data(), hdat.size() * 2));
+    MG_TRY(up(h.goff, goff.data(), goff.size() * 4));
+    MG_TRY(up(h.pslot, pslot.data(), pslot.size() * 4));
+    MG_TRY(up(h.segg, segg.data(), segg.size() * 4));
+    MG_TRY(up(h.cpart, cpart.data(), cpart.size() * 4));
+    MG_TRY(up(h.pseg, pseg.data(), pseg.size() * 4));
+    MG_TRY(up(h.wb, wb.data(), wb.size() * 4));
     MG_TRY(up(h.pair_off, pair_off.data(), pair_off.size() * 4));
     MG_TRY(up(h.toff, toff.data(), toff.size() * 4));
     MG_TRY(up(h.tcol, tcol.data(), (size_t)toff[n] * 4));
-    MG_TRY(up(h.cnext, cnext.data(), (size_t)nchunks * 4));
-    MG_TRY(up(h.clong, clong.data(), clong.size() * 4));
-    MG_TRY(dev_alloc(h.P, (size_t)std::max<int64_t>(npairs, 1) * 4));
-    MG_TRY(dev_alloc(h.chead, (size_t)std::max(nchunks, 1) * 4));
-    MG_TRY(dev_alloc(h.ctail, (size_t)std::max(nchunks, 1) * 4));
-    MG_TRY(dev_alloc(h.cstart, (size_t)std::max(nchunks, 1) * 4));
-    MG_TRY(dev_alloc(h.err, 16));
-    MG_CUDA(cudaMemsetAsync(h.err.p, 0, 16, s));
+    MG_TRY(up(h.fin, fin.data(), fin.size() * 4));
+    MG_TRY(dev_alloc(h.P, (size_t)(npieces + 1) * 4));
     MG_CUDA(cudaStreamSynchronize(s));
     h.H = H;
     h.nseg = nseg;
-    h.nchunks = nchunks;
-    h.npairs = npairs;
-    h.nlong = (int32_t)clong.size();
+    h.ngroups = ngroups;
+    h.npieces = npieces;
     h.covered = covered;
     h.ntail = toff[n];
     h.grid = G;
+    h.nfw = nfw;
+    h.nfg = nfg;
+    h.nft = nft;
     h.use = true;
     h.valid = true;
     return MG_OK;
 }
 
+bool hub_covers_all(const mg_graph *g) { return (int64_t)g->nv <= (int64_t)SEG_MAX * SEG_H; }
+
 size_t hub_smem_bytes(const mg_graph *g) { return (size_t)(g->hub.H + 4) * 4; }
 
 mg_status hub_launch(mg_graph *g, const float *c0, const float *c1, const int32_t *cur, const int32_t *more,
-                     const int32_t *off, cudaStream_t st, int slot_sweep, int slot_fix)
+                     const int32_t *off, cudaStream_t st, int slot_sweep)
 {
     HubSplit &h = g->hub;
     HubArgs a;
     std::memset(&a, 0, sizeof(a));
-    a.hcol = h.hcol.as<uint16_t>();
-    a.rstart = h.rstart.as<uint32_t>();
-    a.crow = h.crow.as<int32_t>();
-    a.slot = h.slot.as<int32_t>();
-    a.segchunk = h.segchunk.as<int32_t>();
-    a.cta_lo = h.cta_lo.as<int32_t>();
+    a.hdat = h.hdat.as<uint2>();
+    a.goff = h.goff.as<int32_t>();
+    a.pslot = h.pslot.as<int4>();
+    a.cpart = h.cpart.as<int32_t>();
+    a.pseg = h.pseg.as<int32_t>();
+    a.wb = h.wb.as<int32_t>();
     a.c[0] = c0;
     a.c[1] = c1;
     a.cur = cur;
     a.more = more;
     a.off = off;
     a.P = h.P.as<float>();
-    a.chead = h.chead.as<float>();
-    a.ctail = h.ctail.as<float>();
-    a.cstart = h.cstart.as<int32_t>();
-    a.cnext = h.cnext.as<int32_t>();
-    a.clong = h.clong.as<int32_t>();
-    a.nlong = h.nlong;
-    a.err = h.err.as<int32_t>();
     a.n = g->nv;
     a.H = h.H;
     a.nseg = h.nseg;
-    a.nchunks = h.nchunks;
     const size_t smem = hub_smem_bytes(g);
     MG_CUDA(cudaFuncSetAttribute(k_hub_sweep, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     Profiler &P = g->prof;
     P.begin(slot_sweep);
     k_hub_sweep<<<h.grid, HUB_THREADS, smem, st>>>(a);
     P.end();
-    P.begin(slot_fix);
-    k_hub_fix<<<std::max(1, std::min(g->num_sms * 4, (h.nchunks + 255) / 256)), 256, 0, st>>>(a);
-    P.end();
     MG_CUDA(cudaGetLastError());
     return MG_OK;
 }
 
-// a bulk-copy wait of some sweep ran out (read after the run)
-mg_status hub_check(mg_graph *g)
-{
-    if (!g->hub.use) return MG_OK;
-    int32_t e = 0;
-    MG_CUDA(cudaMemcpyAsync(&e, g->hub.err.p, 4, cudaMemcpyDeviceToHost, g->stream));
-    MG_CUDA(cudaStreamSynchronize(g->stream));
-    if (e) {
-        MG_CUDA(cudaMemsetAsync(g->hub.err.p, 0, 4, g->stream));
-        return fail(MG_ERR_CUDA, "PageRank segmented sweep: shared-memory staging did not complete");
-    }
-    return MG_OK;
-}
+// The sweep has no waits of its own (plain loads stage the segments), so
+// there is nothing to report after a run.
+mg_status hub_check(mg_graph *) { return MG_OK; }
 
 }  // namespace mgi

@@ -93,6 +93,8 @@ struct PArgs {
     const int32_t *prow_full;
     int32_t chunk;
     int32_t seg_only;        // every in-edge sits in a segment: rows finish in k_pr_seg
+    const int32_t *fin;      // k_pr_seg's rows: [nfw warp rows | nfg 8-lane rows | nft thread rows]
+    int32_t nfw, nfg, nft;
     float *x[2];             // iterate (ping-pong)
     float *c[2];             // gathered quantity: contribution x/deg (PR) or lambda (adjoint)
     const float *gvec;       // adjoint: g
@@ -284,21 +286,32 @@ __device__ __forceinline__ bool pr_row_skipped(const PArgs &a, int32_t v)
     return Op::kDataDriven && a.active[v] == 0;
 }
 
-__device__ __forceinline__ void block_partials(const PArgs &a, int slot, double r, double dg, int any,
+// Per-block partials to bpart[slot]: the L1 change and the dangling mass
+// summed in FP32 within each warp (FP64 arithmetic is slow on this part; a
+// warp adds 32 per-thread FP32 sums), then in FP64 across warps; the
+// data-driven form's active in-edge count and frozen dangling mass stay FP64
+// throughout.
+template <bool kDD>
+__device__ __forceinline__ void block_partials(const PArgs &a, int slot, float r, float dg, int any,
                                                double act = 0.0, double dfz = 0.0)
 {
     __shared__ double sp[NPART - 1][THREADS / 32];
     __shared__ int sa[THREADS / 32];
-    double v[NPART - 1] = {r, dg, act, dfz};
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
-#pragma unroll
-        for (int k = 0; k < NPART - 1; k++) v[k] += __shfl_xor_sync(0xffffffffu, v[k], o);
+        r += __shfl_xor_sync(0xffffffffu, r, o);
+        dg += __shfl_xor_sync(0xffffffffu, dg, o);
         any |= __shfl_xor_sync(0xffffffffu, any, o);
+        if (kDD) {
+            act += __shfl_xor_sync(0xffffffffu, act, o);
+            dfz += __shfl_xor_sync(0xffffffffu, dfz, o);
+        }
     }
     if ((threadIdx.x & 31) == 0) {
-#pragma unroll
-        for (int k = 0; k < NPART - 1; k++) sp[k][threadIdx.x >> 5] = v[k];
+        sp[0][threadIdx.x >> 5] = (double)r;
+        sp[1][threadIdx.x >> 5] = (double)dg;
+        sp[2][threadIdx.x >> 5] = kDD ? act : 0.0;
+        sp[3][threadIdx.x >> 5] = kDD ? dfz : 0.0;
         sa[threadIdx.x >> 5] = any;
     }
     __syncthreads();
@@ -350,10 +363,11 @@ struct PrRowOp {
     }
     __device__ float combine(float x, float y) const { return x + y; }
     __device__ void flush() {}
-    __device__ void finish(int32_t v, float s)
+    __device__ void finish(int32_t v, float s) { finish_row(v, s + seg_sum(a, v)); }
+    // the row's whole in-edge sum s
+    __device__ void finish_row(int32_t v, float s)
     {
         float dg = 0.0f;
-        s += seg_sum(a, v);
         resid += Op::apply(a, c, v, s, any, dg);
         dangs += dg;
         if (Op::kDataDriven) {
@@ -419,7 +433,7 @@ __global__ void __launch_bounds__(THREADS) k_pr_light(PArgs a)
         }
         __syncthreads();
     }
-    block_partials(a, blockIdx.x, op.resid, op.dangs, op.any, op.act, op.dfz);
+    block_partials<Op::kDataDriven>(a, blockIdx.x, op.resid, op.dangs, op.any, op.act, op.dfz);
 }
 
 // Sum of the partials of slots [s0, s1): lane-strided in slot order, then a
@@ -492,17 +506,51 @@ __device__ __forceinline__ bool last_block(PCtl *cp)
 }
 
 // Row finish when every in-edge sits in a segment (no tail, no heavy-row
-// chunks): a thread per row sums its pairs' partials (segments ascending;
-// consecutive rows read consecutive pair ranges) and applies the update.
+// chunks): each row sums its pieces' partials (P[pair_off[v] ..], segments
+// ascending) and applies the update.  Rows are binned by piece count at
+// layout time: long rows a warp each (lane-strided, then a fixed xor tree),
+// the rest a thread each (compensated FP32, four loads in flight) --
+// fixed orders, so sweeps stay reproducible.
 template <class Op>
-__global__ void __launch_bounds__(THREADS) k_pr_seg(PArgs a)
+__global__ void __launch_bounds__(THREADS, 8) k_pr_seg(PArgs a)
 {
     const PCtl c = *a.ctl;
     if (c.more == 0 || c.sparse) return;
     PrRowOp<Op> op{a, c};
-    for (int32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < a.n; v += gridDim.x * blockDim.x)
-        op.finish(v, 0.0f);
-    block_partials(a, blockIdx.x, op.resid, op.dangs, op.any, op.act, op.dfz);
+    const int lane = mgd::lane();
+    const int gwarp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int nwarps = (gridDim.x * blockDim.x) >> 5;
+    const int32_t *fw = a.fin, *ft = a.fin + a.nfw + a.nfg;
+    for (int32_t i = gwarp; i < a.nfw; i += nwarps) {
+        const int32_t v = __ldg(&fw[i]);
+        // compensated sums, lane-strided then a compensated xor tree: a
+        // long row's total stays steady between sweeps
+        float s = 0.0f, r = 0.0f;
+        if (!op.skip(v))
+            for (int32_t p = __ldg(&a.pair_off[v]) + lane, e = __ldg(&a.pair_off[v + 1]); p < e; p += 32)
+                mgd::kahan_add(s, r, __ldcg(&a.P[p]));
+        const float tot = mgd::warp_sum_comp(s, r);
+        if (lane == 0) op.finish_row(v, tot);
+    }
+    for (int32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < a.nft; i += gridDim.x * blockDim.x) {
+        const int32_t v = __ldg(&ft[i]);
+        float s = 0.0f, r = 0.0f;
+        if (!op.skip(v)) {
+            int32_t p = __ldg(&a.pair_off[v]);
+            const int32_t e = __ldg(&a.pair_off[v + 1]);
+            for (; p + 4 <= e; p += 4) {
+                const float f0 = __ldcg(&a.P[p]), f1 = __ldcg(&a.P[p + 1]), f2 = __ldcg(&a.P[p + 2]),
+                            f3 = __ldcg(&a.P[p + 3]);
+                mgd::kahan_add(s, r, f0);
+                mgd::kahan_add(s, r, f1);
+                mgd::kahan_add(s, r, f2);
+                mgd::kahan_add(s, r, f3);
+            }
+            for (; p < e; p++) mgd::kahan_add(s, r, __ldcg(&a.P[p]));
+        }
+        op.finish_row(v, s - r);
+    }
+    block_partials<Op::kDataDriven>(a, blockIdx.x, op.resid, op.dangs, op.any, op.act, op.dfz);
 }
 
 // Heavy rows (warp per row, chunk partials summed lane-strided then by a
@@ -548,7 +596,7 @@ __global__ void __launch_bounds__(THREADS) k_pr_apply(PArgs a, cudaGraphConditio
             else dfz += dg;
         }
     }
-    block_partials(a, a.nblocks + blockIdx.x, resid, dangs, any, act, dfz);
+    block_partials<Op::kDataDriven>(a, a.nblocks + blockIdx.x, (float)resid, (float)dangs, any, act, dfz);
     if (!last_block(cp)) return;
     double T[NPART - 1];
     int A;
@@ -660,7 +708,7 @@ __global__ void __launch_bounds__(THREADS) k_prd_gather(PArgs a)
         qb = __shfl_sync(0xffffffffu, qb, 0);
         if (keep) nextq[qb + __popc(km & ((1u << lane) - 1u))] = v;
     }
-    block_partials(a, blockIdx.x, resid, dangs, any, act, dfz);
+    block_partials<true>(a, blockIdx.x, (float)resid, (float)dangs, any, act, dfz);
 }
 
 // apply the queue sweep's values in place, then the last block updates the
@@ -1006,11 +1054,11 @@ static mg_status pr_loop(mg_graph *g, PArgs &a, const mg_opts &opt, const char *
     const int sh = P.slot(hn.c_str());
     const int apply_grid = std::max(1, std::min(std::min(grid, (a.nhrows + THREADS - 1) / THREADS),
                                                 g->num_sms * APPLY_PER_SM));
-    const int shs = a.P ? P.slot("pr_hub") : -1, shf = a.P ? P.slot("pr_hub_fix") : -1;
+    const int shs = a.P ? P.slot("pr_hub") : -1;
     const int sqc = Op::kDataDriven ? P.slot("prd_compact") : -1, sqg = Op::kDataDriven ? P.slot("prd_gather") : -1,
               sqa = Op::kDataDriven ? P.slot("prd_apply") : -1;
     BodyFn body = [&](cudaStream_t st, cudaGraphConditionalHandle h, int use_cond) -> mg_status {
-        if (a.P) MG_TRY(hub_launch(g, a.c[0], a.c[1], &a.ctl->cur, &a.ctl->more, &a.ctl->sparse, st, shs, shf));
+        if (a.P) MG_TRY(hub_launch(g, a.c[0], a.c[1], &a.ctl->cur, &a.ctl->more, &a.ctl->sparse, st, shs));
         P.begin(sl);
         if (a.seg_only) k_pr_seg<Op><<<grid, THREADS, 0, st>>>(a);
         else k_pr_light<Op><<<grid, THREADS, 0, st>>>(a);
@@ -1100,6 +1148,12 @@ static mg_status pr_setup(mg_graph *g, PArgs &a, bool weighted_or_adj, int32_t l
     a.queue[1] = w->q1.as<int32_t>();
     a.qval = w->qval.as<float>();
     a.m = g->ne;
+    // AUTO: segmented when the segments hold every source id (a graph with
+    // ids past them gathers the rest through L2 and sums each row's parts
+    // one by one, slower than the binned gather sweep), unless mg_autotune
+    // measured otherwise
+    if (layout == MG_PR_LAYOUT_AUTO)
+        layout = (!g->pr_prefer_gather && hub_covers_all(g)) ? MG_PR_LAYOUT_SEGMENTED : MG_PR_LAYOUT_GATHER;
     if (!weighted_or_adj && layout == MG_PR_LAYOUT_SEGMENTED) {
         MG_TRY(hub_prepare(g));
         if (g->hub.use) {
@@ -1110,6 +1164,10 @@ static mg_status pr_setup(mg_graph *g, PArgs &a, bool weighted_or_adj, int32_t l
             if (g->hub.ntail == 0) {
                 // rows finish in k_pr_seg; k_pr_apply only reduces
                 a.seg_only = 1;
+                a.fin = g->hub.fin.as<int32_t>();
+                a.nfw = g->hub.nfw;
+                a.nfg = g->hub.nfg;
+                a.nft = g->hub.nft;
                 a.nhchunks = 0;
                 a.nhrows = 0;
             }
@@ -1161,7 +1219,8 @@ mg_status mg_pagerank(mg_graph *g, int32_t variant, const mg_opts *o, float *ran
     mg_opts opt;
     MG_TRY(begin_run(g, o, opt, info));
     if (variant < 0 || variant > 3) return fail(MG_ERR_INVALID, "unknown PageRank variant %d", variant);
-    if (opt.pr_layout != MG_PR_LAYOUT_GATHER && opt.pr_layout != MG_PR_LAYOUT_SEGMENTED)
+    if (opt.pr_layout != MG_PR_LAYOUT_GATHER && opt.pr_layout != MG_PR_LAYOUT_SEGMENTED &&
+        opt.pr_layout != MG_PR_LAYOUT_AUTO)
         return fail(MG_ERR_INVALID, "unknown PageRank layout %d", opt.pr_layout);
     PArgs a;
     MG_TRY(pr_setup(g, a, false, opt.pr_layout));

@@ -14,7 +14,9 @@
 // in a text file keyed by a graph signature (n, m and a log2 degree
 // histogram).  Cache lines: signature, algorithm, then alpha / beta /
 // direction, or heavy threshold / chunk edges / thread-bin cutoff for
-// PageRank.
+// PageRank, the winner's time, and for PageRank the layout that
+// MG_PR_LAYOUT_AUTO takes on the graph (gather or segmented, whichever ran
+// faster once the gather layout's bins were tuned).
 
 #include "mg_device.cuh"
 
@@ -54,11 +56,14 @@ bool cache_lookup(const char *path, uint64_t sig, int algo, mg_opts *o)
     bool found = false;
     while (std::fgets(line, sizeof(line), f)) {
         unsigned long long s;
-        int a, alpha, beta, dir;
-        if (std::sscanf(line, "%llx %d %d %d %d", &s, &a, &alpha, &beta, &dir) == 5 && s == sig && a == algo) {
+        int a, alpha, beta, dir, lay = -1;
+        double ms;
+        const int k = std::sscanf(line, "%llx %d %d %d %d %lf %d", &s, &a, &alpha, &beta, &dir, &ms, &lay);
+        if (k >= 5 && s == sig && a == algo) {
             o->alpha = alpha;
             o->beta = beta;
             o->direction = dir;
+            if (algo == MG_ALGO_PR && k == 7) o->pr_layout = lay;   // the layout MG_PR_LAYOUT_AUTO takes
             found = true;  // the last entry wins
         }
     }
@@ -71,16 +76,38 @@ void cache_store(const char *path, uint64_t sig, int algo, const mg_opts &o, dou
     if (!path) return;
     FILE *f = std::fopen(path, "a");
     if (!f) return;
-    std::fprintf(f, "%llx %d %d %d %d %.4f\n", (unsigned long long)sig, algo, o.alpha, o.beta, o.direction, ms);
+    std::fprintf(f, "%llx %d %d %d %d %.4f %d\n", (unsigned long long)sig, algo, o.alpha, o.beta, o.direction, ms,
+                 o.pr_layout);
     std::fclose(f);
 }
 
-// PageRank: heavy-row threshold x chunk size of the pull layout
+// median device time of four PageRank runs after a warm-up run
+static mg_status pr_median_ms(mg_graph *g, const mg_opts &o, double *ms)
+{
+    std::vector<double> t;
+    for (int rep = 0; rep < 4; rep++) {
+        mg_run_info info;
+        MG_TRY(mg_pagerank(g, MG_PR_TOPOLOGY, &o, nullptr, &info));
+        if (rep > 0) t.push_back(info.device_ms);  // first run warms the graph
+    }
+    std::sort(t.begin(), t.end());
+    *ms = t[t.size() / 2];
+    return MG_OK;
+}
+
+// PageRank: heavy-row threshold x chunk size x thread-bin cutoff of the
+// gather layout's degree bins (timed with that layout), then whether the
+// segmented layout beats the tuned gather layout on this graph (the choice
+// of MG_PR_LAYOUT_AUTO)
 mg_status tune_pr_layout(mg_graph *g, const char *cache_path, uint64_t sig, const mg_opts &base)
 {
     mg_opts cached = base;
-    if (cache_lookup(cache_path, sig, MG_ALGO_PR, &cached))
+    cached.pr_layout = -1;   // set by a cache line that records the layout
+    if (cache_lookup(cache_path, sig, MG_ALGO_PR, &cached)) {
+        if (cached.pr_layout == MG_PR_LAYOUT_GATHER || cached.pr_layout == MG_PR_LAYOUT_SEGMENTED)
+            g->pr_prefer_gather = cached.pr_layout == MG_PR_LAYOUT_GATHER;
         return mgi::rebin(g, cached.alpha, cached.beta, cached.direction);
+    }
     struct Cand { int heavy, chunk, tbin; };
     std::vector<Cand> cands;
     const int hc[][2] = {{256, 1024}, {256, 2048}, {512, 1024}, {512, 2048}, {512, 4096}, {1024, 2048},
@@ -94,21 +121,26 @@ mg_status tune_pr_layout(mg_graph *g, const char *cache_path, uint64_t sig, cons
         mg_opts o = base;
         o.exec = MG_EXEC_GRAPH;
         o.profile = 0;
-        std::vector<double> t;
-        for (int rep = 0; rep < 4; rep++) {
-            mg_run_info info;
-            MG_TRY(mg_pagerank(g, MG_PR_TOPOLOGY, &o, nullptr, &info));
-            if (rep > 0) t.push_back(info.device_ms);  // first run warms the graph
-        }
-        std::sort(t.begin(), t.end());
-        const double med = t[t.size() / 2];
+        o.pr_layout = MG_PR_LAYOUT_GATHER;
+        double med = 0.0;
+        MG_TRY(pr_median_ms(g, o, &med));
         if (med < best_ms) { best_ms = med; best = c; }
     }
     MG_TRY(mgi::rebin(g, best.heavy, best.chunk, best.tbin));
+    {
+        mg_opts o = base;
+        o.exec = MG_EXEC_GRAPH;
+        o.profile = 0;
+        o.pr_layout = MG_PR_LAYOUT_SEGMENTED;
+        double seg_ms = 0.0;
+        MG_TRY(pr_median_ms(g, o, &seg_ms));
+        g->pr_prefer_gather = seg_ms > best_ms;
+    }
     mg_opts rec = base;
     rec.alpha = best.heavy;
     rec.beta = best.chunk;
     rec.direction = best.tbin;
+    rec.pr_layout = g->pr_prefer_gather ? MG_PR_LAYOUT_GATHER : MG_PR_LAYOUT_SEGMENTED;
     cache_store(cache_path, sig, MG_ALGO_PR, rec, best_ms);
     return MG_OK;
 }

@@ -162,6 +162,31 @@ def test_sssp_small_and_zero_weights(direction, wmax):
     g.free()
 
 
+def test_pagerank_segmented_past_the_segments():
+    """A graph with more vertex ids than the 64 shared-memory segments hold
+    (a 2048 x 2048 lattice with shortcuts: 4.19 M vertices against 3.67 M):
+    the forced segmented layout sums the covered in-edges from shared memory
+    and gathers the rest through L2; the default layout takes the gather
+    sweep there.  Both against the FP64 oracle, and the default bit for bit
+    against the forced gather layout."""
+    h = mg.HostGraph.lattice(2048, 2048, 0.05, seed=5)
+    rp, col, wt = h.arrays()
+    og = O.csr_from_arrays(rp, col, wt)
+    g = mg.Graph(h)
+    try:
+        assert og.nv > 64 * 57344
+        for lay in (mg.PR_LAYOUT_SEGMENTED, mg.PR_LAYOUT_GATHER):
+            x, info = g.pagerank(mg.PR_TOPOLOGY, tol=1e-6, pr_layout=lay)
+            ref, _ = O.pr_norm_f64(og, 0.85, 1e-6, info.iterations)
+            assert float(np.max(np.abs(x.astype(np.float64) - ref))) < 1e-6, lay
+            if lay == mg.PR_LAYOUT_GATHER:
+                xa, _ = g.pagerank(mg.PR_TOPOLOGY, tol=1e-6)
+                assert np.array_equal(xa, x)
+    finally:
+        g.free()
+        h.free()
+
+
 @pytest.mark.parametrize("layout", ["gather", "segmented"])
 @pytest.mark.parametrize("scale", [17, 18])
 def test_pagerank_hub_split(scale, layout):
