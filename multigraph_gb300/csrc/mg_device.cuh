@@ -118,7 +118,8 @@ struct HubSplit {
     DevBuf segg;             // int32 [nseg+1]: first group of each segment
     DevBuf cpart;            // int32 [grid+1]: each CTA's parts (a part: one segment's groups)
     DevBuf pseg;             // int32 [nparts]: each part's segment
-    DevBuf wb;               // int32 [nparts*33]: each part's group range per warp
+    DevBuf pch;              // int32 [nparts+1]: each part's chunks (claimed by its CTA's warps)
+    DevBuf cb;               // int32 [nchunks+1]: chunk boundaries (group indices)
     DevBuf pair_off;         // int32 [n+1]: row v's pieces in P
     DevBuf P;                // float [npieces+1]: piece sums of the current sweep (+ padding slot)
     DevBuf toff, tcol;       // tail rows: offsets [n+1], int32 ids

@@ -26,9 +26,10 @@
 //                     sweep.
 // One sweep: k_hub_sweep gives each CTA a contiguous range of groups
 // (balanced by the groups' steps plus a fixed cost per group), stages the
-// contributions c[s*H, (s+1)*H) of every segment its range enters, and each
-// warp sums one group at a time: a lane adds its four pieces' edges in order
-// from shared memory and stores the four totals to P.  Pieces never cross a
+// contributions c[s*H, (s+1)*H) of every segment its range enters, and its
+// warps claim chunks of consecutive groups from a shared-memory counter and
+// stream them: a lane adds its four pieces' edges in order from shared
+// memory and stores the four totals to P.  Pieces never cross a
 // group, so there are no carries between lanes, warps or CTAs; every sum is
 // formed in a fixed order, so sweeps are reproducible.
 //
@@ -53,6 +54,7 @@ constexpr int HUB_THREADS = 1024;   // one CTA per SM (shared memory bound)
 constexpr int HUB_UNROLL = 4;       // steps (256-byte warp loads) in flight per warp
 constexpr int STAGE_BATCH = 4;      // 16-byte loads in flight per thread while staging a segment
 constexpr int64_t GROUP_COST = 16;  // a group's fixed cost in steps, for balancing CTA ranges
+constexpr int64_t CHUNK_COST = 128; // a chunk's cost (steps + GROUP_COST per group): the unit warps claim
 // finish bins by pieces per row: rows with more than FIN_WARP pieces a warp
 // each, the rest a thread each (8-lane groups, FIN_THREAD < pieces <=
 // FIN_WARP, walked rows one after another and were slower)
@@ -65,7 +67,8 @@ struct HubArgs {
     const int4 *pslot;        // [ngroups*GROUP/4] the four P slots of each lane's pieces
     const int32_t *cpart;     // [grid+1] each CTA's parts
     const int32_t *pseg;      // [nparts] each part's segment
-    const int32_t *wb;        // [nparts*33] each part's group range per warp
+    const int32_t *pch;       // [nparts+1] each part's chunks
+    const int32_t *cb;        // [nchunks+1] chunk k = groups [cb[k], cb[k+1])
     const float *c[2];        // contributions (ping-pong, ctl selects)
     const int32_t *cur;       // current iterate index (loop control block)
     const int32_t *more;      // loop continue flag
@@ -140,7 +143,8 @@ __global__ void __launch_bounds__(HUB_THREADS, 1) k_hub_sweep(HubArgs a)
     if (__ldg(a.more) == 0 || __ldg(a.off) != 0) return;
     const float *c = __ldg(a.cur) ? a.c[1] : a.c[0];
     if (threadIdx.x < 4) s_c[a.H + threadIdx.x] = 0.0f;   // the padding id's slot
-    const int32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    __shared__ int32_t s_next;   // the part's next unclaimed chunk
+    const int32_t lane = threadIdx.x & 31;
     const int32_t p0 = __ldg(&a.cpart[blockIdx.x]), p1 = __ldg(&a.cpart[blockIdx.x + 1]);
     for (int32_t pi = p0; pi < p1; pi++) {
         const int32_t s = __ldg(&a.pseg[pi]);
@@ -149,6 +153,8 @@ __global__ void __launch_bounds__(HUB_THREADS, 1) k_hub_sweep(HubArgs a)
         const int32_t base = s * a.H;
         const int32_t n4 = (min(a.H, a.n - base) + 3) >> 2;
         __syncthreads();   // every warp is done with the previous segment
+        const int32_t k1 = __ldg(&a.pch[pi + 1]);
+        if (threadIdx.x == 0) s_next = __ldg(&a.pch[pi]);
         const float4 *src = reinterpret_cast<const float4 *>(c + base);
         float4 *dst = reinterpret_cast<float4 *>(s_c);
         // all of a thread's loads in flight at once, in batches of STAGE_BATCH
@@ -166,8 +172,14 @@ __global__ void __launch_bounds__(HUB_THREADS, 1) k_hub_sweep(HubArgs a)
             }
         }
         __syncthreads();
-        const int32_t ga = __ldg(&a.wb[pi * 33 + warp]), gb = __ldg(&a.wb[pi * 33 + warp + 1]);
-        if (ga < gb) stream_groups(a, s_c, ga, gb, lane);
+        // the warps claim the part's chunks in order until none is left
+        while (true) {
+            int32_t k = 0;
+            if (lane == 0) k = atomicAdd(&s_next, 1);
+            k = __shfl_sync(0xffffffffu, k, 0);
+            if (k >= k1) break;
+            stream_groups(a, s_c, __ldg(&a.cb[k]), __ldg(&a.cb[k + 1]), lane);
+        }
     }
 }
 
@@ -178,7 +190,7 @@ namespace mgi {
 void hub_free(mg_graph *g)
 {
     HubSplit &h = g->hub;
-    DevBuf *bufs[] = {&h.hdat, &h.goff, &h.pslot, &h.segg, &h.cpart, &h.pseg, &h.wb, &h.pair_off, &h.P, &h.toff,
+    DevBuf *bufs[] = {&h.hdat, &h.goff, &h.pslot, &h.segg, &h.cpart, &h.pseg, &h.pch, &h.cb, &h.pair_off, &h.P, &h.toff,
                       &h.tcol, &h.fin};
     for (DevBuf *b : bufs) dev_free(*b);
     h = HubSplit();
@@ -343,10 +355,9 @@ mg_status hub_prepare(mg_graph *g)
     });
     // CTA ranges, balanced by cost: a group costs its steps plus
     // GROUP_COST (its slot loads and scattered stores); each range cut at
-    // segment boundaries into parts, each part split over the CTA's warps
-    // by the same cost
+    // segment boundaries into parts, each part into chunks of about
+    // CHUNK_COST that the CTA's warps claim one at a time
     const int G = g->num_sms;
-    constexpr int NW = HUB_THREADS / 32;
     std::vector<int64_t> gcum((size_t)ngroups + 1, 0);
     for (int32_t q = 0; q < ngroups; q++) gcum[q + 1] = gcum[q] + glam[q] + GROUP_COST;
     auto cut = [&](int32_t lo, int32_t hi, int parts, int32_t *out) {
@@ -361,7 +372,7 @@ mg_status hub_prepare(mg_graph *g)
     };
     std::vector<int32_t> cta_lo((size_t)G + 1);
     cut(0, ngroups, G, cta_lo.data());
-    std::vector<int32_t> cpart((size_t)G + 1, 0), pseg, wb;
+    std::vector<int32_t> cpart((size_t)G + 1, 0), pseg, pch, cb;
     for (int b = 0; b < G; b++) {
         cpart[b] = (int32_t)pseg.size();
         int32_t lo = cta_lo[b];
@@ -370,12 +381,19 @@ mg_status hub_prepare(mg_graph *g)
             const int32_t sg = (int32_t)(std::upper_bound(segg.begin(), segg.end(), lo) - segg.begin()) - 1;
             const int32_t e = std::min(hi, segg[sg + 1]);
             pseg.push_back(sg);
-            const size_t k = wb.size();
-            wb.resize(k + NW + 1);
-            cut(lo, e, NW, &wb[k]);
+            pch.push_back((int32_t)cb.size());
+            // chunks of about CHUNK_COST each (whole groups)
+            const int64_t cost = gcum[e] - gcum[lo];
+            const int nch = (int)std::max<int64_t>(1, std::min<int64_t>(e - lo, (cost + CHUNK_COST - 1) / CHUNK_COST));
+            std::vector<int32_t> bnd((size_t)nch + 1);
+            cut(lo, e, nch, bnd.data());
+            for (int k = 0; k < nch; k++)
+                if (bnd[k] < bnd[k + 1]) cb.push_back(bnd[k]);
             lo = e;
         }
     }
+    pch.push_back((int32_t)cb.size());
+    cb.push_back(ngroups);
     cpart[G] = (int32_t)pseg.size();
     // finish bins (rows of graphs without a tail finish in k_pr_seg)
     std::vector<int32_t> fin((size_t)n);
@@ -402,7 +420,8 @@ mg_status hub_prepare(mg_graph *g)
     MG_TRY(up(h.segg, segg.data(), segg.size() * 4));
     MG_TRY(up(h.cpart, cpart.data(), cpart.size() * 4));
     MG_TRY(up(h.pseg, pseg.data(), pseg.size() * 4));
-    MG_TRY(up(h.wb, wb.data(), wb.size() * 4));
+    MG_TRY(up(h.pch, pch.data(), pch.size() * 4));
+    MG_TRY(up(h.cb, cb.data(), cb.size() * 4));
     MG_TRY(up(h.pair_off, pair_off.data(), pair_off.size() * 4));
     MG_TRY(up(h.toff, toff.data(), toff.size() * 4));
     MG_TRY(up(h.tcol, tcol.data(), (size_t)toff[n] * 4));
@@ -439,7 +458,8 @@ mg_status hub_launch(mg_graph *g, const float *c0, const float *c1, const int32_
     a.pslot = h.pslot.as<int4>();
     a.cpart = h.cpart.as<int32_t>();
     a.pseg = h.pseg.as<int32_t>();
-    a.wb = h.wb.as<int32_t>();
+    a.pch = h.pch.as<int32_t>();
+    a.cb = h.cb.as<int32_t>();
     a.c[0] = c0;
     a.c[1] = c1;
     a.cur = cur;
