@@ -115,7 +115,6 @@ struct HubSplit {
     DevBuf hdat;             // uint16 local ids: per group [lambda][GROUP], groups segment-major
     DevBuf goff;             // int32 [ngroups+1]: each group's first step (GROUP ids per step)
     DevBuf pslot;            // int32 [ngroups*GROUP]: each piece's place in P (padding: npieces)
-    DevBuf segg;             // int32 [nseg+1]: first group of each segment
     DevBuf cpart;            // int32 [grid+1]: each CTA's parts (a part: one segment's groups)
     DevBuf pseg;             // int32 [nparts]: each part's segment
     DevBuf pch;              // int32 [nparts+1]: each part's chunks (claimed by its CTA's warps)
@@ -124,6 +123,10 @@ struct HubSplit {
     DevBuf P;                // float [npieces+1]: piece sums of the current sweep (+ padding slot)
     DevBuf toff, tcol;       // tail rows: offsets [n+1], int32 ids
     DevBuf fin;              // int32 [n]: rows of the finish bins (warp | 8-lane | thread)
+    DevBuf ctime;            // int64 [grid]: each CTA's clock cycles in the last sweep
+    // host copies for re-splitting the work among the CTAs
+    std::vector<int32_t> hglam, hsegg;  // steps of every group; first group of every segment
+    std::vector<double> w;            // every group's cost weight
 };
 }  // namespace mgi
 
@@ -248,6 +251,8 @@ mg_status hub_launch(mg_graph *g, const float *c0, const float *c1, const int32_
                      const int32_t *off, cudaStream_t st, int slot_sweep);
 mg_status hub_check(mg_graph *g);
 bool hub_covers_all(const mg_graph *g);   // the segments hold every vertex id
+mg_status hub_rebalance(mg_graph *g);     // re-split the sweep's work from the last sweep's per-CTA times
+bool hub_weights(mg_graph *g, std::vector<double> *get, const std::vector<double> *set);
 void hub_free(mg_graph *g);
 
 // Launch with programmatic dependent launch on the stream's previous kernel:

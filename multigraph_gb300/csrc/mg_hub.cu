@@ -40,6 +40,7 @@
 
 #include <algorithm>
 #include <atomic>
+#include <cmath>
 #include <cstring>
 #include <functional>
 #include <thread>
@@ -52,6 +53,7 @@ constexpr int32_t PIECE_MAX = 64;   // edges per piece at most
 constexpr int32_t GROUP = 128;      // pieces per warp group: four per lane
 constexpr int HUB_THREADS = 1024;   // one CTA per SM (shared memory bound)
 constexpr int HUB_UNROLL = 4;       // steps (256-byte warp loads) in flight per warp
+static_assert(HUB_UNROLL == 4, "the full-batch path adds four values pairwise");
 constexpr int STAGE_BATCH = 4;      // 16-byte loads in flight per thread while staging a segment
 constexpr int64_t GROUP_COST = 16;  // a group's fixed cost in steps, for balancing CTA ranges
 constexpr int64_t CHUNK_COST = 128; // a chunk's cost (steps + GROUP_COST per group): the unit warps claim
@@ -74,6 +76,7 @@ struct HubArgs {
     const int32_t *more;      // loop continue flag
     const int32_t *off;       // non-zero: sweeps run elsewhere (queue sweeps)
     float *P;                 // piece sums, row-major
+    long long *ctime;         // [grid] each CTA's clock cycles (read back to re-split the work)
     int32_t n, H, nseg;
 };
 
@@ -105,6 +108,33 @@ __device__ __forceinline__ void stream_groups(const HubArgs &a, const float *s_c
         for (int j = 0; j < HUB_UNROLL; j++) {
             const int32_t q = t + HUB_UNROLL + j;
             wn[j] = q < tend ? __ldcs(D + (int64_t)q * 32) : make_uint2(0u, 0u);
+        }
+        if (t + HUB_UNROLL < gend) {
+            // the whole batch lies inside group g (and more follows): each
+            // piece's four values are added pairwise, then compensated once
+            float b0 = 0.0f, b1 = 0.0f, b2 = 0.0f, b3 = 0.0f;
+            {
+                float x0[HUB_UNROLL], x1[HUB_UNROLL], x2[HUB_UNROLL], x3[HUB_UNROLL];
+#pragma unroll
+                for (int j = 0; j < HUB_UNROLL; j++) {
+                    x0[j] = s_c[wc[j].x & 0xffffu];
+                    x1[j] = s_c[wc[j].x >> 16];
+                    x2[j] = s_c[wc[j].y & 0xffffu];
+                    x3[j] = s_c[wc[j].y >> 16];
+                }
+                b0 = (x0[0] + x0[1]) + (x0[2] + x0[3]);
+                b1 = (x1[0] + x1[1]) + (x1[2] + x1[3]);
+                b2 = (x2[0] + x2[1]) + (x2[2] + x2[3]);
+                b3 = (x3[0] + x3[1]) + (x3[2] + x3[3]);
+            }
+            mgd::kahan_add(s0, r0, b0);
+            mgd::kahan_add(s1, r1, b1);
+            mgd::kahan_add(s2, r2, b2);
+            mgd::kahan_add(s3, r3, b3);
+            t += HUB_UNROLL;
+#pragma unroll
+            for (int j = 0; j < HUB_UNROLL; j++) wc[j] = wn[j];
+            continue;
         }
 #pragma unroll
         for (int j = 0; j < HUB_UNROLL; j++) {
@@ -144,6 +174,7 @@ __global__ void __launch_bounds__(HUB_THREADS, 1) k_hub_sweep(HubArgs a)
     const float *c = __ldg(a.cur) ? a.c[1] : a.c[0];
     if (threadIdx.x < 4) s_c[a.H + threadIdx.x] = 0.0f;   // the padding id's slot
     __shared__ int32_t s_next;   // the part's next unclaimed chunk
+    const long long t_start = clock64();
     const int32_t lane = threadIdx.x & 31;
     const int32_t p0 = __ldg(&a.cpart[blockIdx.x]), p1 = __ldg(&a.cpart[blockIdx.x + 1]);
     for (int32_t pi = p0; pi < p1; pi++) {
@@ -181,22 +212,94 @@ __global__ void __launch_bounds__(HUB_THREADS, 1) k_hub_sweep(HubArgs a)
             stream_groups(a, s_c, __ldg(&a.cb[k]), __ldg(&a.cb[k + 1]), lane);
         }
     }
+    __syncthreads();
+    if (threadIdx.x == 0) a.ctime[blockIdx.x] = clock64() - t_start;
 }
 
 }  // namespace
 
 namespace mgi {
 
+static std::atomic<uint64_t> g_hub_builds{0};
+
 void hub_free(mg_graph *g)
 {
     HubSplit &h = g->hub;
-    DevBuf *bufs[] = {&h.hdat, &h.goff, &h.pslot, &h.segg, &h.cpart, &h.pseg, &h.pch, &h.cb, &h.pair_off, &h.P, &h.toff,
+    DevBuf *bufs[] = {&h.hdat, &h.goff, &h.pslot, &h.cpart, &h.pseg, &h.pch, &h.cb, &h.ctime, &h.pair_off, &h.P, &h.toff,
                       &h.tcol, &h.fin};
     for (DevBuf *b : bufs) dev_free(*b);
     h = HubSplit();
 }
 
-static std::atomic<uint64_t> g_hub_builds{0};
+// Split the groups among the CTAs by the groups' cost weights h.w: each
+// CTA an even share of the total weight (contiguous groups), cut at
+// segment boundaries into parts and each part into chunks of about
+// CHUNK_COST that the CTA's warps claim one at a time.  The captured loops
+// that launch the sweep take the new split (the build number changes).
+static mg_status hub_split(mg_graph *g)
+{
+    HubSplit &h = g->hub;
+    cudaStream_t s = g->stream;
+    const int G = h.grid;
+    const int32_t ngroups = (int32_t)h.hglam.size();
+    const std::vector<int32_t> &segg = h.hsegg;
+    std::vector<double> gcum((size_t)ngroups + 1, 0.0);
+    for (int32_t q = 0; q < ngroups; q++) gcum[q + 1] = gcum[q] + h.w[q];
+    auto cut = [&](int32_t lo, int32_t hi, int parts, int32_t *out) {
+        // out[0..parts]: boundaries in [lo, hi] of equal weight
+        out[0] = lo;
+        for (int k = 1; k < parts; k++) {
+            const double goal = gcum[lo] + (gcum[hi] - gcum[lo]) * k / parts;
+            int32_t b = (int32_t)(std::lower_bound(gcum.begin() + lo, gcum.begin() + hi, goal) - gcum.begin());
+            out[k] = std::min(std::max(b, out[k - 1]), hi);
+        }
+        out[parts] = hi;
+    };
+    // the weight of an average group, for sizing chunks: CHUNK_COST is in
+    // units of the initial weights (steps)
+    double w0 = 0.0, wn = 0.0;
+    for (int32_t q = 0; q < ngroups; q++) {
+        w0 += (double)h.hglam[q] + (double)GROUP_COST;
+        wn += h.w[q];
+    }
+    const double chunk_w = (double)CHUNK_COST * (w0 > 0.0 ? wn / w0 : 1.0);
+    std::vector<int32_t> cta_lo((size_t)G + 1);
+    cut(0, ngroups, G, cta_lo.data());
+    std::vector<int32_t> cpart((size_t)G + 1, 0), pseg, pch, cb;
+    for (int b = 0; b < G; b++) {
+        cpart[b] = (int32_t)pseg.size();
+        int32_t lo = cta_lo[b];
+        const int32_t hi = cta_lo[b + 1];
+        while (lo < hi) {
+            const int32_t sg = (int32_t)(std::upper_bound(segg.begin(), segg.end(), lo) - segg.begin()) - 1;
+            const int32_t e = std::min(hi, segg[sg + 1]);
+            pseg.push_back(sg);
+            pch.push_back((int32_t)cb.size());
+            const double cost = gcum[e] - gcum[lo];
+            const int nch = (int)std::max<int64_t>(1, std::min<int64_t>(e - lo, (int64_t)std::ceil(cost / chunk_w)));
+            std::vector<int32_t> bnd((size_t)nch + 1);
+            cut(lo, e, nch, bnd.data());
+            for (int k = 0; k < nch; k++)
+                if (bnd[k] < bnd[k + 1]) cb.push_back(bnd[k]);
+            lo = e;
+        }
+    }
+    cpart[G] = (int32_t)pseg.size();
+    pch.push_back((int32_t)cb.size());
+    cb.push_back(ngroups);
+    auto up = [&](DevBuf &b, const void *src, size_t bytes) -> mg_status {
+        MG_TRY(dev_alloc(b, std::max<size_t>(bytes, 16) + 16));
+        if (bytes) MG_CUDA(cudaMemcpyAsync(b.p, src, bytes, cudaMemcpyHostToDevice, s));
+        return MG_OK;
+    };
+    MG_TRY(up(h.cpart, cpart.data(), cpart.size() * 4));
+    MG_TRY(up(h.pseg, pseg.data(), pseg.size() * 4));
+    MG_TRY(up(h.pch, pch.data(), pch.size() * 4));
+    MG_TRY(up(h.cb, cb.data(), cb.size() * 4));
+    MG_CUDA(cudaStreamSynchronize(s));   // the host vectors go out of scope
+    h.gen = ++g_hub_builds;
+    return MG_OK;
+}
 
 // Build the segmented layout from the pull CSR (copied back from the
 // device): row-parallel host passes over the edges (count, then write),
@@ -353,48 +456,13 @@ mg_status hub_prepare(mg_graph *g)
             }
         }
     });
-    // CTA ranges, balanced by cost: a group costs its steps plus
-    // GROUP_COST (its slot loads and scattered stores); each range cut at
-    // segment boundaries into parts, each part into chunks of about
-    // CHUNK_COST that the CTA's warps claim one at a time
-    const int G = g->num_sms;
-    std::vector<int64_t> gcum((size_t)ngroups + 1, 0);
-    for (int32_t q = 0; q < ngroups; q++) gcum[q + 1] = gcum[q] + glam[q] + GROUP_COST;
-    auto cut = [&](int32_t lo, int32_t hi, int parts, int32_t *out) {
-        // out[0..parts]: boundaries in [lo, hi] of equal cost
-        out[0] = lo;
-        for (int k = 1; k < parts; k++) {
-            const int64_t goal = gcum[lo] + (gcum[hi] - gcum[lo]) * k / parts;
-            int32_t b = (int32_t)(std::lower_bound(gcum.begin() + lo, gcum.begin() + hi, goal) - gcum.begin());
-            out[k] = std::min(std::max(b, out[k - 1]), hi);
-        }
-        out[parts] = hi;
-    };
-    std::vector<int32_t> cta_lo((size_t)G + 1);
-    cut(0, ngroups, G, cta_lo.data());
-    std::vector<int32_t> cpart((size_t)G + 1, 0), pseg, pch, cb;
-    for (int b = 0; b < G; b++) {
-        cpart[b] = (int32_t)pseg.size();
-        int32_t lo = cta_lo[b];
-        const int32_t hi = cta_lo[b + 1];
-        while (lo < hi) {
-            const int32_t sg = (int32_t)(std::upper_bound(segg.begin(), segg.end(), lo) - segg.begin()) - 1;
-            const int32_t e = std::min(hi, segg[sg + 1]);
-            pseg.push_back(sg);
-            pch.push_back((int32_t)cb.size());
-            // chunks of about CHUNK_COST each (whole groups)
-            const int64_t cost = gcum[e] - gcum[lo];
-            const int nch = (int)std::max<int64_t>(1, std::min<int64_t>(e - lo, (cost + CHUNK_COST - 1) / CHUNK_COST));
-            std::vector<int32_t> bnd((size_t)nch + 1);
-            cut(lo, e, nch, bnd.data());
-            for (int k = 0; k < nch; k++)
-                if (bnd[k] < bnd[k + 1]) cb.push_back(bnd[k]);
-            lo = e;
-        }
-    }
-    pch.push_back((int32_t)cb.size());
-    cb.push_back(ngroups);
-    cpart[G] = (int32_t)pseg.size();
+    h.hglam = glam;
+    h.hsegg = segg;
+    h.w.assign((size_t)ngroups, 0.0);
+    for (int32_t q = 0; q < ngroups; q++) h.w[q] = (double)glam[q] + (double)GROUP_COST;
+    h.grid = g->num_sms;
+    MG_TRY(dev_alloc(h.ctime, (size_t)h.grid * 8));
+    MG_TRY(hub_split(g));
     // finish bins (rows of graphs without a tail finish in k_pr_seg)
     std::vector<int32_t> fin((size_t)n);
     int32_t nfw = 0, nfg = 0, nft = 0;
@@ -417,11 +485,6 @@ mg_status hub_prepare(mg_graph *g)
     MG_TRY(up(h.hdat, hdat.data(), hdat.size() * 2));
     MG_TRY(up(h.goff, goff.data(), goff.size() * 4));
     MG_TRY(up(h.pslot, pslot.data(), pslot.size() * 4));
-    MG_TRY(up(h.segg, segg.data(), segg.size() * 4));
-    MG_TRY(up(h.cpart, cpart.data(), cpart.size() * 4));
-    MG_TRY(up(h.pseg, pseg.data(), pseg.size() * 4));
-    MG_TRY(up(h.pch, pch.data(), pch.size() * 4));
-    MG_TRY(up(h.cb, cb.data(), cb.size() * 4));
     MG_TRY(up(h.pair_off, pair_off.data(), pair_off.size() * 4));
     MG_TRY(up(h.toff, toff.data(), toff.size() * 4));
     MG_TRY(up(h.tcol, tcol.data(), (size_t)toff[n] * 4));
@@ -434,7 +497,6 @@ mg_status hub_prepare(mg_graph *g)
     h.npieces = npieces;
     h.covered = covered;
     h.ntail = toff[n];
-    h.grid = G;
     h.nfw = nfw;
     h.nfg = nfg;
     h.nft = nft;
@@ -444,6 +506,63 @@ mg_status hub_prepare(mg_graph *g)
 }
 
 bool hub_covers_all(const mg_graph *g) { return (int64_t)g->nv <= (int64_t)SEG_MAX * SEG_H; }
+
+// Re-split the sweep's work from the last sweep's per-CTA clock counts:
+// every group's weight is scaled by its CTA's measured time over the
+// CTA's share of the weight (normalised to the mean), so groups whose real
+// cost the initial model (steps + GROUP_COST) misjudges move to other CTAs.
+mg_status hub_rebalance(mg_graph *g)
+{
+    HubSplit &h = g->hub;
+    if (!h.use) return MG_OK;
+    const int G = h.grid;
+    std::vector<long long> t((size_t)G);
+    std::vector<int32_t> cpart((size_t)G + 1), pch, cb;
+    MG_CUDA(cudaMemcpyAsync(t.data(), h.ctime.p, (size_t)G * 8, cudaMemcpyDeviceToHost, g->stream));
+    MG_CUDA(cudaMemcpyAsync(cpart.data(), h.cpart.p, cpart.size() * 4, cudaMemcpyDeviceToHost, g->stream));
+    MG_CUDA(cudaStreamSynchronize(g->stream));
+    // each CTA's first and last group: from its parts' chunks
+    const size_t nparts = (size_t)cpart[G];
+    pch.resize(nparts + 1);
+    MG_CUDA(cudaMemcpy(pch.data(), h.pch.p, pch.size() * 4, cudaMemcpyDeviceToHost));
+    cb.resize((size_t)pch[nparts] + 1);
+    MG_CUDA(cudaMemcpy(cb.data(), h.cb.p, cb.size() * 4, cudaMemcpyDeviceToHost));
+    std::vector<double> ratio((size_t)G, 0.0);
+    double tt = 0.0, tw = 0.0;
+    for (int b = 0; b < G; b++) {
+        if (cpart[b] == cpart[b + 1]) continue;
+        const int32_t lo = cb[(size_t)pch[(size_t)cpart[b]]], hi = cb[(size_t)pch[(size_t)cpart[b + 1]]];
+        double wb = 0.0;
+        for (int32_t q = lo; q < hi; q++) wb += h.w[q];
+        if (wb <= 0.0 || t[b] <= 0) continue;
+        ratio[b] = (double)t[b] / wb;
+        tt += (double)t[b];
+        tw += wb;
+    }
+    if (tt <= 0.0 || tw <= 0.0) return MG_OK;
+    const double mean = tt / tw;
+    for (int b = 0; b < G; b++) {
+        if (ratio[b] <= 0.0) continue;
+        const int32_t lo = cb[(size_t)pch[(size_t)cpart[b]]], hi = cb[(size_t)pch[(size_t)cpart[b + 1]]];
+        for (int32_t q = lo; q < hi; q++) h.w[q] *= ratio[b] / mean;
+    }
+    return hub_split(g);
+}
+
+// Read (get) or replace (set) the groups' cost weights; false when the
+// segmented layout is not in use or set has the wrong length.
+bool hub_weights(mg_graph *g, std::vector<double> *get, const std::vector<double> *set)
+{
+    HubSplit &h = g->hub;
+    if (!h.use) return false;
+    if (get) *get = h.w;
+    if (set) {
+        if (set->size() != h.w.size()) return false;
+        h.w = *set;
+        if (hub_split(g) != MG_OK) return false;
+    }
+    return true;
+}
 
 size_t hub_smem_bytes(const mg_graph *g) { return (size_t)(g->hub.H + 4) * 4; }
 
@@ -466,6 +585,7 @@ mg_status hub_launch(mg_graph *g, const float *c0, const float *c1, const int32_
     a.more = more;
     a.off = off;
     a.P = h.P.as<float>();
+    a.ctime = h.ctime.as<long long>();
     a.n = g->nv;
     a.H = h.H;
     a.nseg = h.nseg;

@@ -505,6 +505,48 @@ __device__ __forceinline__ bool last_block(PCtl *cp)
     return s_last != 0;
 }
 
+// End of a sweep over every row: the last block to arrive sums the blocks'
+// partials of slots [0, nslots) in slot order and updates the loop state
+// (iterate index, residual, dangling mass, continue flag and the graph's
+// loop condition; the data-driven form's switch to queue sweeps).
+template <class Op>
+__device__ __forceinline__ void close_sweep(const PArgs &a, const PCtl &c, int nslots, cudaGraphConditionalHandle h,
+                                            int use_cond)
+{
+    PCtl *cp = a.ctl;
+    if (!last_block(cp)) return;
+    double T[NPART - 1];
+    int A;
+    reduce_slots(a.bpart, 0, nslots, T, A);
+    if (threadIdx.x == 0) {
+        const double R = T[0], D = T[1];
+        int more = 1;
+        cp->done = 0;
+        cp->iter = c.iter + 1;
+        cp->cur = c.cur ^ 1;
+        cp->resid = R;
+        cp->any = A;
+        if (Op::kAdjoint) cp->lam_mean = D / c.n;
+        else cp->dangling = D;
+        pctl_derive(cp);
+        more = Op::more(A, R, c.tol) ? 1 : 0;
+        if (more && cp->iter >= c.max_iter) { cp->status = 1; more = 0; }
+        cp->more = more;
+        if (Op::kDataDriven) {
+            cp->dense_iters = c.dense_iters + 1;
+            cp->act_edges = (long long)T[2];
+            cp->dang_frozen = T[3];
+            if (more && T[2] * SPARSE_ALPHA < (double)a.m) {
+                cp->sparse = 1;
+                cp->need_compact = 1;
+                cp->qc = 0;
+                cp->qn[0] = cp->qn[1] = 0;
+            }
+        }
+        if (use_cond) cudaGraphSetConditional(h, more ? 1u : 0u);
+    }
+}
+
 // Row finish when every in-edge sits in a segment (no tail, no heavy-row
 // chunks): each row sums its pieces' partials (P[pair_off[v] ..], segments
 // ascending) and applies the update.  Rows are binned by piece count at
@@ -512,10 +554,14 @@ __device__ __forceinline__ bool last_block(PCtl *cp)
 // the rest a thread each (compensated FP32, four loads in flight) --
 // fixed orders, so sweeps stay reproducible.
 template <class Op>
-__global__ void __launch_bounds__(THREADS, 8) k_pr_seg(PArgs a)
+__global__ void __launch_bounds__(THREADS, 8) k_pr_seg(PArgs a, cudaGraphConditionalHandle h, int use_cond)
 {
     const PCtl c = *a.ctl;
-    if (c.more == 0 || c.sparse) return;
+    if (c.more == 0) {
+        if (blockIdx.x == 0 && threadIdx.x == 0 && use_cond) cudaGraphSetConditional(h, 0u);
+        return;
+    }
+    if (c.sparse) return;   // queue sweeps (k_prd_*) drive the loop
     PrRowOp<Op> op{a, c};
     const int lane = mgd::lane();
     const int gwarp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -526,9 +572,21 @@ __global__ void __launch_bounds__(THREADS, 8) k_pr_seg(PArgs a)
         // compensated sums, lane-strided then a compensated xor tree: a
         // long row's total stays steady between sweeps
         float s = 0.0f, r = 0.0f;
-        if (!op.skip(v))
-            for (int32_t p = __ldg(&a.pair_off[v]) + lane, e = __ldg(&a.pair_off[v + 1]); p < e; p += 32)
-                mgd::kahan_add(s, r, __ldcg(&a.P[p]));
+        if (!op.skip(v)) {
+            // four loads in flight per lane (the longest rows hold about a
+            // thousand pieces), added in order
+            int32_t p = __ldg(&a.pair_off[v]) + lane;
+            const int32_t e = __ldg(&a.pair_off[v + 1]);
+            for (; p + 96 < e; p += 128) {
+                const float f0 = __ldcg(&a.P[p]), f1 = __ldcg(&a.P[p + 32]), f2 = __ldcg(&a.P[p + 64]),
+                            f3 = __ldcg(&a.P[p + 96]);
+                mgd::kahan_add(s, r, f0);
+                mgd::kahan_add(s, r, f1);
+                mgd::kahan_add(s, r, f2);
+                mgd::kahan_add(s, r, f3);
+            }
+            for (; p < e; p += 32) mgd::kahan_add(s, r, __ldcg(&a.P[p]));
+        }
         const float tot = mgd::warp_sum_comp(s, r);
         if (lane == 0) op.finish_row(v, tot);
     }
@@ -551,6 +609,7 @@ __global__ void __launch_bounds__(THREADS, 8) k_pr_seg(PArgs a)
         op.finish_row(v, s - r);
     }
     block_partials<Op::kDataDriven>(a, blockIdx.x, op.resid, op.dangs, op.any, op.act, op.dfz);
+    close_sweep<Op>(a, c, gridDim.x, h, use_cond);
 }
 
 // Heavy rows (warp per row, chunk partials summed lane-strided then by a
@@ -597,37 +656,7 @@ __global__ void __launch_bounds__(THREADS) k_pr_apply(PArgs a, cudaGraphConditio
         }
     }
     block_partials<Op::kDataDriven>(a, a.nblocks + blockIdx.x, (float)resid, (float)dangs, any, act, dfz);
-    if (!last_block(cp)) return;
-    double T[NPART - 1];
-    int A;
-    reduce_slots(a.bpart, 0, a.nblocks + gridDim.x, T, A);
-    if (threadIdx.x == 0) {
-        const double R = T[0], D = T[1];
-        int more = 1;
-        cp->done = 0;
-        cp->iter = c.iter + 1;
-        cp->cur = c.cur ^ 1;
-        cp->resid = R;
-        cp->any = A;
-        if (Op::kAdjoint) cp->lam_mean = D / c.n;
-        else cp->dangling = D;
-        pctl_derive(cp);
-        more = Op::more(A, R, c.tol) ? 1 : 0;
-        if (more && cp->iter >= c.max_iter) { cp->status = 1; more = 0; }
-        cp->more = more;
-        if (Op::kDataDriven) {
-            cp->dense_iters = c.dense_iters + 1;
-            cp->act_edges = (long long)T[2];
-            cp->dang_frozen = T[3];
-            if (more && T[2] * SPARSE_ALPHA < (double)a.m) {
-                cp->sparse = 1;
-                cp->need_compact = 1;
-                cp->qc = 0;
-                cp->qn[0] = cp->qn[1] = 0;
-            }
-        }
-        if (use_cond) cudaGraphSetConditional(h, more ? 1u : 0u);
-    }
+    close_sweep<Op>(a, c, a.nblocks + gridDim.x, h, use_cond);
 }
 
 // ---------------------------------------------------------------------------
@@ -1060,12 +1089,17 @@ static mg_status pr_loop(mg_graph *g, PArgs &a, const mg_opts &opt, const char *
     BodyFn body = [&](cudaStream_t st, cudaGraphConditionalHandle h, int use_cond) -> mg_status {
         if (a.P) MG_TRY(hub_launch(g, a.c[0], a.c[1], &a.ctl->cur, &a.ctl->more, &a.ctl->sparse, st, shs));
         P.begin(sl);
-        if (a.seg_only) k_pr_seg<Op><<<grid, THREADS, 0, st>>>(a);
-        else k_pr_light<Op><<<grid, THREADS, 0, st>>>(a);
-        P.end();
-        P.begin(sh);
-        MG_TRY(launch_pdl(k_pr_apply<Op>, apply_grid, THREADS, st, a, h, use_cond));
-        P.end();
+        if (a.seg_only) {
+            // every row finishes in k_pr_seg, which also closes the sweep
+            k_pr_seg<Op><<<grid, THREADS, 0, st>>>(a, h, use_cond);
+            P.end();
+        } else {
+            k_pr_light<Op><<<grid, THREADS, 0, st>>>(a);
+            P.end();
+            P.begin(sh);
+            MG_TRY(launch_pdl(k_pr_apply<Op>, apply_grid, THREADS, st, a, h, use_cond));
+            P.end();
+        }
         if (Op::kDataDriven) {
             // queue sweeps once the switch has happened (no-ops before)
             P.begin(sqc);

@@ -98,7 +98,8 @@ static mg_status pr_median_ms(mg_graph *g, const mg_opts &o, double *ms)
 // PageRank: heavy-row threshold x chunk size x thread-bin cutoff of the
 // gather layout's degree bins (timed with that layout), then whether the
 // segmented layout beats the tuned gather layout on this graph (the choice
-// of MG_PR_LAYOUT_AUTO)
+// of MG_PR_LAYOUT_AUTO); for the segmented layout also the split of the
+// sweep's work among the CTAs (mgi::hub_rebalance)
 mg_status tune_pr_layout(mg_graph *g, const char *cache_path, uint64_t sig, const mg_opts &base)
 {
     mg_opts cached = base;
@@ -134,6 +135,19 @@ mg_status tune_pr_layout(mg_graph *g, const char *cache_path, uint64_t sig, cons
         o.pr_layout = MG_PR_LAYOUT_SEGMENTED;
         double seg_ms = 0.0;
         MG_TRY(pr_median_ms(g, o, &seg_ms));
+        // the segmented sweep's split among the CTAs, re-cut three times
+        // from measured per-CTA times; kept only if the runs got faster
+        std::vector<double> w0;
+        if (mgi::hub_weights(g, &w0, nullptr)) {
+            for (int it = 0; it < 3; it++) {
+                MG_TRY(mg_pagerank(g, MG_PR_TOPOLOGY, &o, nullptr, nullptr));
+                MG_TRY(mgi::hub_rebalance(g));
+            }
+            double reb_ms = 0.0;
+            MG_TRY(pr_median_ms(g, o, &reb_ms));
+            if (reb_ms < seg_ms) seg_ms = reb_ms;
+            else mgi::hub_weights(g, nullptr, &w0);
+        }
         g->pr_prefer_gather = seg_ms > best_ms;
     }
     mg_opts rec = base;
