@@ -111,7 +111,7 @@ struct HubSplit {
     int64_t npieces = 0, covered = 0;  // pieces (P entries); edges in the segments
     int64_t ntail = 0;       // edges past the last segment
     int32_t grid = 0;        // CTAs of the sweep (one per SM)
-    int32_t nfw = 0, nfg = 0, nft = 0;  // finish bins: warp / 8-lane / thread rows
+    int32_t nfw = 0, fin_warp = 0;     // row finish: rows of more than fin_warp pieces a warp each (listed in fin)
     DevBuf hdat;             // uint16 local ids: per group [lambda][GROUP], groups segment-major
     DevBuf goff;             // int32 [ngroups+1]: each group's first step (GROUP ids per step)
     DevBuf pslot;            // int32 [ngroups*GROUP]: each piece's place in P (padding: npieces)
@@ -122,7 +122,7 @@ struct HubSplit {
     DevBuf pair_off;         // int32 [n+1]: row v's pieces in P
     DevBuf P;                // float [npieces+1]: piece sums of the current sweep (+ padding slot)
     DevBuf toff, tcol;       // tail rows: offsets [n+1], int32 ids
-    DevBuf fin;              // int32 [n]: rows of the finish bins (warp | 8-lane | thread)
+    DevBuf fin;              // int32 [nfw]: the rows the finish sums a warp each
     DevBuf ctime;            // int64 [grid]: each CTA's clock cycles in the last sweep
     // host copies for re-splitting the work among the CTAs
     std::vector<int32_t> hglam, hsegg;  // steps of every group; first group of every segment

@@ -57,11 +57,10 @@ static_assert(HUB_UNROLL == 4, "the full-batch path adds four values pairwise");
 constexpr int STAGE_BATCH = 4;      // 16-byte loads in flight per thread while staging a segment
 constexpr int64_t GROUP_COST = 16;  // a group's fixed cost in steps, for balancing CTA ranges
 constexpr int64_t CHUNK_COST = 128; // a chunk's cost (steps + GROUP_COST per group): the unit warps claim
-// finish bins by pieces per row: rows with more than FIN_WARP pieces a warp
-// each, the rest a thread each (8-lane groups, FIN_THREAD < pieces <=
-// FIN_WARP, walked rows one after another and were slower)
+// the row finish sums rows with more than FIN_WARP pieces a warp each, the
+// rest a thread each (8-lane groups for rows of 5-64 pieces walked their
+// rows one after another and were slower)
 constexpr int32_t FIN_WARP = 32;
-constexpr int32_t FIN_THREAD = 32;
 
 struct HubArgs {
     const uint2 *hdat;        // groups' ids, four 16-bit ids per lane per step
@@ -463,20 +462,12 @@ mg_status hub_prepare(mg_graph *g)
     h.grid = g->num_sms;
     MG_TRY(dev_alloc(h.ctime, (size_t)h.grid * 8));
     MG_TRY(hub_split(g));
-    // finish bins (rows of graphs without a tail finish in k_pr_seg)
-    std::vector<int32_t> fin((size_t)n);
-    int32_t nfw = 0, nfg = 0, nft = 0;
-    for (int32_t v = 0; v < n; v++) nfw += npc[v] > FIN_WARP;
-    for (int32_t v = 0; v < n; v++) nfg += npc[v] > FIN_THREAD && npc[v] <= FIN_WARP;
-    nft = n - nfw - nfg;
-    {
-        int32_t iw = 0, ig = nfw, it = nfw + nfg;
-        for (int32_t v = 0; v < n; v++) {
-            if (npc[v] > FIN_WARP) fin[(size_t)iw++] = v;
-            else if (npc[v] > FIN_THREAD) fin[(size_t)ig++] = v;
-            else fin[(size_t)it++] = v;
-        }
-    }
+    // rows of more than FIN_WARP pieces, which k_pr_seg sums a warp each
+    // (graphs without a tail finish every row there)
+    std::vector<int32_t> fin;
+    for (int32_t v = 0; v < n; v++)
+        if (npc[v] > FIN_WARP) fin.push_back(v);
+    const int32_t nfw = (int32_t)fin.size();
     auto up = [&](DevBuf &b, const void *src, size_t bytes) -> mg_status {
         MG_TRY(dev_alloc(b, std::max<size_t>(bytes, 16) + 16));
         if (bytes) MG_CUDA(cudaMemcpyAsync(b.p, src, bytes, cudaMemcpyHostToDevice, s));
@@ -488,7 +479,7 @@ mg_status hub_prepare(mg_graph *g)
     MG_TRY(up(h.pair_off, pair_off.data(), pair_off.size() * 4));
     MG_TRY(up(h.toff, toff.data(), toff.size() * 4));
     MG_TRY(up(h.tcol, tcol.data(), (size_t)toff[n] * 4));
-    MG_TRY(up(h.fin, fin.data(), fin.size() * 4));
+    MG_TRY(up(h.fin, fin.data(), fin.size() * 4));   // at least 16 bytes even when empty
     MG_TRY(dev_alloc(h.P, (size_t)(npieces + 1) * 4));
     MG_CUDA(cudaStreamSynchronize(s));
     h.H = H;
@@ -498,8 +489,7 @@ mg_status hub_prepare(mg_graph *g)
     h.covered = covered;
     h.ntail = toff[n];
     h.nfw = nfw;
-    h.nfg = nfg;
-    h.nft = nft;
+    h.fin_warp = FIN_WARP;
     h.use = true;
     h.valid = true;
     return MG_OK;

@@ -93,8 +93,8 @@ struct PArgs {
     const int32_t *prow_full;
     int32_t chunk;
     int32_t seg_only;        // every in-edge sits in a segment: rows finish in k_pr_seg
-    const int32_t *fin;      // k_pr_seg's rows: [nfw warp rows | nfg 8-lane rows | nft thread rows]
-    int32_t nfw, nfg, nft;
+    const int32_t *fin;      // k_pr_seg's warp rows (more than fin_warp pieces)
+    int32_t nfw, fin_warp;
     float *x[2];             // iterate (ping-pong)
     float *c[2];             // gathered quantity: contribution x/deg (PR) or lambda (adjoint)
     const float *gvec;       // adjoint: g
@@ -550,9 +550,9 @@ __device__ __forceinline__ void close_sweep(const PArgs &a, const PCtl &c, int n
 // Row finish when every in-edge sits in a segment (no tail, no heavy-row
 // chunks): each row sums its pieces' partials (P[pair_off[v] ..], segments
 // ascending) and applies the update.  Rows are binned by piece count at
-// layout time: long rows a warp each (lane-strided, then a fixed xor tree),
-// the rest a thread each (compensated FP32, four loads in flight) --
-// fixed orders, so sweeps stay reproducible.
+// layout time: long rows a warp each (lane-strided, then a fixed xor tree;
+// listed), the rest a thread each in row order (compensated FP32, four loads
+// in flight) -- fixed orders, so sweeps stay reproducible.
 template <class Op>
 __global__ void __launch_bounds__(THREADS, 8) k_pr_seg(PArgs a, cudaGraphConditionalHandle h, int use_cond)
 {
@@ -566,7 +566,7 @@ __global__ void __launch_bounds__(THREADS, 8) k_pr_seg(PArgs a, cudaGraphConditi
     const int lane = mgd::lane();
     const int gwarp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int nwarps = (gridDim.x * blockDim.x) >> 5;
-    const int32_t *fw = a.fin, *ft = a.fin + a.nfw + a.nfg;
+    const int32_t *fw = a.fin;
     for (int32_t i = gwarp; i < a.nfw; i += nwarps) {
         const int32_t v = __ldg(&fw[i]);
         // compensated sums, lane-strided then a compensated xor tree: a
@@ -590,12 +590,13 @@ __global__ void __launch_bounds__(THREADS, 8) k_pr_seg(PArgs a, cudaGraphConditi
         const float tot = mgd::warp_sum_comp(s, r);
         if (lane == 0) op.finish_row(v, tot);
     }
-    for (int32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < a.nft; i += gridDim.x * blockDim.x) {
-        const int32_t v = __ldg(&ft[i]);
+    // every other row a thread each, rows in order (the warp rows skipped)
+    for (int32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < a.n; v += gridDim.x * blockDim.x) {
+        int32_t p = __ldg(&a.pair_off[v]);
+        const int32_t e = __ldg(&a.pair_off[v + 1]);
+        if (e - p > a.fin_warp) continue;
         float s = 0.0f, r = 0.0f;
         if (!op.skip(v)) {
-            int32_t p = __ldg(&a.pair_off[v]);
-            const int32_t e = __ldg(&a.pair_off[v + 1]);
             for (; p + 4 <= e; p += 4) {
                 const float f0 = __ldcg(&a.P[p]), f1 = __ldcg(&a.P[p + 1]), f2 = __ldcg(&a.P[p + 2]),
                             f3 = __ldcg(&a.P[p + 3]);
@@ -1200,8 +1201,7 @@ static mg_status pr_setup(mg_graph *g, PArgs &a, bool weighted_or_adj, int32_t l
                 a.seg_only = 1;
                 a.fin = g->hub.fin.as<int32_t>();
                 a.nfw = g->hub.nfw;
-                a.nfg = g->hub.nfg;
-                a.nft = g->hub.nft;
+                a.fin_warp = g->hub.fin_warp;
                 a.nhchunks = 0;
                 a.nhrows = 0;
             }
