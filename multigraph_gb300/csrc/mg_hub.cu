@@ -53,7 +53,6 @@ constexpr int32_t PIECE_MAX = 64;   // edges per piece at most
 constexpr int32_t GROUP = 128;      // pieces per warp group: four per lane
 constexpr int HUB_THREADS = 1024;   // one CTA per SM (shared memory bound)
 constexpr int HUB_UNROLL = 4;       // steps (256-byte warp loads) in flight per warp
-static_assert(HUB_UNROLL == 4, "the full-batch path adds four values pairwise");
 constexpr int STAGE_BATCH = 4;      // 16-byte loads in flight per thread while staging a segment
 constexpr int64_t GROUP_COST = 16;  // a group's fixed cost in steps, for balancing CTA ranges
 constexpr int64_t CHUNK_COST = 128; // a chunk's cost (steps + GROUP_COST per group): the unit warps claim
@@ -82,7 +81,11 @@ struct HubArgs {
 // One warp streams groups [ga, gb) (contiguous in hdat): the next
 // HUB_UNROLL steps are loaded while the current ones are summed, across
 // group ends, so the loads run back to back instead of one latency chain per
-// group.  The groups' first steps come from goff 32 at a time (one load,
+// group.  Every edge gets one compensated add, in edge order, so a piece's
+// sum does not depend on where a warp's range starts (the work split is
+// re-cut from measurements; a faster pairwise add of four steps at a time,
+// applied where a batch of loads fell inside one group, made the rounding
+// follow the split).  The groups' first steps come from goff 32 at a time (one load,
 // then shuffles); each group's slots are loaded when it starts.
 __device__ __forceinline__ void stream_groups(const HubArgs &a, const float *s_c, int32_t ga, int32_t gb, int lane)
 {
@@ -107,33 +110,6 @@ __device__ __forceinline__ void stream_groups(const HubArgs &a, const float *s_c
         for (int j = 0; j < HUB_UNROLL; j++) {
             const int32_t q = t + HUB_UNROLL + j;
             wn[j] = q < tend ? __ldcs(D + (int64_t)q * 32) : make_uint2(0u, 0u);
-        }
-        if (t + HUB_UNROLL < gend) {
-            // the whole batch lies inside group g (and more follows): each
-            // piece's four values are added pairwise, then compensated once
-            float b0 = 0.0f, b1 = 0.0f, b2 = 0.0f, b3 = 0.0f;
-            {
-                float x0[HUB_UNROLL], x1[HUB_UNROLL], x2[HUB_UNROLL], x3[HUB_UNROLL];
-#pragma unroll
-                for (int j = 0; j < HUB_UNROLL; j++) {
-                    x0[j] = s_c[wc[j].x & 0xffffu];
-                    x1[j] = s_c[wc[j].x >> 16];
-                    x2[j] = s_c[wc[j].y & 0xffffu];
-                    x3[j] = s_c[wc[j].y >> 16];
-                }
-                b0 = (x0[0] + x0[1]) + (x0[2] + x0[3]);
-                b1 = (x1[0] + x1[1]) + (x1[2] + x1[3]);
-                b2 = (x2[0] + x2[1]) + (x2[2] + x2[3]);
-                b3 = (x3[0] + x3[1]) + (x3[2] + x3[3]);
-            }
-            mgd::kahan_add(s0, r0, b0);
-            mgd::kahan_add(s1, r1, b1);
-            mgd::kahan_add(s2, r2, b2);
-            mgd::kahan_add(s3, r3, b3);
-            t += HUB_UNROLL;
-#pragma unroll
-            for (int j = 0; j < HUB_UNROLL; j++) wc[j] = wn[j];
-            continue;
         }
 #pragma unroll
         for (int j = 0; j < HUB_UNROLL; j++) {

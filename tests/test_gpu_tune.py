@@ -62,3 +62,30 @@ def test_pagerank_layout_tuning_keeps_results():
     assert np.array_equal(x, x2)
     g.free()
     g2.free()
+
+
+def test_segmented_pagerank_independent_of_work_split():
+    """The segmented sweep's work split among the SMs is re-cut from
+    measured times by the autotuner; every piece is summed in edge order by
+    one lane wherever it runs, so a tuned graph and an untuned one give the
+    same bits (and the gather layout, whose bins the tuner also sets,
+    agrees with the oracle)."""
+    h = mg.HostGraph.rmat(16, 16, seed=16)
+    rp, col, wt = h.arrays()
+    og = O.csr_from_arrays(rp, col, wt)
+    g1, g2 = mg.Graph(h), mg.Graph(h)
+    try:
+        x1, i1 = g1.pagerank(mg.PR_TOPOLOGY, tol=1e-6, pr_layout=mg.PR_LAYOUT_SEGMENTED)
+        g2.autotune(mg.ALGO_PR, 0)
+        for _ in range(2):
+            x2, i2 = g2.pagerank(mg.PR_TOPOLOGY, tol=1e-6, pr_layout=mg.PR_LAYOUT_SEGMENTED)
+            assert i1.iterations == i2.iterations and np.array_equal(x1, x2)
+        ref, _ = O.pr_norm_f64(og, 0.85, 1e-6, i1.iterations)
+        assert float(np.max(np.abs(x1.astype(np.float64) - ref))) < 1e-6
+        xg, ig = g2.pagerank(mg.PR_TOPOLOGY, tol=1e-6, pr_layout=mg.PR_LAYOUT_GATHER)
+        refg, _ = O.pr_norm_f64(og, 0.85, 1e-6, ig.iterations)
+        assert float(np.max(np.abs(xg.astype(np.float64) - refg))) < 1e-6
+    finally:
+        g1.free()
+        g2.free()
+        h.free()
