@@ -34,7 +34,8 @@ enum {
     MG_ERR_CUDA = 5,        /* CUDA runtime error (incl. no device)          */
     MG_ERR_ITER_LIMIT = 6,  /* iteration cap reached before convergence     */
     MG_ERR_INVALID = 7,     /* invalid argument                              */
-    MG_ERR_UNSUPPORTED = 8  /* graph lacks what the call needs (e.g. weights)*/
+    MG_ERR_UNSUPPORTED = 8, /* graph lacks what the call needs (e.g. weights)*/
+    MG_ERR_INTERNAL = 9     /* a self-check found an inconsistency           */
 };
 
 const char *mg_status_string(mg_status s);
@@ -337,6 +338,26 @@ mg_status mg_autotune(mg_graph *dg, int32_t algo, int32_t source, const char *ca
 mg_status mg_pagerank_noalloc(const int32_t *d_row, const int32_t *d_col, int32_t nv, int32_t ne, float damping,
                               float tol, int32_t max_iter, float *d_rank, void *stream, int32_t *iterations_out,
                               double *residual_out);
+
+/* ------------------------------------------------------------------------ */
+/* self-checks (host only, no GPU)                                           */
+/* ------------------------------------------------------------------------ */
+/* Build PageRank's segmented shared-memory layout from a host pull CSR
+ * (row [nv+1], col [ne], the engine's vertex order) on `threads` host
+ * threads and on one, require the two builds to be equal, and verify every
+ * invariant the segmented sweep and the row finish rely on: each in-edge
+ * below the segments' reach in exactly one piece of its (row, segment) pair,
+ * pieces of at most 64 edges with the full ones first, groups of equal-
+ * length pieces with padding that reads a zero, every piece in exactly one
+ * slot of the row-major sums in segment order, the rest of a row's in-edges
+ * in its tail, and the list of rows the finish sums a warp each.  Sums are
+ * checked exactly (each edge's id + 1 stands in for its contribution).
+ * *pieces_out = the pieces (0 when the layout would not be used).  Returns
+ * MG_OK, MG_ERR_INVALID for a malformed CSR, or MG_ERR_INTERNAL with the
+ * first violation in mg_last_error().  No counterpart in the reference: it
+ * tests this library's layout builder on CPU-only machines. */
+mg_status mg_selftest_segmented_layout(int32_t nv, int64_t ne, const int32_t *row, const int32_t *col,
+                                       int32_t threads, int64_t *pieces_out);
 
 #ifdef __cplusplus
 }

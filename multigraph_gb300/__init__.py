@@ -28,7 +28,7 @@ LIB_PATH = os.path.join(_PKG, "libmg.so")
 BIN_DIR = os.path.join(_PKG, "bin")
 
 MG_OK, MG_ERR_IO, MG_ERR_PARSE, MG_ERR_RANGE, MG_ERR_OOM, MG_ERR_CUDA, MG_ERR_ITER_LIMIT, MG_ERR_INVALID, \
-    MG_ERR_UNSUPPORTED = range(9)
+    MG_ERR_UNSUPPORTED, MG_ERR_INTERNAL = range(10)
 LOAD_SYM, LOAD_NSYM, LOAD_CC = 1, 2, 4
 EXEC_GRAPH, EXEC_HOST = 0, 1
 DIR_AUTO, DIR_PUSH, DIR_PULL = 0, 1, 2
@@ -120,6 +120,7 @@ def _load_lib():
         "mg_batch_cc": ([vp, P(Opts), vp, P(RunInfo)], i32),
         "mg_autotune": ([vp, i32, i32, C.c_char_p, P(Opts)], i32),
         "mg_pagerank_noalloc": ([vp, vp, i32, i32, f32, f32, i32, vp, vp, P(i32), P(C.c_double)], i32),
+        "mg_selftest_segmented_layout": ([i32, i64, vp, vp, i32, P(i64)], i32),
     }
     for name, (args, res) in sig.items():
         fn = getattr(L, name)
@@ -151,6 +152,7 @@ EXPORTED = [
     "mg_graph_stream", "mg_graph_set_float_weights", "mg_opts_default", "mg_result_device", "mg_bfs", "mg_sssp",
     "mg_cc", "mg_bc", "mg_bc_multi", "mg_pagerank", "mg_ppr_batch", "mg_wpagerank", "mg_wpagerank_backward",
     "mg_batch_create", "mg_batch_free", "mg_batch_bfs", "mg_batch_cc", "mg_autotune", "mg_pagerank_noalloc",
+    "mg_selftest_segmented_layout",
 ]
 NOALLOC_MAX_VERTICES = 1 << 20
 
@@ -168,6 +170,18 @@ def pagerank_noalloc(d_row: int, d_col: int, nv: int, ne: int, d_rank: int, stre
                                    C.c_void_p(d_rank), C.c_void_p(stream) if stream else None, C.byref(it),
                                    C.byref(res)), "mg_pagerank_noalloc")
     return it.value, res.value
+
+
+def selftest_segmented_layout(row_ptr, col, threads: int = 4) -> int:
+    """Host-only check of PageRank's segmented layout built from a CSR
+    (mg_selftest_segmented_layout); returns the number of pieces, raises
+    MGError on a violation."""
+    rp = np.ascontiguousarray(row_ptr, dtype=np.int32)
+    cl = np.ascontiguousarray(col, dtype=np.int32)
+    pieces = C.c_int64(0)
+    _check(lib.mg_selftest_segmented_layout(len(rp) - 1, len(cl), rp.ctypes.data, cl.ctypes.data if len(cl) else None,
+                                            threads, C.byref(pieces)), "mg_selftest_segmented_layout")
+    return pieces.value
 
 
 def _status_name(s: int) -> str:

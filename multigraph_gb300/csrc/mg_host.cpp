@@ -851,6 +851,7 @@ const char *mg_status_string(mg_status s)
     case MG_ERR_ITER_LIMIT: return "iteration limit";
     case MG_ERR_INVALID: return "invalid argument";
     case MG_ERR_UNSUPPORTED: return "unsupported";
+    case MG_ERR_INTERNAL: return "internal inconsistency";
     default: return "unknown status";
     }
 }

@@ -276,32 +276,31 @@ static mg_status hub_split(mg_graph *g)
     return MG_OK;
 }
 
-// Build the segmented layout from the pull CSR (copied back from the
-// device): row-parallel host passes over the edges (count, then write),
-// each thread a contiguous row range whose pieces take consecutive places
-// in every (segment, length) bucket, so buckets come out rows ascending.
-mg_status hub_prepare(mg_graph *g)
+// Build the segmented layout from a pull CSR on the host (prow [n+1], pcol
+// [m], engine ids): row-parallel passes over the edges (count, then write)
+// on nt threads, each a contiguous row range whose pieces take consecutive
+// places in every (segment, length) bucket, so buckets come out rows
+// ascending and the layout does not depend on nt.  o.use stays false when a
+// quarter of the edges or fewer fall in the segments.
+struct HubHost {
+    bool use = false;
+    int32_t H = 0, nseg = 0, nfw = 0;
+    int64_t covered = 0, npieces = 0;
+    std::vector<uint16_t> hdat;
+    std::vector<int32_t> goff, pslot, glam, segg, pair_off, toff, tcol, fin;
+};
+
+static mg_status build_hub(const std::vector<int32_t> &prow, const std::vector<int32_t> &pcol, int32_t n, int64_t m,
+                           int nt, HubHost &o)
 {
-    HubSplit &h = g->hub;
-    if (h.valid) return MG_OK;
-    h.gen = ++g_hub_builds;
-    h.use = false;
-    cudaStream_t s = g->stream;
-    const int32_t n = g->nv;
-    const int64_t m = g->ne;
-    if (n < 4 || m == 0) {
-        h.valid = true;
-        return MG_OK;
-    }
     const int32_t H = SEG_H;
     const int32_t nseg = std::min<int32_t>(SEG_MAX, (n + H - 1) / H);
     const int64_t cover = std::min<int64_t>(n, (int64_t)nseg * H);
     constexpr int32_t L = PIECE_MAX;
-    std::vector<int32_t> prow((size_t)n + 1), pcol((size_t)m);
-    MG_CUDA(cudaMemcpyAsync(prow.data(), g->trow, ((size_t)n + 1) * 4, cudaMemcpyDeviceToHost, s));
-    MG_CUDA(cudaMemcpyAsync(pcol.data(), g->tcol, (size_t)m * 4, cudaMemcpyDeviceToHost, s));
-    MG_CUDA(cudaStreamSynchronize(s));
-    const int nt = std::max(1, std::min(host_threads(0), 32));
+    o = HubHost();
+    o.H = H;
+    o.nseg = nseg;
+    nt = std::max(1, std::min(nt, 32));
     // row ranges of equal edge counts
     std::vector<int32_t> rlo((size_t)nt + 1, n);
     rlo[0] = 0;
@@ -349,11 +348,9 @@ mg_status hub_prepare(mg_graph *g)
     });
     int64_t covered = 0;
     for (int64_t x : tcov) covered += x;
+    o.covered = covered;
     // the segmented pull pays when a quarter of the edges or more are covered
-    if (covered * 4 < m) {
-        h.valid = true;
-        return MG_OK;
-    }
+    if (covered * 4 < m) return MG_OK;
     // buckets in order: segments ascending, lengths descending; each padded
     // to whole groups.  tb: thread t's first place in its bucket.
     std::vector<int64_t> tb((size_t)nt * NB, 0);
@@ -389,7 +386,7 @@ mg_status hub_prepare(mg_graph *g)
     std::vector<int32_t> goff(goff64.begin(), goff64.end());
     std::vector<uint16_t> hdat((size_t)goff64[ngroups] * GROUP, (uint16_t)H);
     std::vector<int32_t> pslot((size_t)ngroups * GROUP, (int32_t)npieces);
-    std::vector<int32_t> tcol((size_t)std::max<int32_t>(toff[n], 1));
+    std::vector<int32_t> tcol((size_t)toff[n]);
     // pass 2: every row's pieces into their buckets, every edge into its
     // piece's step and lane
     run([&](int t) {
@@ -431,40 +428,78 @@ mg_status hub_prepare(mg_graph *g)
             }
         }
     });
-    h.hglam = glam;
-    h.hsegg = segg;
+    o.hdat.swap(hdat);
+    o.goff.swap(goff);
+    o.pslot.swap(pslot);
+    o.glam.swap(glam);
+    o.segg.swap(segg);
+    o.pair_off.swap(pair_off);
+    o.toff.swap(toff);
+    o.tcol.swap(tcol);
+    o.npieces = npieces;
+    o.use = true;
+    // rows of more than FIN_WARP pieces, which k_pr_seg sums a warp each
+    // (graphs without a tail finish every row there)
+    for (int32_t v = 0; v < n; v++)
+        if (npc[v] > FIN_WARP) o.fin.push_back(v);
+    o.nfw = (int32_t)o.fin.size();
+    return MG_OK;
+}
+
+// Build the segmented layout from the pull CSR (copied back from the
+// device), upload it and split the sweep's work among the CTAs.
+mg_status hub_prepare(mg_graph *g)
+{
+    HubSplit &h = g->hub;
+    if (h.valid) return MG_OK;
+    h.gen = ++g_hub_builds;
+    h.use = false;
+    cudaStream_t s = g->stream;
+    const int32_t n = g->nv;
+    const int64_t m = g->ne;
+    if (n < 4 || m == 0) {
+        h.valid = true;
+        return MG_OK;
+    }
+    std::vector<int32_t> prow((size_t)n + 1), pcol((size_t)m);
+    MG_CUDA(cudaMemcpyAsync(prow.data(), g->trow, ((size_t)n + 1) * 4, cudaMemcpyDeviceToHost, s));
+    MG_CUDA(cudaMemcpyAsync(pcol.data(), g->tcol, (size_t)m * 4, cudaMemcpyDeviceToHost, s));
+    MG_CUDA(cudaStreamSynchronize(s));
+    HubHost o;
+    MG_TRY(build_hub(prow, pcol, n, m, host_threads(0), o));
+    h.covered = o.covered;
+    if (!o.use) {
+        h.valid = true;
+        return MG_OK;
+    }
+    const int32_t ngroups = (int32_t)o.glam.size();
+    h.hglam = o.glam;
+    h.hsegg = o.segg;
     h.w.assign((size_t)ngroups, 0.0);
-    for (int32_t q = 0; q < ngroups; q++) h.w[q] = (double)glam[q] + (double)GROUP_COST;
+    for (int32_t q = 0; q < ngroups; q++) h.w[q] = (double)o.glam[q] + (double)GROUP_COST;
     h.grid = g->num_sms;
     MG_TRY(dev_alloc(h.ctime, (size_t)h.grid * 8));
     MG_TRY(hub_split(g));
-    // rows of more than FIN_WARP pieces, which k_pr_seg sums a warp each
-    // (graphs without a tail finish every row there)
-    std::vector<int32_t> fin;
-    for (int32_t v = 0; v < n; v++)
-        if (npc[v] > FIN_WARP) fin.push_back(v);
-    const int32_t nfw = (int32_t)fin.size();
     auto up = [&](DevBuf &b, const void *src, size_t bytes) -> mg_status {
         MG_TRY(dev_alloc(b, std::max<size_t>(bytes, 16) + 16));
         if (bytes) MG_CUDA(cudaMemcpyAsync(b.p, src, bytes, cudaMemcpyHostToDevice, s));
         return MG_OK;
     };
-    MG_TRY(up(h.hdat, hdat.data(), hdat.size() * 2));
-    MG_TRY(up(h.goff, goff.data(), goff.size() * 4));
-    MG_TRY(up(h.pslot, pslot.data(), pslot.size() * 4));
-    MG_TRY(up(h.pair_off, pair_off.data(), pair_off.size() * 4));
-    MG_TRY(up(h.toff, toff.data(), toff.size() * 4));
-    MG_TRY(up(h.tcol, tcol.data(), (size_t)toff[n] * 4));
-    MG_TRY(up(h.fin, fin.data(), fin.size() * 4));   // at least 16 bytes even when empty
-    MG_TRY(dev_alloc(h.P, (size_t)(npieces + 1) * 4));
+    MG_TRY(up(h.hdat, o.hdat.data(), o.hdat.size() * 2));
+    MG_TRY(up(h.goff, o.goff.data(), o.goff.size() * 4));
+    MG_TRY(up(h.pslot, o.pslot.data(), o.pslot.size() * 4));
+    MG_TRY(up(h.pair_off, o.pair_off.data(), o.pair_off.size() * 4));
+    MG_TRY(up(h.toff, o.toff.data(), o.toff.size() * 4));
+    MG_TRY(up(h.tcol, o.tcol.data(), o.tcol.size() * 4));
+    MG_TRY(up(h.fin, o.fin.data(), o.fin.size() * 4));   // at least 16 bytes even when empty
+    MG_TRY(dev_alloc(h.P, (size_t)(o.npieces + 1) * 4));
     MG_CUDA(cudaStreamSynchronize(s));
-    h.H = H;
-    h.nseg = nseg;
+    h.H = o.H;
+    h.nseg = o.nseg;
     h.ngroups = ngroups;
-    h.npieces = npieces;
-    h.covered = covered;
-    h.ntail = toff[n];
-    h.nfw = nfw;
+    h.npieces = o.npieces;
+    h.ntail = o.toff[n];
+    h.nfw = o.nfw;
     h.fin_warp = FIN_WARP;
     h.use = true;
     h.valid = true;
@@ -570,3 +605,109 @@ mg_status hub_launch(mg_graph *g, const float *c0, const float *c1, const int32_
 mg_status hub_check(mg_graph *) { return MG_OK; }
 
 }  // namespace mgi
+
+// ---------------------------------------------------------------------------
+// Host-only check of the segmented layout (no GPU): builds it from a host
+// pull CSR on `threads` threads and on one, requires the two to be equal,
+// and verifies every invariant the sweep and the row finish rely on, with
+// exact integer sums (each edge's id + 1 in place of its contribution).
+// ---------------------------------------------------------------------------
+extern "C" mg_status mg_selftest_segmented_layout(int32_t nv, int64_t ne, const int32_t *row, const int32_t *col,
+                                                  int32_t threads, int64_t *pieces_out)
+{
+    using namespace mgi;
+    clear_error();
+    if (!row || (ne > 0 && !col) || !pieces_out || nv < 0 || ne < 0 || ne > INT32_MAX)
+        return fail(MG_ERR_INVALID, "bad argument");
+    if (row[0] != 0 || row[nv] != ne) return fail(MG_ERR_INVALID, "row offsets must run from 0 to ne");
+    for (int32_t v = 0; v < nv; v++)
+        if (row[v + 1] < row[v]) return fail(MG_ERR_INVALID, "row offsets decrease at row %d", v);
+    for (int64_t p = 0; p < ne; p++)
+        if (col[p] < 0 || col[p] >= nv) return fail(MG_ERR_INVALID, "column id out of range at %lld", (long long)p);
+    *pieces_out = 0;
+    if (nv < 4 || ne == 0) return MG_OK;
+    const std::vector<int32_t> prow(row, row + nv + 1), pcol(col, col + ne);
+    HubHost a, b;
+    MG_TRY(build_hub(prow, pcol, nv, ne, threads, a));
+    MG_TRY(build_hub(prow, pcol, nv, ne, 1, b));
+    if (a.use != b.use || a.covered != b.covered || a.npieces != b.npieces || a.hdat != b.hdat || a.goff != b.goff ||
+        a.pslot != b.pslot || a.glam != b.glam || a.segg != b.segg || a.pair_off != b.pair_off || a.toff != b.toff ||
+        a.tcol != b.tcol || a.fin != b.fin)
+        return fail(MG_ERR_INTERNAL, "segmented layout differs between %d threads and one", threads);
+    if (!a.use) return MG_OK;
+    const int32_t H = a.H, nseg = a.nseg;
+    const int64_t cover = std::min<int64_t>(nv, (int64_t)nseg * H);
+    const int64_t np = a.npieces;
+    const int32_t ngroups = (int32_t)a.glam.size();
+    if ((int32_t)a.goff.size() != ngroups + 1 || (int64_t)a.hdat.size() != (int64_t)a.goff[ngroups] * GROUP ||
+        (int64_t)a.pslot.size() != (int64_t)ngroups * GROUP || (int32_t)a.segg.size() != nseg + 1 ||
+        a.segg[0] != 0 || a.segg[nseg] != ngroups || (int32_t)a.pair_off.size() != nv + 1 || a.pair_off[0] != 0 ||
+        a.pair_off[nv] != np || (int32_t)a.toff.size() != nv + 1)
+        return fail(MG_ERR_INTERNAL, "segmented layout: array sizes");
+    // every packed piece: its slot (once), segment, length and id sum
+    std::vector<int32_t> seen((size_t)np, 0), pseg((size_t)np, -1), plen((size_t)np, 0);
+    std::vector<int64_t> psum((size_t)np, 0);
+    for (int32_t sg = 0; sg < nseg; sg++) {
+        for (int32_t q = a.segg[sg]; q < a.segg[sg + 1]; q++) {
+            const int32_t lam = a.goff[q + 1] - a.goff[q];
+            if (lam != a.glam[q] || lam < 1 || lam > PIECE_MAX || (q > a.segg[sg] && lam > a.glam[q - 1]))
+                return fail(MG_ERR_INTERNAL, "segmented layout: group %d length", q);
+            for (int32_t j = 0; j < GROUP; j++) {
+                const int32_t slot = a.pslot[(size_t)q * GROUP + j];
+                int64_t sum = 0;
+                bool pad = true, real = true;
+                for (int32_t k = 0; k < lam; k++) {
+                    const int32_t id = a.hdat[((size_t)a.goff[q] + k) * GROUP + j];
+                    pad = pad && id == H;
+                    real = real && id < H && (int64_t)sg * H + id < nv;
+                    sum += (int64_t)sg * H + id + 1;
+                }
+                if (slot == np) {
+                    if (!pad) return fail(MG_ERR_INTERNAL, "segmented layout: padding of group %d", q);
+                    continue;
+                }
+                if (slot < 0 || slot > np || !real || seen[slot]++)
+                    return fail(MG_ERR_INTERNAL, "segmented layout: piece %d of group %d", j, q);
+                pseg[slot] = sg;
+                plen[slot] = lam;
+                psum[slot] = sum;
+            }
+        }
+    }
+    for (int64_t p = 0; p < np; p++)
+        if (seen[p] != 1) return fail(MG_ERR_INTERNAL, "segmented layout: slot %lld unused", (long long)p);
+    // every row: its pieces (segments ascending, full pieces first) hold
+    // exactly its covered in-edges; its tail holds the rest in row order
+    std::vector<int32_t> fin;
+    for (int32_t v = 0; v < nv; v++) {
+        int64_t cnt[SEG_MAX] = {0}, sum[SEG_MAX] = {0};
+        std::vector<int32_t> tail;
+        for (int32_t p = row[v]; p < row[v + 1]; p++) {
+            if (col[p] < cover) {
+                cnt[col[p] / H]++;
+                sum[col[p] / H] += (int64_t)col[p] + 1;
+            } else {
+                tail.push_back(col[p]);
+            }
+        }
+        int64_t pcnt[SEG_MAX] = {0}, pss[SEG_MAX] = {0};
+        for (int32_t p = a.pair_off[v]; p < a.pair_off[v + 1]; p++) {
+            const int32_t sg = pseg[p];
+            if (p > a.pair_off[v] && sg < pseg[p - 1]) return fail(MG_ERR_INTERNAL, "row %d: segments out of order", v);
+            if (p > a.pair_off[v] && sg == pseg[p - 1] && plen[p - 1] != PIECE_MAX)
+                return fail(MG_ERR_INTERNAL, "row %d: a short piece before another of its segment", v);
+            pcnt[sg] += plen[p];
+            pss[sg] += psum[p];
+        }
+        for (int32_t sg = 0; sg < nseg; sg++)
+            if (pcnt[sg] != cnt[sg] || pss[sg] != sum[sg])
+                return fail(MG_ERR_INTERNAL, "row %d: segment %d holds other edges", v, sg);
+        if (a.toff[v + 1] - a.toff[v] != (int32_t)tail.size() ||
+            !std::equal(tail.begin(), tail.end(), a.tcol.begin() + a.toff[v]))
+            return fail(MG_ERR_INTERNAL, "row %d: tail", v);
+        if (a.pair_off[v + 1] - a.pair_off[v] > FIN_WARP) fin.push_back(v);
+    }
+    if (fin != a.fin) return fail(MG_ERR_INTERNAL, "segmented layout: warp-row list");
+    *pieces_out = np;
+    return MG_OK;
+}

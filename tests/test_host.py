@@ -43,10 +43,76 @@ def test_library_exports_every_declared_symbol():
 
 def test_status_strings_and_version():
     assert mg.version().startswith("multigraph-gb300")
-    for s in range(9):
+    for s in range(10):
         assert mg.lib.mg_status_string(s)
     o = mg.default_opts()
     assert o.alpha > 0 and o.beta > 0 and abs(o.damping - 0.85) < 1e-6
+
+
+# --------------------------------------------------------------------------
+# PageRank's segmented layout, built and checked on the host
+# --------------------------------------------------------------------------
+def _hub_first(rp, col):
+    """The engine's pull CSR of a host graph: vertices renumbered by
+    descending floor(log2 degree), input order kept within a degree class,
+    each row's columns in the input row's order."""
+    n = len(rp) - 1
+    deg = np.diff(rp).astype(np.int64)
+    lg = np.floor(np.log2(np.maximum(deg, 1))).astype(np.int64)
+    new2old = np.lexsort((np.arange(n), -lg))
+    old2new = np.empty(n, np.int64)
+    old2new[new2old] = np.arange(n)
+    ndeg = deg[new2old]
+    nrp = np.zeros(n + 1, np.int64)
+    nrp[1:] = np.cumsum(ndeg)
+    starts = rp[:-1].astype(np.int64)[new2old]
+    idx = np.repeat(starts - nrp[:-1], ndeg) + np.arange(nrp[-1])
+    return nrp.astype(np.int32), old2new[col[idx]].astype(np.int32)
+
+
+@pytest.mark.parametrize("scale", [12, 16, 17])
+def test_segmented_layout_rmat(scale):
+    """R-MAT graphs in the engine's hub-first order: one, two and three
+    source segments; every invariant of the layout, and the same layout on
+    one host thread as on four."""
+    h = mg.HostGraph.rmat(scale, 16, seed=scale)
+    rp, col, _ = h.arrays()
+    h.free()
+    nrp, ncol = _hub_first(rp, col)
+    pieces = mg.selftest_segmented_layout(nrp, ncol, threads=4)
+    assert len(ncol) / 64 <= pieces <= len(ncol)
+
+
+def test_segmented_layout_star_and_long_pairs():
+    """A star's centre (19,999 in-edges from one segment: 312 full pieces
+    and one of 31) and a row whose edges alternate between two segments."""
+    n = 70000
+    src = np.concatenate([np.zeros(n - 1, np.int64), np.full(200, 5), np.full(200, 65000)])
+    dst = np.concatenate([np.arange(1, n), np.arange(60000, 60200), np.arange(0, 200)])
+    h = mg.HostGraph.from_entries(n, src.astype(np.int32), dst.astype(np.int32), flags=mg.LOAD_NSYM)
+    rp, col, _ = h.arrays()
+    h.free()
+    assert mg.selftest_segmented_layout(rp, col, threads=3) > 0
+
+
+def test_segmented_layout_ids_past_the_segments():
+    """A 2000 x 2000 lattice (4 M vertices, more than the 64 segments'
+    3.67 M): the in-edges from ids past the segments go to the rows' tails."""
+    h = mg.HostGraph.lattice(2000, 2000, 0.05, seed=3)
+    rp, col, _ = h.arrays()
+    h.free()
+    assert len(rp) - 1 > 64 * 57344
+    assert mg.selftest_segmented_layout(rp, col, threads=8) > 0
+
+
+def test_segmented_layout_rejects_bad_csr():
+    rp = np.array([0, 2, 3], np.int32)
+    with pytest.raises(mg.MGError) as e:
+        mg.selftest_segmented_layout(rp, np.array([0, 5, 1], np.int32))
+    assert e.value.status == mg.MG_ERR_INVALID
+    with pytest.raises(mg.MGError) as e:
+        mg.selftest_segmented_layout(np.array([0, 2, 1], np.int32), np.array([0, 1], np.int32))
+    assert e.value.status == mg.MG_ERR_INVALID
 
 
 # --------------------------------------------------------------------------
