@@ -24,17 +24,20 @@
 //                     with more than SEG_MAX segments' worth of vertices),
 //                     int32 ids gathered through L2 by the degree-binned
 //                     sweep.
-// One sweep: k_hub_sweep gives each CTA a contiguous range of groups
-// (balanced by the groups' steps plus a fixed cost per group), stages the
-// contributions c[s*H, (s+1)*H) of every segment its range enters, and its
-// warps claim chunks of consecutive groups from a shared-memory counter and
-// stream them: a lane adds its four pieces' edges in order from shared
-// memory and stores the four totals to P.  Pieces never cross a
-// group, so there are no carries between lanes, warps or CTAs; every sum is
-// formed in a fixed order, so sweeps are reproducible.
+// One sweep: k_hub_sweep gives each CTA a contiguous range of groups (an
+// even share of the groups' cost weights: steps plus a fixed cost per group
+// at first, re-weighted by mg_autotune from measured per-CTA times), stages
+// the contributions c[s*H, (s+1)*H) of every segment its range enters, and
+// its warps claim chunks of consecutive groups from a shared-memory counter
+// and stream them: a lane adds its four pieces' edges in order from shared
+// memory and stores the four totals to P.  Pieces never cross a group, so
+// there are no carries between lanes, warps or CTAs; every sum is formed in
+// a fixed order, whichever warp runs it, so sweeps are reproducible.
 //
-// Per sweep the streams move 2 B per edge (plus padding, ~5 % on R-MAT) and
-// 8 B per piece, instead of 4 B of ids and a 32-byte L2 sector per gather.
+// Per sweep the streams move 2 B per edge (plus padding, ~2.4 % on R-MAT),
+// a 4-byte slot and a 4-byte store per piece (about one piece per ten
+// edges), instead of 4 B of ids and a 32-byte L2 sector per gather.  The
+// row finish (k_pr_seg in mg_pr.cu) reads each row's piece sums.
 
 #include "mg_device.cuh"
 
