@@ -5,7 +5,14 @@
 // Replaces MultiGraph_V_E_V_NOTIDEM (processi.cu:682-894) with _phase1 /
 // _phase11 / _phase2.  The reference scatters pr/deg with FP32 atomicAdd into
 // an intermediate buffer and gathers it in shared memory (order-dependent
-// sums, ~12.5 B/edge).  Here every sweep is a pull (gather) over in-edges:
+// sums, ~12.5 B/edge).  Here every sweep is a pull over in-edges, in one of
+// two layouts (mg_opts.pr_layout; MG_PR_LAYOUT_AUTO picks):
+//   segmented (the default where the segments hold every id): k_hub_sweep
+//               (mg_hub.cu) sums every in-edge from a source segment staged
+//               in shared memory into per-(row, segment) piece sums, then
+//   k_pr_seg    sums each row's pieces in order, applies the update and
+//               (last block) closes the sweep;
+//   gather (contribution gathers through L2):
 //   k_pr_light  degree bins (mg_bins.cuh): a warp per row of tbin+1..heavy
 //               in-edges (lanes read one 128 B line of column ids per step,
 //               a fixed shuffle tree sums them), a thread per row of <= tbin
@@ -17,8 +24,8 @@
 //               partials in slot order: convergence test, loop condition.
 // Sums are therefore deterministic (fixed order) run to run.
 // Algorithmic bytes per sweep: 4m (column ids) + 4(n+1) (offsets) + 12n
-// (old value read, new value and contribution written); the contribution
-// gathers (4n bytes) are served by L2.
+// (old value read, new value and contribution written); in the gather
+// layout the contribution gathers (4n bytes) are served by L2.
 
 #include "mg_device.cuh"
 #include "mg_ops.cuh"
