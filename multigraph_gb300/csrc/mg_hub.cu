@@ -58,7 +58,7 @@ constexpr int HUB_THREADS = 1024;   // one CTA per SM (shared memory bound)
 constexpr int HUB_UNROLL = 4;       // steps (256-byte warp loads) in flight per warp
 constexpr int STAGE_BATCH = 4;      // 16-byte loads in flight per thread while staging a segment
 constexpr int64_t GROUP_COST = 16;  // a group's fixed cost in steps, for balancing CTA ranges
-constexpr int64_t CHUNK_COST = 128; // a chunk's cost (steps + GROUP_COST per group): the unit warps claim
+constexpr int64_t CHUNK_COST = 64;  // a chunk's cost (steps + GROUP_COST per group): the unit warps claim
 // the row finish sums rows with more than FIN_WARP pieces a warp each, the
 // rest a thread each (8-lane groups for rows of 5-64 pieces walked their
 // rows one after another and were slower)
@@ -100,7 +100,9 @@ __device__ __forceinline__ void stream_groups(const HubArgs &a, const float *s_c
     const int32_t tend = __ldg(&a.goff[gb]);
     int32_t g = ga;
     int32_t gend = __shfl_sync(FULL, cg, 1);
-    int4 sl = __ldg(&a.pslot[(int64_t)g * 32 + lane]);
+    // slots and ids are streamed once per sweep: evict-first loads keep L2
+    // for the piece sums the row finish reads next
+    int4 sl = __ldcs(&a.pslot[(int64_t)g * 32 + lane]);
     // compensated sums (Kahan): a piece of up to PIECE_MAX edges is exact to
     // about one rounding, so a hub row's total does not drift by a few 1e-6
     // from sweep to sweep as its inputs settle
@@ -135,7 +137,7 @@ __device__ __forceinline__ void stream_groups(const HubArgs &a, const float *s_c
                             cg = __ldg(&a.goff[min(cbase + lane, gb)]);
                         }
                         gend = __shfl_sync(FULL, cg, g + 1 - cbase);
-                        sl = __ldg(&a.pslot[(int64_t)g * 32 + lane]);
+                        sl = __ldcs(&a.pslot[(int64_t)g * 32 + lane]);
                     }
                 }
             }
