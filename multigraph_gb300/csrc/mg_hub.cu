@@ -59,6 +59,7 @@ constexpr int HUB_UNROLL = 4;       // steps (256-byte warp loads) in flight per
 constexpr int STAGE_BATCH = 4;      // 16-byte loads in flight per thread while staging a segment
 constexpr int64_t GROUP_COST = 16;  // a group's fixed cost in steps, for balancing CTA ranges
 constexpr int64_t CHUNK_COST = 64;  // a chunk's cost (steps + GROUP_COST per group): the unit warps claim
+                                    // (R-MAT 22 sweep: 128 -> 129-140 us, 64 -> 122 us, 32 -> 124-127, 16 -> 129-131)
 // the row finish sums rows with more than FIN_WARP pieces a warp each, the
 // rest a thread each (8-lane groups for rows of 5-64 pieces walked their
 // rows one after another and were slower)
