@@ -558,8 +558,9 @@ __device__ __forceinline__ void close_sweep(const PArgs &a, const PCtl &c, int n
 // chunks): each row sums its pieces' partials (P[pair_off[v] ..], segments
 // ascending) and applies the update.  Rows are binned by piece count at
 // layout time: long rows a warp each (lane-strided, then a fixed xor tree;
-// listed), the rest a thread each in row order (compensated FP32, four loads
-// in flight) -- fixed orders, so sweeps stay reproducible.
+// listed), the rest a thread each in row order (compensated FP32; a warp's
+// 32 rows read their piece sums as one coalesced window staged in shared
+// memory) -- fixed orders, so sweeps stay reproducible.
 template <class Op>
 __global__ void __launch_bounds__(THREADS, 8) k_pr_seg(PArgs a, cudaGraphConditionalHandle h, int use_cond)
 {
@@ -597,24 +598,58 @@ __global__ void __launch_bounds__(THREADS, 8) k_pr_seg(PArgs a, cudaGraphConditi
         const float tot = mgd::warp_sum_comp(s, r);
         if (lane == 0) op.finish_row(v, tot);
     }
-    // every other row a thread each, rows in order (the warp rows skipped)
-    for (int32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < a.n; v += gridDim.x * blockDim.x) {
-        int32_t p = __ldg(&a.pair_off[v]);
-        const int32_t e = __ldg(&a.pair_off[v + 1]);
-        if (e - p > a.fin_warp) continue;
-        float s = 0.0f, r = 0.0f;
-        if (!op.skip(v)) {
-            for (; p + 4 <= e; p += 4) {
-                const float f0 = __ldcg(&a.P[p]), f1 = __ldcg(&a.P[p + 1]), f2 = __ldcg(&a.P[p + 2]),
-                            f3 = __ldcg(&a.P[p + 3]);
-                mgd::kahan_add(s, r, f0);
-                mgd::kahan_add(s, r, f1);
-                mgd::kahan_add(s, r, f2);
-                mgd::kahan_add(s, r, f3);
+    // every other row a thread each, rows in order (the warp rows skipped):
+    // a warp takes 32 consecutive rows, copies their piece sums (one
+    // contiguous window of P) into shared memory with coalesced loads, and
+    // each lane sums its row from there; windows longer than SEG_WIN (rows
+    // near the hubs) are read from P directly.  Same adds in the same order
+    // either way.
+    constexpr int SEG_WIN = 512;
+    __shared__ float s_win[THREADS / 32][SEG_WIN];
+    float *win = s_win[threadIdx.x >> 5];
+    for (int32_t vb = gwarp * 32; vb < a.n; vb += nwarps * 32) {
+        const int32_t v = vb + lane;
+        const bool act = v < a.n;
+        const int32_t p0 = act ? __ldg(&a.pair_off[v]) : 0;
+        const int32_t p1 = act ? __ldg(&a.pair_off[v + 1]) : 0;
+        const int32_t last = min(a.n - vb, 32) - 1;
+        const int32_t base = __shfl_sync(0xffffffffu, p0, 0), wend = __shfl_sync(0xffffffffu, p1, last);
+        const int32_t len = wend - base;
+        const bool in_win = len <= SEG_WIN;
+        if (in_win) {
+            int32_t i = lane;
+            for (; i + 96 < len; i += 128) {
+                const float f0 = __ldcg(&a.P[base + i]), f1 = __ldcg(&a.P[base + i + 32]),
+                            f2 = __ldcg(&a.P[base + i + 64]), f3 = __ldcg(&a.P[base + i + 96]);
+                win[i] = f0;
+                win[i + 32] = f1;
+                win[i + 64] = f2;
+                win[i + 96] = f3;
             }
-            for (; p < e; p++) mgd::kahan_add(s, r, __ldcg(&a.P[p]));
+            for (; i < len; i += 32) win[i] = __ldcg(&a.P[base + i]);
         }
-        op.finish_row(v, s - r);
+        __syncwarp();
+        if (act && p1 - p0 <= a.fin_warp) {
+            float s = 0.0f, r = 0.0f;
+            if (!op.skip(v)) {
+                if (in_win) {
+                    for (int32_t p = p0 - base; p < p1 - base; p++) mgd::kahan_add(s, r, win[p]);
+                } else {
+                    int32_t p = p0;
+                    for (; p + 4 <= p1; p += 4) {
+                        const float f0 = __ldcg(&a.P[p]), f1 = __ldcg(&a.P[p + 1]), f2 = __ldcg(&a.P[p + 2]),
+                                    f3 = __ldcg(&a.P[p + 3]);
+                        mgd::kahan_add(s, r, f0);
+                        mgd::kahan_add(s, r, f1);
+                        mgd::kahan_add(s, r, f2);
+                        mgd::kahan_add(s, r, f3);
+                    }
+                    for (; p < p1; p++) mgd::kahan_add(s, r, __ldcg(&a.P[p]));
+                }
+            }
+            op.finish_row(v, s - r);
+        }
+        __syncwarp();   // the window is reused by the next 32 rows
     }
     block_partials<Op::kDataDriven>(a, blockIdx.x, op.resid, op.dangs, op.any, op.act, op.dfz);
     close_sweep<Op>(a, c, gridDim.x, h, use_cond);
