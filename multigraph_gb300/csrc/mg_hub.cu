@@ -89,8 +89,8 @@ struct HubArgs {
 // sum does not depend on where a warp's range starts (the work split is
 // re-cut from measurements; a faster pairwise add of four steps at a time,
 // applied where a batch of loads fell inside one group, made the rounding
-// follow the split).  The groups' first steps come from goff 32 at a time (one load,
-// then shuffles); each group's slots are loaded when it starts.
+// follow the split).  The groups' first steps come from goff 32 at a time
+// (one load, then shuffles); each group's slots are loaded when it starts.
 __device__ __forceinline__ void stream_groups(const HubArgs &a, const float *s_c, int32_t ga, int32_t gb, int lane)
 {
     constexpr unsigned FULL = 0xffffffffu;
@@ -148,6 +148,10 @@ __device__ __forceinline__ void stream_groups(const HubArgs &a, const float *s_c
     }
 }
 
+// One sweep over every piece: each CTA walks its parts (one segment each),
+// stages the segment's contributions in shared memory, and its warps claim
+// the part's chunks from a shared-memory counter; the CTA's clock cycles go
+// to ctime for the next re-split.
 __global__ void __launch_bounds__(HUB_THREADS, 1) k_hub_sweep(HubArgs a)
 {
     extern __shared__ __align__(16) float s_c[];   // [H + 4]
