@@ -105,6 +105,49 @@ def test_segmented_layout_ids_past_the_segments():
     assert mg.selftest_segmented_layout(rp, col, threads=8) > 0
 
 
+def _csr_from_rows(n, rows):
+    """CSR with rows[v] = list of column ids (rows not given are empty)."""
+    rp = np.zeros(n + 1, np.int64)
+    for v, cols in rows.items():
+        rp[v + 1] = len(cols)
+    rp = np.cumsum(rp)
+    col = np.zeros(int(rp[-1]), np.int32)
+    for v, cols in rows.items():
+        col[rp[v]:rp[v + 1]] = cols
+    return rp.astype(np.int32), col
+
+
+@pytest.mark.parametrize("n", [57344, 57345, 2 * 57344 + 7])
+def test_segmented_layout_piece_boundaries(n):
+    """Rows with exactly 64, 65, 128 and 129 in-edges from one segment (full
+    pieces only, a full piece and one edge, two full pieces, ...), rows split
+    across segments, empty rows, and segment counts at the boundary of one
+    segment (57,344 vertices) and one past it (a second segment of one
+    vertex)."""
+    rng = np.random.default_rng(n)
+    rows = {0: list(range(64)), 1: list(range(100, 165)), 2: list(range(0, 128)), 3: list(range(1, 130)),
+            4: [n - 1] * 3 + [0, 1], 5: [n - 1], 7: [57343, 57344 % n, 5]}
+    for v in range(8, 200):
+        rows[v] = sorted(rng.integers(0, n, size=int(rng.integers(1, 300))).tolist())
+    rp, col = _csr_from_rows(n, rows)
+    assert mg.selftest_segmented_layout(rp, col, threads=4) > 0
+
+
+def test_segmented_layout_tail_boundary_and_unused():
+    """One vertex past the 64 segments (a tail of one id), and a graph whose
+    in-edges mostly come from past the segments (the layout is not used)."""
+    cover = 64 * 57344
+    n = cover + 1
+    rows = {0: [cover, 1, 2, 3], 1: [0] * 10, 2: [cover - 1, cover]}
+    rp, col = _csr_from_rows(n, rows)
+    assert mg.selftest_segmented_layout(rp, col, threads=2) > 0
+    n = cover + 64
+    rows = {v: list(range(cover, cover + 64)) for v in range(10)}
+    rows[10] = [0]
+    rp, col = _csr_from_rows(n, rows)
+    assert mg.selftest_segmented_layout(rp, col, threads=2) == 0
+
+
 def test_segmented_layout_rejects_bad_csr():
     rp = np.array([0, 2, 3], np.int32)
     with pytest.raises(mg.MGError) as e:
