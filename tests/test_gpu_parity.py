@@ -192,10 +192,10 @@ def test_pagerank_segmented_past_the_segments():
 def test_pagerank_hub_split(scale, layout):
     """Graphs with more vertices than one shared-memory segment holds, in
     both pull layouts: L2 gathers over degree bins, and segments (each
-    sweep sums every row's per-segment parts from shared memory, heavy rows
-    in chunks).  Every form against the oracle; the sums are formed in a
-    fixed order, so two runs agree bit for bit, in graph and host loops
-    alike."""
+    sweep sums every in-edge from a staged segment into its (row, segment)
+    piece, then each row its pieces).  Every form against the oracle; the
+    sums are formed in a fixed order, so two runs agree bit for bit, in
+    graph and host loops alike."""
     h = mg.HostGraph.rmat(scale, 16, seed=scale)
     rp, col, wt = h.arrays()
     og = O.csr_from_arrays(rp, col, wt)
